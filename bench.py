@@ -1,0 +1,443 @@
+"""Benchmark: ms per voxel-cone-tracing frame (voxelize + inject + mip +
+trace) on the large plain frame: 262,144 triangles, 256^3 RGBA16F grid with
+9 levels, 2048^2 shadow map, 1920x1080 G-buffer, 6 diffuse cones (60 deg) +
+1 specular cone (10 deg).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--config large|cornell] [--filter software|hardware]
+
+Our arm: inputs (triangles, shadow map, G-buffer) are resident in HBM; every
+timed step is one vct_frame call through the C ABI, timed with CUDA events on
+its stream, with a 256 MiB write between steps (outside the events) to flush
+the 129 MB L2.  `e2e` repeats the measurement through the same C ABI with the
+inputs in pinned host memory: each step copies the triangles, shadow map and
+G-buffer to the device, runs the frame and copies the composite image back.
+
+Reference arm (--impl reference): the reference's path is OpenGL/GLSL, which
+cannot run here (no graphics stack), so its CPU restatement (oracle/, the
+same code that judges parity) is timed on all host threads; each step
+voxelises, normalises, injects and filters the full grid and traces a row
+sample of the frame, extrapolated to the full frame.
+
+With --gpus N (launched by torchrun) every rank runs an independent replica
+(the path does not shard a single frame); `value` is the job's effective
+ms per frame: the slowest rank's total time over all frames of all ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms/frame voxelize+inject+mip+trace 256³@1080p"
+WORKLOAD = "large plain frame: 262,144 tris, 256^3 RGBA16F x9 levels, 2048^2 shadow map, 1920x1080, 6+1 cones"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="large", choices=["large", "cornell"])
+    ap.add_argument("--filter", default="software", choices=["software", "hardware"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-rows", type=int, default=24, help="rows of the frame traced by the CPU baseline")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ dist
+def dist_init(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if os.environ.get("VCT_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+# ------------------------------------------------------------- workloads
+def make_scene(args):
+    from vct_gb300 import scenes
+
+    return scenes.make(args.config, seed=args.seed)
+
+
+def algorithmic_bytes(sc, stats, launches_per_frame):
+    """Per-launch algorithmic HBM bytes of each frame kernel (the minimum a
+    kernel must move: inputs read once, outputs written once)."""
+    N = sc.dim
+    nv = N ** 3
+    T = sc.ntri
+    W, H = sc.gbuffer_size
+    P = W * H
+    SW, SH = sc.shadow_size
+    F = stats["total_voxel_fragments"]
+    U = stats["unique_voxels"]
+    mip_tail = sum((N >> l) ** 3 for l in range(5, sc.levels))
+    return {
+        # triangles in (pos, normal, albedo), 7 x 4 B accumulator read-modify-write per fragment
+        "accumulate": T * (36 + 36 + 12) + F * 7 * 4 * 2,
+        # shadow map read, lit bit set per texel (bit mask write once)
+        "inject_mark": SW * SH * 4 + nv // 8,
+        # counts read; sums read+cleared for occupied voxels; colour, normal, radiance L0 written; lit mask read;
+        # levels 1..4 written
+        "resolve": nv * 4 + U * 7 * 4 * 2 + nv * 8 * 3 + nv // 8 + sum((N >> l) ** 3 for l in range(1, 5)) * 8,
+        "mip_tail": (N >> 4) ** 3 * 8 + mip_tail * 8,
+        # G-buffer (3 float4) read, composite float4 written
+        "trace": P * (48 + 16),
+    }
+
+
+def run_ours(args, rank, world):
+    import ctypes as C
+
+    import torch
+
+    import oracle as O
+    from vct_gb300 import _lib as L
+    from vct_gb300 import api
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    sc = make_scene(args)
+    W, H = sc.gbuffer_size
+    SW, SH = sc.shadow_size
+    pos = torch.from_numpy(sc.positions).to(dev)
+    nrm = torch.from_numpy(sc.normals).to(dev)
+    alb = torch.from_numpy(sc.albedo).to(dev)
+    tris = api.triangles(pos, nrm, alb)
+    sm = torch.empty(SW * SH, dtype=torch.float32, device=dev)
+    api.render_shadowmap(tris, sc, sm)
+    keys = torch.empty(W * H, dtype=torch.int64, device=dev)
+    gpos, gnrm, galb = (torch.empty(W * H * 4, dtype=torch.float32, device=dev) for _ in range(3))
+    api.render_gbuffer(tris, sc, keys, gpos, gnrm, galb)
+    del keys
+    color = torch.empty(W * H * 4, dtype=torch.float32, device=dev)
+    lights = api.light_array(sc.lights)
+    shadow = api.shadow_desc(sc, sm)
+    gb = api.gbuffer(gpos, gnrm, galb, W, H)
+    out = api.trace_out(color=color)
+    ctx = api.Context(api.config_for(sc, device=local))
+    params = api.scene_params(sc)
+    params.trace_filter = L.VCT_FILTER_HARDWARE if args.filter == "hardware" else L.VCT_FILTER_SOFTWARE
+    ctx.set_params(params)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    lib = L.load()
+
+    def frame():
+        ctx.frame(tris, lights, shadow, sc.eye, gb, out, stream)
+
+    for _ in range(max(3, args.warmup)):
+        frame()
+    torch.cuda.synchronize()
+    stats = ctx.stats()
+    # samples per frame (counted once, outside the timed region)
+    samples = torch.zeros(1, dtype=torch.int64, device=dev)
+    ctx.frame(tris, lights, shadow, sc.eye, gb, api.trace_out(color=color, samples=samples), stream)
+    torch.cuda.synchronize()
+    n_samples = int(samples.item())
+
+    # ---- timed region: K frames, per-frame events, L2 flushed between frames
+    ctx.enable_timers(True)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stage = {k: 0.0 for k in ("voxelize_ms", "radiance_ms", "mipmap_ms", "render_ms", "total_ms")}
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = lib.vct_launch_count()
+    t_wall = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            starts[i].record(stream)
+            frame()
+            ends[i].record(stream)
+            for k, v in ctx.timers().items():  # waits for this frame's end event
+                stage[k] += v
+        torch.cuda.synchronize()
+    barrier(world)
+    wall_s = time.perf_counter() - t_wall
+    launches = lib.vct_launch_count() - launches0
+    ctx.enable_timers(False)
+    frame_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(frame_ms)
+    total_ms_max = max_over_ranks(total_ms, world)
+    ms_per_frame = total_ms_max / (args.steps * world)
+    stage = {k: v / args.steps for k, v in stage.items()}
+
+    # ---- e2e through the C ABI with host buffers (pinned), copies timed
+    h_pos, h_nrm, h_alb = (t.cpu().pin_memory() for t in (pos, nrm, alb))
+    h_sm = sm.cpu().pin_memory()
+    h_gpos, h_gnrm, h_galb = (t.cpu().pin_memory() for t in (gpos, gnrm, galb))
+    h_color = torch.empty(W * H * 4, dtype=torch.float32).pin_memory()
+    d_pos, d_nrm, d_alb, d_sm = (torch.empty_like(t, device=dev) for t in (h_pos, h_nrm, h_alb, h_sm))
+    d_gpos, d_gnrm, d_galb = (torch.empty_like(t, device=dev) for t in (h_gpos, h_gnrm, h_galb))
+    e_tris = api.triangles(d_pos, d_nrm, d_alb)
+    e_shadow = api.shadow_desc(sc, d_sm)
+    e_gb = api.gbuffer(d_gpos, d_gnrm, d_galb, W, H)
+    h2d = sum(t.numel() * t.element_size() for t in (h_pos, h_nrm, h_alb, h_sm, h_gpos, h_gnrm, h_galb))
+    d2h = h_color.numel() * 4
+
+    def e2e_step():
+        for d, h in ((d_pos, h_pos), (d_nrm, h_nrm), (d_alb, h_alb), (d_sm, h_sm), (d_gpos, h_gpos),
+                     (d_gnrm, h_gnrm), (d_galb, h_galb)):
+            d.copy_(h, non_blocking=True)
+        ctx.frame(e_tris, lights, e_shadow, sc.eye, e_gb, api.trace_out(color=color), stream)
+        h_color.copy_(color, non_blocking=True)
+
+    for _ in range(max(3, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    e_starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    e_ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        e_starts[i].record(stream)
+        e2e_step()
+        e_ends[i].record(stream)
+    torch.cuda.synchronize()
+    e2e_total = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(e_starts, e_ends)), world)
+    e2e_ms = e2e_total / (args.steps * world)
+    assert torch.isfinite(h_color).all(), "non-finite output"
+
+    # ---- roofline of the dominant kernel
+    alg = algorithmic_bytes(sc, stats, None)
+    kernel_ms = {"accumulate": stage["voxelize_ms"], "inject_mark": stage["radiance_ms"],
+                 "resolve+mips": stage["mipmap_ms"], "trace": stage["render_ms"]}
+    dom = max(kernel_ms, key=kernel_ms.get)
+    peaks = load_peaks()
+    if dom == "resolve+mips":
+        bytes_dom = alg["resolve"] + alg["mip_tail"]
+    else:
+        bytes_dom = alg[dom]
+    achieved = bytes_dom / (kernel_ms[dom] * 1e-3) / 1e9
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                "peak_source": peaks["source"], "algorithmic_bytes": int(bytes_dom),
+                "kernel_ms": round(kernel_ms[dom], 4)}
+    if dom == "trace":
+        roofline["samples_per_s"] = round(n_samples / (kernel_ms[dom] * 1e-3), 1)
+        roofline["note"] = ("cone tracing is gather-bound (L1/L2 trilinear samples), not HBM-bound: its HBM "
+                            "fraction counts only G-buffer reads and the image write")
+
+    result = {
+        "metric": METRIC, "value": round(ms_per_frame, 4), "unit": "ms/frame", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_frame * world, 4),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32 math, f16 volumes, u32 accumulators",
+        "data": "synthetic seeded scene (no dataset); inputs resident in HBM",
+        "config": {"workload": WORKLOAD if args.config == "large" else f"{args.config} scene",
+                   "scene": args.config, "seed": args.seed, "triangles": sc.ntri, "grid": sc.dim, "levels": sc.levels,
+                   "shadow_map": list(sc.shadow_size), "gbuffer": list(sc.gbuffer_size), "cones": "6x60deg + 1x10deg",
+                   "sampler": args.filter, "parallelism": f"replicas x{world}",
+                   "l2": "256 MiB buffer written between timed frames (outside the events)"},
+        "stage_ms": {k: round(v, 4) for k, v in stage.items()},
+        "frame_ms_min": round(min(frame_ms), 4), "frame_ms_median": round(statistics.median(frame_ms), 4),
+        "wall_s": round(wall_s, 3),
+        "e2e": {"value": round(e2e_ms, 4), "unit": "ms/frame", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "clocks": clk.summary(),
+        "voxelize_stats": stats,
+        "samples_per_frame": n_samples,
+    }
+    ctx.close()
+    return result, sc
+
+
+def load_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+# ----------------------------------------------------------- CPU side
+def cpu_frame_ms(sc, nthreads: int, sample_rows: int, shadowmap=None, gbuf=None) -> tuple[float, dict]:
+    """One CPU-oracle frame: full voxelize/normalize/inject/mips, trace of
+    `sample_rows` evenly spaced rows, extrapolated to the full frame."""
+    import oracle as O
+
+    W, H = sc.gbuffer_size
+    sm = O.render_shadowmap(sc, nthreads) if shadowmap is None else shadowmap
+    gp, gn, ga = O.render_gbuffer(sc) if gbuf is None else gbuf
+    t = {}
+    t0 = time.perf_counter()
+    count, sums, total = O.voxelize(sc, sm, nthreads=nthreads)
+    t1 = time.perf_counter()
+    chain = np.zeros(4 * O.chain_voxels(sc.dim, sc.levels), dtype=np.uint16)
+    color, normal, _, _ = O.normalize(sc, count, sums, radiance=chain, nthreads=nthreads)
+    t2 = time.perf_counter()
+    O.inject(sc, sm, color, normal, chain, nthreads=nthreads)
+    t3 = time.perf_counter()
+    O.build_mips(sc.dim, sc.levels, chain, nthreads)
+    t4 = time.perf_counter()
+    step = max(1, H // max(1, sample_rows))
+    O.trace(sc, chain, gp, gn, ga, precision=32, rows=(0, H), row_step=step, nthreads=nthreads, want=("color",))
+    t5 = time.perf_counter()
+    rows_traced = len(range(0, H, step))
+    t = {"voxelize_ms": (t1 - t0) * 1e3, "normalize_ms": (t2 - t1) * 1e3, "inject_ms": (t3 - t2) * 1e3,
+         "mips_ms": (t4 - t3) * 1e3, "trace_ms_full_frame": (t5 - t4) * 1e3 * H / rows_traced,
+         "rows_traced": rows_traced}
+    return (t4 - t0) * 1e3 + t["trace_ms_full_frame"], t
+
+
+def cpu_model() -> str:
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
+
+
+def run_reference(args, rank, world):
+    sc = make_scene(args)
+    nthreads = os.cpu_count() or 1
+    import oracle as O
+
+    sm = O.render_shadowmap(sc, nthreads)
+    gbuf = O.render_gbuffer(sc)
+    times = []
+    for i in range(args.warmup + args.steps):
+        ms, detail = cpu_frame_ms(sc, nthreads, args.cpu_sample_rows, sm, gbuf)
+        if i >= args.warmup:
+            times.append(ms)
+    value = sum(times) / len(times)
+    sample = (f"each step: full voxelize/normalize/inject/mips of the workload + trace of {detail['rows_traced']} "
+              f"evenly spaced rows of {sc.gbuffer_size[1]}, trace time scaled to the full frame")
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": "ms/frame", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 2), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 math, f16 volumes, u32 accumulators",
+        "data": "synthetic seeded scene (no dataset)",
+        "config": {"workload": WORKLOAD if args.config == "large" else f"{args.config} scene", "scene": args.config,
+                   "seed": args.seed, "triangles": sc.ntri, "grid": sc.dim},
+        "cpu_baseline": {"value": round(value, 2), "unit": "ms/frame", "cores": nthreads, "kind": "port",
+                         "sample": sample, "cpu": cpu_model(),
+                         "why_port": "the reference's own path is OpenGL/GLSL: no graphics stack here or on the GPU box"},
+        "e2e": {"value": round(value, 2), "unit": "ms/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "stage_ms_last": {k: round(v, 2) for k, v in detail.items()},
+    }
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args.gpus)
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args, rank, world)), flush=True)
+        return
+    result, sc = run_ours(args, rank, world)
+    if rank == 0 and not args.no_cpu_baseline:
+        ms, detail = cpu_frame_ms(sc, 1, args.cpu_sample_rows)
+        result["cpu_baseline"] = {"value": round(ms, 2), "unit": "ms/frame", "cores": 1, "kind": "port",
+                                  "sample": f"one frame: full voxelize/normalize/inject/mips + trace of "
+                                            f"{detail['rows_traced']} evenly spaced rows scaled to the full frame, "
+                                            f"single thread", "cpu": cpu_model(), "nproc": os.cpu_count(),
+                                  "stage_ms": {k: round(v, 1) for k, v in detail.items()}}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,285 @@
+/*
+ * vct.h - C ABI of the GB300 voxel cone tracing hot path.
+ *
+ * The reference (sfreed141/vct) drives this path through OpenGL programs whose
+ * operator surface is a set of named uniforms, image/texture bindings and an
+ * SSBO of lights (src/Application.cpp:666-1067).  This header replaces that
+ * surface with plain C entry points over device pointers:
+ *
+ *   reference program / call site                         entry point here
+ *   voxelize.vert/.geom/.frag   src/Application.cpp:666-754   vct_voxelize_accumulate
+ *   transferVoxels.comp         src/Application.cpp:757-785   vct_normalize
+ *   (both, back to back)                                      vct_voxelize
+ *   injectRadiance.comp         src/Application.cpp:788-837   vct_inject
+ *   filterRadiance.comp loop    src/Application.cpp:877-921   vct_build_mips
+ *   phong.frag cone tracing     src/Application.cpp:967-1067  vct_trace
+ *   the four timed regions      src/Application.cpp:583-1067  vct_frame
+ *   VoxelizeInfo SSBO readback  src/Overlay.cpp:104-116       vct_get_stats
+ *   Settings / VCTSettings      src/Application.h:28-103      vct_params
+ *   class VCT (volumes, dims)   src/Application.h:107-156     vct_config + vct_ctx
+ *   struct Light (std140, 80 B) src/Scene.h:13-34             vct_light
+ *
+ * Conventions
+ *  - Every function returns vct_status; nothing throws across the ABI.
+ *  - Pointers named *_dev are CUDA device pointers owned by the caller.
+ *    Volumes (accumulators, colour/normal/radiance mip chains) are owned by
+ *    the context.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *    stream).  Calls are stream ordered; host arguments are copied before
+ *    the call returns.
+ *  - A context is bound to the CUDA device given at creation and is not
+ *    thread safe: use one context per host thread.
+ *  - Matrices are column-major float[16], as glm / GLSL store them.
+ *  - Volumes are RGBA16F (IEEE binary16 x4, 8 bytes per voxel), x fastest:
+ *    voxel (x,y,z) of level l lives at level_offset[l] + (z*S + y)*S + x
+ *    with S = dim >> l.
+ */
+#ifndef VCT_H
+#define VCT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VCT_ABI_VERSION 1
+#define VCT_MAX_LIGHTS 16
+#define VCT_MAX_LEVELS 11 /* dim <= 1024 */
+
+typedef enum vct_status {
+    VCT_OK = 0,
+    VCT_ERR_INVALID_ARGUMENT = 1,
+    VCT_ERR_OUT_OF_MEMORY = 2,
+    VCT_ERR_CUDA = 3,
+    VCT_ERR_STATE = 4,       /* call order violated (e.g. trace before mips) */
+    VCT_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    VCT_ERR_UNSUPPORTED = 6,
+    VCT_ERR_OVERFLOW = 7     /* a voxel received more fragments than the exact range */
+} vct_status;
+
+typedef struct vct_ctx vct_ctx;
+
+/* Light types, as `uint type` in the reference Light block (src/Scene.h:14). */
+#define VCT_LIGHT_POINT 0u
+#define VCT_LIGHT_DIRECTIONAL 1u
+
+/* Byte-for-byte the std140 record the reference writes into its light SSBO
+ * (src/Scene.cpp:64-76, shaders/voxelize.frag:31-44): 80 bytes per light. */
+typedef struct vct_light {
+    float position[3];
+    float _pad0;
+    float direction[3];
+    float _pad1;
+    float color[3];
+    float range;           /* offset 44 */
+    float intensity;       /* offset 48 */
+    uint32_t enabled;      /* offset 52 */
+    uint32_t selected;     /* offset 56 (unused by the path) */
+    uint32_t shadow_caster;/* offset 60 */
+    uint32_t type;         /* offset 64 */
+    uint32_t _pad2[3];
+} vct_light;
+
+/* Volume set-up: the reference's class VCT (src/Application.h:107-156). */
+#define VCT_CONFIG_COLOR_MIPS 1u /* also keep a colour mip chain (reference's second filter loop) */
+
+typedef struct vct_config {
+    int32_t voxel_dim;     /* power of two in [16, 1024]  (VCT::voxelDim) */
+    int32_t voxel_levels;  /* 0 = full chain log2(dim)+1; clamped like VCT::remake */
+    float voxel_min[3];    /* VCT::min, must equal -voxel_max (symmetric, cubic) */
+    float voxel_max[3];    /* VCT::max */
+    float voxel_center[3]; /* VCT::center */
+    int32_t device;        /* CUDA device ordinal */
+    uint32_t flags;        /* VCT_CONFIG_* */
+} vct_config;
+
+/* One cone family: the reference's VCTSettings (src/Application.h:28-34). */
+typedef struct vct_cone_settings {
+    int32_t steps;
+    float cone_angle;          /* radians, full aperture */
+    float bias;                /* start offset along the normal, in voxels */
+    float cone_initial_height; /* in voxels */
+    float lod_offset;
+} vct_cone_settings;
+
+#define VCT_FILTER_SOFTWARE 0 /* fp32 trilinear from the linear volume (exact GL semantics) */
+#define VCT_FILTER_HARDWARE 1 /* texture units' trilinear-mip filtering */
+
+/* Every hot-path uniform of the reference, with vct_default_params giving the
+ * reference defaults of src/Application.h:36-103. */
+typedef struct vct_params {
+    /* voxelize.geom / voxelize.frag */
+    int32_t voxelize_lighting;   /* voxelizeLighting (default 1) */
+    int32_t axis_override;       /* axis_override (-1: dominant axis) */
+    /* transferVoxels.comp */
+    float voxel_set_opacity;     /* voxelSetOpacity (0.5) */
+    int32_t temporal_filter;     /* temporalFilterRadiance (0) */
+    float temporal_decay;        /* temporalDecay (0.8) */
+    /* injectRadiance.comp */
+    int32_t radiance_lighting;   /* radianceLighting (0) */
+    int32_t radiance_dilate;     /* radianceDilate (0) */
+    /* phong.frag */
+    vct_cone_settings diffuse_cone;  /* {16, 60 deg, 1.0, 1.0, 0.5} */
+    vct_cone_settings specular_cone; /* {32, 30 deg, 1.7, 0.5, 0.1} */
+    int32_t enable_indirect;     /* 1 */
+    int32_t enable_reflections;  /* 1 */
+    int32_t draw_occlusion;      /* 1 */
+    int32_t enable_postprocess;  /* 1 */
+    float ambient_scale;         /* 1.0 */
+    float reflect_scale;         /* 1.0 */
+    float max_distance;          /* cone length limit in texture units; <= 0: grid diagonal */
+    int32_t ref_tbn_quirk;       /* 1: map the cone set's y axis to the bitangent as phong.vert's TBN does */
+    int32_t trace_filter;        /* VCT_FILTER_* */
+} vct_params;
+
+/* Caller-owned triangle soup on the device. */
+typedef struct vct_triangles {
+    const float* positions_dev; /* count*9 floats: v0.xyz v1.xyz v2.xyz (world space) */
+    const float* normals_dev;   /* count*9 floats: per-vertex normals */
+    const float* albedo_dev;    /* count*3 floats: diffuse colour per triangle */
+    int64_t count;
+} vct_triangles;
+
+/* G-buffer: one float4 per pixel in each plane, row 0 at the bottom. */
+typedef struct vct_gbuffer {
+    const float* position_dev; /* world xyz, w = 1 covered / 0 background */
+    const float* normal_dev;   /* unit normal xyz */
+    const float* albedo_dev;   /* diffuse rgb */
+    int32_t width, height;
+} vct_gbuffer;
+
+/* Trace outputs, float4 per pixel; any pointer may be NULL. */
+typedef struct vct_trace_out {
+    float* irradiance_dev; /* sum of weighted diffuse cones: rgb, a = accumulated opacity */
+    float* specular_dev;   /* specular cone rgba */
+    float* color_dev;      /* composite (indirect*albedo [*occlusion], post-processed) */
+    unsigned long long* sample_count_dev; /* optional: += number of trilinear-mip samples */
+} vct_trace_out;
+
+/* Light-space inputs of one frame (the mainlight of src/Application.cpp:205-210). */
+typedef struct vct_shadow_desc {
+    const float* shadowmap_dev; /* width*height fp32 depths in [0,1], row 0 at the bottom */
+    int32_t width, height;
+    float ls[16];         /* light projection * view */
+    float ls_inverse[16]; /* inverse(ls), as the host computes it */
+    float light_pos[3];   /* injectRadiance 'lightPos' */
+    float light_int[3];   /* injectRadiance 'lightInt' */
+} vct_shadow_desc;
+
+/* VoxelizeInfo block (shaders/voxelize.frag:53-59). */
+typedef struct vct_stats {
+    uint32_t total_voxel_fragments;
+    uint32_t unique_voxels;
+    uint32_t max_fragments_per_voxel;
+    uint32_t error_flags; /* VCT_STATS_* */
+} vct_stats;
+
+#define VCT_STATS_COUNT_OVERFLOW 1u /* some voxel exceeded VCT_MAX_EXACT_FRAGMENTS */
+#define VCT_MAX_EXACT_FRAGMENTS 65537u
+
+/* Device time of the last vct_frame's stages, the reference's GLBufferedTimer
+ * regions (src/Application.h:192): voxelize = rasterise + accumulate,
+ * radiance = injection marking, mipmap = normalise + inject resolve + mip
+ * chain, render = cone tracing, total = all of them. */
+typedef struct vct_timers {
+    float voxelize_ms;
+    float radiance_ms;
+    float mipmap_ms;
+    float render_ms;
+    float total_ms;
+} vct_timers;
+
+#define VCT_VOLUME_COLOR 0
+#define VCT_VOLUME_NORMAL 1
+#define VCT_VOLUME_RADIANCE 2
+
+/* ---- library ---------------------------------------------------------- */
+int32_t vct_abi_version(void);
+const char* vct_status_string(vct_status s);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* vct_last_error(void);
+/* sizeof of the public structs, for FFI layout checks. */
+void vct_struct_sizes(int64_t* light, int64_t* config, int64_t* params,
+                      int64_t* triangles, int64_t* gbuffer, int64_t* trace_out,
+                      int64_t* shadow_desc, int64_t* stats);
+/* Reference defaults (src/Application.h:36-103). */
+void vct_default_params(vct_params* out);
+/* The three per-axis voxelisation matrices of src/Application.cpp:689-692. */
+vct_status vct_voxel_mvp(const vct_config* cfg, float mvp_xyz[48]);
+
+/* ---- context ---------------------------------------------------------- */
+vct_status vct_create(const vct_config* cfg, vct_ctx** out);
+vct_status vct_destroy(vct_ctx* ctx);
+vct_status vct_set_params(vct_ctx* ctx, const vct_params* params);
+vct_status vct_get_params(const vct_ctx* ctx, vct_params* out);
+vct_status vct_get_config(const vct_ctx* ctx, vct_config* out);
+/* Device pointer of one level of a volume (read-only view for callers). */
+vct_status vct_volume_level(const vct_ctx* ctx, int32_t volume, int32_t level,
+                            const uint16_t** data_dev, int32_t* dim);
+/* Device pointers of the integer accumulators: count[dim^3] and six sums
+ * (r,g,b,nx,ny,nz) of 16-bit fixed point, each dim^3 uint32. */
+vct_status vct_accumulators(const vct_ctx* ctx, const uint32_t** count_dev,
+                            const uint32_t** sums_dev);
+
+/* ---- stages ----------------------------------------------------------- */
+/* voxelize.geom/.frag: rasterise every triangle along its dominant axis and
+ * add colour, normal and count of each fragment into the accumulators. */
+vct_status vct_voxelize_accumulate(vct_ctx* ctx, const vct_triangles* tris,
+                                   const vct_light* lights, int32_t n_lights,
+                                   const vct_shadow_desc* shadow, const float eye[3],
+                                   void* stream);
+/* transferVoxels.comp: divide by count, set opacity, seed radiance level 0,
+ * update the VoxelizeInfo counters and zero the accumulators. */
+vct_status vct_normalize(vct_ctx* ctx, void* stream);
+/* Clear accumulators (only needed after an abandoned accumulate). */
+vct_status vct_clear_accumulators(vct_ctx* ctx, void* stream);
+/* vct_voxelize_accumulate + vct_normalize. */
+vct_status vct_voxelize(vct_ctx* ctx, const vct_triangles* tris, const vct_light* lights,
+                        int32_t n_lights, const vct_shadow_desc* shadow, const float eye[3],
+                        void* stream);
+/* injectRadiance.comp: one thread per shadow-map texel. */
+vct_status vct_inject(vct_ctx* ctx, const vct_shadow_desc* shadow, const float eye[3],
+                      void* stream);
+/* filterRadiance.comp over all levels of VCT_VOLUME_RADIANCE or VCT_VOLUME_COLOR. */
+vct_status vct_build_mips(vct_ctx* ctx, int32_t volume, void* stream);
+/* phong.frag indirect term: six diffuse cones + one specular cone per pixel. */
+vct_status vct_trace(vct_ctx* ctx, const vct_gbuffer* gbuffer, const float eye[3],
+                     const vct_trace_out* out, void* stream);
+/* All four stages; normalisation, injection and the first mip levels are
+ * fused.  Results equal vct_voxelize + vct_inject + vct_build_mips +
+ * vct_trace on the same inputs. */
+vct_status vct_frame(vct_ctx* ctx, const vct_triangles* tris, const vct_light* lights,
+                     int32_t n_lights, const vct_shadow_desc* shadow, const float eye[3],
+                     const vct_gbuffer* gbuffer, const vct_trace_out* out, void* stream);
+/* Synchronises `stream` and returns the VoxelizeInfo counters of the last
+ * vct_normalize / vct_frame. */
+vct_status vct_get_stats(vct_ctx* ctx, vct_stats* out, void* stream);
+
+/* Per-stage CUDA-event timers of vct_frame (off by default). */
+vct_status vct_enable_timers(vct_ctx* ctx, int32_t enable);
+/* Waits for the last timed vct_frame and returns its stage times. */
+vct_status vct_get_timers(vct_ctx* ctx, vct_timers* out);
+/* Number of kernels this library has launched since it was loaded. */
+uint64_t vct_launch_count(void);
+
+/* ---- frame set-up (not part of the timed path) ------------------------ */
+/* Depth-only render of the scene from the light (the reference's shadow
+ * pass, src/Application.cpp:213-233): fp32 depth in [0,1], cleared to 1. */
+vct_status vct_render_shadowmap(const vct_triangles* tris, const float ls[16],
+                                float* depth_dev, int32_t width, int32_t height,
+                                void* stream);
+/* Camera G-buffer (world position, normal, albedo) with a depth test.
+ * `keys_dev` is caller scratch of width*height uint64. */
+vct_status vct_render_gbuffer(const vct_triangles* tris, const float view_proj[16],
+                              const float eye[3], const float inv_view_proj[16],
+                              int32_t width, int32_t height, unsigned long long* keys_dev,
+                              float* position_dev, float* normal_dev, float* albedo_dev,
+                              void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VCT_H */

@@ -1,0 +1,254 @@
+"""numpy binding of the CPU oracle (liboracle.so, built from vct_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY.  The oracle is the correctness judge of the CUDA
+library and the timed CPU baseline.  Only tests/, the smoke check and the
+benchmark's CPU-baseline leg use it; the product never imports it.
+
+Parity status: unpinned by the reference.  The reference (sfreed141/vct)
+ships no tests, fixtures or golden outputs and its OpenGL/GLSL program
+cannot run here (no graphics stack), so the oracle is pinned instead by
+hand-computed known answers in tests/golden (see tests/golden/make_golden.py).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+_lib = None
+
+
+class orc_volume(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("vmin", C.c_float * 3), ("vmax", C.c_float * 3), ("vcenter", C.c_float * 3)]
+
+
+class orc_light(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("_p0", C.c_float), ("direction", C.c_float * 3), ("_p1", C.c_float),
+                ("color", C.c_float * 3), ("range", C.c_float), ("intensity", C.c_float), ("enabled", C.c_uint32),
+                ("selected", C.c_uint32), ("shadow_caster", C.c_uint32), ("type", C.c_uint32),
+                ("_p2", C.c_uint32 * 3)]
+
+
+class orc_cone(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("angle", C.c_float), ("bias", C.c_float), ("h0", C.c_float),
+                ("lod_offset", C.c_float)]
+
+
+class orc_trace_params(C.Structure):
+    _fields_ = [("diffuse", orc_cone), ("specular", orc_cone), ("enable_indirect", C.c_int32),
+                ("enable_reflections", C.c_int32), ("draw_occlusion", C.c_int32), ("enable_postprocess", C.c_int32),
+                ("ambient_scale", C.c_float), ("reflect_scale", C.c_float), ("max_distance", C.c_float),
+                ("ref_tbn_quirk", C.c_int32)]
+
+
+class orc_stats(C.Structure):
+    _fields_ = [("total_voxel_fragments", C.c_uint32), ("unique_voxels", C.c_uint32),
+                ("max_fragments_per_voxel", C.c_uint32), ("error_flags", C.c_uint32)]
+
+
+def build() -> str:
+    """Compile liboracle.so with the Makefile beside this file."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = C.CDLL(LIB_PATH)
+    return _lib
+
+
+def _p(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "arrays must be C-contiguous"
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _f(v, n):
+    return (C.c_float * n)(*np.asarray(v, dtype=np.float32).reshape(n).tolist())
+
+
+def volume(scene, dim: int | None = None) -> orc_volume:
+    v = orc_volume()
+    v.dim = int(dim or scene.dim)
+    v.vmin = _f([-scene.vmax] * 3, 3)
+    v.vmax = _f([scene.vmax] * 3, 3)
+    v.vcenter = _f([0, 0, 0], 3)
+    return v
+
+
+def lights(scene):
+    arr = (orc_light * max(1, len(scene.lights)))()
+    for i, d in enumerate(scene.lights):
+        li = arr[i]
+        li.position = _f(d["position"], 3)
+        li.direction = _f(d["direction"], 3)
+        li.color = _f(d["color"], 3)
+        li.range = float(d["range"])
+        li.intensity = float(d["intensity"])
+        li.enabled = int(d.get("enabled", 1))
+        li.shadow_caster = int(d.get("shadow_caster", 0))
+        li.type = int(d["type"])
+    return arr, len(scene.lights)
+
+
+def trace_params(scene, **over) -> orc_trace_params:
+    t = orc_trace_params()
+    for key in ("diffuse", "specular"):
+        steps, ang, bias, h0, lod = scene.cone[key]
+        setattr(t, key, orc_cone(int(steps), float(ang), float(bias), float(h0), float(lod)))
+    t.enable_indirect = 1
+    t.enable_reflections = 1
+    t.draw_occlusion = 1
+    t.enable_postprocess = 1
+    t.ambient_scale = 1.0
+    t.reflect_scale = 1.0
+    t.max_distance = float(np.sqrt(3.0))
+    t.ref_tbn_quirk = 0
+    for k, v in over.items():
+        setattr(t, k, v)
+    return t
+
+
+def f32_to_f16(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty(x.shape, dtype=np.uint16)
+    load().orc_f32_to_f16_array(_p(x), _p(out), C.c_int64(x.size))
+    return out
+
+
+def voxel_mvp(scene) -> np.ndarray:
+    out = np.zeros(48, dtype=np.float32)
+    v = volume(scene)
+    load().orc_voxel_mvp(C.byref(v), _p(out))
+    return out
+
+
+def voxelize(scene, shadowmap: np.ndarray, lighting: int = 1, axis_override: int = -1, nthreads: int = 1,
+             positions=None, normals=None, albedo=None, dim: int | None = None):
+    """Returns (count[N^3] u32, sums[6*N^3] u32, total_fragments)."""
+    N = int(dim or scene.dim)
+    pos = np.ascontiguousarray(scene.positions if positions is None else positions, dtype=np.float32)
+    nrm = np.ascontiguousarray(scene.normals if normals is None else normals, dtype=np.float32)
+    alb = np.ascontiguousarray(scene.albedo if albedo is None else albedo, dtype=np.float32)
+    count = np.zeros(N ** 3, dtype=np.uint32)
+    sums = np.zeros(6 * N ** 3, dtype=np.uint32)
+    total = C.c_uint32(0)
+    arr, n = lights(scene)
+    v = volume(scene, N)
+    sm = np.ascontiguousarray(shadowmap, dtype=np.float32)
+    sw, sh = scene.shadow_size
+    load().orc_voxelize(C.byref(v), _p(pos), _p(nrm), _p(alb), C.c_int64(pos.shape[0]), arr, n, lighting,
+                        axis_override, _p(sm), sw, sh, _f(scene.ls, 16), _p(count), _p(sums), C.byref(total),
+                        nthreads)
+    return count, sums, int(total.value)
+
+
+def normalize(scene, count, sums, opacity=0.5, temporal=0, decay=0.8, radiance=None, nthreads=1, dim=None,
+              chain_voxels=None):
+    """Returns (color, normal, radiance, stats); radiance is level 0 (or the
+    given array, updated in place, when the temporal filter reads it)."""
+    N = int(dim or scene.dim)
+    nv = N ** 3
+    color = np.zeros(4 * nv, dtype=np.uint16)
+    normal = np.zeros(4 * nv, dtype=np.uint16)
+    rad = radiance if radiance is not None else np.zeros(4 * (chain_voxels or nv), dtype=np.uint16)
+    st = orc_stats()
+    v = volume(scene, N)
+    load().orc_normalize(C.byref(v), C.c_float(opacity), temporal, C.c_float(decay), _p(count), _p(sums),
+                         _p(color), _p(normal), _p(rad), C.byref(st), nthreads)
+    stats = dict(unique_voxels=st.unique_voxels, max_fragments_per_voxel=st.max_fragments_per_voxel,
+                 error_flags=st.error_flags)
+    return color, normal, rad, stats
+
+
+def inject(scene, shadowmap, color, normal, radiance, lighting=0, dilate=0, nthreads=1, dim=None):
+    N = int(dim or scene.dim)
+    v = volume(scene, N)
+    sw, sh = scene.shadow_size
+    sm = np.ascontiguousarray(shadowmap, dtype=np.float32)
+    load().orc_inject(C.byref(v), _p(sm), sw, sh, _f(scene.ls_inverse, 16), _f(scene.light_pos, 3),
+                      _f(scene.light_int, 3), lighting, dilate, _p(color), _p(normal), _p(radiance), nthreads)
+    return radiance
+
+
+def chain_voxels(dim: int, levels: int) -> int:
+    return sum((dim >> l) ** 3 for l in range(levels))
+
+
+def level_offsets(dim: int, levels: int) -> list[int]:
+    offs, o = [], 0
+    for l in range(levels):
+        offs.append(o)
+        o += (dim >> l) ** 3
+    return offs
+
+
+def build_mips(dim: int, levels: int, chain: np.ndarray, nthreads: int = 1) -> np.ndarray:
+    load().orc_build_mips(dim, levels, _p(chain), nthreads)
+    return chain
+
+
+def trace(scene, chain, gpos, gnrm, galb, precision=32, rows=None, row_step=1, nthreads=1, want=("irr", "spec",
+                                                                                                  "color"), **over):
+    W, H = scene.gbuffer_size
+    r0, r1 = rows if rows is not None else (0, H)
+    tp = trace_params(scene, **over)
+    v = volume(scene)
+    irr = np.zeros((H * W * 4,), dtype=np.float32) if "irr" in want else None
+    spec = np.zeros((H * W * 4,), dtype=np.float32) if "spec" in want else None
+    col = np.zeros((H * W * 4,), dtype=np.float32) if "color" in want else None
+    samples = C.c_uint64(0)
+    load().orc_trace(C.byref(v), scene.levels, _p(chain), C.byref(tp), _p(gpos), _p(gnrm), _p(galb), W, H, r0, r1,
+                     row_step, _f(scene.eye, 3), precision, _p(irr), _p(spec), _p(col), C.byref(samples), nthreads)
+    return irr, spec, col, int(samples.value)
+
+
+def render_shadowmap(scene, nthreads=1) -> np.ndarray:
+    W, H = scene.shadow_size
+    out = np.empty(W * H, dtype=np.float32)
+    load().orc_render_shadowmap(_p(scene.positions), C.c_int64(scene.ntri), _f(scene.ls, 16), W, H, _p(out), nthreads)
+    return out
+
+
+def render_gbuffer(scene):
+    W, H = scene.gbuffer_size
+    gp = np.zeros(W * H * 4, dtype=np.float32)
+    gn = np.zeros(W * H * 4, dtype=np.float32)
+    ga = np.zeros(W * H * 4, dtype=np.float32)
+    load().orc_render_gbuffer(_p(scene.positions), _p(scene.normals), _p(scene.albedo), C.c_int64(scene.ntri),
+                              _f(scene.view_proj, 16), _f(scene.eye, 3), _f(scene.inv_view_proj, 16), W, H, _p(gp),
+                              _p(gn), _p(ga))
+    return gp, gn, ga
+
+
+def f16_to_f32(h: np.ndarray) -> np.ndarray:
+    return np.asarray(h, dtype=np.uint16).view(np.float16).astype(np.float32)
+
+
+def frame(scene, nthreads=1, precision=32, rows=None, row_step=1, shadowmap=None, gbuf=None, **trace_over):
+    """The whole reference pipeline on the CPU (voxelize, normalise, inject,
+    mips, trace).  Returns a dict of every intermediate."""
+    sm = render_shadowmap(scene, nthreads) if shadowmap is None else shadowmap
+    count, sums, total = voxelize(scene, sm, nthreads=nthreads)
+    nv = scene.dim ** 3
+    chain = np.zeros(4 * chain_voxels(scene.dim, scene.levels), dtype=np.uint16)
+    color, normal, _, stats = normalize(scene, count, sums, radiance=chain, nthreads=nthreads)
+    inject(scene, sm, color, normal, chain, nthreads=nthreads)
+    build_mips(scene.dim, scene.levels, chain, nthreads)
+    gp, gn, ga = render_gbuffer(scene) if gbuf is None else gbuf
+    irr, spec, col, ns = trace(scene, chain, gp, gn, ga, precision=precision, rows=rows, row_step=row_step,
+                               nthreads=nthreads, **trace_over)
+    stats["total_voxel_fragments"] = total
+    return dict(shadowmap=sm, count=count, sums=sums, color=color, normal=normal, chain=chain, gpos=gp, gnrm=gn,
+                galb=ga, irradiance=irr, specular=spec, out=col, samples=ns, stats=stats, nv=nv)

@@ -1,0 +1,1011 @@
+// CPU oracle of the VCT hot path (test infrastructure only; see vct_oracle.h).
+//
+// Compiled with -ffp-contract=off so that every a*b+c below is two rounded
+// operations, on x86 and on Arm alike.  The order of every fp32 operation in
+// the bit-exact stages (rasterisation, voxelisation, normalisation,
+// injection, mips) is part of the contract the CUDA kernels follow.
+#include "vct_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- helpers
+struct f3 {
+    float x, y, z;
+};
+static inline f3 mk(float x, float y, float z) { return {x, y, z}; }
+static inline f3 add(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+static inline f3 sub(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+static inline f3 mul(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+static inline f3 mulv(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+static inline float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline f3 cross(f3 a, f3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+// normalize(v) = v * (1 / sqrt(dot(v, v))): two IEEE-rounded operations.
+static inline f3 normalize(f3 v) {
+    float inv = 1.0f / std::sqrt(dot(v, v));
+    return mul(v, inv);
+}
+static inline float length(f3 v) { return std::sqrt(dot(v, v)); }
+static inline f3 ld3(const float* p) { return {p[0], p[1], p[2]}; }
+
+// glm-style mat4 (column-major) times vec4, summed over columns in order.
+static inline void mat_vec(const float* m, float x, float y, float z, float w, float out[4]) {
+    for (int r = 0; r < 4; ++r) out[r] = m[0 + r] * x + m[4 + r] * y + m[8 + r] * z + m[12 + r] * w;
+}
+
+static inline float clampf(float x, float lo, float hi) { return std::fmin(std::fmax(x, lo), hi); }
+
+// GLSL smoothstep.
+static inline float smoothstep(float e0, float e1, float x) {
+    float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+
+template <typename F>
+static void parallel_for(int64_t n, int nthreads, F&& fn) {
+    if (nthreads <= 1 || n < 2) {
+        fn(0, n);
+        return;
+    }
+    int nt = (int)std::min<int64_t>(nthreads, n);
+    std::vector<std::thread> th;
+    th.reserve(nt);
+    for (int t = 0; t < nt; ++t) {
+        int64_t a = n * t / nt, b = n * (t + 1) / nt;
+        th.emplace_back([&fn, a, b] { fn(a, b); });
+    }
+    for (auto& t : th) t.join();
+}
+
+// ------------------------------------------------------------ binary16
+uint16_t f2h(float f) {
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    uint32_t sign = (x >> 16) & 0x8000u;
+    uint32_t exp = (x >> 23) & 0xffu;
+    uint32_t man = x & 0x7fffffu;
+    if (exp == 0xffu) return (uint16_t)(man ? 0x7fffu : (sign | 0x7c00u));
+    int e = (int)exp - 127 + 15;
+    if (e >= 31) return (uint16_t)(sign | 0x7c00u);
+    if (e <= 0) {
+        if (e < -10) return (uint16_t)sign;
+        uint32_t full = man | 0x800000u;
+        int shift = 14 - e;
+        uint32_t hm = full >> shift;
+        uint32_t rem = full & ((1u << shift) - 1u);
+        uint32_t half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (hm & 1u))) hm++;
+        return (uint16_t)(sign | hm);
+    }
+    uint32_t h = sign | ((uint32_t)e << 10) | (man >> 13);
+    uint32_t rem = man & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+    return (uint16_t)h;
+}
+
+float h2f(uint16_t h) {
+    uint32_t sign = ((uint32_t)h & 0x8000u) << 16;
+    uint32_t exp = (h >> 10) & 0x1fu;
+    uint32_t man = h & 0x3ffu;
+    uint32_t x;
+    if (exp == 0) {
+        if (man == 0) {
+            x = sign;
+        } else {  // subnormal: renormalise
+            int e = -1;
+            do {
+                man <<= 1;
+                ++e;
+            } while (!(man & 0x400u));
+            man &= 0x3ffu;
+            x = sign | ((uint32_t)(127 - 15 - e) << 23) | (man << 13);
+        }
+    } else if (exp == 31) {
+        x = sign | 0x7f800000u | (man << 13);
+    } else {
+        x = sign | ((exp - 15 + 127) << 23) | (man << 13);
+    }
+    float f;
+    std::memcpy(&f, &x, 4);
+    return f;
+}
+
+// ---------------------------------------------------------- matrices (glm)
+void lookat(const float e[3], const float c[3], const float u[3], float* m) {
+    f3 eye = ld3(e), ctr = ld3(c), up = ld3(u);
+    f3 f = normalize(sub(ctr, eye));
+    f3 s = normalize(cross(f, up));
+    f3 uu = cross(s, f);
+    for (int i = 0; i < 16; ++i) m[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+    m[0] = s.x;
+    m[4] = s.y;
+    m[8] = s.z;
+    m[1] = uu.x;
+    m[5] = uu.y;
+    m[9] = uu.z;
+    m[2] = -f.x;
+    m[6] = -f.y;
+    m[10] = -f.z;
+    m[12] = -dot(s, eye);
+    m[13] = -dot(uu, eye);
+    m[14] = dot(f, eye);
+}
+
+void ortho(float l, float r, float b, float t, float n, float f, float* m) {
+    for (int i = 0; i < 16; ++i) m[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+    m[0] = 2.0f / (r - l);
+    m[5] = 2.0f / (t - b);
+    m[10] = -2.0f / (f - n);
+    m[12] = -(r + l) / (r - l);
+    m[13] = -(t + b) / (t - b);
+    m[14] = -(f + n) / (f - n);
+}
+
+void matmul(const float* a, const float* b, float* out) {
+    float r[16];
+    for (int c = 0; c < 4; ++c)
+        for (int row = 0; row < 4; ++row)
+            r[c * 4 + row] = a[0 * 4 + row] * b[c * 4 + 0] + a[1 * 4 + row] * b[c * 4 + 1] +
+                             a[2 * 4 + row] * b[c * 4 + 2] + a[3 * 4 + row] * b[c * 4 + 3];
+    std::memcpy(out, r, sizeof r);
+}
+
+// src/Application.cpp:689-692.
+void voxel_mvp(const orc_volume* v, float* out) {
+    float proj[16], view[16];
+    ortho(v->vmin[0], v->vmax[0], v->vmin[1], v->vmax[1], 0.0f, v->vmax[2] - v->vmin[2], proj);
+    const float* c = v->vcenter;
+    float ex[3] = {v->vmax[0] + c[0], 0.0f + c[1], 0.0f + c[2]};
+    float ey[3] = {0.0f + c[0], v->vmax[1] + c[1], 0.0f + c[2]};
+    float ez[3] = {0.0f + c[0], 0.0f + c[1], v->vmax[2] + c[2]};
+    float upy[3] = {0, 1, 0}, upz[3] = {0, 0, -1};
+    lookat(ex, c, upy, view);
+    matmul(proj, view, out + 0);
+    lookat(ey, c, upz, view);
+    matmul(proj, view, out + 16);
+    lookat(ez, c, upy, view);
+    matmul(proj, view, out + 32);
+}
+
+// ------------------------------------------------------ rasterisation core
+// Pixel-centre coverage on a 1/256 sub-pixel grid with a top-left tie rule.
+// Window coordinates have the origin at the bottom-left (GL).
+constexpr int64_t kSub = 256;
+
+static inline int64_t snap(float w) {
+    w = clampf(w, -1048576.0f, 1048576.0f);
+    return (int64_t)std::rint(w * 256.0f);
+}
+
+static inline int64_t floordiv(int64_t a, int64_t b) {
+    int64_t q = a / b;
+    if ((a % b != 0) && ((a < 0) != (b < 0))) --q;
+    return q;
+}
+
+struct RasterTri {
+    int64_t X[3], Y[3];
+    int64_t area;
+    int64_t bias[3];  // 0 for top-left edges, -1 otherwise (edge k is opposite vertex k)
+    int px0, px1, py0, py1;
+    int perm[3];      // vertex order after orientation fix
+};
+
+// Edge function of edge a->b at p: > 0 on the interior side of a CCW triangle.
+static inline int64_t edge(int64_t ax, int64_t ay, int64_t bx, int64_t by, int64_t px, int64_t py) {
+    return (bx - ax) * (py - ay) - (by - ay) * (px - ax);
+}
+
+static bool raster_setup(const float wx[3], const float wy[3], int W, int H, RasterTri& t) {
+    int64_t X[3], Y[3];
+    for (int k = 0; k < 3; ++k) {
+        X[k] = snap(wx[k]);
+        Y[k] = snap(wy[k]);
+    }
+    int64_t area = edge(X[0], Y[0], X[1], Y[1], X[2], Y[2]);
+    if (area == 0) return false;
+    int p[3] = {0, 1, 2};
+    if (area < 0) {
+        p[1] = 2;
+        p[2] = 1;
+        area = -area;
+    }
+    for (int k = 0; k < 3; ++k) {
+        t.X[k] = X[p[k]];
+        t.Y[k] = Y[p[k]];
+        t.perm[k] = p[k];
+    }
+    t.area = area;
+    for (int k = 0; k < 3; ++k) {
+        int a = (k + 1) % 3, b = (k + 2) % 3;
+        int64_t dx = t.X[b] - t.X[a], dy = t.Y[b] - t.Y[a];
+        bool tl = (dy < 0) || (dy == 0 && dx < 0);
+        t.bias[k] = tl ? 0 : -1;
+    }
+    int64_t minx = std::min({t.X[0], t.X[1], t.X[2]}), maxx = std::max({t.X[0], t.X[1], t.X[2]});
+    int64_t miny = std::min({t.Y[0], t.Y[1], t.Y[2]}), maxy = std::max({t.Y[0], t.Y[1], t.Y[2]});
+    int64_t x0 = -floordiv(-(minx - kSub / 2), kSub);  // ceil
+    int64_t x1 = floordiv(maxx - kSub / 2, kSub);
+    int64_t y0 = -floordiv(-(miny - kSub / 2), kSub);
+    int64_t y1 = floordiv(maxy - kSub / 2, kSub);
+    x0 = std::max<int64_t>(x0, 0);
+    y0 = std::max<int64_t>(y0, 0);
+    x1 = std::min<int64_t>(x1, W - 1);
+    y1 = std::min<int64_t>(y1, H - 1);
+    if (x0 > x1 || y0 > y1) return false;
+    t.px0 = (int)x0;
+    t.px1 = (int)x1;
+    t.py0 = (int)y0;
+    t.py1 = (int)y1;
+    return true;
+}
+
+// Barycentric edge values at pixel (px,py); returns false when not covered.
+static inline bool raster_cover(const RasterTri& t, int px, int py, int64_t e[3]) {
+    int64_t sx = (int64_t)px * kSub + kSub / 2, sy = (int64_t)py * kSub + kSub / 2;
+    for (int k = 0; k < 3; ++k) {
+        int a = (k + 1) % 3, b = (k + 2) % 3;
+        e[k] = edge(t.X[a], t.Y[a], t.X[b], t.Y[b], sx, sy);
+        if (e[k] + t.bias[k] < 0) return false;
+    }
+    return true;
+}
+
+// Interpolation weights l_k = e_k * (1 / area), in the original vertex order.
+static inline void raster_weights(const RasterTri& t, const int64_t e[3], float l[3]) {
+    float inv = 1.0f / (float)t.area;
+    float lp[3];
+    for (int k = 0; k < 3; ++k) lp[k] = (float)e[k] * inv;
+    for (int k = 0; k < 3; ++k) l[t.perm[k]] = lp[k];
+}
+
+static inline float interp(const float l[3], float a, float b, float c) { return l[0] * a + l[1] * b + l[2] * c; }
+
+// ------------------------------------------------ bilinear shadow-map fetch
+// texture(shadowmap, uv) with GL_LINEAR, clamp-to-border 1.0 and a texel
+// offset as textureOffset adds it (src/Application.cpp:45-53).
+static inline float shadow_fetch(const float* sm, int W, int H, int i, int j) {
+    if (i < 0 || j < 0 || i >= W || j >= H) return 1.0f;
+    return sm[(int64_t)j * W + i];
+}
+static inline float shadow_bilinear(const float* sm, int W, int H, float u, float v, int ox, int oy) {
+    float x = (u * (float)W + (float)ox) - 0.5f;
+    float y = (v * (float)H + (float)oy) - 0.5f;
+    float fx = std::floor(x), fy = std::floor(y);
+    float a = x - fx, b = y - fy;
+    int i = (int)fx, j = (int)fy;
+    float t00 = shadow_fetch(sm, W, H, i, j), t10 = shadow_fetch(sm, W, H, i + 1, j);
+    float t01 = shadow_fetch(sm, W, H, i, j + 1), t11 = shadow_fetch(sm, W, H, i + 1, j + 1);
+    float bot = t00 * (1.0f - a) + t10 * a;
+    float top = t01 * (1.0f - a) + t11 * a;
+    return bot * (1.0f - b) + top * b;
+}
+
+// shaders/voxelize.frag:160-184 (identical to phong.frag:183-207).
+static float shadow_factor(const float* sm, int W, int H, const float ls[16], f3 wp) {
+    float c[4];
+    mat_vec(ls, wp.x, wp.y, wp.z, 1.0f, c);
+    float sx = (c[0] / c[3] + 1.0f) * 0.5f;
+    float sy = (c[1] / c[3] + 1.0f) * 0.5f;
+    float sz = (c[2] / c[3] + 1.0f) * 0.5f;
+    float frag = sz - 0.01f;
+    if (frag > 1.0f) return 0.0f;
+    static const int off[5][2] = {{0, 0}, {1, 0}, {0, 1}, {-1, 0}, {0, -1}};
+    float f = 0.0f;
+    for (int s = 0; s < 5; ++s)
+        if (frag > shadow_bilinear(sm, W, H, sx, sy, off[s][0], off[s][1])) f += 1.0f;
+    return f / 5.0f;
+}
+
+static inline uint32_t quant16(float x) { return (uint32_t)std::rint(clampf(x, 0.0f, 1.0f) * 65535.0f); }
+
+}  // namespace
+
+// ================================================================ C API
+extern "C" {
+
+uint16_t orc_f32_to_f16(float f) { return f2h(f); }
+float orc_f16_to_f32(uint16_t h) { return h2f(h); }
+void orc_f32_to_f16_array(const float* in, uint16_t* out, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) out[i] = f2h(in[i]);
+}
+void orc_voxel_mvp(const orc_volume* vol, float out[48]) { voxel_mvp(vol, out); }
+void orc_lookat(const float eye[3], const float center[3], const float up[3], float out[16]) {
+    lookat(eye, center, up, out);
+}
+void orc_ortho(float l, float r, float b, float t, float n, float f, float out[16]) { ortho(l, r, b, t, n, f, out); }
+void orc_perspective(float fovy, float aspect, float zn, float zf, float* m) {
+    float th = std::tan(fovy / 2.0f);
+    for (int i = 0; i < 16; ++i) m[i] = 0.0f;
+    m[0] = 1.0f / (aspect * th);
+    m[5] = 1.0f / th;
+    m[10] = -(zf + zn) / (zf - zn);
+    m[11] = -1.0f;
+    m[14] = -(2.0f * zf * zn) / (zf - zn);
+}
+void orc_mat4_mul(const float a[16], const float b[16], float out[16]) { matmul(a, b, out); }
+
+// --------------------------------------------------------------- voxelize
+// voxelize.geom picks the axis; GL rasterises at pixel centres in a dim x dim
+// viewport; voxelize.frag lights the fragment and accumulates it.
+void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, const float* albedo,
+                  int64_t ntri, const orc_light* lights, int32_t nlights, int32_t lighting,
+                  int32_t axis_override, const float* sm, int32_t sw, int32_t sh, const float ls[16],
+                  uint32_t* count, uint32_t* sums, uint32_t* total_fragments, int32_t nthreads) {
+    const int N = vol->dim;
+    const int64_t NV = (int64_t)N * N * N;
+    float mvp[48];
+    voxel_mvp(vol, mvp);
+    std::atomic<uint64_t> total{0};
+    const bool atomic = nthreads > 1;
+    auto addu = [atomic](uint32_t* p, uint32_t v) {
+        if (atomic)
+            __atomic_fetch_add(p, v, __ATOMIC_RELAXED);
+        else
+            *p += v;
+    };
+    parallel_for(ntri, nthreads, [&](int64_t t0, int64_t t1) {
+        uint64_t local_total = 0;
+        for (int64_t t = t0; t < t1; ++t) {
+            const float* P = pos + t * 9;
+            const float* Nn = nrm + t * 9;
+            f3 p[3] = {ld3(P), ld3(P + 3), ld3(P + 6)};
+            f3 n[3] = {ld3(Nn), ld3(Nn + 3), ld3(Nn + 6)};
+            // voxelize.geom:28-45 (strict >, ties fall to z).
+            f3 fn = normalize(add(add(n[0], n[1]), n[2]));
+            float ax = std::fabs(fn.x), ay = std::fabs(fn.y), az = std::fabs(fn.z);
+            int axis = 2;
+            if (ax > ay && ax > az)
+                axis = 0;
+            else if (ay > ax && ay > az)
+                axis = 1;
+            if (axis_override >= 0 && axis_override <= 2) axis = axis_override;
+            const float* M = mvp + 16 * axis;
+            float wx[3], wy[3], z[3];
+            for (int k = 0; k < 3; ++k) {
+                float c[4];
+                mat_vec(M, p[k].x, p[k].y, p[k].z, 1.0f, c);
+                float nx = c[0] / c[3], ny = c[1] / c[3];
+                z[k] = c[2] / c[3];
+                wx[k] = (nx + 1.0f) * 0.5f * (float)N;
+                wy[k] = (ny + 1.0f) * 0.5f * (float)N;
+            }
+            RasterTri rt;
+            if (!raster_setup(wx, wy, N, N, rt)) continue;
+            f3 col0 = ld3(albedo + t * 3);
+            for (int py = rt.py0; py <= rt.py1; ++py) {
+                for (int px = rt.px0; px <= rt.px1; ++px) {
+                    int64_t e[3];
+                    if (!raster_cover(rt, px, py, e)) continue;
+                    float l[3];
+                    raster_weights(rt, e, l);
+                    float zf = interp(l, z[0], z[1], z[2]);
+                    if (!(zf >= -1.0f && zf <= 1.0f)) continue;  // clipped by GL
+                    ++local_total;
+                    f3 wp = mk(interp(l, p[0].x, p[1].x, p[2].x), interp(l, p[0].y, p[1].y, p[2].y),
+                               interp(l, p[0].z, p[1].z, p[2].z));
+                    f3 ni = mk(interp(l, n[0].x, n[1].x, n[2].x), interp(l, n[0].y, n[1].y, n[2].y),
+                               interp(l, n[0].z, n[1].z, n[2].z));
+                    f3 Nf = normalize(ni);
+                    f3 color = col0;
+                    if (lighting) {  // voxelize.frag:200-225
+                        f3 fin = mk(0, 0, 0);
+                        for (int li = 0; li < nlights; ++li) {
+                            const orc_light& L = lights[li];
+                            if (!L.enabled) continue;
+                            f3 lc = ld3(L.color);
+                            f3 lit = mk(0, 0, 0);
+                            if (L.type == 0u) {
+                                f3 lp = ld3(L.position);
+                                f3 d = sub(lp, wp);
+                                float ndl = std::fmax(0.0f, dot(Nf, normalize(d)));
+                                lit = mul(mulv(mul(color, L.intensity), lc), ndl);
+                                float att = 1.0f - smoothstep(0.75f * L.range, L.range, length(d));
+                                lit = mul(lit, att);
+                            } else if (L.type == 1u) {
+                                f3 dir = ld3(L.direction);
+                                float ndl = std::fmax(0.0f, dot(Nf, normalize(mk(-dir.x, -dir.y, -dir.z))));
+                                lit = mul(mul(mulv(color, lc), L.intensity), ndl);
+                            }
+                            if (L.shadow_caster) {
+                                float s = 1.0f - shadow_factor(sm, sw, sh, ls, wp);
+                                lit = mul(lit, s);
+                            }
+                            fin = add(fin, lit);
+                        }
+                        color = mk(clampf(fin.x, 0.0f, 1.0f), clampf(fin.y, 0.0f, 1.0f), clampf(fin.z, 0.0f, 1.0f));
+                    }
+                    f3 n01 = mk((Nf.x + 1.0f) * 0.5f, (Nf.y + 1.0f) * 0.5f, (Nf.z + 1.0f) * 0.5f);
+                    // voxelize.frag:79-108 with the swizzle resolved per axis.
+                    float uz = (zf + 1.0f) * 0.5f;
+                    float dz = (float)N * (1.0f - uz);
+                    int iz = (int)dz;
+                    int vx, vy, vz;
+                    if (axis == 0) {
+                        vx = iz;
+                        vy = py;
+                        vz = N - 1 - px;
+                    } else if (axis == 1) {
+                        vx = px;
+                        vy = iz;
+                        vz = N - 1 - py;
+                    } else {
+                        vx = px;
+                        vy = py;
+                        vz = iz;
+                    }
+                    if (vx < 0 || vy < 0 || vz < 0 || vx >= N || vy >= N || vz >= N) continue;
+                    int64_t v = ((int64_t)vz * N + vy) * N + vx;
+                    addu(count + v, 1u);
+                    addu(sums + 0 * NV + v, quant16(color.x));
+                    addu(sums + 1 * NV + v, quant16(color.y));
+                    addu(sums + 2 * NV + v, quant16(color.z));
+                    addu(sums + 3 * NV + v, quant16(n01.x));
+                    addu(sums + 4 * NV + v, quant16(n01.y));
+                    addu(sums + 5 * NV + v, quant16(n01.z));
+                }
+            }
+        }
+        total.fetch_add(local_total);
+    });
+    if (total_fragments) *total_fragments += (uint32_t)total.load();
+}
+
+// --------------------------------------------------------------- normalize
+void orc_normalize(const orc_volume* vol, float opacity, int32_t temporal, float decay,
+                   const uint32_t* count, const uint32_t* sums, uint16_t* color, uint16_t* normal,
+                   uint16_t* radiance, orc_stats* stats, int32_t nthreads) {
+    const int64_t NV = (int64_t)vol->dim * vol->dim * vol->dim;
+    std::atomic<uint32_t> uniq{0}, mx{0}, flags{0};
+    parallel_for(NV, nthreads, [&](int64_t a, int64_t b) {
+        uint32_t lu = 0, lm = 0, lf = 0;
+        for (int64_t v = a; v < b; ++v) {
+            uint32_t c = count[v];
+            float alpha = 0.0f;
+            uint16_t* C = color + 4 * v;
+            uint16_t* Nn = normal + 4 * v;
+            if (c > 0) {
+                ++lu;
+                lm = std::max(lm, c);
+                if (c >= 65537u) lf |= 1u;
+                float denom = 65535.0f * (float)c;
+                alpha = opacity > 0.0f ? opacity : 1.0f;
+                for (int k = 0; k < 3; ++k) C[k] = f2h((float)sums[k * NV + v] / denom);
+                C[3] = f2h(alpha);
+                for (int k = 0; k < 3; ++k) Nn[k] = f2h((float)sums[(3 + k) * NV + v] / denom);
+                Nn[3] = f2h(1.0f);
+            } else {
+                for (int k = 0; k < 4; ++k) C[k] = Nn[k] = 0;
+            }
+            uint16_t* R = radiance + 4 * v;
+            if (temporal) {
+                // transferVoxels.comp:55-62: mix(previous, (0,0,0,a), 1 - decay)
+                float w = 1.0f - decay;
+                float nv[4] = {0.0f, 0.0f, 0.0f, alpha};
+                for (int k = 0; k < 4; ++k) {
+                    float prev = h2f(R[k]);
+                    R[k] = f2h(prev * (1.0f - w) + nv[k] * w);
+                }
+            } else {
+                R[0] = R[1] = R[2] = 0;
+                R[3] = c > 0 ? f2h(alpha) : (uint16_t)0;
+            }
+        }
+        uniq.fetch_add(lu);
+        uint32_t cur = mx.load();
+        while (lm > cur && !mx.compare_exchange_weak(cur, lm)) {
+        }
+        flags.fetch_or(lf);
+    });
+    if (stats) {
+        stats->unique_voxels += uniq.load();
+        stats->max_fragments_per_voxel = std::max(stats->max_fragments_per_voxel, mx.load());
+        stats->error_flags |= flags.load();
+    }
+}
+
+// ------------------------------------------------------------------ inject
+// injectRadiance.comp:40-103.  Stores are idempotent per voxel, so threads
+// are split by shadow-map rows and the (equal) racing stores are harmless;
+// each thread writes through relaxed atomics to stay well defined.
+void orc_inject(const orc_volume* vol, const float* sm, int32_t sw, int32_t sh, const float li[16],
+                const float lpos[3], const float lint[3], int32_t lighting, int32_t dilate,
+                const uint16_t* color, const uint16_t* normal, uint16_t* radiance, int32_t nthreads) {
+    const int N = vol->dim;
+    // The dispatch covers ceil(size/16)*16 threads and the bounds test is
+    // `>`: thread index == size also runs when size is not a multiple of 16.
+    const int nx = std::min(((sw + 15) / 16) * 16, sw + 1);
+    const int ny = std::min(((sh + 15) / 16) * 16, sh + 1);
+    f3 vmin = ld3(vol->vmin), vmax = ld3(vol->vmax), vc = ld3(vol->vcenter);
+    f3 ext = sub(vmax, vmin);
+    auto vindex = [&](f3 w) {
+        f3 tc = mk(((w.x - vc.x) - vmin.x) / ext.x, ((w.y - vc.y) - vmin.y) / ext.y, ((w.z - vc.z) - vmin.z) / ext.z);
+        return mul(tc, (float)N);
+    };
+    f3 lvox = vindex(ld3(lpos));
+    auto store = [&](int x, int y, int z, const uint16_t v[4]) {
+        if (x < 0 || y < 0 || z < 0 || x >= N || y >= N || z >= N) return;
+        uint64_t w;
+        std::memcpy(&w, v, 8);
+        uint64_t* dst = (uint64_t*)(radiance + 4 * (((int64_t)z * N + y) * N + x));
+        __atomic_store_n(dst, w, __ATOMIC_RELAXED);
+    };
+    auto load_c = [&](int x, int y, int z, uint16_t out[4]) {
+        if (x < 0 || y < 0 || z < 0 || x >= N || y >= N || z >= N) {
+            out[0] = out[1] = out[2] = out[3] = 0;
+            return;
+        }
+        std::memcpy(out, color + 4 * (((int64_t)z * N + y) * N + x), 8);
+    };
+    parallel_for(ny, nthreads, [&](int64_t y0, int64_t y1) {
+        for (int y = (int)y0; y < (int)y1; ++y) {
+            for (int x = 0; x < nx; ++x) {
+                float u = (float)x / (float)sw, v = (float)y / (float)sh;
+                float depth = shadow_bilinear(sm, sw, sh, u, v, 0, 0);
+                float ndx = u * 2.0f - 1.0f, ndy = v * 2.0f - 1.0f, ndz = depth * 2.0f - 1.0f;
+                float w4[4];
+                mat_vec(li, ndx, ndy, ndz, 1.0f, w4);
+                f3 vi = vindex(mk(w4[0], w4[1], w4[2]));
+                int ix = (int)vi.x, iy = (int)vi.y, iz = (int)vi.z;
+                if (ix >= N || iy >= N || iz >= N || ix < 0 || iy < 0 || iz < 0) continue;
+                if (dilate) {
+                    static const int off[7][3] = {{0, 0, 0}, {0, 0, 1}, {-1, 0, 0}, {0, 1, 0},
+                                                  {0, -1, 0}, {1, 0, 0}, {-1, 0, 0}};
+                    for (int k = 0; k < 7; ++k) {
+                        uint16_t c[4];
+                        load_c(ix + off[k][0], iy + off[k][1], iz + off[k][2], c);
+                        store(ix + off[k][0], iy + off[k][1], iz + off[k][2], c);
+                    }
+                } else {
+                    uint16_t c[4];
+                    load_c(ix, iy, iz, c);
+                    if (lighting) {
+                        const uint16_t* Nn = normal + 4 * (((int64_t)iz * N + iy) * N + ix);
+                        f3 n = mk(2.0f * h2f(Nn[0]) - 1.0f, 2.0f * h2f(Nn[1]) - 1.0f, 2.0f * h2f(Nn[2]) - 1.0f);
+                        f3 L = normalize(sub(lvox, mk((float)ix, (float)iy, (float)iz)));
+                        float diff = std::fmax(dot(n, L), 0.0f);
+                        uint16_t o[4];
+                        for (int k = 0; k < 3; ++k) o[k] = f2h((diff * lint[k]) * h2f(c[k]));
+                        o[3] = c[3];
+                        store(ix, iy, iz, o);
+                    } else {
+                        store(ix, iy, iz, c);
+                    }
+                }
+            }
+        }
+    });
+}
+
+// -------------------------------------------------------------------- mips
+// filterRadiance.comp BOX2: dst = 0.125 * sum of the 8 children, summed in
+// the shader's offset order (z fastest, then y, then x), rounded to binary16.
+void orc_build_mips(int32_t dim, int32_t levels, uint16_t* chain, int32_t nthreads) {
+    int64_t off = 0;
+    int S = dim;
+    for (int l = 0; l + 1 < levels; ++l) {
+        const uint16_t* src = chain + 4 * off;
+        int D = S / 2;
+        uint16_t* dst = chain + 4 * (off + (int64_t)S * S * S);
+        parallel_for(D, nthreads, [&](int64_t z0, int64_t z1) {
+            for (int z = (int)z0; z < (int)z1; ++z)
+                for (int y = 0; y < D; ++y)
+                    for (int x = 0; x < D; ++x) {
+                        float acc[4] = {0, 0, 0, 0};
+                        for (int ox = 0; ox < 2; ++ox)
+                            for (int oy = 0; oy < 2; ++oy)
+                                for (int oz = 0; oz < 2; ++oz) {
+                                    const uint16_t* s =
+                                        src + 4 * (((int64_t)(2 * z + oz) * S + (2 * y + oy)) * S + (2 * x + ox));
+                                    for (int k = 0; k < 4; ++k) acc[k] += h2f(s[k]);
+                                }
+                        uint16_t* d = dst + 4 * (((int64_t)z * D + y) * D + x);
+                        for (int k = 0; k < 4; ++k) d[k] = f2h(acc[k] * 0.125f);
+                    }
+        });
+        off += (int64_t)S * S * S;
+        S = D;
+    }
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ trace
+namespace {
+
+template <typename T>
+struct V {
+    T x, y, z;
+};
+template <typename T>
+static inline V<T> vadd(V<T> a, V<T> b) {
+    return {a.x + b.x, a.y + b.y, a.z + b.z};
+}
+template <typename T>
+static inline V<T> vsub(V<T> a, V<T> b) {
+    return {a.x - b.x, a.y - b.y, a.z - b.z};
+}
+template <typename T>
+static inline V<T> vmul(V<T> a, T s) {
+    return {a.x * s, a.y * s, a.z * s};
+}
+template <typename T>
+static inline T vdot(V<T> a, V<T> b) {
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <typename T>
+static inline V<T> vnorm(V<T> a) {
+    T inv = T(1) / std::sqrt(vdot(a, a));
+    return vmul(a, inv);
+}
+
+template <typename T>
+struct Sampler {
+    const uint16_t* chain;
+    int dim, levels;
+    int64_t off[16];
+
+    void init(const uint16_t* c, int d, int l) {
+        chain = c;
+        dim = d;
+        levels = l;
+        int64_t o = 0;
+        for (int i = 0; i < l; ++i) {
+            off[i] = o;
+            int64_t s = d >> i;
+            o += s * s * s;
+        }
+    }
+    inline void texel(int l, int S, int x, int y, int z, T out[4]) const {
+        if (x < 0 || y < 0 || z < 0 || x >= S || y >= S || z >= S) {
+            out[0] = out[1] = out[2] = out[3] = T(0);
+            return;
+        }
+        const uint16_t* p = chain + 4 * (off[l] + ((int64_t)z * S + y) * S + x);
+        for (int k = 0; k < 4; ++k) out[k] = (T)h2f(p[k]);
+    }
+    // GL_LINEAR within one level, clamp-to-border (0,0,0,0).
+    void trilinear(int l, V<T> p, T out[4]) const {
+        int S = dim >> l;
+        T u = p.x * (T)S - T(0.5), v = p.y * (T)S - T(0.5), w = p.z * (T)S - T(0.5);
+        T fu = std::floor(u), fv = std::floor(v), fw = std::floor(w);
+        T a = u - fu, b = v - fv, c = w - fw;
+        int i = (int)fu, j = (int)fv, k = (int)fw;
+        T t[8][4];
+        for (int n = 0; n < 8; ++n) texel(l, S, i + (n & 1), j + ((n >> 1) & 1), k + (n >> 2), t[n]);
+        for (int ch = 0; ch < 4; ++ch) {
+            T x00 = t[0][ch] * (T(1) - a) + t[1][ch] * a;
+            T x10 = t[2][ch] * (T(1) - a) + t[3][ch] * a;
+            T x01 = t[4][ch] * (T(1) - a) + t[5][ch] * a;
+            T x11 = t[6][ch] * (T(1) - a) + t[7][ch] * a;
+            T y0 = x00 * (T(1) - b) + x10 * b;
+            T y1 = x01 * (T(1) - b) + x11 * b;
+            out[ch] = y0 * (T(1) - c) + y1 * c;
+        }
+    }
+    // textureLod with GL_LINEAR_MIPMAP_LINEAR minification, GL_NEAREST
+    // magnification, levels [0, levels-1].
+    void sample(V<T> p, T lambda, T out[4]) const {
+        int q = levels - 1;
+        if (lambda <= T(0)) {
+            int S = dim;
+            T u = p.x * (T)S, v = p.y * (T)S, w = p.z * (T)S;
+            texel(0, S, (int)std::floor(u), (int)std::floor(v), (int)std::floor(w), out);
+            return;
+        }
+        if (lambda >= (T)q) {
+            trilinear(q, p, out);
+            return;
+        }
+        T fl = std::floor(lambda);
+        int d1 = (int)fl;
+        T f = lambda - fl;
+        T a[4], b[4];
+        trilinear(d1, p, a);
+        trilinear(d1 + 1, p, b);
+        for (int ch = 0; ch < 4; ++ch) out[ch] = a[ch] * (T(1) - f) + b[ch] * f;
+    }
+};
+
+// phong.frag:135-180 plus a length limit `maxd` in texture units.
+template <typename T>
+static void trace_cone(const Sampler<T>& s, V<T> pos, V<T> n, V<T> dir, const orc_cone& c, T maxd, T out[4],
+                       uint64_t& samples) {
+    dir = vnorm(dir);
+    T col[3] = {0, 0, 0};
+    T alpha = 0;
+    T scale = T(1) / (T)s.dim;
+    V<T> start = vadd(pos, vmul(vmul(n, (T)c.bias), scale));
+    T h = (T)c.h0;
+    T tanh = std::tan((T)c.angle / T(2));
+    for (int i = 0; i < c.steps && alpha < T(0.95); ++i) {
+        T r = h * tanh;
+        T lod = std::log2(std::max(T(1), T(2) * r));
+        V<T> sp = vadd(start, vmul(vmul(dir, h), scale));
+        if (sp.x < T(0) || sp.y < T(0) || sp.z < T(0) || sp.x > T(1) || sp.y > T(1) || sp.z > T(1)) break;
+        if (h * scale > maxd) break;
+        T sc[4];
+        s.sample(sp, lod + (T)c.lod_offset, sc);
+        ++samples;
+        T a = T(1) - alpha;
+        for (int k = 0; k < 3; ++k) col[k] += sc[k] * a;
+        alpha += a * sc[3];
+        h += r;
+    }
+    out[0] = col[0];
+    out[1] = col[1];
+    out[2] = col[2];
+    out[3] = alpha;
+}
+
+// phong.frag:470-478; the -0.5909037 typo is kept.
+static const double kConeDirs[6][3] = {{0, 1, 0},
+                                       {0, 0.5, 0.866025},
+                                       {0.823639, 0.5, 0.267617},
+                                       {0.509037, 0.5, -0.700629},
+                                       {-0.5909037, 0.5, -0.700629},
+                                       {-0.823639, 0.5, 0.267617}};
+static const double kConeWeights[6] = {0.25, 0.15, 0.15, 0.15, 0.15, 0.15};
+
+template <typename T>
+static void trace_rows(const orc_volume* vol, int levels, const uint16_t* chain, const orc_trace_params* tp,
+                       const float* gpos, const float* gnrm, const float* galb, int W, int H, int row0, int row1,
+                       int row_step, const float eye[3], float* irr, float* spec, float* colr, uint64_t* samples_out,
+                       int nthreads) {
+    Sampler<T> s;
+    s.init(chain, vol->dim, levels);
+    V<T> vmin = {(T)vol->vmin[0], (T)vol->vmin[1], (T)vol->vmin[2]};
+    V<T> vmax = {(T)vol->vmax[0], (T)vol->vmax[1], (T)vol->vmax[2]};
+    V<T> vc = {(T)vol->vcenter[0], (T)vol->vcenter[1], (T)vol->vcenter[2]};
+    V<T> E = {(T)eye[0], (T)eye[1], (T)eye[2]};
+    T maxd = tp->max_distance > 0 ? (T)tp->max_distance : std::sqrt(T(3));
+    std::vector<int> rows;
+    for (int r = row0; r < row1; r += std::max(1, row_step)) rows.push_back(r);
+    std::atomic<uint64_t> total{0};
+    parallel_for((int64_t)rows.size(), nthreads, [&](int64_t a, int64_t b) {
+        uint64_t ns = 0;
+        for (int64_t ri = a; ri < b; ++ri) {
+            int y = rows[ri];
+            for (int x = 0; x < W; ++x) {
+                int64_t p = (int64_t)y * W + x;
+                float ir[4] = {0, 0, 0, 0}, sp[4] = {0, 0, 0, 0}, co[4] = {0, 0, 0, 0};
+                if (gpos[4 * p + 3] != 0.0f) {
+                    V<T> P = {(T)gpos[4 * p], (T)gpos[4 * p + 1], (T)gpos[4 * p + 2]};
+                    V<T> Nn = vnorm(V<T>{(T)gnrm[4 * p], (T)gnrm[4 * p + 1], (T)gnrm[4 * p + 2]});
+                    V<T> alb = {(T)galb[4 * p], (T)galb[4 * p + 1], (T)galb[4 * p + 2]};
+                    V<T> out;
+                    if (tp->enable_indirect) {
+                        V<T> vp = {((P.x - vc.x) - vmin.x) / (vmax.x - vmin.x), ((P.y - vc.y) - vmin.y) / (vmax.y - vmin.y),
+                                   ((P.z - vc.z) - vmin.z) / (vmax.z - vmin.z)};
+                        // Orthonormal basis from N: Duff et al. 2017, "Building an
+                        // Orthonormal Basis, Revisited" (JCGT 6(1)).
+                        T sgn = Nn.z >= T(0) ? T(1) : T(-1);
+                        T ca = T(-1) / (sgn + Nn.z);
+                        T cb = Nn.x * Nn.y * ca;
+                        V<T> Tg = {T(1) + sgn * Nn.x * Nn.x * ca, sgn * cb, -sgn * Nn.x};
+                        V<T> Bt = {cb, sgn + Nn.y * Nn.y * ca, -Nn.y};
+                        T ind[4] = {0, 0, 0, 0};
+                        for (int c = 0; c < 6; ++c) {
+                            T dx = (T)kConeDirs[c][0], dy = (T)kConeDirs[c][1], dz = (T)kConeDirs[c][2];
+                            V<T> d;
+                            if (tp->ref_tbn_quirk)  // mat3(T, B, N) * d
+                                d = vadd(vadd(vmul(Tg, dx), vmul(Bt, dy)), vmul(Nn, dz));
+                            else  // y -> N, z -> -B (a proper rotation of the set)
+                                d = vsub(vadd(vmul(Tg, dx), vmul(Nn, dy)), vmul(Bt, dz));
+                            d = vnorm(d);
+                            T cr[4];
+                            trace_cone(s, vp, Nn, d, tp->diffuse, maxd, cr, ns);
+                            T w = (T)kConeWeights[c];
+                            for (int k = 0; k < 4; ++k) ind[k] += w * cr[k];
+                        }
+                        for (int k = 0; k < 4; ++k) ir[k] = (float)ind[k];
+                        T occ = T(1) - std::min(std::max(ind[3], T(0)), T(1));
+                        V<T> rgb = {ind[0], ind[1], ind[2]};
+                        if (tp->enable_reflections) {
+                            V<T> I = vsub(P, E);
+                            V<T> R = vsub(I, vmul(Nn, T(2) * vdot(Nn, I)));
+                            T sr[4];
+                            trace_cone(s, vp, Nn, R, tp->specular, maxd, sr, ns);
+                            for (int k = 0; k < 4; ++k) sp[k] = (float)sr[k];
+                            rgb = vadd(rgb, vmul(V<T>{sr[0], sr[1], sr[2]}, (T)tp->reflect_scale));
+                        }
+                        T as = (T)tp->ambient_scale;
+                        rgb = {rgb.x * (as * alb.x), rgb.y * (as * alb.y), rgb.z * (as * alb.z)};
+                        out = rgb;
+                        if (tp->draw_occlusion) out = vmul(out, occ);
+                    } else {
+                        T as = (T)tp->ambient_scale;
+                        out = {as * alb.x, as * alb.y, as * alb.z};
+                    }
+                    if (tp->enable_postprocess) {
+                        T g = T(1) / T(2.2);
+                        out = {std::pow(out.x / (out.x + T(1)), g), std::pow(out.y / (out.y + T(1)), g),
+                               std::pow(out.z / (out.z + T(1)), g)};
+                    }
+                    co[0] = (float)out.x;
+                    co[1] = (float)out.y;
+                    co[2] = (float)out.z;
+                    co[3] = 1.0f;
+                }
+                if (irr) std::memcpy(irr + 4 * p, ir, 16);
+                if (spec) std::memcpy(spec + 4 * p, sp, 16);
+                if (colr) std::memcpy(colr + 4 * p, co, 16);
+            }
+        }
+        total.fetch_add(ns);
+    });
+    if (samples_out) *samples_out += total.load();
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_trace(const orc_volume* vol, int32_t levels, const uint16_t* chain, const orc_trace_params* tp,
+               const float* gpos, const float* gnrm, const float* galb, int32_t width, int32_t height,
+               int32_t row0, int32_t row1, int32_t row_step, const float eye[3], int32_t precision, float* irradiance,
+               float* specular, float* color, uint64_t* samples, int32_t nthreads) {
+    row0 = std::max(0, row0);
+    row1 = std::min(height, row1);
+    if (precision == 64)
+        trace_rows<double>(vol, levels, chain, tp, gpos, gnrm, galb, width, height, row0, row1, row_step, eye,
+                           irradiance, specular, color, samples, nthreads);
+    else
+        trace_rows<float>(vol, levels, chain, tp, gpos, gnrm, galb, width, height, row0, row1, row_step, eye,
+                          irradiance, specular, color, samples, nthreads);
+}
+
+// ------------------------------------------------------------ set-up passes
+// Depth-only shadow pass (src/Application.cpp:213-233): window depth
+// (ndc.z + 1) / 2, fragments outside [0,1] clipped, LESS test, clear 1.0.
+void orc_render_shadowmap(const float* pos, int64_t ntri, const float ls[16], int32_t W, int32_t H, float* depth,
+                          int32_t nthreads) {
+    for (int64_t i = 0; i < (int64_t)W * H; ++i) depth[i] = 1.0f;
+    // Rows are split across threads; each thread rasterises every triangle
+    // restricted to its rows, so the depth test needs no synchronisation.
+    parallel_for(H, nthreads, [&](int64_t r0, int64_t r1) {
+        for (int64_t t = 0; t < ntri; ++t) {
+            const float* P = pos + t * 9;
+            float wx[3], wy[3], d[3];
+            for (int k = 0; k < 3; ++k) {
+                float c[4];
+                mat_vec(ls, P[3 * k], P[3 * k + 1], P[3 * k + 2], 1.0f, c);
+                float nx = c[0] / c[3], ny = c[1] / c[3], nz = c[2] / c[3];
+                wx[k] = (nx + 1.0f) * 0.5f * (float)W;
+                wy[k] = (ny + 1.0f) * 0.5f * (float)H;
+                d[k] = (nz + 1.0f) * 0.5f;
+            }
+            RasterTri rt;
+            if (!raster_setup(wx, wy, W, H, rt)) continue;
+            int y0 = std::max<int>(rt.py0, (int)r0), y1 = std::min<int>(rt.py1, (int)r1 - 1);
+            for (int py = y0; py <= y1; ++py)
+                for (int px = rt.px0; px <= rt.px1; ++px) {
+                    int64_t e[3];
+                    if (!raster_cover(rt, px, py, e)) continue;
+                    float l[3];
+                    raster_weights(rt, e, l);
+                    float z = interp(l, d[0], d[1], d[2]);
+                    if (!(z >= 0.0f && z <= 1.0f)) continue;
+                    float& dst = depth[(int64_t)py * W + px];
+                    if (z < dst) dst = z;
+                }
+        }
+    });
+}
+
+// Camera G-buffer: nearest triangle per pixel centre (key = depth bits, then
+// triangle id), resolved by intersecting the pixel's ray with that triangle.
+void orc_render_gbuffer(const float* pos, const float* nrm, const float* albedo, int64_t ntri, const float vp[16],
+                        const float eye[3], const float ivp[16], int32_t W, int32_t H, float* gpos, float* gnrm,
+                        float* galb) {
+    std::vector<uint64_t> keys((size_t)W * H, ~0ull);
+    for (int64_t t = 0; t < ntri; ++t) {
+        const float* P = pos + t * 9;
+        float cv[3][4];
+        for (int k = 0; k < 3; ++k) mat_vec(vp, P[3 * k], P[3 * k + 1], P[3 * k + 2], 1.0f, cv[k]);
+        // Clip against the near plane z >= -w (Sutherland-Hodgman).
+        float poly[4][4];
+        int np = 0;
+        for (int k = 0; k < 3; ++k) {
+            const float* a = cv[k];
+            const float* b = cv[(k + 1) % 3];
+            float da = a[2] + a[3], db = b[2] + b[3];
+            if (da >= 0.0f) {
+                std::memcpy(poly[np++], a, 16);
+            }
+            if ((da >= 0.0f) != (db >= 0.0f)) {
+                float s = da / (da - db);
+                for (int c = 0; c < 4; ++c) poly[np][c] = a[c] + s * (b[c] - a[c]);
+                ++np;
+            }
+        }
+        for (int f = 1; f + 1 < np; ++f) {
+            const float* vv[3] = {poly[0], poly[f], poly[f + 1]};
+            float wx[3], wy[3], d[3];
+            bool ok = true;
+            for (int k = 0; k < 3; ++k) {
+                if (!(vv[k][3] > 0.0f)) ok = false;
+                float nx = vv[k][0] / vv[k][3], ny = vv[k][1] / vv[k][3], nz = vv[k][2] / vv[k][3];
+                wx[k] = (nx + 1.0f) * 0.5f * (float)W;
+                wy[k] = (ny + 1.0f) * 0.5f * (float)H;
+                d[k] = (nz + 1.0f) * 0.5f;
+            }
+            if (!ok) continue;
+            RasterTri rt;
+            if (!raster_setup(wx, wy, W, H, rt)) continue;
+            for (int py = rt.py0; py <= rt.py1; ++py)
+                for (int px = rt.px0; px <= rt.px1; ++px) {
+                    int64_t e[3];
+                    if (!raster_cover(rt, px, py, e)) continue;
+                    float l[3];
+                    raster_weights(rt, e, l);
+                    float z = interp(l, d[0], d[1], d[2]);
+                    if (!(z >= 0.0f && z <= 1.0f)) continue;
+                    uint32_t zb;
+                    std::memcpy(&zb, &z, 4);
+                    uint64_t key = ((uint64_t)zb << 32) | (uint64_t)(uint32_t)t;
+                    uint64_t& dst = keys[(size_t)py * W + px];
+                    if (key < dst) dst = key;
+                }
+        }
+    }
+    f3 E = ld3(eye);
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            size_t i = (size_t)py * W + px;
+            float* gp = gpos + 4 * i;
+            float* gn = gnrm + 4 * i;
+            float* ga = galb + 4 * i;
+            if (keys[i] == ~0ull) {
+                for (int k = 0; k < 4; ++k) gp[k] = gn[k] = ga[k] = 0.0f;
+                continue;
+            }
+            int64_t t = (int64_t)(keys[i] & 0xffffffffull);
+            const float* P = pos + t * 9;
+            const float* Nn = nrm + t * 9;
+            f3 p0 = ld3(P), p1 = ld3(P + 3), p2 = ld3(P + 6);
+            float ndx = ((float)px + 0.5f) / (float)W * 2.0f - 1.0f;
+            float ndy = ((float)py + 0.5f) / (float)H * 2.0f - 1.0f;
+            float fw[4];
+            mat_vec(ivp, ndx, ndy, 1.0f, 1.0f, fw);
+            f3 dir = sub(mk(fw[0] / fw[3], fw[1] / fw[3], fw[2] / fw[3]), E);
+            f3 e1 = sub(p1, p0), e2 = sub(p2, p0);
+            f3 pv = cross(dir, e2);
+            float det = dot(e1, pv);
+            float u = 1.0f / 3.0f, v = 1.0f / 3.0f;
+            if (det != 0.0f) {
+                float inv = 1.0f / det;
+                f3 tv = sub(E, p0);
+                u = dot(tv, pv) * inv;
+                f3 qv = cross(tv, e1);
+                v = dot(dir, qv) * inv;
+                u = clampf(u, 0.0f, 1.0f);
+                v = clampf(v, 0.0f, 1.0f - u);
+            }
+            float w0 = 1.0f - u - v;
+            f3 wp = add(add(mul(p0, w0), mul(p1, u)), mul(p2, v));
+            f3 nn = normalize(add(add(mul(ld3(Nn), w0), mul(ld3(Nn + 3), u)), mul(ld3(Nn + 6), v)));
+            gp[0] = wp.x;
+            gp[1] = wp.y;
+            gp[2] = wp.z;
+            gp[3] = 1.0f;
+            gn[0] = nn.x;
+            gn[1] = nn.y;
+            gn[2] = nn.z;
+            gn[3] = 0.0f;
+            ga[0] = albedo[3 * t];
+            ga[1] = albedo[3 * t + 1];
+            ga[2] = albedo[3 * t + 2];
+            ga[3] = 1.0f;
+        }
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+/*
+ * CPU oracle of the VCT hot path.  TEST INFRASTRUCTURE ONLY: it is the
+ * correctness judge of the CUDA library and the timed CPU baseline; nothing
+ * in the product links or calls it.
+ *
+ * It restates, in plain single-threaded C++17, the GLSL of sfreed141/vct:
+ *   shaders/common.glsl:1-64          voxel coordinate mapping
+ *   shaders/voxelize.geom:25-73       dominant-axis projection
+ *   shaders/voxelize.frag:75-108,159-280  fragment lighting, PCF, accumulation
+ *   shaders/transferVoxels.comp:29-70 normalisation / opacity / radiance seed
+ *   shaders/injectRadiance.comp:40-103 shadow-map injection
+ *   shaders/filterRadiance.comp:14-65 2x2x2 box mip
+ *   shaders/phong.frag:135-180,470-511 cone tracing and composite
+ *   src/Application.cpp:200-210,689-692 host matrices
+ * plus the GL fixed-function pieces those shaders rely on (pixel-centre
+ * rasterisation, bilinear / trilinear-mipmap filtering with clamp-to-border,
+ * binary16 rounding).
+ *
+ * Parity is unpinned by the reference: it has no tests, fixtures or golden
+ * outputs, and its OpenGL program cannot run without a graphics stack.  The
+ * oracle is pinned instead by hand-computed known answers (tests/golden).
+ *
+ * Volumes are binary16 RGBA, x fastest, exactly as include/vct.h describes.
+ * Every function with an `nthreads` argument gives bit-identical results for
+ * any thread count (integer accumulation, disjoint outputs).
+ */
+#ifndef VCT_ORACLE_H
+#define VCT_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_volume {
+    int32_t dim;
+    float vmin[3], vmax[3], vcenter[3];
+} orc_volume;
+
+/* Same layout as vct_light (80 bytes). */
+typedef struct orc_light {
+    float position[3], _p0;
+    float direction[3], _p1;
+    float color[3];
+    float range, intensity;
+    uint32_t enabled, selected, shadow_caster, type;
+    uint32_t _p2[3];
+} orc_light;
+
+typedef struct orc_cone {
+    int32_t steps;
+    float angle, bias, h0, lod_offset;
+} orc_cone;
+
+typedef struct orc_trace_params {
+    orc_cone diffuse, specular;
+    int32_t enable_indirect, enable_reflections, draw_occlusion, enable_postprocess;
+    float ambient_scale, reflect_scale, max_distance;
+    int32_t ref_tbn_quirk;
+} orc_trace_params;
+
+typedef struct orc_stats {
+    uint32_t total_voxel_fragments, unique_voxels, max_fragments_per_voxel, error_flags;
+} orc_stats;
+
+uint16_t orc_f32_to_f16(float f);
+float orc_f16_to_f32(uint16_t h);
+void orc_f32_to_f16_array(const float* in, uint16_t* out, int64_t n);
+
+void orc_voxel_mvp(const orc_volume* vol, float out[48]);
+void orc_lookat(const float eye[3], const float center[3], const float up[3], float out[16]);
+void orc_ortho(float l, float r, float b, float t, float n, float f, float out[16]);
+void orc_perspective(float fovy, float aspect, float znear, float zfar, float out[16]);
+void orc_mat4_mul(const float a[16], const float b[16], float out[16]);
+
+/* count[dim^3], sums[6*dim^3] (SoA r,g,b,nx,ny,nz) are ADDED to. */
+void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, const float* albedo,
+                  int64_t ntri, const orc_light* lights, int32_t nlights, int32_t lighting,
+                  int32_t axis_override, const float* shadowmap, int32_t sw, int32_t sh,
+                  const float ls[16], uint32_t* count, uint32_t* sums, uint32_t* total_fragments,
+                  int32_t nthreads);
+
+/* transferVoxels.comp; radiance/colour/normal are dim^3 RGBA16F (uint16 x4). */
+void orc_normalize(const orc_volume* vol, float voxel_set_opacity, int32_t temporal_filter,
+                   float temporal_decay, const uint32_t* count, const uint32_t* sums,
+                   uint16_t* color, uint16_t* normal, uint16_t* radiance, orc_stats* stats,
+                   int32_t nthreads);
+
+void orc_inject(const orc_volume* vol, const float* shadowmap, int32_t sw, int32_t sh,
+                const float ls_inverse[16], const float light_pos[3], const float light_int[3],
+                int32_t radiance_lighting, int32_t radiance_dilate, const uint16_t* color,
+                const uint16_t* normal, uint16_t* radiance, int32_t nthreads);
+
+/* chain: all `levels` levels contiguous; level 0 is read, 1.. are written. */
+void orc_build_mips(int32_t dim, int32_t levels, uint16_t* chain, int32_t nthreads);
+
+/* Rows [row0, row1) of the G-buffer are traced; outputs are full-size float4
+ * images (rows outside the range untouched).  Any output may be NULL.
+ * precision: 32 = the fp32 transcription, 64 = the fp64 judge. */
+void orc_trace(const orc_volume* vol, int32_t levels, const uint16_t* chain,
+               const orc_trace_params* tp, const float* gpos, const float* gnrm,
+               const float* galb, int32_t width, int32_t height, int32_t row0, int32_t row1,
+               int32_t row_step, const float eye[3], int32_t precision, float* irradiance,
+               float* specular, float* color, uint64_t* samples, int32_t nthreads);
+
+void orc_render_shadowmap(const float* pos, int64_t ntri, const float ls[16], int32_t w, int32_t h,
+                          float* depth, int32_t nthreads);
+void orc_render_gbuffer(const float* pos, const float* nrm, const float* albedo, int64_t ntri,
+                        const float vp[16], const float eye[3], const float inv_vp[16], int32_t w,
+                        int32_t h, float* gpos, float* gnrm, float* galb);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

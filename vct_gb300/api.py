@@ -1,0 +1,251 @@
+"""Python mirror of the C ABI, for tests and benchmarks.
+
+Device buffers are torch CUDA tensors (torch is only the allocator and stream
+provider here); every call goes straight to the C entry point of the same
+name in libvct.so.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _ptr(t) -> int:
+    if t is None:
+        return 0
+    if isinstance(t, int):
+        return t
+    if not t.is_contiguous():
+        raise ValueError("tensor must be contiguous")
+    return int(t.data_ptr())
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        import torch
+
+        return int(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return stream
+    return int(stream.cuda_stream)
+
+
+def f3(v) -> C.Array:
+    a = np.asarray(v, dtype=np.float32).reshape(3)
+    return (C.c_float * 3)(*a.tolist())
+
+
+def f16(v) -> C.Array:
+    a = np.asarray(v, dtype=np.float32).reshape(16)
+    return (C.c_float * 16)(*a.tolist())
+
+
+def default_params() -> L.vct_params:
+    p = L.vct_params()
+    L.load().vct_default_params(C.byref(p))
+    return p
+
+
+def scene_params(scene, **overrides) -> L.vct_params:
+    """Reference defaults with the scene's cone settings and overrides."""
+    p = default_params()
+    for key, name in (("diffuse", "diffuse_cone"), ("specular", "specular_cone")):
+        if key in scene.cone:
+            steps, ang, bias, h0, lod = scene.cone[key]
+            setattr(p, name, L.vct_cone_settings(int(steps), float(ang), float(bias), float(h0), float(lod)))
+    p.max_distance = float(np.sqrt(3.0))  # grid diagonal in texture units
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p
+
+
+def light_array(lights) -> tuple:
+    arr = (L.vct_light * max(1, len(lights)))()
+    for i, d in enumerate(lights):
+        li = arr[i]
+        li.position = f3(d["position"])
+        li.direction = f3(d["direction"])
+        li.color = f3(d["color"])
+        li.range = float(d["range"])
+        li.intensity = float(d["intensity"])
+        li.enabled = int(d.get("enabled", 1))
+        li.shadow_caster = int(d.get("shadow_caster", 0))
+        li.type = int(d["type"])
+    return arr, len(lights)
+
+
+def config_for(scene, device: int = 0, flags: int = 0, dim: int | None = None) -> L.vct_config:
+    c = L.vct_config()
+    c.voxel_dim = int(dim or scene.dim)
+    c.voxel_levels = 0
+    c.voxel_min = f3([-scene.vmax] * 3)
+    c.voxel_max = f3([scene.vmax] * 3)
+    c.voxel_center = f3([0, 0, 0])
+    c.device = device
+    c.flags = flags
+    return c
+
+
+def triangles(pos, nrm, alb) -> L.vct_triangles:
+    t = L.vct_triangles()
+    t.positions_dev = _ptr(pos)
+    t.normals_dev = _ptr(nrm)
+    t.albedo_dev = _ptr(alb)
+    t.count = int(pos.shape[0]) if pos is not None else 0
+    return t
+
+
+def shadow_desc(scene, shadowmap) -> L.vct_shadow_desc:
+    s = L.vct_shadow_desc()
+    s.shadowmap_dev = _ptr(shadowmap)
+    s.width, s.height = scene.shadow_size
+    s.ls = f16(scene.ls)
+    s.ls_inverse = f16(scene.ls_inverse)
+    s.light_pos = f3(scene.light_pos)
+    s.light_int = f3(scene.light_int)
+    return s
+
+
+def gbuffer(gpos, gnrm, galb, width: int, height: int) -> L.vct_gbuffer:
+    g = L.vct_gbuffer()
+    g.position_dev, g.normal_dev, g.albedo_dev = _ptr(gpos), _ptr(gnrm), _ptr(galb)
+    g.width, g.height = width, height
+    return g
+
+
+def trace_out(irradiance=None, specular=None, color=None, samples=None) -> L.vct_trace_out:
+    o = L.vct_trace_out()
+    o.irradiance_dev, o.specular_dev, o.color_dev = _ptr(irradiance), _ptr(specular), _ptr(color)
+    o.sample_count_dev = _ptr(samples)
+    return o
+
+
+class Context:
+    """Owns a vct_ctx (volumes on one device)."""
+
+    def __init__(self, config: L.vct_config):
+        self._lib = L.load()
+        h = C.c_void_p()
+        L.check(self._lib.vct_create(C.byref(config), C.byref(h)), "vct_create")
+        self.handle = h
+        cfg = L.vct_config()
+        L.check(self._lib.vct_get_config(h, C.byref(cfg)), "vct_get_config")
+        self.dim = cfg.voxel_dim
+        self.levels = cfg.voxel_levels
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.vct_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_params(self, p: L.vct_params):
+        L.check(self._lib.vct_set_params(self.handle, C.byref(p)), "vct_set_params")
+
+    def get_params(self) -> L.vct_params:
+        p = L.vct_params()
+        L.check(self._lib.vct_get_params(self.handle, C.byref(p)), "vct_get_params")
+        return p
+
+    def voxelize_accumulate(self, tris, lights, shadow, eye, stream=None):
+        arr, n = lights
+        L.check(self._lib.vct_voxelize_accumulate(self.handle, C.byref(tris), arr, n, C.byref(shadow), f3(eye),
+                                                   _stream(stream)), "vct_voxelize_accumulate")
+
+    def normalize(self, stream=None):
+        L.check(self._lib.vct_normalize(self.handle, _stream(stream)), "vct_normalize")
+
+    def voxelize(self, tris, lights, shadow, eye, stream=None):
+        arr, n = lights
+        L.check(self._lib.vct_voxelize(self.handle, C.byref(tris), arr, n, C.byref(shadow), f3(eye), _stream(stream)),
+                "vct_voxelize")
+
+    def inject(self, shadow, eye, stream=None):
+        L.check(self._lib.vct_inject(self.handle, C.byref(shadow), f3(eye), _stream(stream)), "vct_inject")
+
+    def build_mips(self, volume: int = L.VCT_VOLUME_RADIANCE, stream=None):
+        L.check(self._lib.vct_build_mips(self.handle, volume, _stream(stream)), "vct_build_mips")
+
+    def trace(self, gb, eye, out, stream=None):
+        L.check(self._lib.vct_trace(self.handle, C.byref(gb), f3(eye), C.byref(out), _stream(stream)), "vct_trace")
+
+    def frame(self, tris, lights, shadow, eye, gb, out, stream=None):
+        arr, n = lights
+        L.check(self._lib.vct_frame(self.handle, C.byref(tris), arr, n, C.byref(shadow), f3(eye), C.byref(gb),
+                                    C.byref(out), _stream(stream)), "vct_frame")
+
+    def enable_timers(self, on: bool = True):
+        L.check(self._lib.vct_enable_timers(self.handle, int(on)), "vct_enable_timers")
+
+    def timers(self) -> dict:
+        t = L.vct_timers()
+        L.check(self._lib.vct_get_timers(self.handle, C.byref(t)), "vct_get_timers")
+        return {k: getattr(t, k) for k, _ in L.vct_timers._fields_}
+
+    def stats(self, stream=None) -> dict:
+        s = L.vct_stats()
+        L.check(self._lib.vct_get_stats(self.handle, C.byref(s), _stream(stream)), "vct_get_stats")
+        return dict(total_voxel_fragments=s.total_voxel_fragments, unique_voxels=s.unique_voxels,
+                    max_fragments_per_voxel=s.max_fragments_per_voxel, error_flags=s.error_flags)
+
+    def volume_ptr(self, volume: int, level: int) -> tuple[int, int]:
+        p = C.c_void_p()
+        d = C.c_int32()
+        L.check(self._lib.vct_volume_level(self.handle, volume, level, C.byref(p), C.byref(d)), "vct_volume_level")
+        return int(p.value), int(d.value)
+
+    def accumulator_ptrs(self) -> tuple[int, int]:
+        a, b = C.c_void_p(), C.c_void_p()
+        L.check(self._lib.vct_accumulators(self.handle, C.byref(a), C.byref(b)), "vct_accumulators")
+        return int(a.value), int(b.value)
+
+    # -- copies of device state into torch tensors (test helpers)
+    def read_volume(self, volume: int, level: int = 0):
+        """Copy of one volume level as an int16 tensor (binary16 bit patterns)."""
+        ptr, d = self.volume_ptr(volume, level)
+        return device_view(ptr, (d * d * d * 4,), "<i2").clone()
+
+    def read_accumulators(self):
+        """Copies of (count, sums) as int32 tensors (uint32 bit patterns)."""
+        cp, sp = self.accumulator_ptrs()
+        nv = self.dim ** 3
+        return device_view(cp, (nv,), "<i4").clone(), device_view(sp, (6 * nv,), "<i4").clone()
+
+
+class _CudaArray:
+    def __init__(self, ptr: int, shape: tuple, typestr: str):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 2, "strides": None}
+
+
+def device_view(ptr: int, shape: tuple, typestr: str):
+    """Zero-copy torch view of device memory owned by libvct."""
+    import torch
+
+    return torch.as_tensor(_CudaArray(ptr, shape, typestr), device="cuda")
+
+
+def render_shadowmap(tris, scene, out, stream=None):
+    W, H = scene.shadow_size
+    L.call("vct_render_shadowmap", C.byref(tris), f16(scene.ls), _ptr(out), W, H, _stream(stream))
+
+
+def render_gbuffer(tris, scene, keys, gpos, gnrm, galb, stream=None):
+    W, H = scene.gbuffer_size
+    L.call("vct_render_gbuffer", C.byref(tris), f16(scene.view_proj), f3(scene.eye), f16(scene.inv_view_proj), W, H,
+           _ptr(keys), _ptr(gpos), _ptr(gnrm), _ptr(galb), _stream(stream))

@@ -1,0 +1,868 @@
+// C ABI of the VCT hot path (include/vct.h): context lifetime, argument
+// validation, stream-ordered launches.  Compiled with -ffp-contract=off: the
+// host-side matrices and the voxel position of the light are computed with
+// the same fp32 operation order as the GLSL host code they replace.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "vct_internal.h"
+
+using namespace vct;
+
+struct vct_ctx {
+    vct_config cfg;
+    vct_params params;
+    int dim = 0, levels = 0, color_levels = 1, device = 0, num_sms = 0;
+    long long nv = 0;
+    uint32_t* count = nullptr;
+    uint32_t* sums = nullptr;
+    uint32_t* lit = nullptr;
+    uint2* color = nullptr;     // colour chain (color_levels levels)
+    uint2* normal = nullptr;    // one level
+    uint2* radiance = nullptr;  // radiance chain (levels levels)
+    long long level_off[VCT_MAX_LEVELS] = {};
+    StatsDev* stats = nullptr;
+    bool stats_reset_pending = true;
+    bool radiance_ready = false;  // level 0 written since the last accumulate
+    bool mips_ready = false;
+    float mvp[48];
+    cudaMipmappedArray_t tex_array = nullptr;
+    cudaTextureObject_t tex = 0;
+    bool tex_ready = false;
+    bool timers_on = false;
+    bool timers_recorded = false;
+    cudaEvent_t ev[5] = {};
+};
+
+namespace vct {
+static std::atomic<unsigned long long> g_launches{0};
+void note_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+}  // namespace vct
+
+namespace {
+
+thread_local std::string g_err;
+
+vct_status fail(vct_status s, const std::string& msg) {
+    g_err = msg;
+    return s;
+}
+
+#define VCT_CUDA(expr)                                                                      \
+    do {                                                                                    \
+        cudaError_t e_ = (expr);                                                            \
+        if (e_ != cudaSuccess) return fail(VCT_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define VCT_CHECK_LAUNCH(what)                                                               \
+    do {                                                                                     \
+        cudaError_t e_ = cudaGetLastError();                                                 \
+        if (e_ != cudaSuccess) return fail(VCT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Makes the context's device current for the duration of a call and
+// restores the caller's device afterwards.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceScope(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) err = cudaSetDevice(dev);
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ----------------------------------------------------------- glm-style math
+struct hf3 {
+    float x, y, z;
+};
+inline hf3 hsub(hf3 a, hf3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline float hdot(hf3 a, hf3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline hf3 hcross(hf3 a, hf3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline hf3 hnorm(hf3 v) {
+    float inv = 1.0f / std::sqrt(hdot(v, v));
+    return {v.x * inv, v.y * inv, v.z * inv};
+}
+
+void mat_identity(float* m) {
+    for (int i = 0; i < 16; ++i) m[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+}
+// glm::lookAt (right handed).
+void look_at(hf3 eye, hf3 center, hf3 up, float* m) {
+    hf3 f = hnorm(hsub(center, eye));
+    hf3 s = hnorm(hcross(f, up));
+    hf3 u = hcross(s, f);
+    mat_identity(m);
+    m[0] = s.x;
+    m[4] = s.y;
+    m[8] = s.z;
+    m[1] = u.x;
+    m[5] = u.y;
+    m[9] = u.z;
+    m[2] = -f.x;
+    m[6] = -f.y;
+    m[10] = -f.z;
+    m[12] = -hdot(s, eye);
+    m[13] = -hdot(u, eye);
+    m[14] = hdot(f, eye);
+}
+// glm::ortho (depth range -1..1).
+void ortho(float l, float r, float b, float t, float n, float f, float* m) {
+    mat_identity(m);
+    m[0] = 2.0f / (r - l);
+    m[5] = 2.0f / (t - b);
+    m[10] = -2.0f / (f - n);
+    m[12] = -(r + l) / (r - l);
+    m[13] = -(t + b) / (t - b);
+    m[14] = -(f + n) / (f - n);
+}
+// glm operator* for mat4: column c of a*b = sum_k a[k] * b[c][k], in order.
+void mat_mul(const float* a, const float* b, float* out) {
+    float r[16];
+    for (int c = 0; c < 4; ++c)
+        for (int row = 0; row < 4; ++row)
+            r[c * 4 + row] = a[row] * b[c * 4 + 0] + a[4 + row] * b[c * 4 + 1] + a[8 + row] * b[c * 4 + 2] +
+                             a[12 + row] * b[c * 4 + 3];
+    std::memcpy(out, r, sizeof r);
+}
+
+// src/Application.cpp:689-692.
+void voxel_mvp(const vct_config& c, float* out) {
+    float proj[16], view[16];
+    ortho(c.voxel_min[0], c.voxel_max[0], c.voxel_min[1], c.voxel_max[1], 0.0f, c.voxel_max[2] - c.voxel_min[2], proj);
+    hf3 ctr = {c.voxel_center[0], c.voxel_center[1], c.voxel_center[2]};
+    hf3 ex = {c.voxel_max[0] + ctr.x, 0.0f + ctr.y, 0.0f + ctr.z};
+    hf3 ey = {0.0f + ctr.x, c.voxel_max[1] + ctr.y, 0.0f + ctr.z};
+    hf3 ez = {0.0f + ctr.x, 0.0f + ctr.y, c.voxel_max[2] + ctr.z};
+    look_at(ex, ctr, {0, 1, 0}, view);
+    mat_mul(proj, view, out);
+    look_at(ey, ctr, {0, 0, -1}, view);
+    mat_mul(proj, view, out + 16);
+    look_at(ez, ctr, {0, 1, 0}, view);
+    mat_mul(proj, view, out + 32);
+}
+
+bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+int ilog2(int v) {
+    int l = 0;
+    while ((1 << (l + 1)) <= v) ++l;
+    return l;
+}
+
+vct_status validate_config(const vct_config* c) {
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "config is NULL");
+    if (!is_pow2(c->voxel_dim) || c->voxel_dim < 16 || c->voxel_dim > 1024)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "voxel_dim must be a power of two in [16, 1024]");
+    for (int k = 0; k < 3; ++k) {
+        if (!std::isfinite(c->voxel_min[k]) || !std::isfinite(c->voxel_max[k]) || !std::isfinite(c->voxel_center[k]))
+            return fail(VCT_ERR_INVALID_ARGUMENT, "volume bounds must be finite");
+        if (!(c->voxel_max[k] > c->voxel_min[k])) return fail(VCT_ERR_INVALID_ARGUMENT, "voxel_max must exceed voxel_min");
+        // voxelize.frag maps fragments to voxels through the per-axis ortho
+        // projections; that equals voxelLinearPosition only for a symmetric
+        // cubic volume (min = -max, equal extents).
+        if (c->voxel_min[k] != -c->voxel_max[k])
+            return fail(VCT_ERR_INVALID_ARGUMENT, "volume must be symmetric: voxel_min = -voxel_max");
+        if (c->voxel_max[k] != c->voxel_max[0]) return fail(VCT_ERR_INVALID_ARGUMENT, "volume must be cubic");
+    }
+    if (c->voxel_levels < 0) return fail(VCT_ERR_INVALID_ARGUMENT, "voxel_levels must be >= 0");
+    return VCT_OK;
+}
+
+vct_status validate_params(const vct_params* p) {
+    if (!p) return fail(VCT_ERR_INVALID_ARGUMENT, "params is NULL");
+    const vct_cone_settings* cs[2] = {&p->diffuse_cone, &p->specular_cone};
+    for (auto c : cs) {
+        if (c->steps < 0 || c->steps > 4096) return fail(VCT_ERR_INVALID_ARGUMENT, "cone steps must be in [0, 4096]");
+        if (!(c->cone_angle > 0.0f) || !(c->cone_angle < 3.14159f))
+            return fail(VCT_ERR_INVALID_ARGUMENT, "cone angle must be in (0, pi)");
+        if (!std::isfinite(c->bias) || !std::isfinite(c->lod_offset) || !(c->cone_initial_height > 0.0f))
+            return fail(VCT_ERR_INVALID_ARGUMENT, "cone bias/lod offset must be finite, initial height > 0");
+    }
+    if (p->trace_filter != VCT_FILTER_SOFTWARE && p->trace_filter != VCT_FILTER_HARDWARE)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "trace_filter must be VCT_FILTER_SOFTWARE or VCT_FILTER_HARDWARE");
+    if (p->axis_override < -1 || p->axis_override > 2) return fail(VCT_ERR_INVALID_ARGUMENT, "axis_override in [-1, 2]");
+    if (!std::isfinite(p->voxel_set_opacity) || !std::isfinite(p->temporal_decay))
+        return fail(VCT_ERR_INVALID_ARGUMENT, "opacity/decay must be finite");
+    return VCT_OK;
+}
+
+vct_status validate_tris(const vct_triangles* t) {
+    if (!t) return fail(VCT_ERR_INVALID_ARGUMENT, "triangles is NULL");
+    if (t->count < 0 || t->count > 0x7fffffffLL) return fail(VCT_ERR_INVALID_ARGUMENT, "triangle count out of range");
+    if (t->count > 0 && (!t->positions_dev || !t->normals_dev || !t->albedo_dev))
+        return fail(VCT_ERR_INVALID_ARGUMENT, "triangle arrays must be non-NULL");
+    return VCT_OK;
+}
+
+vct_status validate_shadow(const vct_shadow_desc* s, bool needed) {
+    if (!needed) return VCT_OK;
+    if (!s) return fail(VCT_ERR_INVALID_ARGUMENT, "shadow description is NULL");
+    if (!s->shadowmap_dev || s->width <= 0 || s->height <= 0 || s->width > 32768 || s->height > 32768)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "shadow map pointer/size invalid");
+    return VCT_OK;
+}
+
+vct_status validate_lights(const vct_light* lights, int n, bool* needs_shadow) {
+    *needs_shadow = false;
+    if (n < 0 || n > VCT_MAX_LIGHTS) return fail(VCT_ERR_INVALID_ARGUMENT, "n_lights must be in [0, 16]");
+    if (n > 0 && !lights) return fail(VCT_ERR_INVALID_ARGUMENT, "lights is NULL");
+    for (int i = 0; i < n; ++i) {
+        if (lights[i].type > 1u) return fail(VCT_ERR_INVALID_ARGUMENT, "light type must be 0 (point) or 1 (directional)");
+        if (lights[i].enabled && lights[i].shadow_caster) *needs_shadow = true;
+    }
+    return VCT_OK;
+}
+
+vct_status validate_gbuffer(const vct_gbuffer* g) {
+    if (!g) return fail(VCT_ERR_INVALID_ARGUMENT, "gbuffer is NULL");
+    if (g->width <= 0 || g->height <= 0 || g->width > 16384 || g->height > 16384)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "gbuffer size out of range");
+    if (!g->position_dev || !g->normal_dev || !g->albedo_dev)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "gbuffer planes must be non-NULL");
+    return VCT_OK;
+}
+
+uint2* level_ptr(uint2* chain, const vct_ctx* ctx, int l) { return chain + ctx->level_off[l]; }
+
+f3 to_f3(const float* p) { return {p[0], p[1], p[2]}; }
+
+vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lights, int n,
+                      const vct_shadow_desc* sh, AccumParams& P) {
+    std::memset(&P, 0, sizeof P);
+    P.pos = t->positions_dev;
+    P.nrm = t->normals_dev;
+    P.albedo = t->albedo_dev;
+    P.ntri = t->count;
+    P.dim = ctx->dim;
+    P.lighting = ctx->params.voxelize_lighting;
+    P.axis_override = ctx->params.axis_override;
+    P.nlights = n;
+    for (int i = 0; i < n; ++i) {
+        LightDev& L = P.lights[i];
+        L.position = to_f3(lights[i].position);
+        L.direction = to_f3(lights[i].direction);
+        L.color = to_f3(lights[i].color);
+        L.range = lights[i].range;
+        L.intensity = lights[i].intensity;
+        L.enabled = lights[i].enabled;
+        L.shadow_caster = lights[i].shadow_caster;
+        L.type = lights[i].type;
+    }
+    std::memcpy(P.mvp, ctx->mvp, sizeof P.mvp);
+    if (sh) {
+        std::memcpy(P.ls, sh->ls, sizeof P.ls);
+        P.shadowmap = sh->shadowmap_dev;
+        P.sw = sh->width;
+        P.sh = sh->height;
+    }
+    P.count = ctx->count;
+    P.sums = ctx->sums;
+    P.stats = ctx->stats;
+    P.num_sms = ctx->num_sms;
+    return VCT_OK;
+}
+
+void fill_norm(vct_ctx* ctx, NormalizeParams& P) {
+    P.dim = ctx->dim;
+    P.opacity = ctx->params.voxel_set_opacity;
+    P.temporal = ctx->params.temporal_filter;
+    P.decay = ctx->params.temporal_decay;
+    P.count = ctx->count;
+    P.sums = ctx->sums;
+    P.color = ctx->color;
+    P.normal = ctx->normal;
+    P.radiance = ctx->radiance;
+    P.stats = ctx->stats;
+    P.num_sms = ctx->num_sms;
+}
+
+// voxelIndex(p) of common.glsl:62-64 with warping off: dim * (p - center - min) / (max - min).
+f3 voxel_index_host(const vct_config& c, int dim, const float* p) {
+    float out[3];
+    for (int k = 0; k < 3; ++k) {
+        float ext = c.voxel_max[k] - c.voxel_min[k];
+        float tc = ((p[k] - c.voxel_center[k]) - c.voxel_min[k]) / ext;
+        out[k] = tc * (float)dim;
+    }
+    return {out[0], out[1], out[2]};
+}
+
+void fill_inject(vct_ctx* ctx, const vct_shadow_desc* s, InjectParams& P) {
+    std::memset(&P, 0, sizeof P);
+    P.dim = ctx->dim;
+    P.shadowmap = s->shadowmap_dev;
+    P.sw = s->width;
+    P.sh = s->height;
+    // The dispatch covers ceil(size/16)*16 invocations and the bounds test in
+    // injectRadiance.comp:44 is `>`, so index == size also runs when size is
+    // not a multiple of 16.
+    P.nx = std::min(((s->width + 15) / 16) * 16, s->width + 1);
+    P.ny = std::min(((s->height + 15) / 16) * 16, s->height + 1);
+    std::memcpy(P.ls_inverse, s->ls_inverse, sizeof P.ls_inverse);
+    P.vmin = to_f3(ctx->cfg.voxel_min);
+    P.vmax = to_f3(ctx->cfg.voxel_max);
+    P.vcenter = to_f3(ctx->cfg.voxel_center);
+    P.light_vox = voxel_index_host(ctx->cfg, ctx->dim, s->light_pos);
+    P.light_int = to_f3(s->light_int);
+    P.lighting = ctx->params.radiance_lighting;
+    P.dilate = ctx->params.radiance_dilate;
+    P.color = ctx->color;
+    P.normal = ctx->normal;
+    P.radiance = ctx->radiance;
+    P.lit = ctx->lit;
+}
+
+MipLevels mip_levels(vct_ctx* ctx, uint2* chain, int levels) {
+    MipLevels M;
+    std::memset(&M, 0, sizeof M);
+    M.dim = ctx->dim;
+    M.levels = levels;
+    for (int l = 0; l < levels; ++l) M.level[l] = level_ptr(chain, ctx, l);
+    return M;
+}
+
+vct_status ensure_texture(vct_ctx* ctx) {
+    if (ctx->tex_array) return VCT_OK;
+    cudaChannelFormatDesc desc = cudaCreateChannelDescHalf4();
+    cudaExtent ext = make_cudaExtent(ctx->dim, ctx->dim, ctx->dim);
+    VCT_CUDA(cudaMallocMipmappedArray(&ctx->tex_array, &desc, ext, ctx->levels, 0));
+    cudaResourceDesc res;
+    std::memset(&res, 0, sizeof res);
+    res.resType = cudaResourceTypeMipmappedArray;
+    res.res.mipmap.mipmap = ctx->tex_array;
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof td);
+    for (int k = 0; k < 3; ++k) td.addressMode[k] = cudaAddressModeBorder;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    td.mipmapFilterMode = cudaFilterModeLinear;
+    td.minMipmapLevelClamp = 0.0f;
+    td.maxMipmapLevelClamp = (float)(ctx->levels - 1);
+    td.maxAnisotropy = 1;
+    VCT_CUDA(cudaCreateTextureObject(&ctx->tex, &res, &td, nullptr));
+    return VCT_OK;
+}
+
+// Copies the linear radiance chain into the mip-mapped array of the
+// texture-unit sampler.
+vct_status refresh_texture(vct_ctx* ctx, cudaStream_t s) {
+    vct_status st = ensure_texture(ctx);
+    if (st != VCT_OK) return st;
+    for (int l = 0; l < ctx->levels; ++l) {
+        cudaArray_t arr;
+        VCT_CUDA(cudaGetMipmappedArrayLevel(&arr, ctx->tex_array, l));
+        int S = ctx->dim >> l;
+        cudaMemcpy3DParms p;
+        std::memset(&p, 0, sizeof p);
+        p.srcPtr = make_cudaPitchedPtr(level_ptr(ctx->radiance, ctx, l), (size_t)S * 8, S, S);
+        p.dstArray = arr;
+        p.extent = make_cudaExtent(S, S, S);
+        p.kind = cudaMemcpyDeviceToDevice;
+        VCT_CUDA(cudaMemcpy3DAsync(&p, s));
+    }
+    ctx->tex_ready = true;
+    return VCT_OK;
+}
+
+vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], const vct_trace_out* out,
+                      TraceParams& P) {
+    std::memset(&P, 0, sizeof P);
+    P.gpos = reinterpret_cast<const float4*>(g->position_dev);
+    P.gnrm = reinterpret_cast<const float4*>(g->normal_dev);
+    P.galb = reinterpret_cast<const float4*>(g->albedo_dev);
+    P.width = g->width;
+    P.height = g->height;
+    P.irradiance = reinterpret_cast<float4*>(out->irradiance_dev);
+    P.specular = reinterpret_cast<float4*>(out->specular_dev);
+    P.color = reinterpret_cast<float4*>(out->color_dev);
+    P.samples = out->sample_count_dev;
+    P.chain = ctx->radiance;
+    for (int l = 0; l < ctx->levels; ++l) P.level_off[l] = ctx->level_off[l];
+    P.dim = ctx->dim;
+    P.levels = ctx->levels;
+    P.vmin = to_f3(ctx->cfg.voxel_min);
+    P.vmax = to_f3(ctx->cfg.voxel_max);
+    P.vcenter = to_f3(ctx->cfg.voxel_center);
+    P.eye = to_f3(eye);
+    const vct_params& pr = ctx->params;
+    P.diffuse = pr.diffuse_cone;
+    P.specular_cone = pr.specular_cone;
+    P.enable_indirect = pr.enable_indirect;
+    P.enable_reflections = pr.enable_reflections;
+    P.draw_occlusion = pr.draw_occlusion;
+    P.enable_postprocess = pr.enable_postprocess;
+    P.ambient_scale = pr.ambient_scale;
+    P.reflect_scale = pr.reflect_scale;
+    P.max_distance = pr.max_distance > 0.0f ? pr.max_distance : std::sqrt(3.0f);
+    P.ref_tbn_quirk = pr.ref_tbn_quirk;
+    P.hardware = pr.trace_filter == VCT_FILTER_HARDWARE;
+    P.tex = ctx->tex;
+    for (auto p : {(const void*)g->position_dev, (const void*)g->normal_dev, (const void*)g->albedo_dev,
+                   (const void*)out->irradiance_dev, (const void*)out->specular_dev, (const void*)out->color_dev})
+        if (reinterpret_cast<uintptr_t>(p) % 16 != 0) return fail(VCT_ERR_INVALID_ARGUMENT, "float4 planes must be 16-byte aligned");
+    return VCT_OK;
+}
+
+}  // namespace
+
+// ==================================================================== API
+extern "C" {
+
+int32_t vct_abi_version(void) { return VCT_ABI_VERSION; }
+
+const char* vct_status_string(vct_status s) {
+    switch (s) {
+        case VCT_OK: return "ok";
+        case VCT_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case VCT_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case VCT_ERR_CUDA: return "CUDA error";
+        case VCT_ERR_STATE: return "invalid call order";
+        case VCT_ERR_TIMEOUT: return "device wait timed out";
+        case VCT_ERR_UNSUPPORTED: return "unsupported";
+        case VCT_ERR_OVERFLOW: return "accumulator overflow";
+    }
+    return "unknown status";
+}
+
+const char* vct_last_error(void) { return g_err.c_str(); }
+
+void vct_struct_sizes(int64_t* light, int64_t* config, int64_t* params, int64_t* triangles, int64_t* gbuffer,
+                      int64_t* trace_out, int64_t* shadow_desc, int64_t* stats) {
+    if (light) *light = sizeof(vct_light);
+    if (config) *config = sizeof(vct_config);
+    if (params) *params = sizeof(vct_params);
+    if (triangles) *triangles = sizeof(vct_triangles);
+    if (gbuffer) *gbuffer = sizeof(vct_gbuffer);
+    if (trace_out) *trace_out = sizeof(vct_trace_out);
+    if (shadow_desc) *shadow_desc = sizeof(vct_shadow_desc);
+    if (stats) *stats = sizeof(vct_stats);
+}
+
+void vct_default_params(vct_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    const float deg = 3.14159265358979323846f / 180.0f;
+    p->voxelize_lighting = 1;
+    p->axis_override = -1;
+    p->voxel_set_opacity = 0.5f;
+    p->temporal_filter = 0;
+    p->temporal_decay = 0.8f;
+    p->radiance_lighting = 0;
+    p->radiance_dilate = 0;
+    p->diffuse_cone = {16, 60.0f * deg, 1.0f, 1.0f, 0.5f};
+    p->specular_cone = {32, 30.0f * deg, 1.7f, 0.5f, 0.1f};
+    p->enable_indirect = 1;
+    p->enable_reflections = 1;
+    p->draw_occlusion = 1;
+    p->enable_postprocess = 1;
+    p->ambient_scale = 1.0f;
+    p->reflect_scale = 1.0f;
+    p->max_distance = 0.0f;
+    p->ref_tbn_quirk = 0;
+    p->trace_filter = VCT_FILTER_SOFTWARE;
+}
+
+vct_status vct_voxel_mvp(const vct_config* cfg, float mvp_xyz[48]) {
+    vct_status s = validate_config(cfg);
+    if (s != VCT_OK) return s;
+    if (!mvp_xyz) return fail(VCT_ERR_INVALID_ARGUMENT, "output is NULL");
+    voxel_mvp(*cfg, mvp_xyz);
+    return VCT_OK;
+}
+
+vct_status vct_create(const vct_config* cfg, vct_ctx** out) {
+    if (!out) return fail(VCT_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    vct_status s = validate_config(cfg);
+    if (s != VCT_OK) return s;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(VCT_ERR_CUDA, "no CUDA device available");
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) return fail(VCT_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    DeviceScope ds(cfg->device);
+    VCT_CUDA(ds.err);
+    vct_ctx* c = new (std::nothrow) vct_ctx;
+    if (!c) return fail(VCT_ERR_OUT_OF_MEMORY, "host allocation failed");
+    c->cfg = *cfg;
+    c->dim = cfg->voxel_dim;
+    int maxl = ilog2(c->dim) + 1;
+    c->levels = cfg->voxel_levels == 0 ? maxl : std::min(std::max(cfg->voxel_levels, 1), maxl);
+    c->color_levels = (cfg->flags & VCT_CONFIG_COLOR_MIPS) ? c->levels : 1;
+    c->device = cfg->device;
+    c->nv = (long long)c->dim * c->dim * c->dim;
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    vct_default_params(&c->params);
+    voxel_mvp(*cfg, c->mvp);
+    long long off = 0;
+    for (int l = 0; l < c->levels; ++l) {
+        c->level_off[l] = off;
+        long long S = c->dim >> l;
+        off += S * S * S;
+    }
+    long long chain_vox = off;
+    long long color_vox = c->color_levels > 1 ? chain_vox : c->nv;
+    struct Alloc {
+        void** p;
+        size_t bytes;
+    } allocs[] = {
+        {(void**)&c->count, (size_t)c->nv * 4},
+        {(void**)&c->sums, (size_t)c->nv * 4 * 6},
+        {(void**)&c->lit, (size_t)((c->nv + 31) / 32) * 4},
+        {(void**)&c->color, (size_t)color_vox * 8},
+        {(void**)&c->normal, (size_t)c->nv * 8},
+        {(void**)&c->radiance, (size_t)chain_vox * 8},
+        {(void**)&c->stats, sizeof(StatsDev)},
+    };
+    for (auto& a : allocs) {
+        cudaError_t e = cudaMalloc(a.p, a.bytes);
+        if (e == cudaSuccess) e = cudaMemset(*a.p, 0, a.bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            std::string msg = std::string("device allocation failed: ") + cudaGetErrorString(e);
+            vct_destroy(c);
+            return fail(e == cudaErrorMemoryAllocation ? VCT_ERR_OUT_OF_MEMORY : VCT_ERR_CUDA, msg);
+        }
+    }
+    *out = c;
+    return VCT_OK;
+}
+
+vct_status vct_destroy(vct_ctx* c) {
+    if (!c) return VCT_OK;
+    DeviceScope ds(c->device);
+    for (auto e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->tex) cudaDestroyTextureObject(c->tex);
+    if (c->tex_array) cudaFreeMipmappedArray(c->tex_array);
+    void* ptrs[] = {c->count, c->sums, c->lit, c->color, c->normal, c->radiance, c->stats};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete c;
+    return VCT_OK;
+}
+
+vct_status vct_set_params(vct_ctx* c, const vct_params* p) {
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    vct_status s = validate_params(p);
+    if (s != VCT_OK) return s;
+    c->params = *p;
+    return VCT_OK;
+}
+
+vct_status vct_get_params(const vct_ctx* c, vct_params* out) {
+    if (!c || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = c->params;
+    return VCT_OK;
+}
+
+vct_status vct_get_config(const vct_ctx* c, vct_config* out) {
+    if (!c || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = c->cfg;
+    out->voxel_levels = c->levels;
+    return VCT_OK;
+}
+
+vct_status vct_volume_level(const vct_ctx* c, int32_t volume, int32_t level, const uint16_t** data, int32_t* dim) {
+    if (!c || !data) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    uint2* base = nullptr;
+    int nl = 0;
+    switch (volume) {
+        case VCT_VOLUME_COLOR: base = c->color; nl = c->color_levels; break;
+        case VCT_VOLUME_NORMAL: base = c->normal; nl = 1; break;
+        case VCT_VOLUME_RADIANCE: base = c->radiance; nl = c->levels; break;
+        default: return fail(VCT_ERR_INVALID_ARGUMENT, "unknown volume");
+    }
+    if (level < 0 || level >= nl) return fail(VCT_ERR_INVALID_ARGUMENT, "level out of range for this volume");
+    *data = reinterpret_cast<const uint16_t*>(base + c->level_off[level]);
+    if (dim) *dim = c->dim >> level;
+    return VCT_OK;
+}
+
+vct_status vct_accumulators(const vct_ctx* c, const uint32_t** count, const uint32_t** sums) {
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (count) *count = c->count;
+    if (sums) *sums = c->sums;
+    return VCT_OK;
+}
+
+vct_status vct_voxelize_accumulate(vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n,
+                                   const vct_shadow_desc* shadow, const float eye[3], void* stream) {
+    (void)eye;  // only used by the warped-voxel modes
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    vct_status s = validate_tris(tris);
+    if (s != VCT_OK) return s;
+    bool need_shadow = false;
+    if ((s = validate_lights(lights, n, &need_shadow)) != VCT_OK) return s;
+    need_shadow = need_shadow && c->params.voxelize_lighting;
+    if ((s = validate_shadow(shadow, need_shadow)) != VCT_OK) return s;
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    cudaStream_t st = as_stream(stream);
+    if (c->stats_reset_pending) {
+        VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
+        c->stats_reset_pending = false;
+    }
+    AccumParams P;
+    fill_accum(c, tris, lights, n, need_shadow ? shadow : nullptr, P);
+    launch_accumulate(P, st);
+    VCT_CHECK_LAUNCH("voxelize accumulate");
+    c->radiance_ready = false;
+    c->mips_ready = false;
+    return VCT_OK;
+}
+
+vct_status vct_normalize(vct_ctx* c, void* stream) {
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    cudaStream_t st = as_stream(stream);
+    if (c->stats_reset_pending) VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
+    NormalizeParams P;
+    fill_norm(c, P);
+    launch_normalize(P, st);
+    VCT_CHECK_LAUNCH("normalize");
+    c->stats_reset_pending = true;
+    c->radiance_ready = true;
+    c->mips_ready = false;
+    return VCT_OK;
+}
+
+vct_status vct_clear_accumulators(vct_ctx* c, void* stream) {
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    cudaStream_t st = as_stream(stream);
+    VCT_CUDA(cudaMemsetAsync(c->count, 0, (size_t)c->nv * 4, st));
+    VCT_CUDA(cudaMemsetAsync(c->sums, 0, (size_t)c->nv * 24, st));
+    c->stats_reset_pending = true;
+    return VCT_OK;
+}
+
+vct_status vct_voxelize(vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n,
+                        const vct_shadow_desc* shadow, const float eye[3], void* stream) {
+    vct_status s = vct_voxelize_accumulate(c, tris, lights, n, shadow, eye, stream);
+    if (s != VCT_OK) return s;
+    return vct_normalize(c, stream);
+}
+
+vct_status vct_inject(vct_ctx* c, const vct_shadow_desc* shadow, const float eye[3], void* stream) {
+    (void)eye;
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    vct_status s = validate_shadow(shadow, true);
+    if (s != VCT_OK) return s;
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    InjectParams P;
+    fill_inject(c, shadow, P);
+    launch_inject(P, as_stream(stream));
+    VCT_CHECK_LAUNCH("inject");
+    c->mips_ready = false;
+    return VCT_OK;
+}
+
+vct_status vct_build_mips(vct_ctx* c, int32_t volume, void* stream) {
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    cudaStream_t st = as_stream(stream);
+    if (volume == VCT_VOLUME_RADIANCE) {
+        launch_mips(mip_levels(c, c->radiance, c->levels), 0, st);
+        VCT_CHECK_LAUNCH("build mips");
+        if (c->params.trace_filter == VCT_FILTER_HARDWARE) {
+            vct_status s = refresh_texture(c, st);
+            if (s != VCT_OK) return s;
+        }
+        c->mips_ready = true;
+        return VCT_OK;
+    }
+    if (volume == VCT_VOLUME_COLOR) {
+        if (c->color_levels < 2) return fail(VCT_ERR_UNSUPPORTED, "context created without VCT_CONFIG_COLOR_MIPS");
+        launch_mips(mip_levels(c, c->color, c->color_levels), 0, st);
+        VCT_CHECK_LAUNCH("build colour mips");
+        return VCT_OK;
+    }
+    return fail(VCT_ERR_INVALID_ARGUMENT, "volume must be VCT_VOLUME_RADIANCE or VCT_VOLUME_COLOR");
+}
+
+vct_status vct_trace(vct_ctx* c, const vct_gbuffer* g, const float eye[3], const vct_trace_out* out, void* stream) {
+    if (!c || !eye || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    vct_status s = validate_gbuffer(g);
+    if (s != VCT_OK) return s;
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    cudaStream_t st = as_stream(stream);
+    if (c->params.trace_filter == VCT_FILTER_HARDWARE && !c->tex_ready) {
+        if ((s = refresh_texture(c, st)) != VCT_OK) return s;
+    }
+    TraceParams P;
+    if ((s = fill_trace(c, g, eye, out, P)) != VCT_OK) return s;
+    launch_trace(P, st);
+    VCT_CHECK_LAUNCH("trace");
+    return VCT_OK;
+}
+
+vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n,
+                     const vct_shadow_desc* shadow, const float eye[3], const vct_gbuffer* g,
+                     const vct_trace_out* out, void* stream) {
+    if (!c || !eye || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    vct_status s = validate_tris(tris);
+    if (s != VCT_OK) return s;
+    bool need_shadow = false;
+    if ((s = validate_lights(lights, n, &need_shadow)) != VCT_OK) return s;
+    if ((s = validate_shadow(shadow, true)) != VCT_OK) return s;
+    if ((s = validate_gbuffer(g)) != VCT_OK) return s;
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    cudaStream_t st = as_stream(stream);
+    const bool timed = c->timers_on;
+    if (timed) VCT_CUDA(cudaEventRecord(c->ev[0], st));
+    VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
+    VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, st));
+    AccumParams A;
+    fill_accum(c, tris, lights, n, shadow, A);
+    launch_accumulate(A, st);
+    VCT_CHECK_LAUNCH("frame: accumulate");
+    if (timed) VCT_CUDA(cudaEventRecord(c->ev[1], st));
+    InjectParams I;
+    fill_inject(c, shadow, I);
+    launch_inject_mark(I, st);
+    VCT_CHECK_LAUNCH("frame: inject mark");
+    if (timed) VCT_CUDA(cudaEventRecord(c->ev[2], st));
+    ResolveParams R;
+    std::memset(&R, 0, sizeof R);
+    fill_norm(c, R.norm);
+    R.lighting = c->params.radiance_lighting;
+    R.dilate = c->params.radiance_dilate;
+    R.light_vox = I.light_vox;
+    R.light_int = I.light_int;
+    R.lit = c->lit;
+    R.mip_levels = std::min(4, c->levels - 1);
+    for (int l = 0; l <= R.mip_levels; ++l) R.radiance_levels[l] = level_ptr(c->radiance, c, l);
+    launch_resolve(R, st);
+    VCT_CHECK_LAUNCH("frame: resolve");
+    if (c->levels > 5) {
+        launch_mips(mip_levels(c, c->radiance, c->levels), 4, st);
+        VCT_CHECK_LAUNCH("frame: coarse mips");
+    }
+    c->stats_reset_pending = true;
+    c->radiance_ready = true;
+    c->mips_ready = true;
+    if (c->params.trace_filter == VCT_FILTER_HARDWARE) {
+        if ((s = refresh_texture(c, st)) != VCT_OK) return s;
+    }
+    if (timed) VCT_CUDA(cudaEventRecord(c->ev[3], st));
+    TraceParams T;
+    if ((s = fill_trace(c, g, eye, out, T)) != VCT_OK) return s;
+    launch_trace(T, st);
+    VCT_CHECK_LAUNCH("frame: trace");
+    if (timed) {
+        VCT_CUDA(cudaEventRecord(c->ev[4], st));
+        c->timers_recorded = true;
+    }
+    return VCT_OK;
+}
+
+vct_status vct_enable_timers(vct_ctx* c, int32_t enable) {
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    if (enable && !c->ev[0]) {
+        for (auto& e : c->ev) VCT_CUDA(cudaEventCreate(&e));
+    }
+    c->timers_on = enable != 0;
+    c->timers_recorded = false;
+    return VCT_OK;
+}
+
+vct_status vct_get_timers(vct_ctx* c, vct_timers* out) {
+    if (!c || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!c->timers_recorded) return fail(VCT_ERR_STATE, "no timed vct_frame since timers were enabled");
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    VCT_CUDA(cudaEventSynchronize(c->ev[4]));
+    float* dst[5] = {&out->voxelize_ms, &out->radiance_ms, &out->mipmap_ms, &out->render_ms, &out->total_ms};
+    const int a[5] = {0, 1, 2, 3, 0}, b[5] = {1, 2, 3, 4, 4};
+    for (int i = 0; i < 5; ++i) VCT_CUDA(cudaEventElapsedTime(dst[i], c->ev[a[i]], c->ev[b[i]]));
+    return VCT_OK;
+}
+
+uint64_t vct_launch_count(void) { return g_launches.load(); }
+
+vct_status vct_get_stats(vct_ctx* c, vct_stats* out, void* stream) {
+    if (!c || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    StatsDev h;
+    VCT_CUDA(cudaMemcpyAsync(&h, c->stats, sizeof h, cudaMemcpyDeviceToHost, as_stream(stream)));
+    VCT_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    out->total_voxel_fragments = h.total_voxel_fragments;
+    out->unique_voxels = h.unique_voxels;
+    out->max_fragments_per_voxel = h.max_fragments_per_voxel;
+    out->error_flags = h.error_flags;
+    return VCT_OK;
+}
+
+vct_status vct_render_shadowmap(const vct_triangles* tris, const float ls[16], float* depth, int32_t w, int32_t h,
+                                void* stream) {
+    vct_status s = validate_tris(tris);
+    if (s != VCT_OK) return s;
+    if (!ls || !depth || w <= 0 || h <= 0 || w > 32768 || h > 32768)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "shadow map arguments invalid");
+    int dev = 0;
+    VCT_CUDA(cudaGetDevice(&dev));
+    ShadowRasterParams P;
+    std::memset(&P, 0, sizeof P);
+    P.pos = tris->positions_dev;
+    P.ntri = tris->count;
+    std::memcpy(P.ls, ls, sizeof P.ls);
+    P.depth_bits = reinterpret_cast<unsigned int*>(depth);
+    P.w = w;
+    P.h = h;
+    cudaDeviceGetAttribute(&P.num_sms, cudaDevAttrMultiProcessorCount, dev);
+    launch_shadow_raster(P, as_stream(stream));
+    VCT_CHECK_LAUNCH("shadow map");
+    return VCT_OK;
+}
+
+vct_status vct_render_gbuffer(const vct_triangles* tris, const float vp[16], const float eye[3], const float ivp[16],
+                              int32_t w, int32_t h, unsigned long long* keys, float* gpos, float* gnrm, float* galb,
+                              void* stream) {
+    vct_status s = validate_tris(tris);
+    if (s != VCT_OK) return s;
+    if (!vp || !eye || !ivp || !keys || !gpos || !gnrm || !galb || w <= 0 || h <= 0 || w > 16384 || h > 16384)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "gbuffer arguments invalid");
+    int dev = 0;
+    VCT_CUDA(cudaGetDevice(&dev));
+    GbufferRasterParams P;
+    std::memset(&P, 0, sizeof P);
+    P.pos = tris->positions_dev;
+    P.nrm = tris->normals_dev;
+    P.albedo = tris->albedo_dev;
+    P.ntri = tris->count;
+    std::memcpy(P.vp, vp, sizeof P.vp);
+    std::memcpy(P.ivp, ivp, sizeof P.ivp);
+    P.eye = to_f3(eye);
+    P.keys = keys;
+    P.gpos = reinterpret_cast<float4*>(gpos);
+    P.gnrm = reinterpret_cast<float4*>(gnrm);
+    P.galb = reinterpret_cast<float4*>(galb);
+    P.w = w;
+    P.h = h;
+    cudaDeviceGetAttribute(&P.num_sms, cudaDevAttrMultiProcessorCount, dev);
+    launch_gbuffer_raster(P, as_stream(stream));
+    VCT_CHECK_LAUNCH("gbuffer");
+    return VCT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+// Voxel cone tracing: shaders/phong.frag:135-180 (traceCone) and the
+// indirect / specular / composite code of phong.frag:455-520.
+//
+// One thread per pixel; a CTA shades a 16x16 tile and each warp an 8x4
+// sub-tile, so the 32 lanes of a warp march neighbouring cones through
+// neighbouring voxels at the same time (the cone step sequence depends only on
+// the cone parameters, so every lane is at the same mip level each step).
+// A lane leaves its cone at alpha >= 0.95 or on leaving the volume; the warp
+// moves to the next cone once all lanes are done.
+//
+// Two samplers implement textureLod with GL_LINEAR_MIPMAP_LINEAR, LOD clamped
+// to [0, levels-1] and a (0,0,0,0) border (src/Application.cpp:1088-1116):
+//  - software: fp32 trilinear over 8 binary16 texels of two levels read with
+//    8-byte read-only loads from the linear chain (exact GL arithmetic);
+//  - hardware: tex3DLod on a mip-mapped CUDA array (texture units, with
+//    their fixed-point filter weights).
+#include "vct_device.cuh"
+
+namespace vct {
+
+namespace {
+
+__constant__ float kConeDir[6][3] = {{0.f, 1.f, 0.f},
+                                     {0.f, 0.5f, 0.866025f},
+                                     {0.823639f, 0.5f, 0.267617f},
+                                     {0.509037f, 0.5f, -0.700629f},
+                                     {-0.5909037f, 0.5f, -0.700629f},  // sic, phong.frag:475
+                                     {-0.823639f, 0.5f, 0.267617f}};
+__constant__ float kConeWeight[6] = {0.25f, 0.15f, 0.15f, 0.15f, 0.15f, 0.15f};
+
+__device__ __forceinline__ f3 fnormalize(f3 v) { return mul(v, rsqrtf(dot(v, v))); }
+
+__device__ __forceinline__ float4 texel(const uint2* __restrict__ base, int S, int i, int j, int k) {
+    if ((unsigned)i >= (unsigned)S || (unsigned)j >= (unsigned)S || (unsigned)k >= (unsigned)S)
+        return make_float4(0.f, 0.f, 0.f, 0.f);
+    return unpack_h4(__ldg(base + ((k * S + j) * S + i)));
+}
+
+__device__ __forceinline__ float4 lerp4(float4 p, float4 q, float t) {
+    float s = 1.0f - t;
+    return make_float4(p.x * s + q.x * t, p.y * s + q.y * t, p.z * s + q.z * t, p.w * s + q.w * t);
+}
+
+__device__ __forceinline__ float4 trilinear(const TraceParams& P, int l, f3 p) {
+    const int S = P.dim >> l;
+    const uint2* base = P.chain + P.level_off[l];
+    float u = p.x * (float)S - 0.5f, v = p.y * (float)S - 0.5f, w = p.z * (float)S - 0.5f;
+    float fu = floorf(u), fv = floorf(v), fw = floorf(w);
+    float a = u - fu, b = v - fv, c = w - fw;
+    int i = (int)fu, j = (int)fv, k = (int)fw;
+    float4 x00 = lerp4(texel(base, S, i, j, k), texel(base, S, i + 1, j, k), a);
+    float4 x10 = lerp4(texel(base, S, i, j + 1, k), texel(base, S, i + 1, j + 1, k), a);
+    float4 x01 = lerp4(texel(base, S, i, j, k + 1), texel(base, S, i + 1, j, k + 1), a);
+    float4 x11 = lerp4(texel(base, S, i, j + 1, k + 1), texel(base, S, i + 1, j + 1, k + 1), a);
+    return lerp4(lerp4(x00, x10, b), lerp4(x01, x11, b), c);
+}
+
+template <bool HW>
+__device__ __forceinline__ float4 sample_lod(const TraceParams& P, f3 p, float lambda) {
+    if (HW) return tex3DLod<float4>(P.tex, p.x, p.y, p.z, lambda);
+    const int q = P.levels - 1;
+    if (lambda <= 0.0f) {  // magnification: GL_NEAREST on level 0
+        const int S = P.dim;
+        return texel(P.chain, S, (int)floorf(p.x * S), (int)floorf(p.y * S), (int)floorf(p.z * S));
+    }
+    if (lambda >= (float)q) return trilinear(P, q, p);
+    float fl = floorf(lambda);
+    int d1 = (int)fl;
+    float f = lambda - fl;
+    return lerp4(trilinear(P, d1, p), trilinear(P, d1 + 1, p), f);
+}
+
+template <bool HW>
+__device__ float4 trace_cone(const TraceParams& P, f3 pos, f3 n, f3 dir, const vct_cone_settings& c, float maxd,
+                             unsigned& ns) {
+    dir = fnormalize(dir);
+    const float scale = 1.0f / (float)P.dim;
+    const f3 start = add(pos, mul(mul(n, c.bias), scale));
+    const float tanh = tanf(c.cone_angle * 0.5f);
+    float h = c.cone_initial_height;
+    float alpha = 0.0f;
+    f3 col = mk(0.f, 0.f, 0.f);
+    for (int i = 0; i < c.steps && alpha < 0.95f; ++i) {
+        float r = h * tanh;
+        float lod = log2f(fmaxf(1.0f, 2.0f * r));
+        f3 sp = add(start, mul(mul(dir, h), scale));
+        if (sp.x < 0.f || sp.y < 0.f || sp.z < 0.f || sp.x > 1.f || sp.y > 1.f || sp.z > 1.f) break;
+        if (h * scale > maxd) break;
+        float4 s = sample_lod<HW>(P, sp, lod + c.lod_offset);
+        ++ns;
+        float a = 1.0f - alpha;
+        col = add(col, mul(mk(s.x, s.y, s.z), a));
+        alpha += a * s.w;
+        h += r;
+    }
+    return make_float4(col.x, col.y, col.z, alpha);
+}
+
+template <bool HW>
+__global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int x = blockIdx.x * 16 + (wid & 1) * 8 + (lane & 7);
+    const int y = blockIdx.y * 16 + (wid >> 1) * 4 + (lane >> 3);
+    unsigned ns = 0;
+    if (x < P.width && y < P.height) {
+        const long long pix = (long long)y * P.width + x;
+        float4 irr = make_float4(0.f, 0.f, 0.f, 0.f), spc = irr, out = irr;
+        const float4 gp = __ldg(P.gpos + pix);
+        if (gp.w != 0.0f) {
+            const float4 gn = __ldg(P.gnrm + pix);
+            const float4 ga = __ldg(P.galb + pix);
+            const f3 N = fnormalize(mk(gn.x, gn.y, gn.z));
+            f3 rgb;
+            if (P.enable_indirect) {
+                const f3 ext = sub(P.vmax, P.vmin);
+                const f3 vp = mk(((gp.x - P.vcenter.x) - P.vmin.x) / ext.x, ((gp.y - P.vcenter.y) - P.vmin.y) / ext.y,
+                                 ((gp.z - P.vcenter.z) - P.vmin.z) / ext.z);
+                // Orthonormal basis from N: Duff et al. 2017, "Building an
+                // Orthonormal Basis, Revisited" (JCGT 6(1)).
+                const float sgn = N.z >= 0.0f ? 1.0f : -1.0f;
+                const float ca = -1.0f / (sgn + N.z);
+                const float cb = N.x * N.y * ca;
+                const f3 T = mk(1.0f + sgn * N.x * N.x * ca, sgn * cb, -sgn * N.x);
+                const f3 B = mk(cb, sgn + N.y * N.y * ca, -N.y);
+                float4 ind = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+                for (int c = 0; c < 6; ++c) {
+                    const float dx = kConeDir[c][0], dy = kConeDir[c][1], dz = kConeDir[c][2];
+                    f3 d = P.ref_tbn_quirk ? add(add(mul(T, dx), mul(B, dy)), mul(N, dz))
+                                           : sub(add(mul(T, dx), mul(N, dy)), mul(B, dz));
+                    float4 cr = trace_cone<HW>(P, vp, N, d, P.diffuse, P.max_distance, ns);
+                    const float w = kConeWeight[c];
+                    ind.x += w * cr.x;
+                    ind.y += w * cr.y;
+                    ind.z += w * cr.z;
+                    ind.w += w * cr.w;
+                }
+                irr = ind;
+                const float occ = 1.0f - clampf(ind.w, 0.0f, 1.0f);
+                rgb = mk(ind.x, ind.y, ind.z);
+                if (P.enable_reflections) {
+                    const f3 I = sub(mk(gp.x, gp.y, gp.z), P.eye);
+                    const f3 R = sub(I, mul(N, 2.0f * dot(N, I)));
+                    spc = trace_cone<HW>(P, vp, N, R, P.specular_cone, P.max_distance, ns);
+                    rgb = add(rgb, mul(mk(spc.x, spc.y, spc.z), P.reflect_scale));
+                }
+                const float as = P.ambient_scale;
+                rgb = mk(rgb.x * (as * ga.x), rgb.y * (as * ga.y), rgb.z * (as * ga.z));
+                if (P.draw_occlusion) rgb = mul(rgb, occ);
+            } else {
+                rgb = mk(P.ambient_scale * ga.x, P.ambient_scale * ga.y, P.ambient_scale * ga.z);
+            }
+            if (P.enable_postprocess) {
+                const float g = 1.0f / 2.2f;
+                rgb = mk(powf(rgb.x / (rgb.x + 1.0f), g), powf(rgb.y / (rgb.y + 1.0f), g),
+                         powf(rgb.z / (rgb.z + 1.0f), g));
+            }
+            out = make_float4(rgb.x, rgb.y, rgb.z, 1.0f);
+        }
+        if (P.irradiance) P.irradiance[pix] = irr;
+        if (P.specular) P.specular[pix] = spc;
+        if (P.color) P.color[pix] = out;
+    }
+    if (P.samples) {
+        unsigned tot = __reduce_add_sync(0xffffffffu, ns);
+        if (lane == 0 && tot) atomicAdd(P.samples, (unsigned long long)tot);
+    }
+}
+
+}  // namespace
+
+void launch_trace(const TraceParams& P, cudaStream_t s) {
+    dim3 grid((P.width + 15) / 16, (P.height + 15) / 16);
+    if (P.hardware)
+        trace_kernel<true><<<grid, 256, 0, s>>>(P);
+    else
+        trace_kernel<false><<<grid, 256, 0, s>>>(P);
+    note_launches(1);
+}
+
+}  // namespace vct

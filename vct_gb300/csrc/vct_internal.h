@@ -1,0 +1,157 @@
+// Internal declarations shared by the C ABI (capi.cpp) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/vct.h"
+
+namespace vct {
+
+struct f3 {
+    float x, y, z;
+};
+
+struct LightDev {
+    f3 position;
+    f3 direction;
+    f3 color;
+    float range, intensity;
+    uint32_t enabled, shadow_caster, type;
+};
+
+struct StatsDev {
+    uint32_t total_voxel_fragments;
+    uint32_t unique_voxels;
+    uint32_t max_fragments_per_voxel;
+    uint32_t error_flags;
+};
+
+struct AccumParams {
+    const float* pos;
+    const float* nrm;
+    const float* albedo;
+    long long ntri;
+    int dim;
+    int lighting;
+    int axis_override;
+    int nlights;
+    LightDev lights[VCT_MAX_LIGHTS];
+    float mvp[48];
+    float ls[16];
+    const float* shadowmap;
+    int sw, sh;
+    uint32_t* count;
+    uint32_t* sums;
+    StatsDev* stats;
+    int num_sms;
+};
+
+struct NormalizeParams {
+    int dim;
+    float opacity;
+    int temporal;
+    float decay;
+    uint32_t* count;
+    uint32_t* sums;
+    uint2* color;     // level 0 of the colour volume
+    uint2* normal;
+    uint2* radiance;  // level 0 of the radiance chain
+    StatsDev* stats;
+    int num_sms;
+};
+
+struct InjectParams {
+    int dim;
+    const float* shadowmap;
+    int sw, sh;
+    int nx, ny;  // texel threads that pass the shader's bounds test
+    float ls_inverse[16];
+    f3 vmin, vmax, vcenter;
+    f3 light_vox;  // voxelIndex(lightPos)
+    f3 light_int;
+    int lighting, dilate;
+    const uint2* color;
+    const uint2* normal;
+    uint2* radiance;
+    uint32_t* lit;  // fused path: bit mask of voxels the shader would store to
+};
+
+// Fused normalisation + injection resolve + first mip levels (vct_frame).
+struct ResolveParams {
+    NormalizeParams norm;
+    int lighting, dilate;
+    f3 light_vox, light_int;
+    uint32_t* lit;
+    uint2* radiance_levels[5];  // levels 0..4 of the radiance chain
+    int mip_levels;             // number of levels below 0 to write from the brick (<= 4)
+};
+
+struct MipLevels {
+    uint2* level[VCT_MAX_LEVELS];
+    int dim;
+    int levels;
+};
+
+struct TraceParams {
+    const float4* gpos;
+    const float4* gnrm;
+    const float4* galb;
+    int width, height;
+    float4* irradiance;
+    float4* specular;
+    float4* color;
+    unsigned long long* samples;
+    const uint2* chain;
+    long long level_off[VCT_MAX_LEVELS];
+    int dim, levels;
+    f3 vmin, vmax, vcenter, eye;
+    vct_cone_settings diffuse, specular_cone;
+    int enable_indirect, enable_reflections, draw_occlusion, enable_postprocess;
+    float ambient_scale, reflect_scale, max_distance;
+    int ref_tbn_quirk;
+    int hardware;
+    cudaTextureObject_t tex;
+};
+
+struct ShadowRasterParams {
+    const float* pos;
+    long long ntri;
+    float ls[16];
+    unsigned int* depth_bits;
+    int w, h;
+    int num_sms;
+};
+
+struct GbufferRasterParams {
+    const float* pos;
+    const float* nrm;
+    const float* albedo;
+    long long ntri;
+    float vp[16];
+    float ivp[16];
+    f3 eye;
+    unsigned long long* keys;
+    float4* gpos;
+    float4* gnrm;
+    float4* galb;
+    int w, h;
+    int num_sms;
+};
+
+// Counts kernel launches (vct_launch_count).
+void note_launches(int n);
+
+void launch_accumulate(const AccumParams& P, cudaStream_t s);
+void launch_normalize(const NormalizeParams& P, cudaStream_t s);
+void launch_inject(const InjectParams& P, cudaStream_t s);
+void launch_inject_mark(const InjectParams& P, cudaStream_t s);
+void launch_resolve(const ResolveParams& P, cudaStream_t s);
+// Builds levels [first+1, levels) from level `first`.
+void launch_mips(const MipLevels& M, int first, cudaStream_t s);
+void launch_trace(const TraceParams& P, cudaStream_t s);
+void launch_shadow_raster(const ShadowRasterParams& P, cudaStream_t s);
+void launch_gbuffer_raster(const GbufferRasterParams& P, cudaStream_t s);
+void launch_fill_u32(uint32_t* p, uint32_t v, long long n, cudaStream_t s);
+
+}  // namespace vct

@@ -1,0 +1,376 @@
+// Volume passes: normalisation (transferVoxels.comp), radiance injection
+// (injectRadiance.comp), the 2x2x2 box mip chain (filterRadiance.comp) and
+// the fused resolve used by vct_frame.  Compiled with --fmad=false.
+//
+// Layout: RGBA16F voxels (8 bytes, handled as uint2), x fastest.  All passes
+// over the dense grid walk 16^3 bricks so that one CTA owns one brick: its
+// loads and stores are full 128-byte rows along x, and the brick's first
+// four mip levels are reduced in shared memory without touching HBM again.
+#include "vct_device.cuh"
+
+namespace vct {
+
+namespace {
+
+constexpr int kBrick = 16;
+constexpr int kBrickVox = kBrick * kBrick * kBrick;  // 4096
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ void block_stats(StatsDev* stats, uint32_t uniq, uint32_t mx, uint32_t flags) {
+    uniq = __reduce_add_sync(0xffffffffu, uniq);
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    flags = __reduce_or_sync(0xffffffffu, flags);
+    __shared__ uint32_t s_u, s_m, s_f;
+    if (threadIdx.x == 0) {
+        s_u = 0;
+        s_m = 0;
+        s_f = 0;
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&s_u, uniq);
+        atomicMax(&s_m, mx);
+        atomicOr(&s_f, flags);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_u) atomicAdd(&stats->unique_voxels, s_u);
+        if (s_m) atomicMax(&stats->max_fragments_per_voxel, s_m);
+        if (s_f) atomicOr(&stats->error_flags, s_f);
+    }
+}
+
+// transferVoxels.comp:37-69 for one voxel.  Reads and then zeroes its
+// accumulators.  Returns the voxel's alpha (0 when empty).
+struct Normalized {
+    uint2 color, normal;
+    float alpha;
+    uint32_t count;
+};
+
+__device__ __forceinline__ Normalized normalize_voxel(const NormalizeParams& P, long long v, long long NV) {
+    Normalized r;
+    uint32_t c = P.count[v];
+    r.count = c;
+    r.alpha = 0.0f;
+    r.color = make_uint2(0u, 0u);
+    r.normal = make_uint2(0u, 0u);
+    if (c > 0) {
+        float denom = 65535.0f * __uint2float_rn(c);
+        uint32_t s[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            s[k] = P.sums[k * NV + v];
+            P.sums[k * NV + v] = 0u;
+        }
+        P.count[v] = 0u;
+        r.alpha = P.opacity > 0.0f ? P.opacity : 1.0f;
+        r.color = pack_h4(__fdiv_rn(__uint2float_rn(s[0]), denom), __fdiv_rn(__uint2float_rn(s[1]), denom),
+                          __fdiv_rn(__uint2float_rn(s[2]), denom), r.alpha);
+        r.normal = pack_h4(__fdiv_rn(__uint2float_rn(s[3]), denom), __fdiv_rn(__uint2float_rn(s[4]), denom),
+                           __fdiv_rn(__uint2float_rn(s[5]), denom), 1.0f);
+    }
+    return r;
+}
+
+__device__ __forceinline__ uint2 seed_radiance(const NormalizeParams& P, long long v, const Normalized& n) {
+    if (P.temporal) {
+        float w = 1.0f - P.decay;
+        float4 prev = unpack_h4(P.radiance[v]);
+        return pack_h4(prev.x * (1.0f - w) + 0.0f * w, prev.y * (1.0f - w) + 0.0f * w,
+                       prev.z * (1.0f - w) + 0.0f * w, prev.w * (1.0f - w) + n.alpha * w);
+    }
+    return n.count > 0 ? pack_h4(0.0f, 0.0f, 0.0f, n.alpha) : make_uint2(0u, 0u);
+}
+
+__global__ void __launch_bounds__(kThreads) normalize_kernel(const NormalizeParams P) {
+    const long long NV = (long long)P.dim * P.dim * P.dim;
+    uint32_t uniq = 0, mx = 0, flags = 0;
+    for (long long v = (long long)blockIdx.x * kThreads + threadIdx.x; v < NV; v += (long long)gridDim.x * kThreads) {
+        Normalized n = normalize_voxel(P, v, NV);
+        if (n.count > 0) {
+            ++uniq;
+            mx = max(mx, n.count);
+            if (n.count >= VCT_MAX_EXACT_FRAGMENTS) flags |= VCT_STATS_COUNT_OVERFLOW;
+        }
+        P.color[v] = n.color;
+        P.normal[v] = n.normal;
+        P.radiance[v] = seed_radiance(P, v, n);
+    }
+    block_stats(P.stats, uniq, mx, flags);
+}
+
+// injectRadiance.comp:40-56: texel -> voxel.  Returns false when the shader
+// would return early.
+__device__ __forceinline__ bool inject_voxel(const InjectParams& P, int x, int y, int& ix, int& iy, int& iz) {
+    float u = __fdiv_rn((float)x, (float)P.sw), v = __fdiv_rn((float)y, (float)P.sh);
+    float depth = shadow_bilinear(P.shadowmap, P.sw, P.sh, u, v, 0, 0);
+    float ndx = u * 2.0f - 1.0f, ndy = v * 2.0f - 1.0f, ndz = depth * 2.0f - 1.0f;
+    float w[4];
+    mat_vec(P.ls_inverse, ndx, ndy, ndz, 1.0f, w);
+    f3 ext = sub(P.vmax, P.vmin);
+    float N = (float)P.dim;
+    float tx = __fdiv_rn((w[0] - P.vcenter.x) - P.vmin.x, ext.x);
+    float ty = __fdiv_rn((w[1] - P.vcenter.y) - P.vmin.y, ext.y);
+    float tz = __fdiv_rn((w[2] - P.vcenter.z) - P.vmin.z, ext.z);
+    ix = __float2int_rz(tx * N);
+    iy = __float2int_rz(ty * N);
+    iz = __float2int_rz(tz * N);
+    return !(ix >= P.dim || iy >= P.dim || iz >= P.dim || ix < 0 || iy < 0 || iz < 0);
+}
+
+__device__ __forceinline__ bool in_grid(int x, int y, int z, int N) {
+    return x >= 0 && y >= 0 && z >= 0 && x < N && y < N && z < N;
+}
+
+// radianceLighting branch (injectRadiance.comp:222-230).
+__device__ __forceinline__ uint2 light_voxel(f3 light_vox, f3 light_int, uint2 color, uint2 normal, int x, int y,
+                                             int z) {
+    float4 c = unpack_h4(color);
+    float4 nn = unpack_h4(normal);
+    f3 n = mk(2.0f * nn.x - 1.0f, 2.0f * nn.y - 1.0f, 2.0f * nn.z - 1.0f);
+    f3 L = normalize(sub(light_vox, mk((float)x, (float)y, (float)z)));
+    float diff = fmaxf(dot(n, L), 0.0f);
+    return pack_h4((diff * light_int.x) * c.x, (diff * light_int.y) * c.y, (diff * light_int.z) * c.z, c.w);
+}
+
+__constant__ int kDilate[7][3] = {{0, 0, 0}, {0, 0, 1}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {1, 0, 0}, {-1, 0, 0}};
+
+__global__ void __launch_bounds__(kThreads) inject_kernel(const InjectParams P) {
+    int x = blockIdx.x * 16 + (threadIdx.x & 15);
+    int y = blockIdx.y * 16 + (threadIdx.x >> 4);
+    if (x >= P.nx || y >= P.ny) return;
+    int ix, iy, iz;
+    if (!inject_voxel(P, x, y, ix, iy, iz)) return;
+    const int N = P.dim;
+    if (P.dilate) {
+        for (int k = 0; k < 7; ++k) {
+            int a = ix + kDilate[k][0], b = iy + kDilate[k][1], c = iz + kDilate[k][2];
+            if (!in_grid(a, b, c, N)) continue;
+            long long v = ((long long)c * N + b) * N + a;
+            P.radiance[v] = P.color[v];
+        }
+        return;
+    }
+    long long v = ((long long)iz * N + iy) * N + ix;
+    if (P.lighting)
+        P.radiance[v] = light_voxel(P.light_vox, P.light_int, P.color[v], P.normal[v], ix, iy, iz);
+    else
+        P.radiance[v] = P.color[v];
+}
+
+// Fused path: mark the voxels injectRadiance would store to.
+__global__ void __launch_bounds__(kThreads) inject_mark_kernel(const InjectParams P) {
+    int x = blockIdx.x * 16 + (threadIdx.x & 15);
+    int y = blockIdx.y * 16 + (threadIdx.x >> 4);
+    if (x >= P.nx || y >= P.ny) return;
+    int ix, iy, iz;
+    if (!inject_voxel(P, x, y, ix, iy, iz)) return;
+    const int N = P.dim;
+    const int nk = P.dilate ? 7 : 1;
+    for (int k = 0; k < nk; ++k) {
+        int a = ix + kDilate[k][0], b = iy + kDilate[k][1], c = iz + kDilate[k][2];
+        if (!in_grid(a, b, c, N)) continue;
+        long long v = ((long long)c * N + b) * N + a;
+        atomicOr(P.lit + (v >> 5), 1u << (v & 31));
+    }
+}
+
+// -------------------------------------------------------------------- mips
+// filterRadiance.comp BOX2: fp32 sum over the children in the shader's order
+// (z fastest, then y, then x), times 0.125, rounded to binary16.
+__device__ __forceinline__ uint2 box8(const uint2 c[8]) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        float4 t = unpack_h4(c[i]);
+        acc.x += t.x;
+        acc.y += t.y;
+        acc.z += t.z;
+        acc.w += t.w;
+    }
+    return pack_h4(acc.x * 0.125f, acc.y * 0.125f, acc.z * 0.125f, acc.w * 0.125f);
+}
+
+// Reduces a cube of side S (in shared memory, x fastest) into side S/2.
+// Child order index i = ox*4 + oy*2 + oz.
+__device__ __forceinline__ void reduce_level(const uint2* src, uint2* dst, int S, uint2* gdst, int gS, int gx0,
+                                             int gy0, int gz0) {
+    const int D = S / 2;
+    const int n = D * D * D;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        int x = t % D, y = (t / D) % D, z = t / (D * D);
+        uint2 c[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            int ox = i >> 2, oy = (i >> 1) & 1, oz = i & 1;
+            c[i] = src[((2 * z + oz) * S + (2 * y + oy)) * S + (2 * x + ox)];
+        }
+        uint2 r = box8(c);
+        dst[t] = r;
+        gdst[((long long)(gz0 + z) * gS + (gy0 + y)) * gS + (gx0 + x)] = r;
+    }
+}
+
+// One 16^3 brick of level `first` -> up to 4 coarser levels.
+__global__ void __launch_bounds__(kThreads) mip_brick_kernel(const MipLevels M, int first, int nlev) {
+    __shared__ uint2 s0[kBrickVox];
+    __shared__ uint2 s1[kBrickVox / 8];
+    const int S = M.dim >> first;
+    const int bpa = S / kBrick;
+    const int bx = blockIdx.x % bpa, by = (blockIdx.x / bpa) % bpa, bz = blockIdx.x / (bpa * bpa);
+    const uint2* src = M.level[first];
+    for (int t = threadIdx.x; t < kBrickVox; t += kThreads) {
+        int x = t & 15, y = (t >> 4) & 15, z = t >> 8;
+        s0[t] = src[((long long)(bz * kBrick + z) * S + (by * kBrick + y)) * S + (bx * kBrick + x)];
+    }
+    __syncthreads();
+    uint2* a = s0;
+    uint2* b = s1;
+    int side = kBrick;
+    for (int l = 1; l <= nlev; ++l) {
+        int gS = S >> l;
+        int sub = side / 2;
+        reduce_level(a, b, side, M.level[first + l], gS, bx * sub, by * sub, bz * sub);
+        __syncthreads();
+        uint2* t = a;
+        a = b;
+        b = t;
+        side = sub;
+    }
+}
+
+// Small levels (side <= 16): one CTA builds every remaining level.
+__global__ void __launch_bounds__(kThreads) mip_tail_kernel(const MipLevels M, int first) {
+    __shared__ uint2 s0[kBrickVox];
+    __shared__ uint2 s1[kBrickVox / 8];
+    const int S = M.dim >> first;
+    const uint2* src = M.level[first];
+    for (int t = threadIdx.x; t < S * S * S; t += kThreads) s0[t] = src[t];
+    __syncthreads();
+    uint2* a = s0;
+    uint2* b = s1;
+    int side = S;
+    for (int l = first + 1; l < M.levels; ++l) {
+        reduce_level(a, b, side, M.level[l], side / 2, 0, 0, 0);
+        __syncthreads();
+        uint2* t = a;
+        a = b;
+        b = t;
+        side /= 2;
+    }
+}
+
+// Fused: normalisation + injection resolve + radiance levels 1..4 of one
+// 16^3 brick.  Equivalent to normalize_kernel; inject_kernel; the first four
+// filterRadiance dispatches, because the injected value of a voxel depends
+// only on that voxel (idempotent stores).
+__global__ void __launch_bounds__(kThreads) resolve_kernel(const ResolveParams R) {
+    __shared__ uint2 s0[kBrickVox];
+    __shared__ uint2 s1[kBrickVox / 8];
+    const NormalizeParams& P = R.norm;
+    const int N = P.dim;
+    const long long NV = (long long)N * N * N;
+    const int bpa = N / kBrick;
+    const int bx = blockIdx.x % bpa, by = (blockIdx.x / bpa) % bpa, bz = blockIdx.x / (bpa * bpa);
+    uint32_t uniq = 0, mx = 0, flags = 0;
+    for (int t = threadIdx.x; t < kBrickVox; t += kThreads) {
+        int x = bx * kBrick + (t & 15), y = by * kBrick + ((t >> 4) & 15), z = bz * kBrick + (t >> 8);
+        long long v = ((long long)z * N + y) * N + x;
+        Normalized n = normalize_voxel(P, v, NV);
+        if (n.count > 0) {
+            ++uniq;
+            mx = max(mx, n.count);
+            if (n.count >= VCT_MAX_EXACT_FRAGMENTS) flags |= VCT_STATS_COUNT_OVERFLOW;
+        }
+        P.color[v] = n.color;
+        P.normal[v] = n.normal;
+        uint2 rad = seed_radiance(P, v, n);
+        uint32_t word = R.lit[v >> 5];
+        if (word & (1u << (v & 31))) {
+            if (R.lighting && !R.dilate)
+                rad = light_voxel(R.light_vox, R.light_int, n.color, n.normal, x, y, z);
+            else
+                rad = n.color;
+        }
+        P.radiance[v] = rad;
+        s0[t] = rad;
+    }
+    __syncthreads();
+    block_stats(P.stats, uniq, mx, flags);
+    uint2* a = s0;
+    uint2* b = s1;
+    int side = kBrick;
+    for (int l = 1; l <= R.mip_levels; ++l) {
+        int gS = N >> l;
+        int sub = side / 2;
+        reduce_level(a, b, side, R.radiance_levels[l], gS, bx * sub, by * sub, bz * sub);
+        __syncthreads();
+        uint2* t = a;
+        a = b;
+        b = t;
+        side = sub;
+    }
+}
+
+__global__ void fill_u32_kernel(uint32_t* p, uint32_t v, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+}  // namespace
+
+void launch_normalize(const NormalizeParams& P, cudaStream_t s) {
+    long long NV = (long long)P.dim * P.dim * P.dim;
+    long long blocks = (NV + kThreads - 1) / kThreads;
+    long long maxb = (long long)P.num_sms * 16;
+    normalize_kernel<<<(unsigned)(blocks < maxb ? blocks : maxb), kThreads, 0, s>>>(P);
+    note_launches(1);
+}
+
+void launch_inject(const InjectParams& P, cudaStream_t s) {
+    dim3 grid((P.nx + 15) / 16, (P.ny + 15) / 16);
+    inject_kernel<<<grid, kThreads, 0, s>>>(P);
+    note_launches(1);
+}
+
+void launch_inject_mark(const InjectParams& P, cudaStream_t s) {
+    dim3 grid((P.nx + 15) / 16, (P.ny + 15) / 16);
+    inject_mark_kernel<<<grid, kThreads, 0, s>>>(P);
+    note_launches(1);
+}
+
+void launch_resolve(const ResolveParams& R, cudaStream_t s) {
+    int bpa = R.norm.dim / kBrick;
+    resolve_kernel<<<bpa * bpa * bpa, kThreads, 0, s>>>(R);
+    note_launches(1);
+}
+
+void launch_mips(const MipLevels& M, int first, cudaStream_t s) {
+    int l = first;
+    while (l + 1 < M.levels) {
+        int S = M.dim >> l;
+        if (S > kBrick) {
+            int nlev = M.levels - 1 - l;
+            if (nlev > 4) nlev = 4;
+            int bpa = S / kBrick;
+            mip_brick_kernel<<<bpa * bpa * bpa, kThreads, 0, s>>>(M, l, nlev);
+            note_launches(1);
+            l += nlev;
+        } else {
+            mip_tail_kernel<<<1, kThreads, 0, s>>>(M, l);
+            note_launches(1);
+            break;
+        }
+    }
+}
+
+void launch_fill_u32(uint32_t* p, uint32_t v, long long n, cudaStream_t s) {
+    if (n <= 0) return;
+    long long blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    fill_u32_kernel<<<(unsigned)blocks, 256, 0, s>>>(p, v, n);
+    note_launches(1);
+}
+
+}  // namespace vct

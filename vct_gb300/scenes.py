@@ -1,0 +1,289 @@
+"""Seeded synthetic scenes for the VCT hot path.
+
+The reference renders Sponza (missing from its repository); the benchmark
+configurations instead name seeded synthetic scenes, generated here with
+numpy only (deterministic for a given seed):
+
+  cornell  - 5 axis-aligned wall quads (an open-top box, 10 triangles) with a
+             per-wall albedo in [0.1, 0.9] plus a 3x subdivided icosphere
+             (1280 triangles, radius 0.3); 64^3 grid, 7 levels; one
+             directional light from the upper hemisphere; 512^2 shadow map;
+             640x360 G-buffer.
+  large    - 4096 boxes (12 triangles each) and 64 floor-to-ceiling cylinder
+             columns (3328 side triangles each) = 262,144 triangles, sizes
+             log-uniform in 0.01-0.2 of the scene extent, albedo in [0,1]^3
+             per instance; 256^3 grid, 9 levels; one directional light plus
+             4 point lights; 2048^2 shadow map; 1920x1080 G-buffer.
+
+Matrices follow glm's formulas (column-major float32, flattened
+column by column as GLSL stores them).
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+DEG = np.pi / 180.0
+
+
+# --------------------------------------------------------------- matrices
+def _normalize(v):
+    v = np.asarray(v, dtype=np.float64)
+    return v / np.linalg.norm(v)
+
+
+def look_at(eye, center, up) -> np.ndarray:
+    """glm::lookAt (right handed) as a 4x4 row-major numpy matrix."""
+    eye, center, up = (np.asarray(a, dtype=np.float64) for a in (eye, center, up))
+    f = _normalize(center - eye)
+    s = _normalize(np.cross(f, up))
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[0, :3] = s
+    m[1, :3] = u
+    m[2, :3] = -f
+    m[0, 3] = -s @ eye
+    m[1, 3] = -u @ eye
+    m[2, 3] = f @ eye
+    return m
+
+
+def ortho(l, r, b, t, n, f) -> np.ndarray:
+    m = np.eye(4)
+    m[0, 0] = 2 / (r - l)
+    m[1, 1] = 2 / (t - b)
+    m[2, 2] = -2 / (f - n)
+    m[0, 3] = -(r + l) / (r - l)
+    m[1, 3] = -(t + b) / (t - b)
+    m[2, 3] = -(f + n) / (f - n)
+    return m
+
+
+def perspective(fovy, aspect, zn, zf) -> np.ndarray:
+    th = np.tan(fovy / 2)
+    m = np.zeros((4, 4))
+    m[0, 0] = 1 / (aspect * th)
+    m[1, 1] = 1 / th
+    m[2, 2] = -(zf + zn) / (zf - zn)
+    m[3, 2] = -1
+    m[2, 3] = -(2 * zf * zn) / (zf - zn)
+    return m
+
+
+def colmajor(m: np.ndarray) -> np.ndarray:
+    """4x4 matrix -> 16 float32 in GLSL (column-major) order."""
+    return np.ascontiguousarray(np.asarray(m, dtype=np.float64).T.reshape(16)).astype(np.float32)
+
+
+# ------------------------------------------------------------------ scene
+@dataclass
+class Scene:
+    name: str
+    positions: np.ndarray  # (T, 9) float32
+    normals: np.ndarray  # (T, 9) float32
+    albedo: np.ndarray  # (T, 3) float32
+    lights: list  # dicts: position, direction, color, range, intensity, shadow_caster, type
+    dim: int
+    levels: int
+    vmax: float  # volume is [-vmax, vmax]^3 centred at the origin
+    shadow_size: tuple
+    ls: np.ndarray  # (16,) float32 column-major light projection * view
+    ls_inverse: np.ndarray
+    light_pos: np.ndarray  # (3,)
+    light_int: np.ndarray  # (3,)
+    eye: np.ndarray
+    view_proj: np.ndarray  # (16,)
+    inv_view_proj: np.ndarray
+    gbuffer_size: tuple
+    cone: dict = field(default_factory=dict)  # trace settings (radians)
+
+    @property
+    def ntri(self) -> int:
+        return int(self.positions.shape[0])
+
+
+def _quad(p0, p1, p2, p3, n):
+    """Two CCW triangles (p0,p1,p2) and (p0,p2,p3) with a flat normal."""
+    tris = np.array([[p0, p1, p2], [p0, p2, p3]], dtype=np.float64)
+    nrm = np.broadcast_to(np.asarray(n, dtype=np.float64), (2, 3, 3))
+    return tris, nrm
+
+
+def icosphere(subdiv: int) -> np.ndarray:
+    """Unit icosphere triangles (F, 3, 3) after `subdiv` 4:1 subdivisions."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], dtype=np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2],
+                  [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5], [2, 4, 11],
+                  [6, 2, 10], [8, 6, 7], [9, 8, 1]])
+    tris = v[f]
+    for _ in range(subdiv):
+        a, b, c = tris[:, 0], tris[:, 1], tris[:, 2]
+        ab, bc, ca = a + b, b + c, c + a
+        ab /= np.linalg.norm(ab, axis=1, keepdims=True)
+        bc /= np.linalg.norm(bc, axis=1, keepdims=True)
+        ca /= np.linalg.norm(ca, axis=1, keepdims=True)
+        tris = np.stack([np.stack([a, ab, ca], 1), np.stack([ab, b, bc], 1), np.stack([ca, bc, c], 1),
+                         np.stack([ab, bc, ca], 1)], 1).reshape(-1, 3, 3)
+    return tris
+
+
+def _box(rng, size, center, yaw):
+    """12 triangles of an axis-aligned box rotated by `yaw` about +y."""
+    hx, hy, hz = np.asarray(size) / 2
+    c = np.array([[-hx, -hy, -hz], [hx, -hy, -hz], [hx, hy, -hz], [-hx, hy, -hz],
+                  [-hx, -hy, hz], [hx, -hy, hz], [hx, hy, hz], [-hx, hy, hz]])
+    faces = [((0, 3, 2, 1), (0, 0, -1)), ((4, 5, 6, 7), (0, 0, 1)), ((0, 4, 7, 3), (-1, 0, 0)),
+             ((1, 2, 6, 5), (1, 0, 0)), ((0, 1, 5, 4), (0, -1, 0)), ((3, 7, 6, 2), (0, 1, 0))]
+    cs, sn = np.cos(yaw), np.sin(yaw)
+    R = np.array([[cs, 0, sn], [0, 1, 0], [-sn, 0, cs]])
+    tris, nrms = [], []
+    for (i0, i1, i2, i3), n in faces:
+        t, nn = _quad(c[i0], c[i1], c[i2], c[i3], n)
+        tris.append(t)
+        nrms.append(nn)
+    tris = np.concatenate(tris) @ R.T + center
+    nrms = np.concatenate(nrms) @ R.T
+    return tris, nrms
+
+
+def _cylinder(radius, y0, y1, cx, cz, segments):
+    a = np.arange(segments + 1) * (2 * np.pi / segments)
+    x, z = np.cos(a), np.sin(a)
+    b = np.stack([cx + radius * x, np.full_like(x, y0), cz + radius * z], 1)
+    t = np.stack([cx + radius * x, np.full_like(x, y1), cz + radius * z], 1)
+    n = np.stack([x, np.zeros_like(x), z], 1)
+    k0, k1 = slice(0, segments), slice(1, segments + 1)
+    tri1 = np.stack([b[k0], t[k1], b[k1]], 1)
+    nrm1 = np.stack([n[k0], n[k1], n[k1]], 1)
+    tri2 = np.stack([b[k0], t[k0], t[k1]], 1)
+    nrm2 = np.stack([n[k0], n[k0], n[k1]], 1)
+    tris = np.stack([tri1, tri2], 1).reshape(-1, 3, 3)
+    nrms = np.stack([nrm1, nrm2], 1).reshape(-1, 3, 3)
+    return tris, nrms
+
+
+def _directional_light(rng, vmax):
+    """Directional light from a random upper-hemisphere direction, placed
+    outside the volume with an ortho frustum covering its bounding sphere."""
+    y = rng.uniform(0.3, 0.95)
+    phi = rng.uniform(0, 2 * np.pi)
+    u = np.array([np.sqrt(1 - y * y) * np.cos(phi), y, np.sqrt(1 - y * y) * np.sin(phi)])
+    direction = -u
+    bound = vmax * np.sqrt(3.0)
+    pos = u * (3.0 * vmax)
+    ls = ortho(-bound, bound, -bound, bound, 0.0, 6.0 * vmax) @ look_at(pos, pos + direction, (0, 1, 0))
+    return dict(position=pos, direction=direction, color=np.ones(3), range=5.0, intensity=1.0, shadow_caster=1,
+                type=1), ls
+
+
+def _finish(name, tris, nrms, alb, lights, ls, dim, levels, vmax, shadow_size, eye, target, fovy, gsize, cone):
+    W, H = gsize
+    vpm = perspective(fovy, W / H, 0.1, 20.0) @ look_at(eye, target, (0, 1, 0))
+    main = lights[0]
+    return Scene(
+        name=name,
+        positions=np.ascontiguousarray(tris.reshape(-1, 9), dtype=np.float32),
+        normals=np.ascontiguousarray(nrms.reshape(-1, 9), dtype=np.float32),
+        albedo=np.ascontiguousarray(alb, dtype=np.float32),
+        lights=lights, dim=dim, levels=levels, vmax=vmax, shadow_size=shadow_size,
+        ls=colmajor(ls), ls_inverse=colmajor(np.linalg.inv(ls)),
+        light_pos=np.asarray(main["position"], dtype=np.float32),
+        light_int=np.asarray(main["color"], dtype=np.float32),
+        eye=np.asarray(eye, dtype=np.float32), view_proj=colmajor(vpm), inv_view_proj=colmajor(np.linalg.inv(vpm)),
+        gbuffer_size=gsize, cone=cone)
+
+
+BASELINE_CONES = dict(diffuse=(16, 60 * DEG, 1.0, 1.0, 0.5), specular=(32, 10 * DEG, 1.7, 0.5, 0.1))
+
+
+def cornell(seed: int = 0, dim: int = 64, shadow: int = 512, gbuffer=(640, 360)) -> Scene:
+    rng = np.random.default_rng(seed)
+    w = 0.95
+    walls = [
+        ((-w, -w, -w), (-w, -w, w), (w, -w, w), (w, -w, -w), (0, 1, 0)),    # floor
+        ((-w, -w, -w), (w, -w, -w), (w, w, -w), (-w, w, -w), (0, 0, 1)),    # back
+        ((-w, -w, w), (-w, w, w), (w, w, w), (w, -w, w), (0, 0, -1)),       # front
+        ((-w, -w, -w), (-w, w, -w), (-w, w, w), (-w, -w, w), (1, 0, 0)),    # left
+        ((w, -w, -w), (w, -w, w), (w, w, w), (w, w, -w), (-1, 0, 0)),       # right
+    ]
+    tris, nrms, alb = [], [], []
+    for p0, p1, p2, p3, n in walls:
+        t, nn = _quad(np.array(p0), np.array(p1), np.array(p2), np.array(p3), n)
+        tris.append(t)
+        nrms.append(nn)
+        alb.append(np.repeat(rng.uniform(0.1, 0.9, size=(1, 3)), 2, 0))
+    sph = icosphere(3)
+    c = rng.uniform(-0.6, 0.6, size=3)
+    tris.append(sph * 0.3 + c)
+    nrms.append(sph.copy())
+    alb.append(np.repeat(rng.uniform(0.1, 0.9, size=(1, 3)), sph.shape[0], 0))
+    light, ls = _directional_light(rng, 1.0)
+    levels = int(np.log2(dim)) + 1
+    return _finish("cornell", np.concatenate(tris), np.concatenate(nrms), np.concatenate(alb), [light], ls, dim,
+                   levels, 1.0, (shadow, shadow), np.array([0.0, 1.6, 2.6]), np.array([0.0, -0.4, 0.0]), 50 * DEG,
+                   tuple(gbuffer), BASELINE_CONES)
+
+
+def large(seed: int = 0, dim: int = 256, shadow: int = 2048, gbuffer=(1920, 1080), n_boxes: int = 4096,
+          n_cyl: int = 64, cyl_segments: int = 1664) -> Scene:
+    rng = np.random.default_rng(seed)
+    extent = 2.0
+    lo, hi = np.log(0.01 * extent), np.log(0.2 * extent)
+    tris, nrms, alb = [], [], []
+    for _ in range(n_boxes):
+        size = np.exp(rng.uniform(lo, hi, size=3))
+        center = rng.uniform(-0.9, 0.9, size=3)
+        yaw = rng.uniform(0, 2 * np.pi)
+        t, n = _box(rng, size, center, yaw)
+        tris.append(t)
+        nrms.append(n)
+        alb.append(np.repeat(rng.uniform(0, 1, size=(1, 3)), 12, 0))
+    for _ in range(n_cyl):
+        radius = 0.5 * np.exp(rng.uniform(lo, hi))
+        cx, cz = rng.uniform(-0.9, 0.9, size=2)
+        t, n = _cylinder(radius, -0.95, 0.95, cx, cz, cyl_segments)
+        tris.append(t)
+        nrms.append(n)
+        alb.append(np.repeat(rng.uniform(0, 1, size=(1, 3)), t.shape[0], 0))
+    light, ls = _directional_light(rng, 1.0)
+    lights = [light]
+    for _ in range(4):
+        lights.append(dict(position=rng.uniform(-0.9, 0.9, size=3), direction=np.array([0.0, -1.0, 0.0]),
+                           color=rng.uniform(0.5, 1.0, size=3), range=float(rng.uniform(0.3, 0.8)), intensity=1.0,
+                           shadow_caster=0, type=0))
+    levels = int(np.log2(dim)) + 1
+    return _finish("large", np.concatenate(tris), np.concatenate(nrms), np.concatenate(alb), lights, ls, dim, levels,
+                   1.0, (shadow, shadow), np.array([0.0, 0.5, 2.8]), np.array([0.0, 0.0, 0.0]), 55 * DEG,
+                   tuple(gbuffer), BASELINE_CONES)
+
+
+def tiny(seed: int = 0, dim: int = 16, shadow: int = 64, gbuffer=(48, 32), n_boxes: int = 6) -> Scene:
+    """A few boxes in a 16^3 grid: small enough for pure-CPU oracle tests."""
+    rng = np.random.default_rng(seed)
+    tris, nrms, alb = [], [], []
+    for _ in range(n_boxes):
+        size = rng.uniform(0.2, 0.8, size=3)
+        center = rng.uniform(-0.6, 0.6, size=3)
+        t, n = _box(rng, size, center, rng.uniform(0, 2 * np.pi))
+        tris.append(t)
+        nrms.append(n)
+        alb.append(np.repeat(rng.uniform(0, 1, size=(1, 3)), 12, 0))
+    light, ls = _directional_light(rng, 1.0)
+    lights = [light, dict(position=np.array([0.2, 0.5, 0.1]), direction=np.array([0.0, -1.0, 0.0]),
+                          color=np.array([1.0, 0.8, 0.6]), range=1.5, intensity=1.0, shadow_caster=0, type=0)]
+    levels = int(np.log2(dim)) + 1
+    return _finish("tiny", np.concatenate(tris), np.concatenate(nrms), np.concatenate(alb), lights, ls, dim, levels,
+                   1.0, (shadow, shadow), np.array([0.3, 0.9, 2.4]), np.array([0.0, 0.0, 0.0]), 50 * DEG,
+                   tuple(gbuffer), BASELINE_CONES)
+
+
+SCENES = {"cornell": cornell, "large": large, "tiny": tiny}
+
+
+def make(name: str, seed: int = 0, **kw) -> Scene:
+    return SCENES[name](seed=seed, **kw)
