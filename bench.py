@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-rows", type=int, default=24, help="rows of the frame traced by the CPU baseline")
+    ap.add_argument("--profile-frames", type=int, default=0,
+                    help="only run this many frames (no timing, no JSON): the command profiled with ncu")
     return ap.parse_args()
 
 
@@ -218,6 +220,13 @@ def run_ours(args, rank, world):
 
     def frame():
         ctx.frame(tris, lights, shadow, sc.eye, gb, out, stream)
+
+    if args.profile_frames:
+        for _ in range(args.profile_frames):
+            frame()
+        torch.cuda.synchronize()
+        ctx.close()
+        return None, sc
 
     for _ in range(max(3, args.warmup)):
         frame()
@@ -424,6 +433,8 @@ def main():
             print(json.dumps(run_reference(args, rank, world)), flush=True)
         return
     result, sc = run_ours(args, rank, world)
+    if result is None:  # --profile-frames
+        return
     if rank == 0 and not args.no_cpu_baseline:
         ms, detail = cpu_frame_ms(sc, 1, args.cpu_sample_rows)
         result["cpu_baseline"] = {"value": round(ms, 2), "unit": "ms/frame", "cores": 1, "kind": "port",

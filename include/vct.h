@@ -218,10 +218,13 @@ vct_status vct_get_config(const vct_ctx* ctx, vct_config* out);
 /* Device pointer of one level of a volume (read-only view for callers). */
 vct_status vct_volume_level(const vct_ctx* ctx, int32_t volume, int32_t level,
                             const uint16_t** data_dev, int32_t* dim);
-/* Device pointers of the integer accumulators: count[dim^3] and six sums
- * (r,g,b,nx,ny,nz) of 16-bit fixed point, each dim^3 uint32. */
-vct_status vct_accumulators(const vct_ctx* ctx, const uint32_t** count_dev,
-                            const uint32_t** sums_dev);
+/* Device pointers of the integer accumulators: one 8 x uint32 record per
+ * voxel {count, r, g, b, nx, ny, nz, 0} (sums of round(x * 65535)), voxel v
+ * at records_dev[8*v], and the occupancy bit mask (bit v%32 of word v/32).
+ * Between vct_voxelize_accumulate and vct_normalize they hold the sums of
+ * the frame; vct_normalize / vct_frame leave them zeroed. */
+vct_status vct_accumulators(const vct_ctx* ctx, const uint32_t** records_dev,
+                            const uint32_t** occupancy_dev);
 
 /* ---- stages ----------------------------------------------------------- */
 /* voxelize.geom/.frag: rasterise every triangle along its dominant axis and

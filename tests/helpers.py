@@ -60,6 +60,16 @@ class GpuScene:
         return irr, spec, col, samples
 
 
+def split_records(rec, occ):
+    """GPU accumulator records -> (count, SoA sums, occupancy bools) as the
+    oracle lays them out."""
+    r = u32(rec).reshape(-1, 8)
+    count = np.ascontiguousarray(r[:, 0])
+    sums = np.ascontiguousarray(r[:, 1:7].T).reshape(-1)
+    bits = np.unpackbits(u32(occ).view(np.uint8), bitorder="little")[: r.shape[0]].astype(bool)
+    return count, sums, bits, r[:, 7]
+
+
 def read_chain(ctx, volume=L.VCT_VOLUME_RADIANCE) -> np.ndarray:
     return np.concatenate([u16(ctx.read_volume(volume, l)) for l in range(ctx.levels)])
 

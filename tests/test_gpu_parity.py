@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import GpuScene, read_chain, rel_l2, rgb, u16, u32
+from helpers import GpuScene, read_chain, rel_l2, rgb, split_records, u16, u32
 from vct_gb300 import _lib as L
 from vct_gb300 import api, scenes
 
@@ -44,9 +44,10 @@ def run_stages(sc, g, params=None, hardware=False):
     ctx.set_params(p)
     ctx.voxelize_accumulate(g.tris, g.lights, g.shadow, sc.eye)
     torch.cuda.synchronize()
-    cnt, sums = ctx.read_accumulators()
+    cnt, sums, occ, pad = split_records(*ctx.read_accumulators())
     ctx.normalize()
     torch.cuda.synchronize()
+    after = split_records(*ctx.read_accumulators())
     color0 = u16(ctx.read_volume(L.VCT_VOLUME_COLOR, 0))
     normal0 = u16(ctx.read_volume(L.VCT_VOLUME_NORMAL, 0))
     rad_seed = u16(ctx.read_volume(L.VCT_VOLUME_RADIANCE, 0))
@@ -55,7 +56,7 @@ def run_stages(sc, g, params=None, hardware=False):
     irr, spec, col, samples = g.new_outputs()
     ctx.trace(g.gb, sc.eye, api.trace_out(irr, spec, col, samples))
     torch.cuda.synchronize()
-    out = dict(count=u32(cnt), sums=u32(sums), color=color0, normal=normal0, rad_seed=rad_seed, chain=read_chain(ctx),
+    out = dict(count=cnt, sums=sums, occ=occ, pad=pad, after=after, color=color0, normal=normal0, rad_seed=rad_seed, chain=read_chain(ctx),
                irr=irr.cpu().numpy(), spec=spec.cpu().numpy(), col=col.cpu().numpy(),
                samples=int(samples.item()), stats=ctx.stats())
     ctx.close()
@@ -89,6 +90,14 @@ def test_accumulators_bitexact(cornell, stages):
     assert np.array_equal(stages["count"], ref["count"])
     assert np.array_equal(stages["sums"], ref["sums"])
     assert (stages["count"] > 0).sum() == ref["stats"]["unique_voxels"]
+    # occupancy mask is exactly the set of voxels with fragments
+    assert np.array_equal(stages["occ"], ref["count"] > 0)
+    assert not stages["pad"].any()
+
+
+def test_normalize_leaves_accumulators_zero(stages):
+    count, sums, occ, pad = stages["after"]
+    assert not count.any() and not sums.any() and not occ.any() and not pad.any()
 
 
 def test_normalize_bitexact(cornell, stages):
@@ -136,6 +145,25 @@ def test_trace_hardware_sampler(cornell):
     assert e <= 1e-2
 
 
+def test_frame_fused_hardware_sampler(cornell):
+    """The fused frame writes the texture-unit copy of the mip chain through
+    surfaces; tracing it must give exactly what the staged path (which copies
+    the linear chain into the array) gives."""
+    import torch
+
+    sc, g, ref, ref64 = cornell
+    staged = run_stages(sc, g, hardware=True)
+    with api.Context(api.config_for(sc)) as ctx:
+        ctx.set_params(api.scene_params(sc, trace_filter=L.VCT_FILTER_HARDWARE))
+        irr, spec, col, samples = g.new_outputs()
+        for _ in range(2):
+            ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(irr, spec, col, samples))
+        torch.cuda.synchronize()
+        assert np.array_equal(read_chain(ctx), ref["chain"])
+        assert np.array_equal(irr.cpu().numpy(), staged["irr"])
+        assert np.array_equal(spec.cpu().numpy(), staged["spec"])
+
+
 def test_frame_fused_equals_stages(cornell, stages):
     import torch
 
@@ -169,9 +197,9 @@ def test_triangle_order_independence(cornell, stages):
         ctx.set_params(api.scene_params(sc2))
         ctx.voxelize_accumulate(g2.tris, g2.lights, g2.shadow, sc2.eye)
         torch.cuda.synchronize()
-        cnt, sums = ctx.read_accumulators()
-    assert np.array_equal(u32(cnt), stages["count"])
-    assert np.array_equal(u32(sums), stages["sums"])
+        cnt, sums, _, _ = split_records(*ctx.read_accumulators())
+    assert np.array_equal(cnt, stages["count"])
+    assert np.array_equal(sums, stages["sums"])
 
 
 @pytest.mark.parametrize("opt", [dict(radiance_lighting=1), dict(radiance_dilate=1), dict(voxelize_lighting=0),
@@ -186,7 +214,7 @@ def test_options_bitexact(opt):
         ctx.set_params(api.scene_params(sc, **opt))
         ctx.voxelize_accumulate(g.tris, g.lights, g.shadow, sc.eye)
         torch.cuda.synchronize()
-        cnt, sums = ctx.read_accumulators()
+        cnt, sums, _, _ = split_records(*ctx.read_accumulators())
         ctx.normalize()
         ctx.inject(g.shadow, sc.eye)
         ctx.build_mips()
@@ -195,8 +223,8 @@ def test_options_bitexact(opt):
         # fused frame on a second context must agree too
     count, rsums, _ = O.voxelize(sc, sm, lighting=opt.get("voxelize_lighting", 1),
                                  axis_override=opt.get("axis_override", -1))
-    assert np.array_equal(u32(cnt), count)
-    assert np.array_equal(u32(sums), rsums)
+    assert np.array_equal(cnt, count)
+    assert np.array_equal(sums, rsums)
     rchain = np.zeros(4 * O.chain_voxels(sc.dim, sc.levels), dtype=np.uint16)
     color, normal, _, _ = O.normalize(sc, count, rsums, opacity=opt.get("voxel_set_opacity", 0.5), radiance=rchain)
     O.inject(sc, sm, color, normal, rchain, lighting=opt.get("radiance_lighting", 0),

@@ -221,10 +221,11 @@ class Context:
         return device_view(ptr, (d * d * d * 4,), "<i2").clone()
 
     def read_accumulators(self):
-        """Copies of (count, sums) as int32 tensors (uint32 bit patterns)."""
-        cp, sp = self.accumulator_ptrs()
+        """Copies of (records [dim^3, 8], occupancy mask) as int32 tensors
+        (uint32 bit patterns); record = {count, r, g, b, nx, ny, nz, 0}."""
+        rp, op = self.accumulator_ptrs()
         nv = self.dim ** 3
-        return device_view(cp, (nv,), "<i4").clone(), device_view(sp, (6 * nv,), "<i4").clone()
+        return (device_view(rp, (nv, 8), "<i4").clone(), device_view(op, ((nv + 31) // 32,), "<i4").clone())
 
 
 class _CudaArray:

@@ -18,8 +18,8 @@ struct vct_ctx {
     vct_params params;
     int dim = 0, levels = 0, color_levels = 1, device = 0, num_sms = 0;
     long long nv = 0;
-    uint32_t* count = nullptr;
-    uint32_t* sums = nullptr;
+    uint32_t* acc = nullptr;  // accumulator records (kAccWords uint32 per voxel)
+    uint32_t* occ = nullptr;  // occupancy bit mask
     uint32_t* lit = nullptr;
     uint2* color = nullptr;     // colour chain (color_levels levels)
     uint2* normal = nullptr;    // one level
@@ -32,10 +32,13 @@ struct vct_ctx {
     float mvp[48];
     cudaMipmappedArray_t tex_array = nullptr;
     cudaTextureObject_t tex = 0;
+    cudaSurfaceObject_t surf[VCT_MAX_LEVELS] = {};
     bool tex_ready = false;
     bool timers_on = false;
     bool timers_recorded = false;
     cudaEvent_t ev[5] = {};
+    void* vox_scratch = nullptr;  // voxeliser work-distribution arrays
+    long long vox_scratch_bytes = 0;
 };
 
 namespace vct {
@@ -255,6 +258,11 @@ vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lig
         L.enabled = lights[i].enabled;
         L.shadow_caster = lights[i].shadow_caster;
         L.type = lights[i].type;
+        // Hoisted per-light terms of voxelize.frag, same fp32 operations.
+        hf3 nd = {-lights[i].direction[0], -lights[i].direction[1], -lights[i].direction[2]};
+        hf3 ndn = hnorm(nd);
+        L.neg_dir_n = {ndn.x, ndn.y, ndn.z};
+        L.range075 = 0.75f * lights[i].range;
     }
     std::memcpy(P.mvp, ctx->mvp, sizeof P.mvp);
     if (sh) {
@@ -263,10 +271,23 @@ vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lig
         P.sw = sh->width;
         P.sh = sh->height;
     }
-    P.count = ctx->count;
-    P.sums = ctx->sums;
+    P.acc = ctx->acc;
+    P.occ = ctx->occ;
     P.stats = ctx->stats;
     P.num_sms = ctx->num_sms;
+    const long long need = accumulate_scratch_bytes(t->count);
+    if (need > ctx->vox_scratch_bytes) {
+        if (ctx->vox_scratch) cudaFree(ctx->vox_scratch);
+        ctx->vox_scratch = nullptr;
+        ctx->vox_scratch_bytes = 0;
+        cudaError_t e = cudaMalloc(&ctx->vox_scratch, (size_t)need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(VCT_ERR_OUT_OF_MEMORY, std::string("voxeliser scratch: ") + cudaGetErrorString(e));
+        }
+        ctx->vox_scratch_bytes = need;
+    }
+    accumulate_bind_scratch(P, ctx->vox_scratch);
     return VCT_OK;
 }
 
@@ -275,8 +296,8 @@ void fill_norm(vct_ctx* ctx, NormalizeParams& P) {
     P.opacity = ctx->params.voxel_set_opacity;
     P.temporal = ctx->params.temporal_filter;
     P.decay = ctx->params.temporal_decay;
-    P.count = ctx->count;
-    P.sums = ctx->sums;
+    P.acc = ctx->acc;
+    P.occ = ctx->occ;
     P.color = ctx->color;
     P.normal = ctx->normal;
     P.radiance = ctx->radiance;
@@ -333,7 +354,16 @@ vct_status ensure_texture(vct_ctx* ctx) {
     if (ctx->tex_array) return VCT_OK;
     cudaChannelFormatDesc desc = cudaCreateChannelDescHalf4();
     cudaExtent ext = make_cudaExtent(ctx->dim, ctx->dim, ctx->dim);
-    VCT_CUDA(cudaMallocMipmappedArray(&ctx->tex_array, &desc, ext, ctx->levels, 0));
+    VCT_CUDA(cudaMallocMipmappedArray(&ctx->tex_array, &desc, ext, ctx->levels, cudaArraySurfaceLoadStore));
+    for (int l = 0; l < ctx->levels; ++l) {
+        cudaArray_t arr;
+        VCT_CUDA(cudaGetMipmappedArrayLevel(&arr, ctx->tex_array, l));
+        cudaResourceDesc sres;
+        std::memset(&sres, 0, sizeof sres);
+        sres.resType = cudaResourceTypeArray;
+        sres.res.array.array = arr;
+        VCT_CUDA(cudaCreateSurfaceObject(&ctx->surf[l], &sres));
+    }
     cudaResourceDesc res;
     std::memset(&res, 0, sizeof res);
     res.resType = cudaResourceTypeMipmappedArray;
@@ -516,8 +546,8 @@ vct_status vct_create(const vct_config* cfg, vct_ctx** out) {
         void** p;
         size_t bytes;
     } allocs[] = {
-        {(void**)&c->count, (size_t)c->nv * 4},
-        {(void**)&c->sums, (size_t)c->nv * 4 * 6},
+        {(void**)&c->acc, (size_t)c->nv * 4 * kAccWords},
+        {(void**)&c->occ, (size_t)((c->nv + 31) / 32) * 4},
         {(void**)&c->lit, (size_t)((c->nv + 31) / 32) * 4},
         {(void**)&c->color, (size_t)color_vox * 8},
         {(void**)&c->normal, (size_t)c->nv * 8},
@@ -545,7 +575,9 @@ vct_status vct_destroy(vct_ctx* c) {
         if (e) cudaEventDestroy(e);
     if (c->tex) cudaDestroyTextureObject(c->tex);
     if (c->tex_array) cudaFreeMipmappedArray(c->tex_array);
-    void* ptrs[] = {c->count, c->sums, c->lit, c->color, c->normal, c->radiance, c->stats};
+    for (auto sf : c->surf)
+        if (sf) cudaDestroySurfaceObject(sf);
+    void* ptrs[] = {c->acc, c->occ, c->lit, c->color, c->normal, c->radiance, c->stats, c->vox_scratch};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -589,10 +621,10 @@ vct_status vct_volume_level(const vct_ctx* c, int32_t volume, int32_t level, con
     return VCT_OK;
 }
 
-vct_status vct_accumulators(const vct_ctx* c, const uint32_t** count, const uint32_t** sums) {
+vct_status vct_accumulators(const vct_ctx* c, const uint32_t** records, const uint32_t** occupancy) {
     if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
-    if (count) *count = c->count;
-    if (sums) *sums = c->sums;
+    if (records) *records = c->acc;
+    if (occupancy) *occupancy = c->occ;
     return VCT_OK;
 }
 
@@ -614,7 +646,7 @@ vct_status vct_voxelize_accumulate(vct_ctx* c, const vct_triangles* tris, const 
         c->stats_reset_pending = false;
     }
     AccumParams P;
-    fill_accum(c, tris, lights, n, need_shadow ? shadow : nullptr, P);
+    if ((s = fill_accum(c, tris, lights, n, need_shadow ? shadow : nullptr, P)) != VCT_OK) return s;
     launch_accumulate(P, st);
     VCT_CHECK_LAUNCH("voxelize accumulate");
     c->radiance_ready = false;
@@ -632,6 +664,9 @@ vct_status vct_normalize(vct_ctx* c, void* stream) {
     fill_norm(c, P);
     launch_normalize(P, st);
     VCT_CHECK_LAUNCH("normalize");
+    // Records of occupied voxels were zeroed by the kernel; the mask is
+    // cleared here so that the next accumulate starts from an empty grid.
+    VCT_CUDA(cudaMemsetAsync(c->occ, 0, (size_t)((c->nv + 31) / 32) * 4, st));
     c->stats_reset_pending = true;
     c->radiance_ready = true;
     c->mips_ready = false;
@@ -643,8 +678,8 @@ vct_status vct_clear_accumulators(vct_ctx* c, void* stream) {
     DeviceScope ds(c->device);
     VCT_CUDA(ds.err);
     cudaStream_t st = as_stream(stream);
-    VCT_CUDA(cudaMemsetAsync(c->count, 0, (size_t)c->nv * 4, st));
-    VCT_CUDA(cudaMemsetAsync(c->sums, 0, (size_t)c->nv * 24, st));
+    VCT_CUDA(cudaMemsetAsync(c->acc, 0, (size_t)c->nv * 4 * kAccWords, st));
+    VCT_CUDA(cudaMemsetAsync(c->occ, 0, (size_t)((c->nv + 31) / 32) * 4, st));
     c->stats_reset_pending = true;
     return VCT_OK;
 }
@@ -730,7 +765,7 @@ vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lig
     VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
     VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, st));
     AccumParams A;
-    fill_accum(c, tris, lights, n, shadow, A);
+    if ((s = fill_accum(c, tris, lights, n, shadow, A)) != VCT_OK) return s;
     launch_accumulate(A, st);
     VCT_CHECK_LAUNCH("frame: accumulate");
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[1], st));
@@ -739,28 +774,36 @@ vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lig
     launch_inject_mark(I, st);
     VCT_CHECK_LAUNCH("frame: inject mark");
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[2], st));
+    const bool hw = c->params.trace_filter == VCT_FILTER_HARDWARE;
+    if (hw && (s = ensure_texture(c)) != VCT_OK) return s;
     ResolveParams R;
     std::memset(&R, 0, sizeof R);
     fill_norm(c, R.norm);
+    R.fused = 1;
     R.lighting = c->params.radiance_lighting;
     R.dilate = c->params.radiance_dilate;
     R.light_vox = I.light_vox;
     R.light_int = I.light_int;
     R.lit = c->lit;
     R.mip_levels = std::min(4, c->levels - 1);
-    for (int l = 0; l <= R.mip_levels; ++l) R.radiance_levels[l] = level_ptr(c->radiance, c, l);
+    for (int l = 0; l <= R.mip_levels; ++l) {
+        R.radiance_levels[l] = level_ptr(c->radiance, c, l);
+        R.surf[l] = hw ? c->surf[l] : 0;
+    }
     launch_resolve(R, st);
     VCT_CHECK_LAUNCH("frame: resolve");
+    VCT_CUDA(cudaMemsetAsync(c->occ, 0, (size_t)((c->nv + 31) / 32) * 4, st));
     if (c->levels > 5) {
-        launch_mips(mip_levels(c, c->radiance, c->levels), 4, st);
+        MipLevels M = mip_levels(c, c->radiance, c->levels);
+        if (hw)
+            for (int l = 0; l < c->levels; ++l) M.surf[l] = c->surf[l];
+        launch_mips(M, 4, st);
         VCT_CHECK_LAUNCH("frame: coarse mips");
     }
+    c->tex_ready = hw;
     c->stats_reset_pending = true;
     c->radiance_ready = true;
     c->mips_ready = true;
-    if (c->params.trace_filter == VCT_FILTER_HARDWARE) {
-        if ((s = refresh_texture(c, st)) != VCT_OK) return s;
-    }
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[3], st));
     TraceParams T;
     if ((s = fill_trace(c, g, eye, out, T)) != VCT_OK) return s;

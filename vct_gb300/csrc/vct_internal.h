@@ -18,6 +18,10 @@ struct LightDev {
     f3 color;
     float range, intensity;
     uint32_t enabled, shadow_caster, type;
+    // normalize(-direction) and 0.75 * range, computed on the host with the
+    // same fp32 operations the shader evaluates per fragment.
+    f3 neg_dir_n;
+    float range075;
 };
 
 struct StatsDev {
@@ -41,19 +45,36 @@ struct AccumParams {
     float ls[16];
     const float* shadowmap;
     int sw, sh;
-    uint32_t* count;
-    uint32_t* sums;
+    uint32_t* acc;  // accumulator records, kAccWords uint32 per voxel
+    uint32_t* occ;  // occupancy bit mask, one bit per voxel
     StatsDev* stats;
     int num_sms;
+    // Work distribution scratch (sized for ntri; see voxelize.cu).
+    uint4* tri_rec;          // 3 x uint4 per triangle
+    uint32_t* tri_units;     // work units per triangle
+    uint32_t* tri_scan;      // block-local exclusive scan of tri_units
+    uint32_t* block_off;     // exclusive scan of per-block unit totals (+ total at [nblocks])
 };
+
+// Scratch bytes the voxeliser needs for `ntri` triangles.
+long long accumulate_scratch_bytes(long long ntri);
+// Carves the scratch buffer into the AccumParams work arrays.
+void accumulate_bind_scratch(AccumParams& P, void* scratch);
+
+// One 32-byte accumulator record per voxel: {count, r, g, b, nx, ny, nz, 0}.
+// Sums are of 16-bit fixed point (round(x * 65535)); they are updated as
+// four 64-bit atomics whose low halves (count, g, nx, nz) never carry into
+// the high halves while a voxel receives fewer than VCT_MAX_EXACT_FRAGMENTS
+// fragments, so the record then equals seven independent 32-bit sums.
+constexpr int kAccWords = 8;
 
 struct NormalizeParams {
     int dim;
     float opacity;
     int temporal;
     float decay;
-    uint32_t* count;
-    uint32_t* sums;
+    uint32_t* acc;
+    const uint32_t* occ;
     uint2* color;     // level 0 of the colour volume
     uint2* normal;
     uint2* radiance;  // level 0 of the radiance chain
@@ -80,15 +101,18 @@ struct InjectParams {
 // Fused normalisation + injection resolve + first mip levels (vct_frame).
 struct ResolveParams {
     NormalizeParams norm;
+    int fused;  // 0: plain normalisation (transferVoxels.comp)
     int lighting, dilate;
     f3 light_vox, light_int;
-    uint32_t* lit;
+    const uint32_t* lit;
     uint2* radiance_levels[5];  // levels 0..4 of the radiance chain
     int mip_levels;             // number of levels below 0 to write from the brick (<= 4)
+    cudaSurfaceObject_t surf[5];  // texture-unit copy of levels 0..4 (0 = none)
 };
 
 struct MipLevels {
     uint2* level[VCT_MAX_LEVELS];
+    cudaSurfaceObject_t surf[VCT_MAX_LEVELS];  // optional texture-unit copy (0 = none)
     int dim;
     int levels;
 };

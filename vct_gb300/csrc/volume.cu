@@ -2,10 +2,12 @@
 // (injectRadiance.comp), the 2x2x2 box mip chain (filterRadiance.comp) and
 // the fused resolve used by vct_frame.  Compiled with --fmad=false.
 //
-// Layout: RGBA16F voxels (8 bytes, handled as uint2), x fastest.  All passes
-// over the dense grid walk 16^3 bricks so that one CTA owns one brick: its
-// loads and stores are full 128-byte rows along x, and the brick's first
-// four mip levels are reduced in shared memory without touching HBM again.
+// Layout: RGBA16F voxels (8 bytes, handled as uint2), x fastest.  The dense
+// passes walk 16^3 bricks, one CTA per brick, each thread owning runs of 4
+// voxels along x: the occupancy and lit masks are read as 4-bit fields, only
+// occupied voxels touch their 32-byte accumulator record, and the colour,
+// normal and radiance outputs leave as 32-byte vector stores.  The fused
+// resolve also reduces the brick's first four mip levels in shared memory.
 #include "vct_device.cuh"
 
 namespace vct {
@@ -40,66 +42,176 @@ __device__ __forceinline__ void block_stats(StatsDev* stats, uint32_t uniq, uint
     }
 }
 
-// transferVoxels.comp:37-69 for one voxel.  Reads and then zeroes its
-// accumulators.  Returns the voxel's alpha (0 when empty).
-struct Normalized {
-    uint2 color, normal;
-    float alpha;
-    uint32_t count;
-};
+__device__ __forceinline__ void store4(uint2* dst, const uint2 v[4]) {
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    d[0] = make_uint4(v[0].x, v[0].y, v[1].x, v[1].y);
+    d[1] = make_uint4(v[2].x, v[2].y, v[3].x, v[3].y);
+}
 
-__device__ __forceinline__ Normalized normalize_voxel(const NormalizeParams& P, long long v, long long NV) {
-    Normalized r;
-    uint32_t c = P.count[v];
-    r.count = c;
-    r.alpha = 0.0f;
-    r.color = make_uint2(0u, 0u);
-    r.normal = make_uint2(0u, 0u);
-    if (c > 0) {
-        float denom = 65535.0f * __uint2float_rn(c);
-        uint32_t s[6];
+__device__ __forceinline__ bool in_grid(int x, int y, int z, int N) {
+    return x >= 0 && y >= 0 && z >= 0 && x < N && y < N && z < N;
+}
+
+// radianceLighting branch (injectRadiance.comp:222-230).
+__device__ __forceinline__ uint2 light_voxel(f3 light_vox, f3 light_int, uint2 color, uint2 normal, int x, int y,
+                                             int z) {
+    float4 c = unpack_h4(color);
+    float4 nn = unpack_h4(normal);
+    f3 n = mk(2.0f * nn.x - 1.0f, 2.0f * nn.y - 1.0f, 2.0f * nn.z - 1.0f);
+    f3 L = normalize(sub(light_vox, mk((float)x, (float)y, (float)z)));
+    float diff = fmaxf(dot(n, L), 0.0f);
+    return pack_h4((diff * light_int.x) * c.x, (diff * light_int.y) * c.y, (diff * light_int.z) * c.z, c.w);
+}
+
+// -------------------------------------------------------------------- mips
+// filterRadiance.comp BOX2: fp32 sum over the children in the shader's order
+// (z fastest, then y, then x), times 0.125, rounded to binary16.
+__device__ __forceinline__ uint2 box8(const uint2 c[8]) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            s[k] = P.sums[k * NV + v];
-            P.sums[k * NV + v] = 0u;
+    for (int i = 0; i < 8; ++i) {
+        float4 t = unpack_h4(c[i]);
+        acc.x += t.x;
+        acc.y += t.y;
+        acc.z += t.z;
+        acc.w += t.w;
+    }
+    return pack_h4(acc.x * 0.125f, acc.y * 0.125f, acc.z * 0.125f, acc.w * 0.125f);
+}
+
+// Reduces a cube of side S (in shared memory, x fastest) into side S/2,
+// writing the result to shared memory, to the linear level and (when `surf`
+// is set) to the texture-unit copy of the level.
+__device__ __forceinline__ void reduce_level(const uint2* src, uint2* dst, int S, uint2* gdst, cudaSurfaceObject_t surf,
+                                             int gS, int gx0, int gy0, int gz0) {
+    const int D = S / 2;
+    const int n = D * D * D;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        int x = t % D, y = (t / D) % D, z = t / (D * D);
+        uint2 c[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            int ox = i >> 2, oy = (i >> 1) & 1, oz = i & 1;
+            c[i] = src[((2 * z + oz) * S + (2 * y + oy)) * S + (2 * x + ox)];
         }
-        P.count[v] = 0u;
-        r.alpha = P.opacity > 0.0f ? P.opacity : 1.0f;
-        r.color = pack_h4(__fdiv_rn(__uint2float_rn(s[0]), denom), __fdiv_rn(__uint2float_rn(s[1]), denom),
-                          __fdiv_rn(__uint2float_rn(s[2]), denom), r.alpha);
-        r.normal = pack_h4(__fdiv_rn(__uint2float_rn(s[3]), denom), __fdiv_rn(__uint2float_rn(s[4]), denom),
-                           __fdiv_rn(__uint2float_rn(s[5]), denom), 1.0f);
+        uint2 r = box8(c);
+        dst[t] = r;
+        gdst[((long long)(gz0 + z) * gS + (gy0 + y)) * gS + (gx0 + x)] = r;
+        if (surf) surf3Dwrite(r, surf, (gx0 + x) * (int)sizeof(uint2), gy0 + y, gz0 + z);
     }
-    return r;
 }
 
-__device__ __forceinline__ uint2 seed_radiance(const NormalizeParams& P, long long v, const Normalized& n) {
-    if (P.temporal) {
-        float w = 1.0f - P.decay;
-        float4 prev = unpack_h4(P.radiance[v]);
-        return pack_h4(prev.x * (1.0f - w) + 0.0f * w, prev.y * (1.0f - w) + 0.0f * w,
-                       prev.z * (1.0f - w) + 0.0f * w, prev.w * (1.0f - w) + n.alpha * w);
-    }
-    return n.count > 0 ? pack_h4(0.0f, 0.0f, 0.0f, n.alpha) : make_uint2(0u, 0u);
-}
-
-__global__ void __launch_bounds__(kThreads) normalize_kernel(const NormalizeParams P) {
-    const long long NV = (long long)P.dim * P.dim * P.dim;
+// ----------------------------------------------------------- brick resolve
+// FUSED = false: transferVoxels.comp (radiance level 0 = (0,0,0,alpha)).
+// FUSED = true : additionally applies injectRadiance's stores (voxels marked
+//                in the lit mask take their colour, or the relit colour) and
+//                builds radiance levels 1..mip_levels of the brick.  The
+//                result equals normalise; inject; filter because the value
+//                injectRadiance stores into a voxel depends only on that
+//                voxel (its stores are idempotent).
+template <bool FUSED>
+__global__ void __launch_bounds__(kThreads) resolve_kernel(const ResolveParams R) {
+    __shared__ uint2 s0[FUSED ? kBrickVox : 1];
+    __shared__ uint2 s1[FUSED ? kBrickVox / 8 : 1];
+    const NormalizeParams& P = R.norm;
+    const int N = P.dim;
+    const int bpa = N / kBrick;
+    const int bx = blockIdx.x % bpa, by = (blockIdx.x / bpa) % bpa, bz = blockIdx.x / (bpa * bpa);
     uint32_t uniq = 0, mx = 0, flags = 0;
-    for (long long v = (long long)blockIdx.x * kThreads + threadIdx.x; v < NV; v += (long long)gridDim.x * kThreads) {
-        Normalized n = normalize_voxel(P, v, NV);
-        if (n.count > 0) {
-            ++uniq;
-            mx = max(mx, n.count);
-            if (n.count >= VCT_MAX_EXACT_FRAGMENTS) flags |= VCT_STATS_COUNT_OVERFLOW;
+#pragma unroll 1
+    for (int it = 0; it < kBrickVox / 4 / kThreads; ++it) {
+        const int q = threadIdx.x + it * kThreads;
+        const int lx = (q & 3) * 4, ly = (q >> 2) & 15, lz = q >> 6;
+        const int x = bx * kBrick + lx, y = by * kBrick + ly, z = bz * kBrick + lz;
+        const long long v0 = ((long long)z * N + y) * N + x;
+        const uint32_t ob = (__ldg(P.occ + (v0 >> 5)) >> (v0 & 31)) & 15u;
+        uint32_t lb = 0;
+        if (FUSED) lb = (__ldg(R.lit + (v0 >> 5)) >> (v0 & 31)) & 15u;
+        uint4 rec[4][2];
+        uint4* recp = reinterpret_cast<uint4*>(P.acc + (long long)kAccWords * v0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if ((ob >> j) & 1u) {
+                rec[j][0] = __ldcs(recp + 2 * j);
+                rec[j][1] = __ldcs(recp + 2 * j + 1);
+            } else {
+                rec[j][0] = rec[j][1] = make_uint4(0u, 0u, 0u, 0u);
+            }
         }
-        P.color[v] = n.color;
-        P.normal[v] = n.normal;
-        P.radiance[v] = seed_radiance(P, v, n);
+        uint4 prev[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+        if (P.temporal) {
+            const uint4* rp = reinterpret_cast<const uint4*>(P.radiance + v0);
+            prev[0] = rp[0];
+            prev[1] = rp[1];
+        }
+        uint2 col[4], nrm[4], rad[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t c = rec[j][0].x;
+            float alpha = 0.0f;
+            col[j] = make_uint2(0u, 0u);
+            nrm[j] = make_uint2(0u, 0u);
+            if ((ob >> j) & 1u) {
+                __stcs(recp + 2 * j, make_uint4(0u, 0u, 0u, 0u));
+                __stcs(recp + 2 * j + 1, make_uint4(0u, 0u, 0u, 0u));
+                ++uniq;
+                mx = max(mx, c);
+                if (c >= VCT_MAX_EXACT_FRAGMENTS) flags |= VCT_STATS_COUNT_OVERFLOW;
+                // transferVoxels.comp:37-51: colour / count, opacity override.
+                const float denom = 65535.0f * __uint2float_rn(c);
+                alpha = P.opacity > 0.0f ? P.opacity : 1.0f;
+                col[j] = pack_h4(__fdiv_rn(__uint2float_rn(rec[j][0].y), denom),
+                                 __fdiv_rn(__uint2float_rn(rec[j][0].z), denom),
+                                 __fdiv_rn(__uint2float_rn(rec[j][0].w), denom), alpha);
+                nrm[j] = pack_h4(__fdiv_rn(__uint2float_rn(rec[j][1].x), denom),
+                                 __fdiv_rn(__uint2float_rn(rec[j][1].y), denom),
+                                 __fdiv_rn(__uint2float_rn(rec[j][1].z), denom), 1.0f);
+            }
+            // transferVoxels.comp:53-62: radiance seed.
+            if (P.temporal) {
+                const float w = 1.0f - P.decay;
+                const uint2 pv = (j & 1) ? make_uint2(prev[j >> 1].z, prev[j >> 1].w)
+                                         : make_uint2(prev[j >> 1].x, prev[j >> 1].y);
+                const float4 p4 = unpack_h4(pv);
+                rad[j] = pack_h4(p4.x * (1.0f - w) + 0.0f * w, p4.y * (1.0f - w) + 0.0f * w,
+                                 p4.z * (1.0f - w) + 0.0f * w, p4.w * (1.0f - w) + alpha * w);
+            } else {
+                rad[j] = ((ob >> j) & 1u) ? pack_h4(0.0f, 0.0f, 0.0f, alpha) : make_uint2(0u, 0u);
+            }
+            if (FUSED && ((lb >> j) & 1u))
+                rad[j] = (R.lighting && !R.dilate) ? light_voxel(R.light_vox, R.light_int, col[j], nrm[j], x + j, y, z)
+                                                   : col[j];
+        }
+        store4(P.color + v0, col);
+        store4(P.normal + v0, nrm);
+        store4(P.radiance + v0, rad);
+        if (FUSED) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                s0[(lz * kBrick + ly) * kBrick + lx + j] = rad[j];
+                if (R.surf[0]) surf3Dwrite(rad[j], R.surf[0], (x + j) * (int)sizeof(uint2), y, z);
+            }
+        }
     }
+    if (FUSED) __syncthreads();
     block_stats(P.stats, uniq, mx, flags);
+    if (FUSED) {
+        uint2* a = s0;
+        uint2* b = s1;
+        int side = kBrick;
+        for (int l = 1; l <= R.mip_levels; ++l) {
+            const int sub = side / 2;
+            reduce_level(a, b, side, R.radiance_levels[l], R.surf[l], N >> l, bx * sub, by * sub, bz * sub);
+            __syncthreads();
+            uint2* t = a;
+            a = b;
+            b = t;
+            side = sub;
+        }
+    }
 }
 
+// ------------------------------------------------------------- injection
 // injectRadiance.comp:40-56: texel -> voxel.  Returns false when the shader
 // would return early.
 __device__ __forceinline__ bool inject_voxel(const InjectParams& P, int x, int y, int& ix, int& iy, int& iz) {
@@ -119,21 +231,7 @@ __device__ __forceinline__ bool inject_voxel(const InjectParams& P, int x, int y
     return !(ix >= P.dim || iy >= P.dim || iz >= P.dim || ix < 0 || iy < 0 || iz < 0);
 }
 
-__device__ __forceinline__ bool in_grid(int x, int y, int z, int N) {
-    return x >= 0 && y >= 0 && z >= 0 && x < N && y < N && z < N;
-}
-
-// radianceLighting branch (injectRadiance.comp:222-230).
-__device__ __forceinline__ uint2 light_voxel(f3 light_vox, f3 light_int, uint2 color, uint2 normal, int x, int y,
-                                             int z) {
-    float4 c = unpack_h4(color);
-    float4 nn = unpack_h4(normal);
-    f3 n = mk(2.0f * nn.x - 1.0f, 2.0f * nn.y - 1.0f, 2.0f * nn.z - 1.0f);
-    f3 L = normalize(sub(light_vox, mk((float)x, (float)y, (float)z)));
-    float diff = fmaxf(dot(n, L), 0.0f);
-    return pack_h4((diff * light_int.x) * c.x, (diff * light_int.y) * c.y, (diff * light_int.z) * c.z, c.w);
-}
-
+// injectRadiance.comp:58-72, sic: (-1,0,0) twice and no (0,0,-1).
 __constant__ int kDilate[7][3] = {{0, 0, 0}, {0, 0, 1}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {1, 0, 0}, {-1, 0, 0}};
 
 __global__ void __launch_bounds__(kThreads) inject_kernel(const InjectParams P) {
@@ -176,42 +274,6 @@ __global__ void __launch_bounds__(kThreads) inject_mark_kernel(const InjectParam
     }
 }
 
-// -------------------------------------------------------------------- mips
-// filterRadiance.comp BOX2: fp32 sum over the children in the shader's order
-// (z fastest, then y, then x), times 0.125, rounded to binary16.
-__device__ __forceinline__ uint2 box8(const uint2 c[8]) {
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        float4 t = unpack_h4(c[i]);
-        acc.x += t.x;
-        acc.y += t.y;
-        acc.z += t.z;
-        acc.w += t.w;
-    }
-    return pack_h4(acc.x * 0.125f, acc.y * 0.125f, acc.z * 0.125f, acc.w * 0.125f);
-}
-
-// Reduces a cube of side S (in shared memory, x fastest) into side S/2.
-// Child order index i = ox*4 + oy*2 + oz.
-__device__ __forceinline__ void reduce_level(const uint2* src, uint2* dst, int S, uint2* gdst, int gS, int gx0,
-                                             int gy0, int gz0) {
-    const int D = S / 2;
-    const int n = D * D * D;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        int x = t % D, y = (t / D) % D, z = t / (D * D);
-        uint2 c[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            int ox = i >> 2, oy = (i >> 1) & 1, oz = i & 1;
-            c[i] = src[((2 * z + oz) * S + (2 * y + oy)) * S + (2 * x + ox)];
-        }
-        uint2 r = box8(c);
-        dst[t] = r;
-        gdst[((long long)(gz0 + z) * gS + (gy0 + y)) * gS + (gx0 + x)] = r;
-    }
-}
-
 // One 16^3 brick of level `first` -> up to 4 coarser levels.
 __global__ void __launch_bounds__(kThreads) mip_brick_kernel(const MipLevels M, int first, int nlev) {
     __shared__ uint2 s0[kBrickVox];
@@ -229,9 +291,8 @@ __global__ void __launch_bounds__(kThreads) mip_brick_kernel(const MipLevels M, 
     uint2* b = s1;
     int side = kBrick;
     for (int l = 1; l <= nlev; ++l) {
-        int gS = S >> l;
         int sub = side / 2;
-        reduce_level(a, b, side, M.level[first + l], gS, bx * sub, by * sub, bz * sub);
+        reduce_level(a, b, side, M.level[first + l], M.surf[first + l], S >> l, bx * sub, by * sub, bz * sub);
         __syncthreads();
         uint2* t = a;
         a = b;
@@ -252,64 +313,12 @@ __global__ void __launch_bounds__(kThreads) mip_tail_kernel(const MipLevels M, i
     uint2* b = s1;
     int side = S;
     for (int l = first + 1; l < M.levels; ++l) {
-        reduce_level(a, b, side, M.level[l], side / 2, 0, 0, 0);
+        reduce_level(a, b, side, M.level[l], M.surf[l], side / 2, 0, 0, 0);
         __syncthreads();
         uint2* t = a;
         a = b;
         b = t;
         side /= 2;
-    }
-}
-
-// Fused: normalisation + injection resolve + radiance levels 1..4 of one
-// 16^3 brick.  Equivalent to normalize_kernel; inject_kernel; the first four
-// filterRadiance dispatches, because the injected value of a voxel depends
-// only on that voxel (idempotent stores).
-__global__ void __launch_bounds__(kThreads) resolve_kernel(const ResolveParams R) {
-    __shared__ uint2 s0[kBrickVox];
-    __shared__ uint2 s1[kBrickVox / 8];
-    const NormalizeParams& P = R.norm;
-    const int N = P.dim;
-    const long long NV = (long long)N * N * N;
-    const int bpa = N / kBrick;
-    const int bx = blockIdx.x % bpa, by = (blockIdx.x / bpa) % bpa, bz = blockIdx.x / (bpa * bpa);
-    uint32_t uniq = 0, mx = 0, flags = 0;
-    for (int t = threadIdx.x; t < kBrickVox; t += kThreads) {
-        int x = bx * kBrick + (t & 15), y = by * kBrick + ((t >> 4) & 15), z = bz * kBrick + (t >> 8);
-        long long v = ((long long)z * N + y) * N + x;
-        Normalized n = normalize_voxel(P, v, NV);
-        if (n.count > 0) {
-            ++uniq;
-            mx = max(mx, n.count);
-            if (n.count >= VCT_MAX_EXACT_FRAGMENTS) flags |= VCT_STATS_COUNT_OVERFLOW;
-        }
-        P.color[v] = n.color;
-        P.normal[v] = n.normal;
-        uint2 rad = seed_radiance(P, v, n);
-        uint32_t word = R.lit[v >> 5];
-        if (word & (1u << (v & 31))) {
-            if (R.lighting && !R.dilate)
-                rad = light_voxel(R.light_vox, R.light_int, n.color, n.normal, x, y, z);
-            else
-                rad = n.color;
-        }
-        P.radiance[v] = rad;
-        s0[t] = rad;
-    }
-    __syncthreads();
-    block_stats(P.stats, uniq, mx, flags);
-    uint2* a = s0;
-    uint2* b = s1;
-    int side = kBrick;
-    for (int l = 1; l <= R.mip_levels; ++l) {
-        int gS = N >> l;
-        int sub = side / 2;
-        reduce_level(a, b, side, R.radiance_levels[l], gS, bx * sub, by * sub, bz * sub);
-        __syncthreads();
-        uint2* t = a;
-        a = b;
-        b = t;
-        side = sub;
     }
 }
 
@@ -321,10 +330,11 @@ __global__ void fill_u32_kernel(uint32_t* p, uint32_t v, long long n) {
 }  // namespace
 
 void launch_normalize(const NormalizeParams& P, cudaStream_t s) {
-    long long NV = (long long)P.dim * P.dim * P.dim;
-    long long blocks = (NV + kThreads - 1) / kThreads;
-    long long maxb = (long long)P.num_sms * 16;
-    normalize_kernel<<<(unsigned)(blocks < maxb ? blocks : maxb), kThreads, 0, s>>>(P);
+    ResolveParams R;
+    memset(&R, 0, sizeof R);
+    R.norm = P;
+    const int bpa = P.dim / kBrick;
+    resolve_kernel<false><<<bpa * bpa * bpa, kThreads, 0, s>>>(R);
     note_launches(1);
 }
 
@@ -341,8 +351,8 @@ void launch_inject_mark(const InjectParams& P, cudaStream_t s) {
 }
 
 void launch_resolve(const ResolveParams& R, cudaStream_t s) {
-    int bpa = R.norm.dim / kBrick;
-    resolve_kernel<<<bpa * bpa * bpa, kThreads, 0, s>>>(R);
+    const int bpa = R.norm.dim / kBrick;
+    resolve_kernel<true><<<bpa * bpa * bpa, kThreads, 0, s>>>(R);
     note_launches(1);
 }
 

@@ -1,23 +1,53 @@
 // Triangle voxelisation: shaders/voxelize.geom:25-73 + voxelize.frag:75-280.
 //
-// One warp per triangle (grid-stride).  All lanes run the geometry-shader
-// part (dominant axis, per-axis projection, snapping) redundantly, then the
-// lanes stride over the triangle's pixel bounding box and each covered pixel
-// centre becomes one fragment: it is lit by every enabled light (shadowed by
-// the 5-tap PCF for shadow casters), and its colour, normal and a count of 1
-// are added into the integer accumulators with atomics.  Integer sums make
-// the result independent of fragment order: it is bit-exact against the CPU
-// oracle.  Compiled with --fmad=false (see vct_device.cuh).
+// Three launches, balanced at fragment granularity (triangle sizes vary by
+// more than three orders of magnitude in one scene):
+//  1. setup_kernel, one thread per triangle: the geometry-shader part
+//     (dominant axis from the summed vertex normals, per-axis ortho
+//     projection, snapping to the 1/256 sub-pixel grid, bounding box) into a
+//     48-byte record, and the triangle's share of work: its bounding box in
+//     units of kUnit pixels, with a block-local exclusive scan;
+//  2. scan_kernel, one CTA: exclusive scan of the per-block unit totals;
+//  3. raster_kernel, persistent: every warp takes an equal contiguous range
+//     of work units, tests 32 pixel centres at a time for coverage, compacts
+//     covered fragments (clipped to the depth range) with a ballot into a
+//     per-warp queue in shared memory, and whenever 32 are queued each lane
+//     lights one fragment (all enabled lights, 5-tap PCF for shadow casters)
+//     and adds it into the voxel's 32-byte accumulator record with four
+//     64-bit atomics.
+//
+// Integer sums make the result independent of fragment order: it is
+// bit-exact against the CPU oracle.  Compiled with --fmad=false (see
+// vct_device.cuh).
 #include "vct_device.cuh"
 
 namespace vct {
 
+namespace {
+
+constexpr int kWarps = 8;
+constexpr int kQueue = 64;
+constexpr int kSetupThreads = 256;
+constexpr int kUnit = 512;  // bounding-box pixels per work unit
+
+struct FragQueue {
+    int tri[kQueue];
+    uint32_t pix[kQueue];  // px | py << 11 | axis << 22
+    float l0[kQueue], l1[kQueue], l2[kQueue], z[kQueue];
+};
+
 __device__ __forceinline__ float shadow_factor(const AccumParams& P, f3 wp) {
     float c[4];
     mat_vec(P.ls, wp.x, wp.y, wp.z, 1.0f, c);
-    float sx = (__fdiv_rn(c[0], c[3]) + 1.0f) * 0.5f;
-    float sy = (__fdiv_rn(c[1], c[3]) + 1.0f) * 0.5f;
-    float sz = (__fdiv_rn(c[2], c[3]) + 1.0f) * 0.5f;
+    // x / 1 == x exactly: skip the divide for an orthographic light.
+    if (c[3] != 1.0f) {
+        c[0] = __fdiv_rn(c[0], c[3]);
+        c[1] = __fdiv_rn(c[1], c[3]);
+        c[2] = __fdiv_rn(c[2], c[3]);
+    }
+    float sx = (c[0] + 1.0f) * 0.5f;
+    float sy = (c[1] + 1.0f) * 0.5f;
+    float sz = (c[2] + 1.0f) * 0.5f;
     float frag = sz - 0.01f;
     if (frag > 1.0f) return 0.0f;
     const int ox[5] = {0, 1, 0, -1, 0};
@@ -29,20 +59,15 @@ __device__ __forceinline__ float shadow_factor(const AccumParams& P, f3 wp) {
     return __fdiv_rn(f, 5.0f);
 }
 
-__global__ void __launch_bounds__(256) accumulate_kernel(const AccumParams P) {
-    const int lane = threadIdx.x & 31;
-    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    const int N = P.dim;
-    const long long NV = (long long)N * N * N;
-    unsigned frag_count = 0;
-
-    for (long long t = warp; t < P.ntri; t += nwarps) {
+// ------------------------------------------------------------- 1. setup
+__global__ void __launch_bounds__(kSetupThreads) setup_kernel(const AccumParams P) {
+    const long long t = (long long)blockIdx.x * kSetupThreads + threadIdx.x;
+    uint32_t units = 0;
+    if (t < P.ntri) {
         const float* Pp = P.pos + t * 9;
         const float* Pn = P.nrm + t * 9;
-        f3 p[3] = {ld3(Pp), ld3(Pp + 3), ld3(Pp + 6)};
-        f3 n[3] = {ld3(Pn), ld3(Pn + 3), ld3(Pn + 6)};
-        f3 fn = normalize(add(add(n[0], n[1]), n[2]));
+        f3 n0 = ld3(Pn), n1 = ld3(Pn + 3), n2 = ld3(Pn + 6);
+        f3 fn = normalize(add(add(n0, n1), n2));
         float ax = fabsf(fn.x), ay = fabsf(fn.y), az = fabsf(fn.z);
         int axis = 2;
         if (ax > ay && ax > az)
@@ -51,100 +76,309 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const AccumParams P) {
             axis = 1;
         if (P.axis_override >= 0 && P.axis_override <= 2) axis = P.axis_override;
         const float* M = P.mvp + 16 * axis;
+        const int N = P.dim;
         float wx[3], wy[3], z[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             float c[4];
-            mat_vec(M, p[k].x, p[k].y, p[k].z, 1.0f, c);
+            mat_vec(M, Pp[3 * k], Pp[3 * k + 1], Pp[3 * k + 2], 1.0f, c);
             float nx = __fdiv_rn(c[0], c[3]), ny = __fdiv_rn(c[1], c[3]);
             z[k] = __fdiv_rn(c[2], c[3]);
             wx[k] = (nx + 1.0f) * 0.5f * (float)N;
             wy[k] = (ny + 1.0f) * 0.5f * (float)N;
         }
         RasterTri rt;
-        if (!raster_setup(wx, wy, N, N, rt)) continue;
-        const f3 col0 = ld3(P.albedo + t * 3);
-        const int bw = rt.px1 - rt.px0 + 1;
-        const int npx = bw * (rt.py1 - rt.py0 + 1);
-        for (int idx = lane; idx < npx; idx += 32) {
-            const int py = rt.py0 + idx / bw;
-            const int px = rt.px0 + idx % bw;
-            long long e[3];
-            if (!raster_cover(rt, px, py, e)) continue;
-            float l[3];
-            raster_weights(rt, e, l);
-            float zf = interp(l, z[0], z[1], z[2]);
-            if (!(zf >= -1.0f && zf <= 1.0f)) continue;
-            ++frag_count;
-            f3 wp = mk(interp(l, p[0].x, p[1].x, p[2].x), interp(l, p[0].y, p[1].y, p[2].y),
-                       interp(l, p[0].z, p[1].z, p[2].z));
-            f3 ni = mk(interp(l, n[0].x, n[1].x, n[2].x), interp(l, n[0].y, n[1].y, n[2].y),
-                       interp(l, n[0].z, n[1].z, n[2].z));
-            f3 Nf = normalize(ni);
-            f3 color = col0;
-            if (P.lighting) {
-                f3 fin = mk(0.0f, 0.0f, 0.0f);
-                for (int li = 0; li < P.nlights; ++li) {
-                    const LightDev& L = P.lights[li];
-                    if (!L.enabled) continue;
-                    f3 lit = mk(0.0f, 0.0f, 0.0f);
-                    if (L.type == 0u) {
-                        f3 d = sub(L.position, wp);
-                        float ndl = fmaxf(0.0f, dot(Nf, normalize(d)));
-                        lit = mul(mulv(mul(color, L.intensity), L.color), ndl);
-                        float att = 1.0f - smoothstep(0.75f * L.range, L.range, length(d));
-                        lit = mul(lit, att);
-                    } else if (L.type == 1u) {
-                        float ndl = fmaxf(0.0f, dot(Nf, normalize(mk(-L.direction.x, -L.direction.y, -L.direction.z))));
-                        lit = mul(mul(mulv(color, L.color), L.intensity), ndl);
+        if (raster_setup(wx, wy, N, N, rt)) {
+            const uint32_t bw = rt.px1 - rt.px0 + 1, bh = rt.py1 - rt.py0 + 1;
+            const uint32_t bias = (rt.bias[0] ? 1u : 0u) | (rt.bias[1] ? 2u : 0u) | (rt.bias[2] ? 4u : 0u);
+            const float inv = __fdiv_rn(1.0f, __ll2float_rn(rt.area));
+            uint4* rec = P.tri_rec + 3 * t;
+            rec[0] = make_uint4((uint32_t)rt.X[0], (uint32_t)rt.Y[0], (uint32_t)rt.X[1], (uint32_t)rt.Y[1]);
+            rec[1] = make_uint4((uint32_t)rt.X[2], (uint32_t)rt.Y[2], __float_as_uint(z[0]), __float_as_uint(z[1]));
+            rec[2] = make_uint4(__float_as_uint(z[2]), __float_as_uint(inv),
+                                (uint32_t)rt.px0 | ((uint32_t)rt.py0 << 11) | ((uint32_t)axis << 22) |
+                                    ((uint32_t)rt.perm1 << 24) | (bias << 25),
+                                bw | (bh << 11));
+            units = (bw * bh + kUnit - 1) / kUnit;
+        }
+        P.tri_units[t] = units;
+    }
+    // Block-local exclusive scan of the unit counts.
+    __shared__ uint32_t warp_tot[kSetupThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t incl = units;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kSetupThreads / 32; ++w) {
+        before += (w < wid) ? warp_tot[w] : 0u;
+        total += warp_tot[w];
+    }
+    if (t < P.ntri) P.tri_scan[t] = before + incl - units;
+    if (threadIdx.x == 0) P.block_off[blockIdx.x] = total;
+}
+
+// --------------------------------------------------------------- 2. scan
+__global__ void __launch_bounds__(1024) scan_kernel(uint32_t* block_off, int nblocks) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int base = 0; base < nblocks; base += 1024) {
+        const int i = base + threadIdx.x;
+        const uint32_t v = i < nblocks ? block_off[i] : 0u;
+        uint32_t incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t s = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += s;
+        }
+        if (lane == 31) warp_tot[wid] = incl;
+        __syncthreads();
+        uint32_t before = carry, total = 0;
+        for (int w = 0; w < 32; ++w) {
+            before += (w < wid) ? warp_tot[w] : 0u;
+            total += warp_tot[w];
+        }
+        if (i < nblocks) block_off[i] = before + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) block_off[nblocks] = carry;
+}
+
+// ------------------------------------------------------------- 3. raster
+// voxelize.frag:186-280 for one queued fragment.
+__device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQueue& q, int e) {
+    const long long t = q.tri[e];
+    const uint32_t pix = q.pix[e];
+    const int px = (int)(pix & 0x7ffu), py = (int)((pix >> 11) & 0x7ffu), axis = (int)(pix >> 22);
+    const float l[3] = {q.l0[e], q.l1[e], q.l2[e]};
+    const float zf = q.z[e];
+    const float* Pp = P.pos + t * 9;
+    const float* Pn = P.nrm + t * 9;
+    const f3 p0 = ld3(Pp), p1 = ld3(Pp + 3), p2 = ld3(Pp + 6);
+    const f3 n0 = ld3(Pn), n1 = ld3(Pn + 3), n2 = ld3(Pn + 6);
+    const f3 wp = mk(interp(l, p0.x, p1.x, p2.x), interp(l, p0.y, p1.y, p2.y), interp(l, p0.z, p1.z, p2.z));
+    const f3 ni = mk(interp(l, n0.x, n1.x, n2.x), interp(l, n0.y, n1.y, n2.y), interp(l, n0.z, n1.z, n2.z));
+    const f3 Nf = normalize(ni);
+    f3 color = ld3(P.albedo + t * 3);
+    if (P.lighting) {
+        f3 fin = mk(0.0f, 0.0f, 0.0f);
+        for (int li = 0; li < P.nlights; ++li) {
+            const LightDev& L = P.lights[li];
+            if (!L.enabled) continue;
+            f3 lit = mk(0.0f, 0.0f, 0.0f);
+            if (L.type == 0u) {
+                f3 d = sub(L.position, wp);
+                float ndl = fmaxf(0.0f, dot(Nf, normalize(d)));
+                lit = mul(mulv(mul(color, L.intensity), L.color), ndl);
+                float att = 1.0f - smoothstep(L.range075, L.range, length(d));
+                lit = mul(lit, att);
+            } else if (L.type == 1u) {
+                float ndl = fmaxf(0.0f, dot(Nf, L.neg_dir_n));
+                lit = mul(mul(mulv(color, L.color), L.intensity), ndl);
+            }
+            if (L.shadow_caster) lit = mul(lit, 1.0f - shadow_factor(P, wp));
+            fin = add(fin, lit);
+        }
+        color = mk(clampf(fin.x, 0.0f, 1.0f), clampf(fin.y, 0.0f, 1.0f), clampf(fin.z, 0.0f, 1.0f));
+    }
+    const f3 n01 = mk((Nf.x + 1.0f) * 0.5f, (Nf.y + 1.0f) * 0.5f, (Nf.z + 1.0f) * 0.5f);
+    // voxelize.frag:79-108 with the axis swizzle resolved: the projected
+    // coordinates are the pixel indices, the depth axis is trunc(N*(1-u.z)).
+    const int N = P.dim;
+    const float uz = (zf + 1.0f) * 0.5f;
+    const int iz = __float2int_rz((float)N * (1.0f - uz));
+    int vx, vy, vz;
+    if (axis == 0) {
+        vx = iz;
+        vy = py;
+        vz = N - 1 - px;
+    } else if (axis == 1) {
+        vx = px;
+        vy = iz;
+        vz = N - 1 - py;
+    } else {
+        vx = px;
+        vy = py;
+        vz = iz;
+    }
+    if (vx < 0 || vy < 0 || vz < 0 || vx >= N || vy >= N || vz >= N) return;
+    const long long v = ((long long)vz * N + vy) * N + vx;
+    unsigned long long* rec = reinterpret_cast<unsigned long long*>(P.acc + (long long)kAccWords * v);
+    const unsigned long long qr = quant16(color.x), qg = quant16(color.y), qb = quant16(color.z);
+    const unsigned long long qx = quant16(n01.x), qy = quant16(n01.y), qz = quant16(n01.z);
+    const unsigned long long old = atomicAdd(rec + 0, 1ull | (qr << 32));
+    atomicAdd(rec + 1, qg | (qb << 32));
+    atomicAdd(rec + 2, qx | (qy << 32));
+    atomicAdd(rec + 3, qz);
+    if ((uint32_t)old == 0u) atomicOr(P.occ + (v >> 5), 1u << (v & 31));
+}
+
+__device__ __forceinline__ long long unit_start(const AccumParams& P, long long t) {
+    return (long long)P.block_off[t / kSetupThreads] + P.tri_scan[t];
+}
+
+__global__ void __launch_bounds__(kWarps * 32, 2) raster_kernel(const AccumParams P, int nblocks) {
+    __shared__ FragQueue queues[kWarps];
+    const int lane = threadIdx.x & 31;
+    FragQueue& q = queues[threadIdx.x >> 5];
+    const unsigned FULL = 0xffffffffu;
+    const long long nw = (long long)gridDim.x * kWarps;
+    const long long w = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const long long total = P.block_off[nblocks];
+    const long long u0 = total * w / nw, u1 = total * (w + 1) / nw;
+    int qn = 0;  // queued fragments (warp-uniform)
+    unsigned shaded = 0;
+
+    if (u0 < u1) {
+        // Triangle owning unit u0: binary search over the block offsets, then
+        // over the block-local scan.
+        int lo = 0, hi = nblocks - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((long long)P.block_off[mid] <= u0)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        long long tlo = (long long)lo * kSetupThreads;
+        long long thi = min(tlo + kSetupThreads, P.ntri) - 1;
+        while (tlo < thi) {
+            const long long mid = (tlo + thi + 1) >> 1;
+            if (unit_start(P, mid) <= u0)
+                tlo = mid;
+            else
+                thi = mid - 1;
+        }
+        long long t = tlo;
+        long long start = unit_start(P, t);
+        uint32_t nunits = P.tri_units[t];
+        for (long long u = u0; u < u1; ++u) {
+            while (u >= start + nunits) {
+                ++t;
+                start = unit_start(P, t);
+                nunits = P.tri_units[t];
+            }
+            const uint4* rp = P.tri_rec + 3 * t;
+            const uint4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
+            const int X[3] = {(int)r0.x, (int)r0.z, (int)r1.x};
+            const int Y[3] = {(int)r0.y, (int)r0.w, (int)r1.y};
+            const float z[3] = {__uint_as_float(r1.z), __uint_as_float(r1.w), __uint_as_float(r2.x)};
+            const float inv = __uint_as_float(r2.y);
+            const int px0 = (int)(r2.z & 0x7ffu), py0 = (int)((r2.z >> 11) & 0x7ffu);
+            const int axis = (int)((r2.z >> 22) & 3u), perm1 = (int)((r2.z >> 24) & 1u), bias = (int)(r2.z >> 25);
+            const int bw = (int)(r2.w & 0x7ffu), bh = (int)(r2.w >> 11);
+            const int p_begin = (int)(u - start) * kUnit;
+            const int p_end = min(p_begin + kUnit, bw * bh);
+            for (int c = p_begin; c < p_end; c += 32) {
+                const int idx = c + lane;
+                bool cov = false;
+                float l[3] = {0.f, 0.f, 0.f}, zf = 0.f;
+                int px = 0, py = 0;
+                if (idx < p_end) {
+                    const int row = idx / bw;
+                    py = py0 + row;
+                    px = px0 + (idx - row * bw);
+                    const long long sx = (long long)px * kSub + kSub / 2, sy = (long long)py * kSub + kSub / 2;
+                    long long e[3];
+                    cov = true;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const int a = (k + 1) % 3, b = (k + 2) % 3;
+                        e[k] = (long long)(X[b] - X[a]) * (sy - Y[a]) - (long long)(Y[b] - Y[a]) * (sx - X[a]);
+                        cov = cov && (e[k] - ((bias >> k) & 1) >= 0);
                     }
-                    if (L.shadow_caster) lit = mul(lit, 1.0f - shadow_factor(P, wp));
-                    fin = add(fin, lit);
+                    if (cov) {
+                        const float w0 = __ll2float_rn(e[0]) * inv, w1 = __ll2float_rn(e[1]) * inv,
+                                    w2 = __ll2float_rn(e[2]) * inv;
+                        l[0] = w0;
+                        l[1] = perm1 ? w2 : w1;
+                        l[2] = perm1 ? w1 : w2;
+                        zf = interp(l, z[0], z[1], z[2]);
+                        cov = zf >= -1.0f && zf <= 1.0f;  // GL clipping
+                    }
                 }
-                color = mk(clampf(fin.x, 0.0f, 1.0f), clampf(fin.y, 0.0f, 1.0f), clampf(fin.z, 0.0f, 1.0f));
+                const unsigned m = __ballot_sync(FULL, cov);
+                if (cov) {
+                    const int slot = qn + __popc(m & ((1u << lane) - 1u));
+                    q.tri[slot] = (int)t;
+                    q.pix[slot] = (uint32_t)px | ((uint32_t)py << 11) | ((uint32_t)axis << 22);
+                    q.l0[slot] = l[0];
+                    q.l1[slot] = l[1];
+                    q.l2[slot] = l[2];
+                    q.z[slot] = zf;
+                }
+                qn += __popc(m);
+                if (qn >= 32) {
+                    __syncwarp();
+                    shade_fragment(P, q, lane);
+                    ++shaded;
+                    __syncwarp();
+                    if (lane < qn - 32) {
+                        const int src = 32 + lane;
+                        q.tri[lane] = q.tri[src];
+                        q.pix[lane] = q.pix[src];
+                        q.l0[lane] = q.l0[src];
+                        q.l1[lane] = q.l1[src];
+                        q.l2[lane] = q.l2[src];
+                        q.z[lane] = q.z[src];
+                    }
+                    __syncwarp();
+                    qn -= 32;
+                }
             }
-            f3 n01 = mk((Nf.x + 1.0f) * 0.5f, (Nf.y + 1.0f) * 0.5f, (Nf.z + 1.0f) * 0.5f);
-            float uz = (zf + 1.0f) * 0.5f;
-            float dz = (float)N * (1.0f - uz);
-            int iz = __float2int_rz(dz);
-            int vx, vy, vz;
-            if (axis == 0) {
-                vx = iz;
-                vy = py;
-                vz = N - 1 - px;
-            } else if (axis == 1) {
-                vx = px;
-                vy = iz;
-                vz = N - 1 - py;
-            } else {
-                vx = px;
-                vy = py;
-                vz = iz;
-            }
-            if (vx < 0 || vy < 0 || vz < 0 || vx >= N || vy >= N || vz >= N) continue;
-            const long long v = ((long long)vz * N + vy) * N + vx;
-            atomicAdd(P.count + v, 1u);
-            atomicAdd(P.sums + 0 * NV + v, quant16(color.x));
-            atomicAdd(P.sums + 1 * NV + v, quant16(color.y));
-            atomicAdd(P.sums + 2 * NV + v, quant16(color.z));
-            atomicAdd(P.sums + 3 * NV + v, quant16(n01.x));
-            atomicAdd(P.sums + 4 * NV + v, quant16(n01.y));
-            atomicAdd(P.sums + 5 * NV + v, quant16(n01.z));
         }
     }
-    // Warp-aggregated fragment counter (VoxelizeInfo.totalVoxelFragments).
-    unsigned total = __reduce_add_sync(0xffffffffu, frag_count);
-    if (lane == 0 && total) atomicAdd(&P.stats->total_voxel_fragments, total);
+    __syncwarp();
+    if (lane < qn) {
+        shade_fragment(P, q, lane);
+        ++shaded;
+    }
+    // VoxelizeInfo.totalVoxelFragments, aggregated per warp.
+    const unsigned tot = __reduce_add_sync(FULL, shaded);
+    if (lane == 0 && tot) atomicAdd(&P.stats->total_voxel_fragments, tot);
+}
+
+inline long long align256(long long b) { return (b + 255) & ~255LL; }
+
+}  // namespace
+
+long long accumulate_scratch_bytes(long long ntri) {
+    const long long nblocks = (ntri + kSetupThreads - 1) / kSetupThreads;
+    return align256(ntri * 48) + align256(ntri * 4) * 2 + align256((nblocks + 1) * 4);
+}
+
+void accumulate_bind_scratch(AccumParams& P, void* scratch) {
+    char* p = static_cast<char*>(scratch);
+    const long long ntri = P.ntri;
+    const long long nblocks = (ntri + kSetupThreads - 1) / kSetupThreads;
+    P.tri_rec = reinterpret_cast<uint4*>(p);
+    p += align256(ntri * 48);
+    P.tri_units = reinterpret_cast<uint32_t*>(p);
+    p += align256(ntri * 4);
+    P.tri_scan = reinterpret_cast<uint32_t*>(p);
+    p += align256(ntri * 4);
+    P.block_off = reinterpret_cast<uint32_t*>(p);
+    (void)nblocks;
 }
 
 void launch_accumulate(const AccumParams& P, cudaStream_t s) {
     if (P.ntri <= 0) return;
-    long long warps_needed = P.ntri;
-    long long blocks = (warps_needed * 32 + 255) / 256;
-    int maxb = P.num_sms * 8;
-    if (blocks > maxb) blocks = maxb;
-    accumulate_kernel<<<(unsigned)blocks, 256, 0, s>>>(P);
-    note_launches(1);
+    const int nblocks = (int)((P.ntri + kSetupThreads - 1) / kSetupThreads);
+    setup_kernel<<<nblocks, kSetupThreads, 0, s>>>(P);
+    scan_kernel<<<1, 1024, 0, s>>>(P.block_off, nblocks);
+    raster_kernel<<<P.num_sms * 2, kWarps * 32, 0, s>>>(P, nblocks);
+    note_launches(3);
 }
 
 }  // namespace vct
