@@ -267,6 +267,39 @@ vct_status vct_get_timers(vct_ctx* ctx, vct_timers* out);
 /* Number of kernels this library has launched since it was loaded. */
 uint64_t vct_launch_count(void);
 
+/* ---- voxelisation without allocation ---------------------------------- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a host application whose device memory is all reserved up front by its
+ * own allocator, a plugin in a process whose CUDA memory pool belongs to
+ * someone else, or a frame loop that must not allocate): vct_voxelize
+ * (accumulate + normalise) into volumes the caller owns, with no context and
+ * no device allocation by this library or anything it calls.  Its scratch
+ * (accumulator records, occupancy mask, work-distribution arrays, counters)
+ * is one fixed __device__ array of about 9 MiB that every GPU that loads the
+ * library keeps until the process exits.
+ *  - cfg->voxel_dim <= VCT_STATIC_MAX_DIM and tris->count <=
+ *    VCT_STATIC_MAX_TRIANGLES, otherwise VCT_ERR_INVALID_ARGUMENT.
+ *  - color_dev, normal_dev, radiance_dev: dim^3 RGBA16F voxels each
+ *    (8 bytes per voxel, x fastest), 16-byte aligned; radiance_dev receives
+ *    level 0 as transferVoxels.comp seeds it (and is read first when the
+ *    temporal filter is on).
+ *  - Runs on the current CUDA device, which must be cfg->device (checked;
+ *    this call never changes the current device).  The first call on a device looks up
+ *    the array's device address (cudaGetSymbolAddress) for that device; make
+ *    that first call before any stream capture.
+ *  - All calls share the one array: calls whose work overlaps on the GPU
+ *    (different streams, or different host threads) race.  Each call clears
+ *    the parts of the array that must start at zero.
+ *  - stats (host pointer) may be NULL; when given, the call synchronises
+ *    `stream` and returns the VoxelizeInfo counters of this call. */
+#define VCT_STATIC_MAX_DIM 64
+#define VCT_STATIC_MAX_TRIANGLES 16384
+vct_status vct_voxelize_static(const vct_config* cfg, const vct_params* params,
+                               const vct_triangles* tris, const vct_light* lights,
+                               int32_t n_lights, const vct_shadow_desc* shadow,
+                               uint16_t* color_dev, uint16_t* normal_dev,
+                               uint16_t* radiance_dev, vct_stats* stats, void* stream);
+
 /* ---- frame set-up (not part of the timed path) ------------------------ */
 /* Depth-only render of the scene from the light (the reference's shadow
  * pass, src/Application.cpp:213-233): fp32 depth in [0,1], cleared to 1. */

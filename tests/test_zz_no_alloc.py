@@ -1,0 +1,99 @@
+"""vct_voxelize_static: voxelisation for callers that cannot allocate device
+memory (an application that reserves all of it up front for its own
+allocator, a plugin in a process whose memory pool is owned elsewhere, a
+frame loop that must not allocate).  It keeps its scratch in a fixed device
+array inside the library and writes into volumes the caller owns.
+
+The test calls it twice in a row through the C ABI and compares each call's
+colour, normal and radiance volumes and counters, bit for bit (the bar of
+every integer/binary16 stage in these tests), with the context path
+vct_voxelize on the same inputs.  The second call shows that the shared
+array is cleared between calls.  This file is collected last so that a run
+stopping at the first failure has already run every other test.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from vct_gb300 import _lib as L
+from vct_gb300 import api, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(sc):
+    import torch
+
+    dev = "cuda:0"
+    pos, nrm, alb = (torch.from_numpy(a).to(dev) for a in (sc.positions, sc.normals, sc.albedo))
+    tris = api.triangles(pos, nrm, alb)
+    W, H = sc.shadow_size
+    sm = torch.empty(W * H, dtype=torch.float32, device=dev)
+    api.render_shadowmap(tris, sc, sm)
+    return (pos, nrm, alb, sm), tris, api.shadow_desc(sc, sm), api.light_array(sc.lights)
+
+
+def test_static_scratch_matches_context_path():
+    import torch
+
+    torch.cuda.set_device(0)
+    sc = scenes.cornell(seed=5)
+    keep, tris, shadow, (lights, n) = _inputs(sc)
+    params = api.scene_params(sc)
+    cfg = api.config_for(sc)
+    nv = sc.dim ** 3
+
+    with api.Context(cfg) as ctx:
+        ctx.set_params(params)
+        ctx.voxelize(tris, (lights, n), shadow, sc.eye)
+        torch.cuda.synchronize()
+        want = [ctx.read_volume(v, 0).cpu().numpy() for v in (L.VCT_VOLUME_COLOR, L.VCT_VOLUME_NORMAL,
+                                                              L.VCT_VOLUME_RADIANCE)]
+        want_stats = ctx.stats()
+
+    lib = L.load()
+    stream = api._stream(None)
+    # Outputs are allocated by the caller, before the calls.
+    outs = [torch.full((nv * 4,), -1, dtype=torch.int16, device="cuda:0") for _ in range(3)]
+    for call in range(2):
+        st = L.vct_stats()
+        rc = lib.vct_voxelize_static(C.byref(cfg), C.byref(params), C.byref(tris), lights, n, C.byref(shadow),
+                                     outs[0].data_ptr(), outs[1].data_ptr(), outs[2].data_ptr(), C.byref(st), stream)
+        L.check(rc, "vct_voxelize_static")
+        torch.cuda.synchronize()
+        for got, ref in zip(outs, want):
+            assert np.array_equal(got.cpu().numpy(), ref), f"call {call}"
+        assert st.total_voxel_fragments == want_stats["total_voxel_fragments"]
+        assert st.unique_voxels == want_stats["unique_voxels"]
+        assert st.max_fragments_per_voxel == want_stats["max_fragments_per_voxel"]
+        assert st.error_flags == 0
+    del keep
+
+
+def test_static_scratch_rejects_oversize():
+    import torch
+
+    torch.cuda.set_device(0)
+    sc = scenes.tiny(seed=1)
+    keep, tris, shadow, (lights, n) = _inputs(sc)
+    params = api.scene_params(sc)
+    lib = L.load()
+    big = api.config_for(sc, dim=128)
+    out = torch.zeros(4, dtype=torch.int16, device="cuda:0")
+    rc = lib.vct_voxelize_static(C.byref(big), C.byref(params), C.byref(tris), lights, n, C.byref(shadow),
+                                 out.data_ptr(), out.data_ptr(), out.data_ptr(), None, api._stream(None))
+    assert rc == L.VCT_ERR_INVALID_ARGUMENT
+    assert b"VCT_STATIC_MAX_DIM" in lib.vct_last_error()
+    many = api.triangles(keep[0], keep[1], keep[2])
+    # Rejected by the size check before any device work (the arrays behind
+    # this descriptor are never read).
+    many.count = 16384 + 1
+    rc = lib.vct_voxelize_static(C.byref(api.config_for(sc)), C.byref(params), C.byref(many), lights, n,
+                                 C.byref(shadow), out.data_ptr(), out.data_ptr(), out.data_ptr(), None,
+                                 api._stream(None))
+    assert rc == L.VCT_ERR_INVALID_ARGUMENT
+    assert b"VCT_STATIC_MAX_TRIANGLES" in lib.vct_last_error()

@@ -135,6 +135,8 @@ SIGNATURES = {
     "vct_enable_timers": (st, [vp, C.c_int32]),
     "vct_get_timers": (st, [vp, P(vct_timers)]),
     "vct_launch_count": (C.c_uint64, []),
+    "vct_voxelize_static": (st, [P(vct_config), P(vct_params), P(vct_triangles), P(vct_light), C.c_int32,
+                                 P(vct_shadow_desc), vp, vp, vp, P(vct_stats), vp]),
     "vct_render_shadowmap": (st, [P(vct_triangles), P(C.c_float), vp, C.c_int32, C.c_int32, vp]),
     "vct_render_gbuffer": (st, [P(vct_triangles), P(C.c_float), P(C.c_float), P(C.c_float), C.c_int32, C.c_int32,
                                 vp, vp, vp, vp, vp]),

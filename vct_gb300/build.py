@@ -34,6 +34,7 @@ CUDA_SOURCES = [
     ("volume.cu", ["--fmad=false"]),
     ("raster.cu", ["--fmad=false"]),
     ("trace.cu", []),
+    ("static_scratch.cu", []),
 ]
 CXX_SOURCES = ["capi.cpp"]
 

@@ -237,16 +237,35 @@ uint2* level_ptr(uint2* chain, const vct_ctx* ctx, int l) { return chain + ctx->
 
 f3 to_f3(const float* p) { return {p[0], p[1], p[2]}; }
 
-vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lights, int n,
-                      const vct_shadow_desc* sh, AccumParams& P) {
+}  // namespace
+
+namespace vct {
+
+vct_status set_error(vct_status s, const char* msg) { return fail(s, msg); }
+
+void voxel_mvp_host(const vct_config& c, float out[48]) { voxel_mvp(c, out); }
+
+vct_status validate_voxelize_inputs(const vct_config* cfg, const vct_params* p, const vct_triangles* t,
+                                    const vct_light* lights, int n, const vct_shadow_desc* shadow, bool* need_shadow) {
+    vct_status s = validate_config(cfg);
+    if (s == VCT_OK) s = validate_params(p);
+    if (s == VCT_OK) s = validate_tris(t);
+    if (s == VCT_OK) s = validate_lights(lights, n, need_shadow);
+    if (s != VCT_OK) return s;
+    *need_shadow = *need_shadow && p->voxelize_lighting;
+    return validate_shadow(shadow, *need_shadow);
+}
+
+void fill_accum_inputs(const vct_config& cfg, const vct_params& prm, const float mvp[48], const vct_triangles* t,
+                       const vct_light* lights, int n, const vct_shadow_desc* sh, AccumParams& P) {
     std::memset(&P, 0, sizeof P);
     P.pos = t->positions_dev;
     P.nrm = t->normals_dev;
     P.albedo = t->albedo_dev;
     P.ntri = t->count;
-    P.dim = ctx->dim;
-    P.lighting = ctx->params.voxelize_lighting;
-    P.axis_override = ctx->params.axis_override;
+    P.dim = cfg.voxel_dim;
+    P.lighting = prm.voxelize_lighting;
+    P.axis_override = prm.axis_override;
     P.nlights = n;
     for (int i = 0; i < n; ++i) {
         LightDev& L = P.lights[i];
@@ -264,13 +283,22 @@ vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lig
         L.neg_dir_n = {ndn.x, ndn.y, ndn.z};
         L.range075 = 0.75f * lights[i].range;
     }
-    std::memcpy(P.mvp, ctx->mvp, sizeof P.mvp);
+    std::memcpy(P.mvp, mvp, sizeof P.mvp);
     if (sh) {
         std::memcpy(P.ls, sh->ls, sizeof P.ls);
         P.shadowmap = sh->shadowmap_dev;
         P.sw = sh->width;
         P.sh = sh->height;
     }
+}
+
+}  // namespace vct
+
+namespace {
+
+vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lights, int n,
+                      const vct_shadow_desc* sh, AccumParams& P) {
+    fill_accum_inputs(ctx->cfg, ctx->params, ctx->mvp, t, lights, n, sh, P);
     P.acc = ctx->acc;
     P.occ = ctx->occ;
     P.stats = ctx->stats;

@@ -56,8 +56,14 @@ struct AccumParams {
     uint32_t* block_off;     // exclusive scan of per-block unit totals (+ total at [nblocks])
 };
 
-// Scratch bytes the voxeliser needs for `ntri` triangles.
-long long accumulate_scratch_bytes(long long ntri);
+constexpr int kSetupThreads = 256;  // triangles per setup block
+constexpr long long align256(long long b) { return (b + 255) & ~255LL; }
+// Scratch bytes the voxeliser needs for `ntri` triangles: a 48-byte setup
+// record, a unit count and a scan entry per triangle, one offset per block.
+constexpr long long accumulate_scratch_bytes(long long ntri) {
+    return align256(ntri * 48) + align256(ntri * 4) * 2 +
+           align256(((ntri + kSetupThreads - 1) / kSetupThreads + 1) * 4);
+}
 // Carves the scratch buffer into the AccumParams work arrays.
 void accumulate_bind_scratch(AccumParams& P, void* scratch);
 
@@ -165,6 +171,15 @@ struct GbufferRasterParams {
 
 // Counts kernel launches (vct_launch_count).
 void note_launches(int n);
+
+// Host helpers of the C ABI (capi.cpp), shared with the other entry points.
+vct_status set_error(vct_status s, const char* msg);
+void voxel_mvp_host(const vct_config& c, float out[48]);
+vct_status validate_voxelize_inputs(const vct_config* cfg, const vct_params* p, const vct_triangles* t,
+                                    const vct_light* lights, int n, const vct_shadow_desc* shadow, bool* need_shadow);
+// Fills every input field of AccumParams (not the accumulators, stats or scratch).
+void fill_accum_inputs(const vct_config& cfg, const vct_params& prm, const float mvp[48], const vct_triangles* t,
+                       const vct_light* lights, int n, const vct_shadow_desc* sh, AccumParams& P);
 
 void launch_accumulate(const AccumParams& P, cudaStream_t s);
 void launch_normalize(const NormalizeParams& P, cudaStream_t s);

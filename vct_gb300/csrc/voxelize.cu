@@ -27,7 +27,6 @@ namespace {
 
 constexpr int kWarps = 8;
 constexpr int kQueue = 64;
-constexpr int kSetupThreads = 256;
 constexpr int kUnit = 512;  // bounding-box pixels per work unit
 
 struct FragQueue {
@@ -349,19 +348,11 @@ __global__ void __launch_bounds__(kWarps * 32, 2) raster_kernel(const AccumParam
     if (lane == 0 && tot) atomicAdd(&P.stats->total_voxel_fragments, tot);
 }
 
-inline long long align256(long long b) { return (b + 255) & ~255LL; }
-
 }  // namespace
-
-long long accumulate_scratch_bytes(long long ntri) {
-    const long long nblocks = (ntri + kSetupThreads - 1) / kSetupThreads;
-    return align256(ntri * 48) + align256(ntri * 4) * 2 + align256((nblocks + 1) * 4);
-}
 
 void accumulate_bind_scratch(AccumParams& P, void* scratch) {
     char* p = static_cast<char*>(scratch);
     const long long ntri = P.ntri;
-    const long long nblocks = (ntri + kSetupThreads - 1) / kSetupThreads;
     P.tri_rec = reinterpret_cast<uint4*>(p);
     p += align256(ntri * 48);
     P.tri_units = reinterpret_cast<uint32_t*>(p);
@@ -369,7 +360,6 @@ void accumulate_bind_scratch(AccumParams& P, void* scratch) {
     P.tri_scan = reinterpret_cast<uint32_t*>(p);
     p += align256(ntri * 4);
     P.block_off = reinterpret_cast<uint32_t*>(p);
-    (void)nblocks;
 }
 
 void launch_accumulate(const AccumParams& P, cudaStream_t s) {
