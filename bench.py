@@ -52,7 +52,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="large", choices=["large", "cornell"])
-    ap.add_argument("--filter", default="software", choices=["software", "hardware"])
+    ap.add_argument("--filter", default="software", choices=["software", "levels", "hardware"],
+                    help="cone sampler: fp32 trilinear (exact), texture units per level + fp32 level blend, "
+                         "or texture units' trilinear-mip")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-rows", type=int, default=24, help="rows of the frame traced by the CPU baseline")
@@ -212,7 +214,8 @@ def run_ours(args, rank, world):
     out = api.trace_out(color=color)
     ctx = api.Context(api.config_for(sc, device=local))
     params = api.scene_params(sc)
-    params.trace_filter = L.VCT_FILTER_HARDWARE if args.filter == "hardware" else L.VCT_FILTER_SOFTWARE
+    params.trace_filter = {"software": L.VCT_FILTER_SOFTWARE, "levels": L.VCT_FILTER_HARDWARE_LEVELS,
+                           "hardware": L.VCT_FILTER_HARDWARE}[args.filter]
     ctx.set_params(params)
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)

@@ -106,6 +106,7 @@ typedef struct vct_cone_settings {
 
 #define VCT_FILTER_SOFTWARE 0 /* fp32 trilinear from the linear volume (exact GL semantics) */
 #define VCT_FILTER_HARDWARE 1 /* texture units' trilinear-mip filtering */
+#define VCT_FILTER_HARDWARE_LEVELS 2 /* texture units' trilinear filtering per level, levels blended in fp32 */
 
 /* Every hot-path uniform of the reference, with vct_default_params giving the
  * reference defaults of src/Application.h:36-103. */

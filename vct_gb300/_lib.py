@@ -26,6 +26,7 @@ VCT_LIGHT_DIRECTIONAL = 1
 VCT_CONFIG_COLOR_MIPS = 1
 VCT_FILTER_SOFTWARE = 0
 VCT_FILTER_HARDWARE = 1
+VCT_FILTER_HARDWARE_LEVELS = 2
 VCT_VOLUME_COLOR = 0
 VCT_VOLUME_NORMAL = 1
 VCT_VOLUME_RADIANCE = 2

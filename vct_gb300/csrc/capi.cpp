@@ -189,8 +189,9 @@ vct_status validate_params(const vct_params* p) {
         if (!std::isfinite(c->bias) || !std::isfinite(c->lod_offset) || !(c->cone_initial_height > 0.0f))
             return fail(VCT_ERR_INVALID_ARGUMENT, "cone bias/lod offset must be finite, initial height > 0");
     }
-    if (p->trace_filter != VCT_FILTER_SOFTWARE && p->trace_filter != VCT_FILTER_HARDWARE)
-        return fail(VCT_ERR_INVALID_ARGUMENT, "trace_filter must be VCT_FILTER_SOFTWARE or VCT_FILTER_HARDWARE");
+    if (p->trace_filter != VCT_FILTER_SOFTWARE && p->trace_filter != VCT_FILTER_HARDWARE &&
+        p->trace_filter != VCT_FILTER_HARDWARE_LEVELS)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "trace_filter must be one of VCT_FILTER_*");
     if (p->axis_override < -1 || p->axis_override > 2) return fail(VCT_ERR_INVALID_ARGUMENT, "axis_override in [-1, 2]");
     if (!std::isfinite(p->voxel_set_opacity) || !std::isfinite(p->temporal_decay))
         return fail(VCT_ERR_INVALID_ARGUMENT, "opacity/decay must be finite");
@@ -462,7 +463,7 @@ vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], co
     P.reflect_scale = pr.reflect_scale;
     P.max_distance = pr.max_distance > 0.0f ? pr.max_distance : std::sqrt(3.0f);
     P.ref_tbn_quirk = pr.ref_tbn_quirk;
-    P.hardware = pr.trace_filter == VCT_FILTER_HARDWARE;
+    P.filter = pr.trace_filter;
     P.tex = ctx->tex;
     for (auto p : {(const void*)g->position_dev, (const void*)g->normal_dev, (const void*)g->albedo_dev,
                    (const void*)out->irradiance_dev, (const void*)out->specular_dev, (const void*)out->color_dev})
@@ -742,7 +743,7 @@ vct_status vct_build_mips(vct_ctx* c, int32_t volume, void* stream) {
     if (volume == VCT_VOLUME_RADIANCE) {
         launch_mips(mip_levels(c, c->radiance, c->levels), 0, st);
         VCT_CHECK_LAUNCH("build mips");
-        if (c->params.trace_filter == VCT_FILTER_HARDWARE) {
+        if (c->params.trace_filter != VCT_FILTER_SOFTWARE) {
             vct_status s = refresh_texture(c, st);
             if (s != VCT_OK) return s;
         }
@@ -765,7 +766,7 @@ vct_status vct_trace(vct_ctx* c, const vct_gbuffer* g, const float eye[3], const
     DeviceScope ds(c->device);
     VCT_CUDA(ds.err);
     cudaStream_t st = as_stream(stream);
-    if (c->params.trace_filter == VCT_FILTER_HARDWARE && !c->tex_ready) {
+    if (c->params.trace_filter != VCT_FILTER_SOFTWARE && !c->tex_ready) {
         if ((s = refresh_texture(c, st)) != VCT_OK) return s;
     }
     TraceParams P;
@@ -802,7 +803,7 @@ vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lig
     launch_inject_mark(I, st);
     VCT_CHECK_LAUNCH("frame: inject mark");
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[2], st));
-    const bool hw = c->params.trace_filter == VCT_FILTER_HARDWARE;
+    const bool hw = c->params.trace_filter != VCT_FILTER_SOFTWARE;
     if (hw && (s = ensure_texture(c)) != VCT_OK) return s;
     ResolveParams R;
     std::memset(&R, 0, sizeof R);

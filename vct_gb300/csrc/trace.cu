@@ -55,10 +55,19 @@ __device__ __forceinline__ float4 trilinear(const TraceParams& P, int l, f3 p) {
     return lerp4(lerp4(x00, x10, b), lerp4(x01, x11, b), c);
 }
 
-template <bool HW>
+template <int MODE>
 __device__ __forceinline__ float4 sample_lod(const TraceParams& P, f3 p, float lambda) {
-    if (HW) return tex3DLod<float4>(P.tex, p.x, p.y, p.z, lambda);
+    if (MODE == VCT_FILTER_HARDWARE) return tex3DLod<float4>(P.tex, p.x, p.y, p.z, lambda);
     const int q = P.levels - 1;
+    if (MODE == VCT_FILTER_HARDWARE_LEVELS) {
+        // Texture units filter within each level; the two levels are blended
+        // with the exact fp32 fraction (GL_LINEAR_MIPMAP_LINEAR level choice).
+        if (lambda <= 0.0f) return tex3DLod<float4>(P.tex, p.x, p.y, p.z, 0.0f);
+        if (lambda >= (float)q) return tex3DLod<float4>(P.tex, p.x, p.y, p.z, (float)q);
+        const float fl = floorf(lambda);
+        return lerp4(tex3DLod<float4>(P.tex, p.x, p.y, p.z, fl), tex3DLod<float4>(P.tex, p.x, p.y, p.z, fl + 1.0f),
+                     lambda - fl);
+    }
     if (lambda <= 0.0f) {  // magnification: GL_NEAREST on level 0
         const int S = P.dim;
         return texel(P.chain, S, (int)floorf(p.x * S), (int)floorf(p.y * S), (int)floorf(p.z * S));
@@ -70,7 +79,7 @@ __device__ __forceinline__ float4 sample_lod(const TraceParams& P, f3 p, float l
     return lerp4(trilinear(P, d1, p), trilinear(P, d1 + 1, p), f);
 }
 
-template <bool HW>
+template <int MODE>
 __device__ float4 trace_cone(const TraceParams& P, f3 pos, f3 n, f3 dir, const vct_cone_settings& c, float maxd,
                              unsigned& ns) {
     dir = fnormalize(dir);
@@ -86,7 +95,7 @@ __device__ float4 trace_cone(const TraceParams& P, f3 pos, f3 n, f3 dir, const v
         f3 sp = add(start, mul(mul(dir, h), scale));
         if (sp.x < 0.f || sp.y < 0.f || sp.z < 0.f || sp.x > 1.f || sp.y > 1.f || sp.z > 1.f) break;
         if (h * scale > maxd) break;
-        float4 s = sample_lod<HW>(P, sp, lod + c.lod_offset);
+        float4 s = sample_lod<MODE>(P, sp, lod + c.lod_offset);
         ++ns;
         float a = 1.0f - alpha;
         col = add(col, mul(mk(s.x, s.y, s.z), a));
@@ -96,7 +105,7 @@ __device__ float4 trace_cone(const TraceParams& P, f3 pos, f3 n, f3 dir, const v
     return make_float4(col.x, col.y, col.z, alpha);
 }
 
-template <bool HW>
+template <int MODE>
 __global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int x = blockIdx.x * 16 + (wid & 1) * 8 + (lane & 7);
@@ -128,7 +137,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
                     const float dx = kConeDir[c][0], dy = kConeDir[c][1], dz = kConeDir[c][2];
                     f3 d = P.ref_tbn_quirk ? add(add(mul(T, dx), mul(B, dy)), mul(N, dz))
                                            : sub(add(mul(T, dx), mul(N, dy)), mul(B, dz));
-                    float4 cr = trace_cone<HW>(P, vp, N, d, P.diffuse, P.max_distance, ns);
+                    float4 cr = trace_cone<MODE>(P, vp, N, d, P.diffuse, P.max_distance, ns);
                     const float w = kConeWeight[c];
                     ind.x += w * cr.x;
                     ind.y += w * cr.y;
@@ -141,7 +150,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
                 if (P.enable_reflections) {
                     const f3 I = sub(mk(gp.x, gp.y, gp.z), P.eye);
                     const f3 R = sub(I, mul(N, 2.0f * dot(N, I)));
-                    spc = trace_cone<HW>(P, vp, N, R, P.specular_cone, P.max_distance, ns);
+                    spc = trace_cone<MODE>(P, vp, N, R, P.specular_cone, P.max_distance, ns);
                     rgb = add(rgb, mul(mk(spc.x, spc.y, spc.z), P.reflect_scale));
                 }
                 const float as = P.ambient_scale;
@@ -171,10 +180,12 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
 
 void launch_trace(const TraceParams& P, cudaStream_t s) {
     dim3 grid((P.width + 15) / 16, (P.height + 15) / 16);
-    if (P.hardware)
-        trace_kernel<true><<<grid, 256, 0, s>>>(P);
+    if (P.filter == VCT_FILTER_HARDWARE)
+        trace_kernel<VCT_FILTER_HARDWARE><<<grid, 256, 0, s>>>(P);
+    else if (P.filter == VCT_FILTER_HARDWARE_LEVELS)
+        trace_kernel<VCT_FILTER_HARDWARE_LEVELS><<<grid, 256, 0, s>>>(P);
     else
-        trace_kernel<false><<<grid, 256, 0, s>>>(P);
+        trace_kernel<VCT_FILTER_SOFTWARE><<<grid, 256, 0, s>>>(P);
     note_launches(1);
 }
 

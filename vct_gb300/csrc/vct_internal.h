@@ -140,7 +140,7 @@ struct TraceParams {
     int enable_indirect, enable_reflections, draw_occlusion, enable_postprocess;
     float ambient_scale, reflect_scale, max_distance;
     int ref_tbn_quirk;
-    int hardware;
+    int filter;  // VCT_FILTER_*
     cudaTextureObject_t tex;
 };
 
