@@ -730,7 +730,8 @@ static void trace_cone(const Sampler<T>& s, V<T> pos, V<T> n, V<T> dir, const or
         T r = h * tanh;
         T lod = std::log2(std::max(T(1), T(2) * r));
         V<T> sp = vadd(start, vmul(vmul(dir, h), scale));
-        if (sp.x < T(0) || sp.y < T(0) || sp.z < T(0) || sp.x > T(1) || sp.y > T(1) || sp.z > T(1)) break;
+        // any(notEqual(p, clamp(p, 0, 1))): leaves the volume, or is NaN.
+        if (!(sp.x >= T(0) && sp.y >= T(0) && sp.z >= T(0) && sp.x <= T(1) && sp.y <= T(1) && sp.z <= T(1))) break;
         if (h * scale > maxd) break;
         T sc[4];
         s.sample(sp, lod + (T)c.lod_offset, sc);

@@ -39,6 +39,8 @@ struct vct_ctx {
     cudaEvent_t ev[5] = {};
     void* vox_scratch = nullptr;  // voxeliser work-distribution arrays
     long long vox_scratch_bytes = 0;
+    uint2* pchain = nullptr;  // bordered radiance chain read by the software sampler
+    bool pad_ready = false;   // pchain holds the current radiance chain
 };
 
 namespace vct {
@@ -445,7 +447,7 @@ vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], co
     P.color = reinterpret_cast<float4*>(out->color_dev);
     P.samples = out->sample_count_dev;
     P.chain = ctx->radiance;
-    for (int l = 0; l < ctx->levels; ++l) P.level_off[l] = ctx->level_off[l];
+    P.pchain = ctx->pchain;
     P.dim = ctx->dim;
     P.levels = ctx->levels;
     P.vmin = to_f3(ctx->cfg.voxel_min);
@@ -582,6 +584,7 @@ vct_status vct_create(const vct_config* cfg, vct_ctx** out) {
         {(void**)&c->normal, (size_t)c->nv * 8},
         {(void**)&c->radiance, (size_t)chain_vox * 8},
         {(void**)&c->stats, sizeof(StatsDev)},
+        {(void**)&c->pchain, (size_t)padded_level_offset(c->dim, c->levels) * 8},
     };
     for (auto& a : allocs) {
         cudaError_t e = cudaMalloc(a.p, a.bytes);
@@ -606,7 +609,7 @@ vct_status vct_destroy(vct_ctx* c) {
     if (c->tex_array) cudaFreeMipmappedArray(c->tex_array);
     for (auto sf : c->surf)
         if (sf) cudaDestroySurfaceObject(sf);
-    void* ptrs[] = {c->acc, c->occ, c->lit, c->color, c->normal, c->radiance, c->stats, c->vox_scratch};
+    void* ptrs[] = {c->acc, c->occ, c->lit, c->color, c->normal, c->radiance, c->stats, c->vox_scratch, c->pchain};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -680,6 +683,8 @@ vct_status vct_voxelize_accumulate(vct_ctx* c, const vct_triangles* tris, const 
     VCT_CHECK_LAUNCH("voxelize accumulate");
     c->radiance_ready = false;
     c->mips_ready = false;
+    c->pad_ready = false;
+    c->tex_ready = false;
     return VCT_OK;
 }
 
@@ -699,6 +704,8 @@ vct_status vct_normalize(vct_ctx* c, void* stream) {
     c->stats_reset_pending = true;
     c->radiance_ready = true;
     c->mips_ready = false;
+    c->pad_ready = false;
+    c->tex_ready = false;
     return VCT_OK;
 }
 
@@ -732,6 +739,8 @@ vct_status vct_inject(vct_ctx* c, const vct_shadow_desc* shadow, const float eye
     launch_inject(P, as_stream(stream));
     VCT_CHECK_LAUNCH("inject");
     c->mips_ready = false;
+    c->pad_ready = false;
+    c->tex_ready = false;
     return VCT_OK;
 }
 
@@ -746,6 +755,10 @@ vct_status vct_build_mips(vct_ctx* c, int32_t volume, void* stream) {
         if (c->params.trace_filter != VCT_FILTER_SOFTWARE) {
             vct_status s = refresh_texture(c, st);
             if (s != VCT_OK) return s;
+        } else {
+            launch_pad_copy(c->radiance, c->pchain, c->dim, c->levels, st);
+            VCT_CHECK_LAUNCH("bordered chain copy");
+            c->pad_ready = true;
         }
         c->mips_ready = true;
         return VCT_OK;
@@ -768,6 +781,11 @@ vct_status vct_trace(vct_ctx* c, const vct_gbuffer* g, const float eye[3], const
     cudaStream_t st = as_stream(stream);
     if (c->params.trace_filter != VCT_FILTER_SOFTWARE && !c->tex_ready) {
         if ((s = refresh_texture(c, st)) != VCT_OK) return s;
+    }
+    if (c->params.trace_filter == VCT_FILTER_SOFTWARE && !c->pad_ready) {
+        launch_pad_copy(c->radiance, c->pchain, c->dim, c->levels, st);
+        VCT_CHECK_LAUNCH("bordered chain copy");
+        c->pad_ready = true;
     }
     TraceParams P;
     if ((s = fill_trace(c, g, eye, out, P)) != VCT_OK) return s;
@@ -815,21 +833,27 @@ vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lig
     R.light_int = I.light_int;
     R.lit = c->lit;
     R.mip_levels = std::min(4, c->levels - 1);
+    // The sampler's own copy of the chain is written by the same kernels:
+    // texture-unit surfaces, or the bordered chain of the software sampler.
     for (int l = 0; l <= R.mip_levels; ++l) {
         R.radiance_levels[l] = level_ptr(c->radiance, c, l);
         R.surf[l] = hw ? c->surf[l] : 0;
+        R.pad_levels[l] = hw ? nullptr : c->pchain + padded_level_offset(c->dim, l);
     }
     launch_resolve(R, st);
     VCT_CHECK_LAUNCH("frame: resolve");
     VCT_CUDA(cudaMemsetAsync(c->occ, 0, (size_t)((c->nv + 31) / 32) * 4, st));
     if (c->levels > 5) {
         MipLevels M = mip_levels(c, c->radiance, c->levels);
-        if (hw)
-            for (int l = 0; l < c->levels; ++l) M.surf[l] = c->surf[l];
+        for (int l = 0; l < c->levels; ++l) {
+            M.surf[l] = hw ? c->surf[l] : 0;
+            M.pad[l] = hw ? nullptr : c->pchain + padded_level_offset(c->dim, l);
+        }
         launch_mips(M, 4, st);
         VCT_CHECK_LAUNCH("frame: coarse mips");
     }
     c->tex_ready = hw;
+    c->pad_ready = !hw;
     c->stats_reset_pending = true;
     c->radiance_ready = true;
     c->mips_ready = true;

@@ -41,22 +41,52 @@ __device__ __forceinline__ float4 lerp4(float4 p, float4 q, float t) {
     return make_float4(p.x * s + q.x * t, p.y * s + q.y * t, p.z * s + q.z * t, p.w * s + q.w * t);
 }
 
-__device__ __forceinline__ float4 trilinear(const TraceParams& P, int l, f3 p) {
-    const int S = P.dim >> l;
-    const uint2* base = P.chain + P.level_off[l];
-    float u = p.x * (float)S - 0.5f, v = p.y * (float)S - 0.5f, w = p.z * (float)S - 0.5f;
-    float fu = floorf(u), fv = floorf(v), fw = floorf(w);
-    float a = u - fu, b = v - fv, c = w - fw;
-    int i = (int)fu, j = (int)fv, k = (int)fw;
-    float4 x00 = lerp4(texel(base, S, i, j, k), texel(base, S, i + 1, j, k), a);
-    float4 x10 = lerp4(texel(base, S, i, j + 1, k), texel(base, S, i + 1, j + 1, k), a);
-    float4 x01 = lerp4(texel(base, S, i, j, k + 1), texel(base, S, i + 1, j, k + 1), a);
-    float4 x11 = lerp4(texel(base, S, i, j + 1, k + 1), texel(base, S, i + 1, j + 1, k + 1), a);
-    return lerp4(lerp4(x00, x10, b), lerp4(x01, x11, b), c);
+// RGBA as two packed fp32 pairs: Blackwell issues one FFMA2/FMUL2 per pair.
+struct rgba2 {
+    float2 rg, ba;
+};
+
+__device__ __forceinline__ rgba2 ld_texel(const uint2* __restrict__ p) {
+    const uint2 v = __ldg(p);
+    return {__half22float2(*reinterpret_cast<const __half2*>(&v.x)),
+            __half22float2(*reinterpret_cast<const __half2*>(&v.y))};
+}
+
+// t*q + (p - t*p) on both pairs: two FFMA2 per pair.
+__device__ __forceinline__ rgba2 lerp2(rgba2 p, rgba2 q, float t) {
+    const float2 tt = make_float2(t, t), nt = make_float2(-t, -t);
+    return {__ffma2_rn(tt, q.rg, __ffma2_rn(nt, p.rg, p.rg)), __ffma2_rn(tt, q.ba, __ffma2_rn(nt, p.ba, p.ba))};
+}
+
+__device__ __forceinline__ float4 to_float4(rgba2 v) { return make_float4(v.rg.x, v.rg.y, v.ba.x, v.ba.y); }
+
+// GL_LINEAR within level l with a (0,0,0,0) border, read from the bordered
+// chain: for a position in [0,1]^3 the footprint's lower corner is in
+// [-1, S-1]^3, i.e. [0, S]^3 of the (S+2)^3 bordered level, so the eight
+// texels are plain loads at constant offsets with no bounds tests.
+__device__ __forceinline__ rgba2 trilinear2(const TraceParams& P, const int* __restrict__ off, int l, f3 p) {
+    const int S = P.dim >> l, Pd = S + 2;
+    const uint2* base = P.pchain + off[l];
+    const float u = p.x * (float)S - 0.5f, v = p.y * (float)S - 0.5f, w = p.z * (float)S - 0.5f;
+    const float fu = floorf(u), fv = floorf(v), fw = floorf(w);
+    const float a = u - fu, b = v - fv, c = w - fw;
+    const int i = (int)fu + 1, j = (int)fv + 1, k = (int)fw + 1;
+    const uint2* q = base + ((k * Pd + j) * Pd + i);
+    const int sy = Pd, sz = Pd * Pd;
+    const rgba2 t0 = ld_texel(q), t1 = ld_texel(q + 1), t2 = ld_texel(q + sy), t3 = ld_texel(q + sy + 1);
+    const rgba2 t4 = ld_texel(q + sz), t5 = ld_texel(q + sz + 1), t6 = ld_texel(q + sz + sy),
+                t7 = ld_texel(q + sz + sy + 1);
+    const rgba2 x00 = lerp2(t0, t1, a), x10 = lerp2(t2, t3, a);
+    const rgba2 x01 = lerp2(t4, t5, a), x11 = lerp2(t6, t7, a);
+    return lerp2(lerp2(x00, x10, b), lerp2(x01, x11, b), c);
+}
+
+__device__ __forceinline__ float4 trilinear(const TraceParams& P, const int* off, int l, f3 p) {
+    return to_float4(trilinear2(P, off, l, p));
 }
 
 template <int MODE>
-__device__ __forceinline__ float4 sample_lod(const TraceParams& P, f3 p, float lambda) {
+__device__ __forceinline__ float4 sample_lod(const TraceParams& P, const int* off, f3 p, float lambda) {
     if (MODE == VCT_FILTER_HARDWARE) return tex3DLod<float4>(P.tex, p.x, p.y, p.z, lambda);
     const int q = P.levels - 1;
     if (MODE == VCT_FILTER_HARDWARE_LEVELS) {
@@ -68,20 +98,21 @@ __device__ __forceinline__ float4 sample_lod(const TraceParams& P, f3 p, float l
         return lerp4(tex3DLod<float4>(P.tex, p.x, p.y, p.z, fl), tex3DLod<float4>(P.tex, p.x, p.y, p.z, fl + 1.0f),
                      lambda - fl);
     }
-    if (lambda <= 0.0f) {  // magnification: GL_NEAREST on level 0
+    if (lambda <= 0.0f) {  // magnification: GL_NEAREST on level 0 (index S = border)
         const int S = P.dim;
         return texel(P.chain, S, (int)floorf(p.x * S), (int)floorf(p.y * S), (int)floorf(p.z * S));
     }
-    if (lambda >= (float)q) return trilinear(P, q, p);
+    if (lambda >= (float)q) return trilinear(P, off, q, p);
     float fl = floorf(lambda);
     int d1 = (int)fl;
     float f = lambda - fl;
-    return lerp4(trilinear(P, d1, p), trilinear(P, d1 + 1, p), f);
+    return to_float4(lerp2(trilinear2(P, off, d1, p), trilinear2(P, off, d1 + 1, p), f));
 }
 
 template <int MODE>
-__device__ float4 trace_cone(const TraceParams& P, f3 pos, f3 n, f3 dir, const vct_cone_settings& c, float maxd,
-                             unsigned& ns) {
+__device__ __forceinline__ float4 trace_cone(const TraceParams& P, const int* off, f3 pos, f3 n, f3 dir,
+                                             const vct_cone_settings c,
+                             float maxd, unsigned& ns) {
     dir = fnormalize(dir);
     const float scale = 1.0f / (float)P.dim;
     const f3 start = add(pos, mul(mul(n, c.bias), scale));
@@ -91,11 +122,12 @@ __device__ float4 trace_cone(const TraceParams& P, f3 pos, f3 n, f3 dir, const v
     f3 col = mk(0.f, 0.f, 0.f);
     for (int i = 0; i < c.steps && alpha < 0.95f; ++i) {
         float r = h * tanh;
-        float lod = log2f(fmaxf(1.0f, 2.0f * r));
+        float lod = __log2f(fmaxf(1.0f, 2.0f * r));
         f3 sp = add(start, mul(mul(dir, h), scale));
-        if (sp.x < 0.f || sp.y < 0.f || sp.z < 0.f || sp.x > 1.f || sp.y > 1.f || sp.z > 1.f) break;
+        // any(notEqual(p, clamp(p, 0, 1))): outside, or NaN
+        if (!(sp.x >= 0.f && sp.y >= 0.f && sp.z >= 0.f && sp.x <= 1.f && sp.y <= 1.f && sp.z <= 1.f)) break;
         if (h * scale > maxd) break;
-        float4 s = sample_lod<MODE>(P, sp, lod + c.lod_offset);
+        float4 s = sample_lod<MODE>(P, off, sp, lod + c.lod_offset);
         ++ns;
         float a = 1.0f - alpha;
         col = add(col, mul(mk(s.x, s.y, s.z), a));
@@ -110,6 +142,11 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int x = blockIdx.x * 16 + (wid & 1) * 8 + (lane & 7);
     const int y = blockIdx.y * 16 + (wid >> 1) * 4 + (lane >> 3);
+    // Offsets of the bordered levels (32-bit: the chain holds < 2^31 voxels).
+    __shared__ int s_off[VCT_MAX_LEVELS];
+    if (threadIdx.x < VCT_MAX_LEVELS)
+        s_off[threadIdx.x] = threadIdx.x < P.levels ? (int)padded_level_offset(P.dim, threadIdx.x) : 0;
+    __syncthreads();
     unsigned ns = 0;
     if (x < P.width && y < P.height) {
         const long long pix = (long long)y * P.width + x;
@@ -137,7 +174,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
                     const float dx = kConeDir[c][0], dy = kConeDir[c][1], dz = kConeDir[c][2];
                     f3 d = P.ref_tbn_quirk ? add(add(mul(T, dx), mul(B, dy)), mul(N, dz))
                                            : sub(add(mul(T, dx), mul(N, dy)), mul(B, dz));
-                    float4 cr = trace_cone<MODE>(P, vp, N, d, P.diffuse, P.max_distance, ns);
+                    float4 cr = trace_cone<MODE>(P, s_off, vp, N, d, P.diffuse, P.max_distance, ns);
                     const float w = kConeWeight[c];
                     ind.x += w * cr.x;
                     ind.y += w * cr.y;
@@ -150,7 +187,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
                 if (P.enable_reflections) {
                     const f3 I = sub(mk(gp.x, gp.y, gp.z), P.eye);
                     const f3 R = sub(I, mul(N, 2.0f * dot(N, I)));
-                    spc = trace_cone<MODE>(P, vp, N, R, P.specular_cone, P.max_distance, ns);
+                    spc = trace_cone<MODE>(P, s_off, vp, N, R, P.specular_cone, P.max_distance, ns);
                     rgb = add(rgb, mul(mk(spc.x, spc.y, spc.z), P.reflect_scale));
                 }
                 const float as = P.ambient_scale;

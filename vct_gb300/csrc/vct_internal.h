@@ -6,11 +6,28 @@
 
 #include "../../include/vct.h"
 
+#ifdef __CUDACC__
+#define VCT_HD __host__ __device__
+#else
+#define VCT_HD
+#endif
+
 namespace vct {
 
 struct f3 {
     float x, y, z;
 };
+
+// The software cone sampler reads a private copy of the radiance mip chain in
+// which every level of side S is stored as (S+2)^3 voxels: the level plus a
+// one-voxel shell of zeros (the GL clamp-to-border colour), so that any
+// trilinear footprint of a position in [0,1]^3 lies inside the array.
+// Offset (in voxels) of padded level l:
+//   sum_{i<l} (S_i + 2)^3 = 8(N^3-S^3)/7 + 8(N^2-S^2) + 24(N-S) + 8l,  S = N >> l.
+VCT_HD inline long long padded_level_offset(int N, int l) {
+    const long long n = N, s = N >> l;
+    return (n * n * n - s * s * s) / 7 * 8 + 8 * (n * n - s * s) + 24 * (n - s) + 8LL * l;
+}
 
 struct LightDev {
     f3 position;
@@ -114,11 +131,13 @@ struct ResolveParams {
     uint2* radiance_levels[5];  // levels 0..4 of the radiance chain
     int mip_levels;             // number of levels below 0 to write from the brick (<= 4)
     cudaSurfaceObject_t surf[5];  // texture-unit copy of levels 0..4 (0 = none)
+    uint2* pad_levels[5];         // bordered copy of levels 0..4 (nullptr = none)
 };
 
 struct MipLevels {
     uint2* level[VCT_MAX_LEVELS];
     cudaSurfaceObject_t surf[VCT_MAX_LEVELS];  // optional texture-unit copy (0 = none)
+    uint2* pad[VCT_MAX_LEVELS];                // optional bordered copy (nullptr = none)
     int dim;
     int levels;
 };
@@ -132,8 +151,8 @@ struct TraceParams {
     float4* specular;
     float4* color;
     unsigned long long* samples;
-    const uint2* chain;
-    long long level_off[VCT_MAX_LEVELS];
+    const uint2* chain;   // linear chain (nearest-level magnification)
+    const uint2* pchain;  // bordered chain (software trilinear)
     int dim, levels;
     f3 vmin, vmax, vcenter, eye;
     vct_cone_settings diffuse, specular_cone;
@@ -192,5 +211,7 @@ void launch_trace(const TraceParams& P, cudaStream_t s);
 void launch_shadow_raster(const ShadowRasterParams& P, cudaStream_t s);
 void launch_gbuffer_raster(const GbufferRasterParams& P, cudaStream_t s);
 void launch_fill_u32(uint32_t* p, uint32_t v, long long n, cudaStream_t s);
+// Copies every level of a linear chain into the interior of the bordered chain.
+void launch_pad_copy(const uint2* chain, uint2* pchain, int dim, int levels, cudaStream_t s);
 
 }  // namespace vct

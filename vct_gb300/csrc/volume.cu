@@ -79,11 +79,17 @@ __device__ __forceinline__ uint2 box8(const uint2 c[8]) {
     return pack_h4(acc.x * 0.125f, acc.y * 0.125f, acc.z * 0.125f, acc.w * 0.125f);
 }
 
+// Interior voxel (x,y,z) of a bordered level of side S.
+__device__ __forceinline__ long long pad_index(int x, int y, int z, int S) {
+    const long long P = S + 2;
+    return ((long long)(z + 1) * P + (y + 1)) * P + (x + 1);
+}
+
 // Reduces a cube of side S (in shared memory, x fastest) into side S/2,
-// writing the result to shared memory, to the linear level and (when `surf`
-// is set) to the texture-unit copy of the level.
+// writing the result to shared memory, to the linear level and, when given,
+// to the texture-unit copy (`surf`) and the bordered copy (`pdst`).
 __device__ __forceinline__ void reduce_level(const uint2* src, uint2* dst, int S, uint2* gdst, cudaSurfaceObject_t surf,
-                                             int gS, int gx0, int gy0, int gz0) {
+                                             uint2* pdst, int gS, int gx0, int gy0, int gz0) {
     const int D = S / 2;
     const int n = D * D * D;
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
@@ -98,6 +104,7 @@ __device__ __forceinline__ void reduce_level(const uint2* src, uint2* dst, int S
         dst[t] = r;
         gdst[((long long)(gz0 + z) * gS + (gy0 + y)) * gS + (gx0 + x)] = r;
         if (surf) surf3Dwrite(r, surf, (gx0 + x) * (int)sizeof(uint2), gy0 + y, gz0 + z);
+        if (pdst) pdst[pad_index(gx0 + x, gy0 + y, gz0 + z, gS)] = r;
     }
 }
 
@@ -190,6 +197,7 @@ __global__ void __launch_bounds__(kThreads) resolve_kernel(const ResolveParams R
             for (int j = 0; j < 4; ++j) {
                 s0[(lz * kBrick + ly) * kBrick + lx + j] = rad[j];
                 if (R.surf[0]) surf3Dwrite(rad[j], R.surf[0], (x + j) * (int)sizeof(uint2), y, z);
+                if (R.pad_levels[0]) R.pad_levels[0][pad_index(x + j, y, z, N)] = rad[j];
             }
         }
     }
@@ -201,7 +209,8 @@ __global__ void __launch_bounds__(kThreads) resolve_kernel(const ResolveParams R
         int side = kBrick;
         for (int l = 1; l <= R.mip_levels; ++l) {
             const int sub = side / 2;
-            reduce_level(a, b, side, R.radiance_levels[l], R.surf[l], N >> l, bx * sub, by * sub, bz * sub);
+            reduce_level(a, b, side, R.radiance_levels[l], R.surf[l], R.pad_levels[l], N >> l, bx * sub, by * sub,
+                         bz * sub);
             __syncthreads();
             uint2* t = a;
             a = b;
@@ -292,7 +301,8 @@ __global__ void __launch_bounds__(kThreads) mip_brick_kernel(const MipLevels M, 
     int side = kBrick;
     for (int l = 1; l <= nlev; ++l) {
         int sub = side / 2;
-        reduce_level(a, b, side, M.level[first + l], M.surf[first + l], S >> l, bx * sub, by * sub, bz * sub);
+        reduce_level(a, b, side, M.level[first + l], M.surf[first + l], M.pad[first + l], S >> l, bx * sub, by * sub,
+                     bz * sub);
         __syncthreads();
         uint2* t = a;
         a = b;
@@ -313,12 +323,21 @@ __global__ void __launch_bounds__(kThreads) mip_tail_kernel(const MipLevels M, i
     uint2* b = s1;
     int side = S;
     for (int l = first + 1; l < M.levels; ++l) {
-        reduce_level(a, b, side, M.level[l], M.surf[l], side / 2, 0, 0, 0);
+        reduce_level(a, b, side, M.level[l], M.surf[l], M.pad[l], side / 2, 0, 0, 0);
         __syncthreads();
         uint2* t = a;
         a = b;
         b = t;
         side /= 2;
+    }
+}
+
+// Linear level -> interior of the bordered level (borders stay zero).
+__global__ void pad_copy_kernel(const uint2* __restrict__ src, uint2* __restrict__ dst, int S) {
+    const long long n = (long long)S * S * S;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(v % S), y = (int)((v / S) % S), z = (int)(v / ((long long)S * S));
+        dst[pad_index(x, y, z, S)] = src[v];
     }
 }
 
@@ -372,6 +391,19 @@ void launch_mips(const MipLevels& M, int first, cudaStream_t s) {
             note_launches(1);
             break;
         }
+    }
+}
+
+void launch_pad_copy(const uint2* chain, uint2* pchain, int dim, int levels, cudaStream_t s) {
+    long long off = 0;
+    for (int l = 0; l < levels; ++l) {
+        const int S = dim >> l;
+        const long long n = (long long)S * S * S;
+        long long blocks = (n + 255) / 256;
+        if (blocks > 8192) blocks = 8192;
+        pad_copy_kernel<<<(unsigned)blocks, 256, 0, s>>>(chain + off, pchain + padded_level_offset(dim, l), S);
+        note_launches(1);
+        off += n;
     }
 }
 

@@ -2,13 +2,13 @@
 //
 // Three launches, balanced at fragment granularity (triangle sizes vary by
 // more than three orders of magnitude in one scene):
-//  1. setup_kernel, one thread per triangle: the geometry-shader part
+//  1. voxelize_setup_kernel, one thread per triangle: the geometry-shader part
 //     (dominant axis from the summed vertex normals, per-axis ortho
 //     projection, snapping to the 1/256 sub-pixel grid, bounding box) into a
 //     48-byte record, and the triangle's share of work: its bounding box in
 //     units of kUnit pixels, with a block-local exclusive scan;
-//  2. scan_kernel, one CTA: exclusive scan of the per-block unit totals;
-//  3. raster_kernel, persistent: every warp takes an equal contiguous range
+//  2. voxelize_scan_kernel, one CTA: exclusive scan of the per-block unit totals;
+//  3. voxelize_raster_kernel, persistent: every warp takes an equal contiguous range
 //     of work units, tests 32 pixel centres at a time for coverage, compacts
 //     covered fragments (clipped to the depth range) with a ballot into a
 //     per-warp queue in shared memory, and whenever 32 are queued each lane
@@ -59,7 +59,7 @@ __device__ __forceinline__ float shadow_factor(const AccumParams& P, f3 wp) {
 }
 
 // ------------------------------------------------------------- 1. setup
-__global__ void __launch_bounds__(kSetupThreads) setup_kernel(const AccumParams P) {
+__global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const AccumParams P) {
     const long long t = (long long)blockIdx.x * kSetupThreads + threadIdx.x;
     uint32_t units = 0;
     if (t < P.ntri) {
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(const AccumParams 
 }
 
 // --------------------------------------------------------------- 2. scan
-__global__ void __launch_bounds__(1024) scan_kernel(uint32_t* block_off, int nblocks) {
+__global__ void __launch_bounds__(1024) voxelize_scan_kernel(uint32_t* block_off, int nblocks) {
     __shared__ uint32_t warp_tot[32];
     __shared__ uint32_t carry;
     if (threadIdx.x == 0) carry = 0;
@@ -227,7 +227,7 @@ __device__ __forceinline__ long long unit_start(const AccumParams& P, long long 
     return (long long)P.block_off[t / kSetupThreads] + P.tri_scan[t];
 }
 
-__global__ void __launch_bounds__(kWarps * 32, 2) raster_kernel(const AccumParams P, int nblocks) {
+__global__ void __launch_bounds__(kWarps * 32, 2) voxelize_raster_kernel(const AccumParams P, int nblocks) {
     __shared__ FragQueue queues[kWarps];
     const int lane = threadIdx.x & 31;
     FragQueue& q = queues[threadIdx.x >> 5];
@@ -365,9 +365,9 @@ void accumulate_bind_scratch(AccumParams& P, void* scratch) {
 void launch_accumulate(const AccumParams& P, cudaStream_t s) {
     if (P.ntri <= 0) return;
     const int nblocks = (int)((P.ntri + kSetupThreads - 1) / kSetupThreads);
-    setup_kernel<<<nblocks, kSetupThreads, 0, s>>>(P);
-    scan_kernel<<<1, 1024, 0, s>>>(P.block_off, nblocks);
-    raster_kernel<<<P.num_sms * 2, kWarps * 32, 0, s>>>(P, nblocks);
+    voxelize_setup_kernel<<<nblocks, kSetupThreads, 0, s>>>(P);
+    voxelize_scan_kernel<<<1, 1024, 0, s>>>(P.block_off, nblocks);
+    voxelize_raster_kernel<<<P.num_sms * 2, kWarps * 32, 0, s>>>(P, nblocks);
     note_launches(3);
 }
 
