@@ -39,7 +39,7 @@ struct vct_ctx {
     cudaEvent_t ev[5] = {};
     void* vox_scratch = nullptr;  // voxeliser work-distribution arrays
     long long vox_scratch_bytes = 0;
-    uint2* pchain = nullptr;  // bordered radiance chain read by the software sampler
+    float4* pchain = nullptr;  // bordered fp32 radiance chain read by the software sampler
     bool pad_ready = false;   // pchain holds the current radiance chain
 };
 
@@ -584,7 +584,7 @@ vct_status vct_create(const vct_config* cfg, vct_ctx** out) {
         {(void**)&c->normal, (size_t)c->nv * 8},
         {(void**)&c->radiance, (size_t)chain_vox * 8},
         {(void**)&c->stats, sizeof(StatsDev)},
-        {(void**)&c->pchain, (size_t)padded_level_offset(c->dim, c->levels) * 8},
+        {(void**)&c->pchain, (size_t)padded_level_offset(c->dim, c->levels) * 16},
     };
     for (auto& a : allocs) {
         cudaError_t e = cudaMalloc(a.p, a.bytes);

@@ -46,10 +46,11 @@ struct rgba2 {
     float2 rg, ba;
 };
 
-__device__ __forceinline__ rgba2 ld_texel(const uint2* __restrict__ p) {
-    const uint2 v = __ldg(p);
-    return {__half22float2(*reinterpret_cast<const __half2*>(&v.x)),
-            __half22float2(*reinterpret_cast<const __half2*>(&v.y))};
+// The bordered chain holds each binary16 texel widened to fp32 (exactly), so
+// a texel is one 16-byte read-only load with no conversion.
+__device__ __forceinline__ rgba2 ld_texel(const float4* __restrict__ p) {
+    const float4 v = __ldg(p);
+    return {make_float2(v.x, v.y), make_float2(v.z, v.w)};
 }
 
 // t*q + (p - t*p) on both pairs: two FFMA2 per pair.
@@ -66,12 +67,12 @@ __device__ __forceinline__ float4 to_float4(rgba2 v) { return make_float4(v.rg.x
 // texels are plain loads at constant offsets with no bounds tests.
 __device__ __forceinline__ rgba2 trilinear2(const TraceParams& P, const int* __restrict__ off, int l, f3 p) {
     const int S = P.dim >> l, Pd = S + 2;
-    const uint2* base = P.pchain + off[l];
+    const float4* base = P.pchain + off[l];
     const float u = p.x * (float)S - 0.5f, v = p.y * (float)S - 0.5f, w = p.z * (float)S - 0.5f;
     const float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     const float a = u - fu, b = v - fv, c = w - fw;
     const int i = (int)fu + 1, j = (int)fv + 1, k = (int)fw + 1;
-    const uint2* q = base + ((k * Pd + j) * Pd + i);
+    const float4* q = base + ((k * Pd + j) * Pd + i);
     const int sy = Pd, sz = Pd * Pd;
     const rgba2 t0 = ld_texel(q), t1 = ld_texel(q + 1), t2 = ld_texel(q + sy), t3 = ld_texel(q + sy + 1);
     const rgba2 t4 = ld_texel(q + sz), t5 = ld_texel(q + sz + 1), t6 = ld_texel(q + sz + sy),

@@ -131,13 +131,13 @@ struct ResolveParams {
     uint2* radiance_levels[5];  // levels 0..4 of the radiance chain
     int mip_levels;             // number of levels below 0 to write from the brick (<= 4)
     cudaSurfaceObject_t surf[5];  // texture-unit copy of levels 0..4 (0 = none)
-    uint2* pad_levels[5];         // bordered copy of levels 0..4 (nullptr = none)
+    float4* pad_levels[5];        // bordered fp32 copy of levels 0..4 (nullptr = none)
 };
 
 struct MipLevels {
     uint2* level[VCT_MAX_LEVELS];
     cudaSurfaceObject_t surf[VCT_MAX_LEVELS];  // optional texture-unit copy (0 = none)
-    uint2* pad[VCT_MAX_LEVELS];                // optional bordered copy (nullptr = none)
+    float4* pad[VCT_MAX_LEVELS];               // optional bordered fp32 copy (nullptr = none)
     int dim;
     int levels;
 };
@@ -152,7 +152,7 @@ struct TraceParams {
     float4* color;
     unsigned long long* samples;
     const uint2* chain;   // linear chain (nearest-level magnification)
-    const uint2* pchain;  // bordered chain (software trilinear)
+    const float4* pchain;  // bordered fp32 chain (software trilinear)
     int dim, levels;
     f3 vmin, vmax, vcenter, eye;
     vct_cone_settings diffuse, specular_cone;
@@ -212,6 +212,6 @@ void launch_shadow_raster(const ShadowRasterParams& P, cudaStream_t s);
 void launch_gbuffer_raster(const GbufferRasterParams& P, cudaStream_t s);
 void launch_fill_u32(uint32_t* p, uint32_t v, long long n, cudaStream_t s);
 // Copies every level of a linear chain into the interior of the bordered chain.
-void launch_pad_copy(const uint2* chain, uint2* pchain, int dim, int levels, cudaStream_t s);
+void launch_pad_copy(const uint2* chain, float4* pchain, int dim, int levels, cudaStream_t s);
 
 }  // namespace vct

@@ -85,14 +85,15 @@ __device__ __forceinline__ long long pad_index(int x, int y, int z, int S) {
     return ((long long)(z + 1) * P + (y + 1)) * P + (x + 1);
 }
 
-// Reduces a cube of side S (in shared memory, x fastest) into side S/2,
-// writing the result to shared memory, to the linear level and, when given,
-// to the texture-unit copy (`surf`) and the bordered copy (`pdst`).
+// Reduces a cube of side S (in shared memory, x fastest) into side S/2 with
+// threads [0, nthr), writing the result to shared memory, to the linear level
+// and, when given, to the texture-unit copy (`surf`) and the bordered fp32
+// copy (`pdst`).
 __device__ __forceinline__ void reduce_level(const uint2* src, uint2* dst, int S, uint2* gdst, cudaSurfaceObject_t surf,
-                                             uint2* pdst, int gS, int gx0, int gy0, int gz0) {
+                                             float4* pdst, int gS, int gx0, int gy0, int gz0, int nthr) {
     const int D = S / 2;
     const int n = D * D * D;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    for (int t = threadIdx.x; t < n; t += nthr) {
         int x = t % D, y = (t / D) % D, z = t / (D * D);
         uint2 c[8];
 #pragma unroll
@@ -104,7 +105,36 @@ __device__ __forceinline__ void reduce_level(const uint2* src, uint2* dst, int S
         dst[t] = r;
         gdst[((long long)(gz0 + z) * gS + (gy0 + y)) * gS + (gx0 + x)] = r;
         if (surf) surf3Dwrite(r, surf, (gx0 + x) * (int)sizeof(uint2), gy0 + y, gz0 + z);
-        if (pdst) pdst[pad_index(gx0 + x, gy0 + y, gz0 + z, gS)] = r;
+        if (pdst) pdst[pad_index(gx0 + x, gy0 + y, gz0 + z, gS)] = unpack_h4(r);
+    }
+}
+
+// Levels 1..nlev of a 16^3 brick held in s0 (shared).  Threads retire as the
+// levels shrink (512, 64, 8, 1 outputs): after the first level only two warps
+// continue (synchronised by a 64-thread named barrier), after the second one.
+// Threads that are no longer needed return, so call this last.
+__device__ __forceinline__ void brick_mips(uint2* s0, uint2* s1, int nlev, uint2* const* gdst,
+                                           const cudaSurfaceObject_t* surf, float4* const* pdst, int S0, int bx, int by,
+                                           int bz) {
+    uint2* a = s0;
+    uint2* b = s1;
+    int side = kBrick;
+    for (int l = 1; l <= nlev; ++l) {
+        const int sub = side / 2;
+        const int nout = sub * sub * sub;
+        const int nthr = nout >= kThreads ? kThreads : (nout >= 64 ? 64 : 32);
+        if ((int)threadIdx.x >= nthr) return;
+        reduce_level(a, b, side, gdst[l], surf[l], pdst[l], S0 >> l, bx * sub, by * sub, bz * sub, nthr);
+        if (nthr == kThreads)
+            __syncthreads();
+        else if (nthr == 64)
+            asm volatile("bar.sync 1, 64;" ::: "memory");
+        else
+            __syncwarp();
+        uint2* t = a;
+        a = b;
+        b = t;
+        side = sub;
     }
 }
 
@@ -117,7 +147,7 @@ __device__ __forceinline__ void reduce_level(const uint2* src, uint2* dst, int S
 //                injectRadiance stores into a voxel depends only on that
 //                voxel (its stores are idempotent).
 template <bool FUSED>
-__global__ void __launch_bounds__(kThreads) resolve_kernel(const ResolveParams R) {
+__global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const ResolveParams R) {
     __shared__ uint2 s0[FUSED ? kBrickVox : 1];
     __shared__ uint2 s1[FUSED ? kBrickVox / 8 : 1];
     const NormalizeParams& P = R.norm;
@@ -197,26 +227,14 @@ __global__ void __launch_bounds__(kThreads) resolve_kernel(const ResolveParams R
             for (int j = 0; j < 4; ++j) {
                 s0[(lz * kBrick + ly) * kBrick + lx + j] = rad[j];
                 if (R.surf[0]) surf3Dwrite(rad[j], R.surf[0], (x + j) * (int)sizeof(uint2), y, z);
-                if (R.pad_levels[0]) R.pad_levels[0][pad_index(x + j, y, z, N)] = rad[j];
+                if (R.pad_levels[0]) R.pad_levels[0][pad_index(x + j, y, z, N)] = unpack_h4(rad[j]);
             }
         }
     }
     if (FUSED) __syncthreads();
     block_stats(P.stats, uniq, mx, flags);
     if (FUSED) {
-        uint2* a = s0;
-        uint2* b = s1;
-        int side = kBrick;
-        for (int l = 1; l <= R.mip_levels; ++l) {
-            const int sub = side / 2;
-            reduce_level(a, b, side, R.radiance_levels[l], R.surf[l], R.pad_levels[l], N >> l, bx * sub, by * sub,
-                         bz * sub);
-            __syncthreads();
-            uint2* t = a;
-            a = b;
-            b = t;
-            side = sub;
-        }
+        brick_mips(s0, s1, R.mip_levels, R.radiance_levels, R.surf, R.pad_levels, N, bx, by, bz);
     }
 }
 
@@ -296,19 +314,7 @@ __global__ void __launch_bounds__(kThreads) mip_brick_kernel(const MipLevels M, 
         s0[t] = src[((long long)(bz * kBrick + z) * S + (by * kBrick + y)) * S + (bx * kBrick + x)];
     }
     __syncthreads();
-    uint2* a = s0;
-    uint2* b = s1;
-    int side = kBrick;
-    for (int l = 1; l <= nlev; ++l) {
-        int sub = side / 2;
-        reduce_level(a, b, side, M.level[first + l], M.surf[first + l], M.pad[first + l], S >> l, bx * sub, by * sub,
-                     bz * sub);
-        __syncthreads();
-        uint2* t = a;
-        a = b;
-        b = t;
-        side = sub;
-    }
+    brick_mips(s0, s1, nlev, M.level + first, M.surf + first, M.pad + first, S, bx, by, bz);
 }
 
 // Small levels (side <= 16): one CTA builds every remaining level.
@@ -323,7 +329,7 @@ __global__ void __launch_bounds__(kThreads) mip_tail_kernel(const MipLevels M, i
     uint2* b = s1;
     int side = S;
     for (int l = first + 1; l < M.levels; ++l) {
-        reduce_level(a, b, side, M.level[l], M.surf[l], M.pad[l], side / 2, 0, 0, 0);
+        reduce_level(a, b, side, M.level[l], M.surf[l], M.pad[l], side / 2, 0, 0, 0, kThreads);
         __syncthreads();
         uint2* t = a;
         a = b;
@@ -333,11 +339,11 @@ __global__ void __launch_bounds__(kThreads) mip_tail_kernel(const MipLevels M, i
 }
 
 // Linear level -> interior of the bordered level (borders stay zero).
-__global__ void pad_copy_kernel(const uint2* __restrict__ src, uint2* __restrict__ dst, int S) {
+__global__ void pad_copy_kernel(const uint2* __restrict__ src, float4* __restrict__ dst, int S) {
     const long long n = (long long)S * S * S;
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
         const int x = (int)(v % S), y = (int)((v / S) % S), z = (int)(v / ((long long)S * S));
-        dst[pad_index(x, y, z, S)] = src[v];
+        dst[pad_index(x, y, z, S)] = unpack_h4(src[v]);
     }
 }
 
@@ -394,7 +400,7 @@ void launch_mips(const MipLevels& M, int first, cudaStream_t s) {
     }
 }
 
-void launch_pad_copy(const uint2* chain, uint2* pchain, int dim, int levels, cudaStream_t s) {
+void launch_pad_copy(const uint2* chain, float4* pchain, int dim, int levels, cudaStream_t s) {
     long long off = 0;
     for (int l = 0; l < levels; ++l) {
         const int S = dim >> l;

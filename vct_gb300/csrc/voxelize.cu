@@ -28,6 +28,7 @@ namespace {
 constexpr int kWarps = 8;
 constexpr int kQueue = 64;
 constexpr int kUnit = 512;  // bounding-box pixels per work unit
+constexpr int kRasterBlocksPerSM = 3;
 
 struct FragQueue {
     int tri[kQueue];
@@ -216,18 +217,20 @@ __device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQ
     unsigned long long* rec = reinterpret_cast<unsigned long long*>(P.acc + (long long)kAccWords * v);
     const unsigned long long qr = quant16(color.x), qg = quant16(color.y), qb = quant16(color.z);
     const unsigned long long qx = quant16(n01.x), qy = quant16(n01.y), qz = quant16(n01.z);
-    const unsigned long long old = atomicAdd(rec + 0, 1ull | (qr << 32));
+    // Fire-and-forget reductions: no result is waited for.
+    atomicAdd(rec + 0, 1ull | (qr << 32));
     atomicAdd(rec + 1, qg | (qb << 32));
     atomicAdd(rec + 2, qx | (qy << 32));
     atomicAdd(rec + 3, qz);
-    if ((uint32_t)old == 0u) atomicOr(P.occ + (v >> 5), 1u << (v & 31));
+    atomicOr(P.occ + (v >> 5), 1u << (v & 31));
 }
 
 __device__ __forceinline__ long long unit_start(const AccumParams& P, long long t) {
     return (long long)P.block_off[t / kSetupThreads] + P.tri_scan[t];
 }
 
-__global__ void __launch_bounds__(kWarps * 32, 2) voxelize_raster_kernel(const AccumParams P, int nblocks) {
+__global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM) voxelize_raster_kernel(const AccumParams P,
+                                                                                          int nblocks) {
     __shared__ FragQueue queues[kWarps];
     const int lane = threadIdx.x & 31;
     FragQueue& q = queues[threadIdx.x >> 5];
@@ -367,7 +370,7 @@ void launch_accumulate(const AccumParams& P, cudaStream_t s) {
     const int nblocks = (int)((P.ntri + kSetupThreads - 1) / kSetupThreads);
     voxelize_setup_kernel<<<nblocks, kSetupThreads, 0, s>>>(P);
     voxelize_scan_kernel<<<1, 1024, 0, s>>>(P.block_off, nblocks);
-    voxelize_raster_kernel<<<P.num_sms * 2, kWarps * 32, 0, s>>>(P, nblocks);
+    voxelize_raster_kernel<<<P.num_sms * kRasterBlocksPerSM, kWarps * 32, 0, s>>>(P, nblocks);
     note_launches(3);
 }
 
