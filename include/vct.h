@@ -268,6 +268,38 @@ vct_status vct_get_timers(vct_ctx* ctx, vct_timers* out);
 /* Number of kernels this library has launched since it was loaded. */
 uint64_t vct_launch_count(void);
 
+/* ---- batched scenes ---------------------------------------------------- */
+/* No counterpart in the reference (it renders one scene per frame).  A batch
+ * owns one context per scene (grids may differ, each <= 256^3, all on one
+ * device) and runs vct_frame for every scene with one launch per stage:
+ * the voxeliser's work units, the shadow texels, the resolve bricks and the
+ * pixel tiles of all scenes are concatenated and each launch maps a global
+ * work index back to its scene.  Results equal vct_frame per scene. */
+typedef struct vct_batch vct_batch;
+
+typedef struct vct_scene_desc {
+    vct_triangles triangles;
+    const vct_light* lights; /* host array */
+    int32_t n_lights;
+    vct_shadow_desc shadow;
+    float eye[3];
+    vct_gbuffer gbuffer;
+    vct_trace_out out;
+} vct_scene_desc;
+
+vct_status vct_batch_create(const vct_config* configs, int32_t n_scenes, vct_batch** out);
+vct_status vct_batch_destroy(vct_batch* batch);
+/* Parameters of one scene (scene = -1: every scene); all scenes must use the
+ * same trace_filter. */
+vct_status vct_batch_set_params(vct_batch* batch, int32_t scene, const vct_params* params);
+vct_status vct_batch_frame(vct_batch* batch, const vct_scene_desc* scenes, int32_t n_scenes, void* stream);
+/* Records vct_batch_frame for `scenes` into a CUDA graph owned by the batch
+ * (the descriptors are copied: replays run the captured scenes). */
+vct_status vct_batch_capture(vct_batch* batch, const vct_scene_desc* scenes, int32_t n_scenes, void* stream);
+vct_status vct_batch_replay(vct_batch* batch, void* stream);
+/* The context of one scene (volumes, stats, timers) for reading. */
+vct_status vct_batch_context(vct_batch* batch, int32_t scene, vct_ctx** ctx);
+
 /* ---- voxelisation without allocation ---------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a host application whose device memory is all reserved up front by its

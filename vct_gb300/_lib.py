@@ -103,6 +103,12 @@ class vct_stats(C.Structure):
                 ("max_fragments_per_voxel", C.c_uint32), ("error_flags", C.c_uint32)]
 
 
+class vct_scene_desc(C.Structure):
+    _fields_ = [("triangles", vct_triangles), ("lights", C.POINTER(vct_light)), ("n_lights", C.c_int32),
+                ("shadow", vct_shadow_desc), ("eye", C.c_float * 3), ("gbuffer", vct_gbuffer),
+                ("out", vct_trace_out)]
+
+
 P = C.POINTER
 vp = C.c_void_p
 st = C.c_int
@@ -141,6 +147,13 @@ SIGNATURES = {
     "vct_render_shadowmap": (st, [P(vct_triangles), P(C.c_float), vp, C.c_int32, C.c_int32, vp]),
     "vct_render_gbuffer": (st, [P(vct_triangles), P(C.c_float), P(C.c_float), P(C.c_float), C.c_int32, C.c_int32,
                                 vp, vp, vp, vp, vp]),
+    "vct_batch_create": (st, [P(vct_config), C.c_int32, P(vp)]),
+    "vct_batch_destroy": (st, [vp]),
+    "vct_batch_set_params": (st, [vp, C.c_int32, P(vct_params)]),
+    "vct_batch_frame": (st, [vp, P(vct_scene_desc), C.c_int32, vp]),
+    "vct_batch_capture": (st, [vp, P(vct_scene_desc), C.c_int32, vp]),
+    "vct_batch_replay": (st, [vp, vp]),
+    "vct_batch_context": (st, [vp, C.c_int32, P(vp)]),
 }
 
 _lib = None

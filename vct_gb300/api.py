@@ -125,12 +125,17 @@ def trace_out(irradiance=None, specular=None, color=None, samples=None) -> L.vct
 
 
 class Context:
-    """Owns a vct_ctx (volumes on one device)."""
+    """Owns a vct_ctx (volumes on one device); with `handle`, a view of a
+    context owned by a Batch, never destroyed through the view."""
 
-    def __init__(self, config: L.vct_config):
+    def __init__(self, config: L.vct_config | None = None, *, handle: C.c_void_p | None = None):
         self._lib = L.load()
-        h = C.c_void_p()
-        L.check(self._lib.vct_create(C.byref(config), C.byref(h)), "vct_create")
+        self._owned = handle is None
+        if handle is None:
+            h = C.c_void_p()
+            L.check(self._lib.vct_create(C.byref(config), C.byref(h)), "vct_create")
+        else:
+            h = handle
         self.handle = h
         cfg = L.vct_config()
         L.check(self._lib.vct_get_config(h, C.byref(cfg)), "vct_get_config")
@@ -139,7 +144,8 @@ class Context:
 
     def close(self):
         if getattr(self, "handle", None):
-            self._lib.vct_destroy(self.handle)
+            if self._owned:
+                self._lib.vct_destroy(self.handle)
             self.handle = None
 
     def __del__(self):
@@ -226,6 +232,63 @@ class Context:
         rp, op = self.accumulator_ptrs()
         nv = self.dim ** 3
         return (device_view(rp, (nv, 8), "<i4").clone(), device_view(op, ((nv + 31) // 32,), "<i4").clone())
+
+
+def scene_desc(tris, lights, shadow, eye, gb, out) -> L.vct_scene_desc:
+    """vct_scene_desc of one batched scene; `lights` is light_array()'s pair
+    (the array must stay alive until the frame or capture call returns)."""
+    arr, n = lights
+    d = L.vct_scene_desc()
+    d.triangles, d.lights, d.n_lights, d.shadow = tris, arr, n, shadow
+    d.eye = f3(eye)
+    d.gbuffer, d.out = gb, out
+    return d
+
+
+class Batch:
+    """Owns a vct_batch: one context per scene, one launch per frame stage."""
+
+    def __init__(self, configs):
+        self._lib = L.load()
+        n = len(configs)
+        arr = (L.vct_config * n)(*configs)
+        h = C.c_void_p()
+        L.check(self._lib.vct_batch_create(arr, n, C.byref(h)), "vct_batch_create")
+        self.handle = h
+        self.n = n
+        self.scenes = []
+        for i in range(n):
+            c = C.c_void_p()
+            L.check(self._lib.vct_batch_context(h, i, C.byref(c)), "vct_batch_context")
+            self.scenes.append(Context(handle=c))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.vct_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, p: L.vct_params, scene: int = -1):
+        L.check(self._lib.vct_batch_set_params(self.handle, scene, C.byref(p)), "vct_batch_set_params")
+
+    def _descs(self, descs):
+        return (L.vct_scene_desc * len(descs))(*descs), len(descs)
+
+    def frame(self, descs, stream=None):
+        arr, n = self._descs(descs)
+        L.check(self._lib.vct_batch_frame(self.handle, arr, n, _stream(stream)), "vct_batch_frame")
+
+    def capture(self, descs, stream):
+        arr, n = self._descs(descs)
+        L.check(self._lib.vct_batch_capture(self.handle, arr, n, _stream(stream)), "vct_batch_capture")
+
+    def replay(self, stream=None):
+        L.check(self._lib.vct_batch_replay(self.handle, _stream(stream)), "vct_batch_replay")
 
 
 class _CudaArray:

@@ -4,10 +4,12 @@ Every translation unit is compiled in parallel straight with nvcc / g++
 (no cmake, no torch extension machinery) and linked into one shared library
 that exports the C ABI of include/vct.h.
 
-Kernels whose results must be bit-exact against the CPU oracle (rasterising,
-voxelising, normalising, injecting, mip filtering) are compiled with
---fmad=false so that no multiply-add is contracted; the cone tracer, which is
-checked against a tolerance, keeps FMA contraction.
+Every kernel translation unit is compiled with --fmad=false so that no
+multiply-add is contracted behind the source's back: the rasterising,
+voxelising, normalising, injecting and mip filtering kernels are bit-exact
+against the CPU oracle, and the cone tracer writes each of its fused
+multiply-adds explicitly, so that every instantiation of it (one scene, a
+batch of scenes) rounds the same way.
 """
 
 from __future__ import annotations
@@ -33,7 +35,7 @@ CUDA_SOURCES = [
     ("voxelize.cu", ["--fmad=false"]),
     ("volume.cu", ["--fmad=false"]),
     ("raster.cu", ["--fmad=false"]),
-    ("trace.cu", []),
+    ("trace.cu", ["--fmad=false"]),
     ("static_scratch.cu", []),
 ]
 CXX_SOURCES = ["capi.cpp"]

@@ -10,10 +10,14 @@
 //
 // Two samplers implement textureLod with GL_LINEAR_MIPMAP_LINEAR, LOD clamped
 // to [0, levels-1] and a (0,0,0,0) border (src/Application.cpp:1088-1116):
-//  - software: fp32 trilinear over 8 binary16 texels of two levels read with
-//    8-byte read-only loads from the linear chain (exact GL arithmetic);
+//  - software: fp32 trilinear over 8 texels of two levels, read with 16-byte
+//    read-only loads from a bordered fp32 copy of the chain (no bounds tests);
 //  - hardware: tex3DLod on a mip-mapped CUDA array (texture units, with
 //    their fixed-point filter weights).
+//
+// The file is compiled without FMA contraction: every fused multiply-add is
+// written out (fmaf, __ffma2_rn), so the single-scene and the batched
+// instantiations of the kernel give bit-identical results.
 #include "vct_device.cuh"
 
 namespace vct {
@@ -37,8 +41,8 @@ __device__ __forceinline__ float4 texel(const uint2* __restrict__ base, int S, i
 }
 
 __device__ __forceinline__ float4 lerp4(float4 p, float4 q, float t) {
-    float s = 1.0f - t;
-    return make_float4(p.x * s + q.x * t, p.y * s + q.y * t, p.z * s + q.z * t, p.w * s + q.w * t);
+    return make_float4(fmaf(t, q.x, fmaf(-t, p.x, p.x)), fmaf(t, q.y, fmaf(-t, p.y, p.y)),
+                       fmaf(t, q.z, fmaf(-t, p.z, p.z)), fmaf(t, q.w, fmaf(-t, p.w, p.w)));
 }
 
 // RGBA as two packed fp32 pairs: Blackwell issues one FFMA2/FMUL2 per pair.
@@ -68,7 +72,7 @@ __device__ __forceinline__ float4 to_float4(rgba2 v) { return make_float4(v.rg.x
 __device__ __forceinline__ rgba2 trilinear2(const TraceParams& P, const int* __restrict__ off, int l, f3 p) {
     const int S = P.dim >> l, Pd = S + 2;
     const float4* base = P.pchain + off[l];
-    const float u = p.x * (float)S - 0.5f, v = p.y * (float)S - 0.5f, w = p.z * (float)S - 0.5f;
+    const float u = fmaf(p.x, (float)S, -0.5f), v = fmaf(p.y, (float)S, -0.5f), w = fmaf(p.z, (float)S, -0.5f);
     const float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     const float a = u - fu, b = v - fv, c = w - fw;
     const int i = (int)fu + 1, j = (int)fv + 1, k = (int)fw + 1;
@@ -124,25 +128,31 @@ __device__ __forceinline__ float4 trace_cone(const TraceParams& P, const int* of
     for (int i = 0; i < c.steps && alpha < 0.95f; ++i) {
         float r = h * tanh;
         float lod = __log2f(fmaxf(1.0f, 2.0f * r));
-        f3 sp = add(start, mul(mul(dir, h), scale));
+        const f3 dh = mul(dir, h);
+        const f3 sp = mk(fmaf(dh.x, scale, start.x), fmaf(dh.y, scale, start.y), fmaf(dh.z, scale, start.z));
         // any(notEqual(p, clamp(p, 0, 1))): outside, or NaN
         if (!(sp.x >= 0.f && sp.y >= 0.f && sp.z >= 0.f && sp.x <= 1.f && sp.y <= 1.f && sp.z <= 1.f)) break;
         if (h * scale > maxd) break;
         float4 s = sample_lod<MODE>(P, off, sp, lod + c.lod_offset);
         ++ns;
         float a = 1.0f - alpha;
-        col = add(col, mul(mk(s.x, s.y, s.z), a));
-        alpha += a * s.w;
+        col = mk(fmaf(s.x, a, col.x), fmaf(s.y, a, col.y), fmaf(s.z, a, col.z));
+        alpha = fmaf(a, s.w, alpha);
         h += r;
     }
     return make_float4(col.x, col.y, col.z, alpha);
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
+template <int MODE, class Scenes>
+__global__ void __launch_bounds__(256) trace_kernel(const Scenes S) {
+    // One CTA per 16x16 tile, tiles of every scene of the launch in a row.
+    long long tile;
+    const TraceParams& P = S.get(S.find(blockIdx.x, tile));
+    const int tiles_x = (P.width + 15) / 16;
+    const int tx = (int)(tile % tiles_x), ty = (int)(tile / tiles_x);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int x = blockIdx.x * 16 + (wid & 1) * 8 + (lane & 7);
-    const int y = blockIdx.y * 16 + (wid >> 1) * 4 + (lane >> 3);
+    const int x = tx * 16 + (wid & 1) * 8 + (lane & 7);
+    const int y = ty * 16 + (wid >> 1) * 4 + (lane >> 3);
     // Offsets of the bordered levels (32-bit: the chain holds < 2^31 voxels).
     __shared__ int s_off[VCT_MAX_LEVELS];
     if (threadIdx.x < VCT_MAX_LEVELS)
@@ -177,10 +187,8 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
                                            : sub(add(mul(T, dx), mul(N, dy)), mul(B, dz));
                     float4 cr = trace_cone<MODE>(P, s_off, vp, N, d, P.diffuse, P.max_distance, ns);
                     const float w = kConeWeight[c];
-                    ind.x += w * cr.x;
-                    ind.y += w * cr.y;
-                    ind.z += w * cr.z;
-                    ind.w += w * cr.w;
+                    ind = make_float4(fmaf(w, cr.x, ind.x), fmaf(w, cr.y, ind.y), fmaf(w, cr.z, ind.z),
+                                      fmaf(w, cr.w, ind.w));
                 }
                 irr = ind;
                 const float occ = 1.0f - clampf(ind.w, 0.0f, 1.0f);
@@ -216,15 +224,26 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceParams P) {
 
 }  // namespace
 
-void launch_trace(const TraceParams& P, cudaStream_t s) {
-    dim3 grid((P.width + 15) / 16, (P.height + 15) / 16);
-    if (P.filter == VCT_FILTER_HARDWARE)
-        trace_kernel<VCT_FILTER_HARDWARE><<<grid, 256, 0, s>>>(P);
-    else if (P.filter == VCT_FILTER_HARDWARE_LEVELS)
-        trace_kernel<VCT_FILTER_HARDWARE_LEVELS><<<grid, 256, 0, s>>>(P);
+template <class Scenes>
+void launch_trace_set(const Scenes& S, int filter, long long tiles, cudaStream_t s) {
+    if (tiles <= 0) return;
+    if (filter == VCT_FILTER_HARDWARE)
+        trace_kernel<VCT_FILTER_HARDWARE><<<(unsigned)tiles, 256, 0, s>>>(S);
+    else if (filter == VCT_FILTER_HARDWARE_LEVELS)
+        trace_kernel<VCT_FILTER_HARDWARE_LEVELS><<<(unsigned)tiles, 256, 0, s>>>(S);
     else
-        trace_kernel<VCT_FILTER_SOFTWARE><<<grid, 256, 0, s>>>(P);
+        trace_kernel<VCT_FILTER_SOFTWARE><<<(unsigned)tiles, 256, 0, s>>>(S);
     note_launches(1);
+}
+
+long long trace_tiles(int width, int height) { return (long long)((width + 15) / 16) * ((height + 15) / 16); }
+
+void launch_trace(const TraceParams& P, cudaStream_t s) {
+    launch_trace_set(OneScene<TraceParams>{P}, P.filter, trace_tiles(P.width, P.height), s);
+}
+
+void launch_trace_batch(const SceneBatch<TraceParams>& B, int filter, long long tiles, cudaStream_t s) {
+    launch_trace_set(ManyScenes<TraceParams>{B}, filter, tiles, s);
 }
 
 }  // namespace vct

@@ -179,4 +179,38 @@ __device__ __forceinline__ float shadow_bilinear(const float* __restrict__ sm, i
 
 __device__ __forceinline__ uint32_t quant16(float x) { return __float2uint_rn(clampf(x, 0.0f, 1.0f) * 65535.0f); }
 
+// ------------------------------------------------------------ scene sets
+// Kernels are templated on a scene set: OneScene keeps the parameters in
+// kernel-parameter space (the single-frame path), ManyScenes reads them from
+// device memory and maps a global work index to (scene, local index).
+template <class Params>
+struct OneScene {
+    Params p;
+    __device__ __forceinline__ int count() const { return 1; }
+    __device__ __forceinline__ const Params& get(int) const { return p; }
+    __device__ __forceinline__ int find(long long w, long long& local) const {
+        local = w;
+        return 0;
+    }
+};
+
+template <class Params>
+struct ManyScenes {
+    SceneBatch<Params> b;
+    __device__ __forceinline__ int count() const { return b.n; }
+    __device__ __forceinline__ const Params& get(int s) const { return b.p[s]; }
+    __device__ __forceinline__ int find(long long w, long long& local) const {
+        int lo = 0, hi = b.n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(b.off + mid) <= w)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        local = w - __ldg(b.off + lo);
+        return lo;
+    }
+};
+
 }  // namespace vct

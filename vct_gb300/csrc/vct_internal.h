@@ -73,6 +73,28 @@ struct AccumParams {
     uint32_t* block_off;     // exclusive scan of per-block unit totals (+ total at [nblocks])
 };
 
+// Several independent scenes processed by one launch per stage: `off` is the
+// exclusive prefix sum (n + 1 entries, in device memory) of the scenes' work
+// items (triangles, shadow texels, bricks or pixel tiles) and `p` their
+// parameters.  A global work index w belongs to scene s with
+// off[s] <= w < off[s+1].
+template <class Params>
+struct SceneBatch {
+    const Params* p;
+    const long long* off;
+    int n;
+};
+
+// Voxeliser work distribution over all triangles of one launch (one scene, or
+// the concatenated triangles of a batch).
+struct VoxWork {
+    uint4* tri_rec;
+    uint32_t* tri_units;
+    uint32_t* tri_scan;
+    uint32_t* block_off;
+    long long ntri;
+};
+
 constexpr int kSetupThreads = 256;  // triangles per setup block
 constexpr long long align256(long long b) { return (b + 255) & ~255LL; }
 // Scratch bytes the voxeliser needs for `ntri` triangles: a 48-byte setup
@@ -140,6 +162,7 @@ struct MipLevels {
     float4* pad[VCT_MAX_LEVELS];               // optional bordered fp32 copy (nullptr = none)
     int dim;
     int levels;
+    int first;  // mip tail: the level the remaining levels are built from
 };
 
 struct TraceParams {
@@ -211,6 +234,15 @@ void launch_trace(const TraceParams& P, cudaStream_t s);
 void launch_shadow_raster(const ShadowRasterParams& P, cudaStream_t s);
 void launch_gbuffer_raster(const GbufferRasterParams& P, cudaStream_t s);
 void launch_fill_u32(uint32_t* p, uint32_t v, long long n, cudaStream_t s);
+
+// Batched frame stages: one launch covers the work of every scene.
+int accumulate_batch_max_scenes();
+void launch_accumulate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, int num_sms, cudaStream_t s);
+void launch_inject_mark_batch(const SceneBatch<InjectParams>& B, long long ntexels, cudaStream_t s);
+void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks, cudaStream_t s);
+void launch_mip_tail_batch(const SceneBatch<MipLevels>& B, cudaStream_t s);
+long long trace_tiles(int width, int height);
+void launch_trace_batch(const SceneBatch<TraceParams>& B, int filter, long long tiles, cudaStream_t s);
 // Copies every level of a linear chain into the interior of the bordered chain.
 void launch_pad_copy(const uint2* chain, float4* pchain, int dim, int levels, cudaStream_t s);
 

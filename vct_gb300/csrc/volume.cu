@@ -146,14 +146,16 @@ __device__ __forceinline__ void brick_mips(uint2* s0, uint2* s1, int nlev, uint2
 //                result equals normalise; inject; filter because the value
 //                injectRadiance stores into a voxel depends only on that
 //                voxel (its stores are idempotent).
-template <bool FUSED>
-__global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const ResolveParams R) {
+template <bool FUSED, class Scenes>
+__global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
     __shared__ uint2 s0[FUSED ? kBrickVox : 1];
     __shared__ uint2 s1[FUSED ? kBrickVox / 8 : 1];
+    long long brick;
+    const ResolveParams& R = S.get(S.find(blockIdx.x, brick));
     const NormalizeParams& P = R.norm;
     const int N = P.dim;
     const int bpa = N / kBrick;
-    const int bx = blockIdx.x % bpa, by = (blockIdx.x / bpa) % bpa, bz = blockIdx.x / (bpa * bpa);
+    const int bx = (int)(brick % bpa), by = (int)((brick / bpa) % bpa), bz = (int)(brick / (bpa * bpa));
     uint32_t uniq = 0, mx = 0, flags = 0;
 #pragma unroll 1
     for (int it = 0; it < kBrickVox / 4 / kThreads; ++it) {
@@ -284,11 +286,15 @@ __global__ void __launch_bounds__(kThreads) inject_kernel(const InjectParams P) 
         P.radiance[v] = P.color[v];
 }
 
-// Fused path: mark the voxels injectRadiance would store to.
-__global__ void __launch_bounds__(kThreads) inject_mark_kernel(const InjectParams P) {
-    int x = blockIdx.x * 16 + (threadIdx.x & 15);
-    int y = blockIdx.y * 16 + (threadIdx.x >> 4);
-    if (x >= P.nx || y >= P.ny) return;
+// Fused path: mark the voxels injectRadiance would store to.  One thread per
+// shadow texel over the texels of every scene of the launch.
+template <class Scenes>
+__global__ void __launch_bounds__(kThreads) inject_mark_kernel(const Scenes S, long long ntexels) {
+    const long long g = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (g >= ntexels) return;
+    long long local;
+    const InjectParams& P = S.get(S.find(g, local));
+    const int y = (int)(local / P.nx), x = (int)(local - (long long)y * P.nx);
     int ix, iy, iz;
     if (!inject_voxel(P, x, y, ix, iy, iz)) return;
     const int N = P.dim;
@@ -317,10 +323,17 @@ __global__ void __launch_bounds__(kThreads) mip_brick_kernel(const MipLevels M, 
     brick_mips(s0, s1, nlev, M.level + first, M.surf + first, M.pad + first, S, bx, by, bz);
 }
 
-// Small levels (side <= 16): one CTA builds every remaining level.
-__global__ void __launch_bounds__(kThreads) mip_tail_kernel(const MipLevels M, int first) {
+// Small levels (side <= 16): one CTA per scene builds every level after
+// M.first.
+template <class Scenes>
+__global__ void __launch_bounds__(kThreads) mip_tail_kernel(const Scenes SS) {
     __shared__ uint2 s0[kBrickVox];
     __shared__ uint2 s1[kBrickVox / 8];
+    const MipLevels& M = SS.get(blockIdx.x);
+    const int first = M.first;
+    // Chains of at most five levels are complete after the resolve; the tail
+    // (side of level `first` <= 16) only exists for longer ones.
+    if (first + 1 >= M.levels) return;
     const int S = M.dim >> first;
     const uint2* src = M.level[first];
     for (int t = threadIdx.x; t < S * S * S; t += kThreads) s0[t] = src[t];
@@ -359,7 +372,7 @@ void launch_normalize(const NormalizeParams& P, cudaStream_t s) {
     memset(&R, 0, sizeof R);
     R.norm = P;
     const int bpa = P.dim / kBrick;
-    resolve_kernel<false><<<bpa * bpa * bpa, kThreads, 0, s>>>(R);
+    resolve_kernel<false><<<bpa * bpa * bpa, kThreads, 0, s>>>(OneScene<ResolveParams>{R});
     note_launches(1);
 }
 
@@ -370,14 +383,14 @@ void launch_inject(const InjectParams& P, cudaStream_t s) {
 }
 
 void launch_inject_mark(const InjectParams& P, cudaStream_t s) {
-    dim3 grid((P.nx + 15) / 16, (P.ny + 15) / 16);
-    inject_mark_kernel<<<grid, kThreads, 0, s>>>(P);
+    const long long n = (long long)P.nx * P.ny;
+    inject_mark_kernel<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(OneScene<InjectParams>{P}, n);
     note_launches(1);
 }
 
 void launch_resolve(const ResolveParams& R, cudaStream_t s) {
     const int bpa = R.norm.dim / kBrick;
-    resolve_kernel<true><<<bpa * bpa * bpa, kThreads, 0, s>>>(R);
+    resolve_kernel<true><<<bpa * bpa * bpa, kThreads, 0, s>>>(OneScene<ResolveParams>{R});
     note_launches(1);
 }
 
@@ -393,11 +406,30 @@ void launch_mips(const MipLevels& M, int first, cudaStream_t s) {
             note_launches(1);
             l += nlev;
         } else {
-            mip_tail_kernel<<<1, kThreads, 0, s>>>(M, l);
+            MipLevels T = M;
+            T.first = l;
+            mip_tail_kernel<<<1, kThreads, 0, s>>>(OneScene<MipLevels>{T});
             note_launches(1);
             break;
         }
     }
+}
+
+void launch_inject_mark_batch(const SceneBatch<InjectParams>& B, long long ntexels, cudaStream_t s) {
+    if (ntexels <= 0) return;
+    inject_mark_kernel<<<(unsigned)((ntexels + kThreads - 1) / kThreads), kThreads, 0, s>>>(
+        ManyScenes<InjectParams>{B}, ntexels);
+    note_launches(1);
+}
+
+void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks, cudaStream_t s) {
+    resolve_kernel<true><<<(unsigned)nbricks, kThreads, 0, s>>>(ManyScenes<ResolveParams>{B});
+    note_launches(1);
+}
+
+void launch_mip_tail_batch(const SceneBatch<MipLevels>& B, cudaStream_t s) {
+    mip_tail_kernel<<<B.n, kThreads, 0, s>>>(ManyScenes<MipLevels>{B});
+    note_launches(1);
 }
 
 void launch_pad_copy(const uint2* chain, float4* pchain, int dim, int levels, cudaStream_t s) {

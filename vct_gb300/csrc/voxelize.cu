@@ -1,20 +1,21 @@
 // Triangle voxelisation: shaders/voxelize.geom:25-73 + voxelize.frag:75-280.
 //
 // Three launches, balanced at fragment granularity (triangle sizes vary by
-// more than three orders of magnitude in one scene):
-//  1. voxelize_setup_kernel, one thread per triangle: the geometry-shader part
-//     (dominant axis from the summed vertex normals, per-axis ortho
+// more than three orders of magnitude in one scene), for one scene or for the
+// concatenated triangles of a batch of scenes:
+//  1. voxelize_setup_kernel, one thread per triangle: the geometry-shader
+//     part (dominant axis from the summed vertex normals, per-axis ortho
 //     projection, snapping to the 1/256 sub-pixel grid, bounding box) into a
 //     48-byte record, and the triangle's share of work: its bounding box in
 //     units of kUnit pixels, with a block-local exclusive scan;
-//  2. voxelize_scan_kernel, one CTA: exclusive scan of the per-block unit totals;
-//  3. voxelize_raster_kernel, persistent: every warp takes an equal contiguous range
-//     of work units, tests 32 pixel centres at a time for coverage, compacts
-//     covered fragments (clipped to the depth range) with a ballot into a
-//     per-warp queue in shared memory, and whenever 32 are queued each lane
-//     lights one fragment (all enabled lights, 5-tap PCF for shadow casters)
-//     and adds it into the voxel's 32-byte accumulator record with four
-//     64-bit atomics.
+//  2. voxelize_scan_kernel, one CTA: exclusive scan of the per-block totals;
+//  3. voxelize_raster_kernel, persistent: every warp takes an equal
+//     contiguous range of work units, tests 32 pixel centres at a time for
+//     coverage, compacts covered fragments (clipped to the depth range) with
+//     a ballot into a per-warp queue in shared memory, and whenever 32 are
+//     queued each lane lights one fragment (all enabled lights, 5-tap PCF for
+//     shadow casters) and adds it into the voxel's 32-byte accumulator record
+//     with fire-and-forget 64-bit reductions.
 //
 // Integer sums make the result independent of fragment order: it is
 // bit-exact against the CPU oracle.  Compiled with --fmad=false (see
@@ -29,10 +30,11 @@ constexpr int kWarps = 8;
 constexpr int kQueue = 64;
 constexpr int kUnit = 512;  // bounding-box pixels per work unit
 constexpr int kRasterBlocksPerSM = 3;
+constexpr int kMaxBatchScenes = 256;  // scene id travels in 8 bits of a queue entry
 
 struct FragQueue {
-    int tri[kQueue];
-    uint32_t pix[kQueue];  // px | py << 11 | axis << 22
+    int tri[kQueue];       // triangle index within its scene
+    uint32_t pix[kQueue];  // px | py << 11 | axis << 22 | scene << 24
     float l0[kQueue], l1[kQueue], l2[kQueue], z[kQueue];
 };
 
@@ -60,10 +62,13 @@ __device__ __forceinline__ float shadow_factor(const AccumParams& P, f3 wp) {
 }
 
 // ------------------------------------------------------------- 1. setup
-__global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const AccumParams P) {
-    const long long t = (long long)blockIdx.x * kSetupThreads + threadIdx.x;
+template <class Scenes>
+__global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Scenes S, const VoxWork W) {
+    const long long g = (long long)blockIdx.x * kSetupThreads + threadIdx.x;
     uint32_t units = 0;
-    if (t < P.ntri) {
+    if (g < W.ntri) {
+        long long t;
+        const AccumParams& P = S.get(S.find(g, t));
         const float* Pp = P.pos + t * 9;
         const float* Pn = P.nrm + t * 9;
         f3 n0 = ld3(Pn), n1 = ld3(Pn + 3), n2 = ld3(Pn + 6);
@@ -92,7 +97,7 @@ __global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Acc
             const uint32_t bw = rt.px1 - rt.px0 + 1, bh = rt.py1 - rt.py0 + 1;
             const uint32_t bias = (rt.bias[0] ? 1u : 0u) | (rt.bias[1] ? 2u : 0u) | (rt.bias[2] ? 4u : 0u);
             const float inv = __fdiv_rn(1.0f, __ll2float_rn(rt.area));
-            uint4* rec = P.tri_rec + 3 * t;
+            uint4* rec = W.tri_rec + 3 * g;
             rec[0] = make_uint4((uint32_t)rt.X[0], (uint32_t)rt.Y[0], (uint32_t)rt.X[1], (uint32_t)rt.Y[1]);
             rec[1] = make_uint4((uint32_t)rt.X[2], (uint32_t)rt.Y[2], __float_as_uint(z[0]), __float_as_uint(z[1]));
             rec[2] = make_uint4(__float_as_uint(z[2]), __float_as_uint(inv),
@@ -101,7 +106,7 @@ __global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Acc
                                 bw | (bh << 11));
             units = (bw * bh + kUnit - 1) / kUnit;
         }
-        P.tri_units[t] = units;
+        W.tri_units[g] = units;
     }
     // Block-local exclusive scan of the unit counts.
     __shared__ uint32_t warp_tot[kSetupThreads / 32];
@@ -120,8 +125,8 @@ __global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Acc
         before += (w < wid) ? warp_tot[w] : 0u;
         total += warp_tot[w];
     }
-    if (t < P.ntri) P.tri_scan[t] = before + incl - units;
-    if (threadIdx.x == 0) P.block_off[blockIdx.x] = total;
+    if (g < W.ntri) W.tri_scan[g] = before + incl - units;
+    if (threadIdx.x == 0) W.block_off[blockIdx.x] = total;
 }
 
 // --------------------------------------------------------------- 2. scan
@@ -160,7 +165,7 @@ __global__ void __launch_bounds__(1024) voxelize_scan_kernel(uint32_t* block_off
 __device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQueue& q, int e) {
     const long long t = q.tri[e];
     const uint32_t pix = q.pix[e];
-    const int px = (int)(pix & 0x7ffu), py = (int)((pix >> 11) & 0x7ffu), axis = (int)(pix >> 22);
+    const int px = (int)(pix & 0x7ffu), py = (int)((pix >> 11) & 0x7ffu), axis = (int)((pix >> 22) & 3u);
     const float l[3] = {q.l0[e], q.l1[e], q.l2[e]};
     const float zf = q.z[e];
     const float* Pp = P.pos + t * 9;
@@ -225,22 +230,40 @@ __device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQ
     atomicOr(P.occ + (v >> 5), 1u << (v & 31));
 }
 
-__device__ __forceinline__ long long unit_start(const AccumParams& P, long long t) {
-    return (long long)P.block_off[t / kSetupThreads] + P.tri_scan[t];
+template <class Scenes>
+__device__ __forceinline__ long long unit_start(const VoxWork& W, long long g) {
+    return (long long)W.block_off[g / kSetupThreads] + W.tri_scan[g];
 }
 
-__global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM) voxelize_raster_kernel(const AccumParams P,
-                                                                                          int nblocks) {
+template <class Scenes>
+__global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
+    voxelize_raster_kernel(const Scenes S, const VoxWork W, int nblocks) {
     __shared__ FragQueue queues[kWarps];
+    __shared__ unsigned frag_count[kMaxBatchScenes];  // VoxelizeInfo.totalVoxelFragments per scene
     const int lane = threadIdx.x & 31;
     FragQueue& q = queues[threadIdx.x >> 5];
     const unsigned FULL = 0xffffffffu;
+    const int nscenes = S.count();
+    for (int i = threadIdx.x; i < nscenes; i += blockDim.x) frag_count[i] = 0;
+    __syncthreads();
     const long long nw = (long long)gridDim.x * kWarps;
     const long long w = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
-    const long long total = P.block_off[nblocks];
+    const long long total = W.block_off[nblocks];
     const long long u0 = total * w / nw, u1 = total * (w + 1) / nw;
     int qn = 0;  // queued fragments (warp-uniform)
-    unsigned shaded = 0;
+
+    // Shades the first 32 queued fragments, one per lane, and counts them
+    // per scene (one shared-memory atomic per distinct scene in the warp).
+    auto shade32 = [&](int nact) {
+        __syncwarp();
+        if (lane < nact) {
+            const int s = (int)(q.pix[lane] >> 24);
+            shade_fragment(S.get(s), q, lane);
+            const unsigned same = __match_any_sync(__activemask(), s);
+            if (lane == __ffs(same) - 1) atomicAdd(&frag_count[s], (unsigned)__popc(same));
+        }
+        __syncwarp();
+    };
 
     if (u0 < u1) {
         // Triangle owning unit u0: binary search over the block offsets, then
@@ -248,30 +271,32 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM) voxelize_rast
         int lo = 0, hi = nblocks - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if ((long long)P.block_off[mid] <= u0)
+            if ((long long)W.block_off[mid] <= u0)
                 lo = mid;
             else
                 hi = mid - 1;
         }
-        long long tlo = (long long)lo * kSetupThreads;
-        long long thi = min(tlo + kSetupThreads, P.ntri) - 1;
-        while (tlo < thi) {
-            const long long mid = (tlo + thi + 1) >> 1;
-            if (unit_start(P, mid) <= u0)
-                tlo = mid;
+        long long glo = (long long)lo * kSetupThreads;
+        long long ghi = min(glo + kSetupThreads, W.ntri) - 1;
+        while (glo < ghi) {
+            const long long mid = (glo + ghi + 1) >> 1;
+            if (unit_start<Scenes>(W, mid) <= u0)
+                glo = mid;
             else
-                thi = mid - 1;
+                ghi = mid - 1;
         }
-        long long t = tlo;
-        long long start = unit_start(P, t);
-        uint32_t nunits = P.tri_units[t];
+        long long g = glo;
+        long long start = unit_start<Scenes>(W, g);
+        uint32_t nunits = W.tri_units[g];
         for (long long u = u0; u < u1; ++u) {
             while (u >= start + nunits) {
-                ++t;
-                start = unit_start(P, t);
-                nunits = P.tri_units[t];
+                ++g;
+                start = unit_start<Scenes>(W, g);
+                nunits = W.tri_units[g];
             }
-            const uint4* rp = P.tri_rec + 3 * t;
+            long long tl;
+            const int scene = S.find(g, tl);
+            const uint4* rp = W.tri_rec + 3 * g;
             const uint4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
             const int X[3] = {(int)r0.x, (int)r0.z, (int)r1.x};
             const int Y[3] = {(int)r0.y, (int)r0.w, (int)r1.y};
@@ -313,8 +338,9 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM) voxelize_rast
                 const unsigned m = __ballot_sync(FULL, cov);
                 if (cov) {
                     const int slot = qn + __popc(m & ((1u << lane) - 1u));
-                    q.tri[slot] = (int)t;
-                    q.pix[slot] = (uint32_t)px | ((uint32_t)py << 11) | ((uint32_t)axis << 22);
+                    q.tri[slot] = (int)tl;
+                    q.pix[slot] = (uint32_t)px | ((uint32_t)py << 11) | ((uint32_t)axis << 22) |
+                                  ((uint32_t)scene << 24);
                     q.l0[slot] = l[0];
                     q.l1[slot] = l[1];
                     q.l2[slot] = l[2];
@@ -322,10 +348,7 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM) voxelize_rast
                 }
                 qn += __popc(m);
                 if (qn >= 32) {
-                    __syncwarp();
-                    shade_fragment(P, q, lane);
-                    ++shaded;
-                    __syncwarp();
+                    shade32(32);
                     if (lane < qn - 32) {
                         const int src = 32 + lane;
                         q.tri[lane] = q.tri[src];
@@ -341,14 +364,20 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM) voxelize_rast
             }
         }
     }
-    __syncwarp();
-    if (lane < qn) {
-        shade_fragment(P, q, lane);
-        ++shaded;
-    }
-    // VoxelizeInfo.totalVoxelFragments, aggregated per warp.
-    const unsigned tot = __reduce_add_sync(FULL, shaded);
-    if (lane == 0 && tot) atomicAdd(&P.stats->total_voxel_fragments, tot);
+    shade32(qn);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nscenes; i += blockDim.x)
+        if (frag_count[i]) atomicAdd(&S.get(i).stats->total_voxel_fragments, frag_count[i]);
+}
+
+template <class Scenes>
+void launch_voxelize(const Scenes& S, const VoxWork& W, int num_sms, cudaStream_t s) {
+    if (W.ntri <= 0) return;
+    const int nblocks = (int)((W.ntri + kSetupThreads - 1) / kSetupThreads);
+    voxelize_setup_kernel<Scenes><<<nblocks, kSetupThreads, 0, s>>>(S, W);
+    voxelize_scan_kernel<<<1, 1024, 0, s>>>(W.block_off, nblocks);
+    voxelize_raster_kernel<Scenes><<<num_sms * kRasterBlocksPerSM, kWarps * 32, 0, s>>>(S, W, nblocks);
+    note_launches(3);
 }
 
 }  // namespace
@@ -366,12 +395,14 @@ void accumulate_bind_scratch(AccumParams& P, void* scratch) {
 }
 
 void launch_accumulate(const AccumParams& P, cudaStream_t s) {
-    if (P.ntri <= 0) return;
-    const int nblocks = (int)((P.ntri + kSetupThreads - 1) / kSetupThreads);
-    voxelize_setup_kernel<<<nblocks, kSetupThreads, 0, s>>>(P);
-    voxelize_scan_kernel<<<1, 1024, 0, s>>>(P.block_off, nblocks);
-    voxelize_raster_kernel<<<P.num_sms * kRasterBlocksPerSM, kWarps * 32, 0, s>>>(P, nblocks);
-    note_launches(3);
+    const VoxWork W = {P.tri_rec, P.tri_units, P.tri_scan, P.block_off, P.ntri};
+    launch_voxelize(OneScene<AccumParams>{P}, W, P.num_sms, s);
+}
+
+int accumulate_batch_max_scenes() { return kMaxBatchScenes; }
+
+void launch_accumulate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, int num_sms, cudaStream_t s) {
+    launch_voxelize(ManyScenes<AccumParams>{B}, W, num_sms, s);
 }
 
 }  // namespace vct

@@ -151,6 +151,25 @@ def _box(rng, size, center, yaw):
     return tris, nrms
 
 
+# Corner indices and normals of the 12 triangles _box emits, in its order.
+_BOX_TRI = np.array([[0, 3, 2], [0, 2, 1], [4, 5, 6], [4, 6, 7], [0, 4, 7], [0, 7, 3], [1, 2, 6], [1, 6, 5],
+                     [0, 1, 5], [0, 5, 4], [3, 7, 6], [3, 6, 2]])
+_BOX_NRM = np.repeat(np.array([(0, 0, -1), (0, 0, 1), (-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0)], float), 2, 0)
+_BOX_CORNER = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1],
+                        [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], float) * 0.5
+
+
+def _boxes(size, center, yaw):
+    """_box for many boxes at once: (B*12, 3, 3) triangles and normals."""
+    cs, sn = np.cos(yaw), np.sin(yaw)
+    R = np.zeros((len(yaw), 3, 3))
+    R[:, 0, 0], R[:, 0, 2], R[:, 1, 1], R[:, 2, 0], R[:, 2, 2] = cs, sn, 1.0, -sn, cs
+    local = _BOX_CORNER[_BOX_TRI][None] * size[:, None, None, :]          # (B, 12, 3, 3)
+    tris = np.einsum("bij,btkj->btki", R, local) + center[:, None, None, :]
+    nrms = np.einsum("bij,tj->bti", R, _BOX_NRM)[:, :, None, :].repeat(3, 2)
+    return tris.reshape(-1, 3, 3), nrms.reshape(-1, 3, 3)
+
+
 def _cylinder(radius, y0, y1, cx, cz, segments):
     a = np.arange(segments + 1) * (2 * np.pi / segments)
     x, z = np.cos(a), np.sin(a)
@@ -280,6 +299,42 @@ def tiny(seed: int = 0, dim: int = 16, shadow: int = 64, gbuffer=(48, 32), n_box
     return _finish("tiny", np.concatenate(tris), np.concatenate(nrms), np.concatenate(alb), lights, ls, dim, levels,
                    1.0, (shadow, shadow), np.array([0.3, 0.9, 2.4]), np.array([0.0, 0.0, 0.0]), 50 * DEG,
                    tuple(gbuffer), BASELINE_CONES)
+
+
+# Batched scene family: per scene a triangle count log-uniform in [1k, 200k]
+# (rotated boxes of log-uniform size), a grid from {64, 128, 256}^3, a 16:9
+# G-buffer from 320x180 to 1920x1080 and 1-4 lights (one directional shadow
+# caster plus point lights).
+BATCH_DIMS = (64, 128, 256)
+BATCH_GBUFFERS = tuple((320 * k, 180 * k) for k in range(1, 7))
+
+
+def batch_scene(seed: int = 0, index: int = 0, shadow: int = 1024) -> Scene:
+    rng = np.random.default_rng((seed, index))
+    ntri = int(np.exp(rng.uniform(np.log(1000), np.log(200000))))
+    n_boxes = max(1, ntri // 12)
+    dim = int(rng.choice(BATCH_DIMS))
+    gsize = BATCH_GBUFFERS[int(rng.integers(len(BATCH_GBUFFERS)))]
+    extent = 2.0
+    # Smaller boxes in denser scenes keep the covered area comparable.
+    hi = np.log(0.2 * extent * min(1.0, (2000.0 / n_boxes) ** 0.5) + 0.02)
+    lo = np.log(0.01 * extent)
+    size = np.exp(rng.uniform(lo, max(hi, lo + 0.1), size=(n_boxes, 3)))
+    center = rng.uniform(-0.9, 0.9, size=(n_boxes, 3))
+    yaw = rng.uniform(0, 2 * np.pi, size=n_boxes)
+    tris, nrms = _boxes(size, center, yaw)
+    alb = np.repeat(rng.uniform(0, 1, size=(n_boxes, 3)), 12, 0)
+    light, ls = _directional_light(rng, 1.0)
+    lights = [light]
+    for _ in range(int(rng.integers(0, 4))):
+        lights.append(dict(position=rng.uniform(-0.9, 0.9, size=3), direction=np.array([0.0, -1.0, 0.0]),
+                           color=rng.uniform(0.5, 1.0, size=3), range=float(rng.uniform(0.3, 0.8)), intensity=1.0,
+                           shadow_caster=0, type=0))
+    phi = rng.uniform(0, 2 * np.pi)
+    eye = np.array([2.8 * np.sin(phi), rng.uniform(0.2, 1.0), 2.8 * np.cos(phi)])
+    levels = int(np.log2(dim)) + 1
+    return _finish(f"batch{index}", tris, nrms, alb, lights, ls, dim, levels, 1.0, (shadow, shadow), eye,
+                   np.zeros(3), 55 * DEG, gsize, BASELINE_CONES)
 
 
 SCENES = {"cornell": cornell, "large": large, "tiny": tiny}
