@@ -51,7 +51,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="large", choices=["large", "cornell"])
+    ap.add_argument("--config", default="large", choices=["large", "cornell", "batch"],
+                    help="large plain frame (default), the small Cornell box, or the batched family: "
+                         "--batch-scenes seeded scenes in one captured graph")
+    ap.add_argument("--batch-scenes", type=int, default=32)
+    ap.add_argument("--no-autotune", action="store_true", help="batched: keep the default launch shapes")
     ap.add_argument("--filter", default="software", choices=["software", "levels", "hardware"],
                     help="cone sampler: fp32 trilinear (exact), texture units per level + fp32 level blend, "
                          "or texture units' trilinear-mip")
@@ -352,6 +356,178 @@ def run_ours(args, rank, world):
     return result, sc
 
 
+# ------------------------------------------------------------- batched
+BATCH_METRIC = "ms per batch of 32 scenes voxelize+inject+mip+trace (one captured graph)"
+
+
+def run_batch(args, rank, world):
+    """Batched family: --batch-scenes seeded scenes (triangles log-uniform in
+    1k-200k, grids from {64,128,256}^3, G-buffers 320x180..1920x1080, 1-4
+    lights) run as one vct_batch frame per step, replayed from a captured
+    CUDA graph, with the launch shapes picked by the library's autotuner.
+    Compared with the same scenes run as sequential vct_frame calls."""
+    import torch
+
+    from vct_gb300 import _lib as L
+    from vct_gb300 import api, scenes
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    t0 = time.perf_counter()
+    scs = [scenes.batch_scene(seed=args.seed + 1000 * rank, index=i) for i in range(args.batch_scenes)]
+    gen_s = time.perf_counter() - t0
+    filt = {"software": L.VCT_FILTER_SOFTWARE, "levels": L.VCT_FILTER_HARDWARE_LEVELS,
+            "hardware": L.VCT_FILTER_HARDWARE}[args.filter]
+    inputs, descs, colors = [], [], []
+    for sc in scs:
+        W, H = sc.gbuffer_size
+        SW, SH = sc.shadow_size
+        pos, nrm, alb = (torch.from_numpy(a).to(dev) for a in (sc.positions, sc.normals, sc.albedo))
+        tris = api.triangles(pos, nrm, alb)
+        sm = torch.empty(SW * SH, dtype=torch.float32, device=dev)
+        api.render_shadowmap(tris, sc, sm)
+        keys = torch.empty(W * H, dtype=torch.int64, device=dev)
+        gpos, gnrm, galb = (torch.empty(W * H * 4, dtype=torch.float32, device=dev) for _ in range(3))
+        api.render_gbuffer(tris, sc, keys, gpos, gnrm, galb)
+        del keys
+        color = torch.empty(W * H * 4, dtype=torch.float32, device=dev)
+        lights = api.light_array(sc.lights)
+        inputs.append(dict(pos=pos, nrm=nrm, alb=alb, sm=sm, gpos=gpos, gnrm=gnrm, galb=galb, lights=lights))
+        descs.append(api.scene_desc(tris, lights, api.shadow_desc(sc, sm), sc.eye,
+                                    api.gbuffer(gpos, gnrm, galb, W, H), api.trace_out(color=color)))
+        colors.append(color)
+    b = api.Batch([api.config_for(sc, device=local) for sc in scs])
+    for i, sc in enumerate(scs):
+        b.set_params(api.scene_params(sc, trace_filter=filt), i)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    lib = L.load()
+    torch.cuda.synchronize()
+    b.frame(descs, stream)
+    stream.synchronize()
+    t0 = time.perf_counter()
+    tuning = b.tuning() if args.no_autotune else b.autotune(descs, reps=3, stream=stream)
+    tune_s = time.perf_counter() - t0
+
+    def timed(step_fn, steps):
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+            st[i].record(stream)
+            step_fn()
+            en[i].record(stream)
+        stream.synchronize()
+        return [a.elapsed_time(e) for a, e in zip(st, en)]
+
+    # per-stage times of a direct (non-graph) batched frame
+    b.enable_timers(True)
+    stage = {k: 0.0 for k in ("voxelize_ms", "mipmap_ms", "render_ms", "total_ms")}
+    for i in range(max(3, args.warmup) + args.steps):
+        b.frame(descs, stream)
+        t = b.timers()
+        if i >= max(3, args.warmup):
+            for k in stage:
+                stage[k] += t[k] / args.steps
+    b.enable_timers(False)
+    direct_ms = timed(lambda: b.frame(descs, stream), args.steps)
+
+    # the headline: graph replays
+    b.capture(descs, stream)
+    for _ in range(max(3, args.warmup)):
+        b.replay(stream)
+    stream.synchronize()
+    barrier(world)
+    launches0 = lib.vct_launch_count()
+    with ClockSampler(local) as clk:
+        graph_ms = timed(lambda: b.replay(stream), args.steps)
+    launches = lib.vct_launch_count() - launches0
+    total = max_over_ranks(sum(graph_ms), world)
+    value = total / (args.steps * world)
+
+    # sequential single-scene frames on the same contexts (default shapes, then the tuned ones)
+    def sequential():
+        for ctx, d in zip(b.scenes, descs):
+            ctx.frame(d.triangles, (d.lights, d.n_lights), d.shadow, list(d.eye), d.gbuffer, d.out, stream)
+
+    for _ in range(2):
+        sequential()
+    seq_default_ms = timed(sequential, args.steps)
+    for ctx in b.scenes:
+        ctx.set_tuning(tuning)
+    seq_tuned_ms = timed(sequential, args.steps)
+
+    # e2e: every step copies all scenes' inputs from pinned host memory, replays, copies the images back
+    host = [{k: v.cpu().pin_memory() for k, v in d.items() if k != "lights"} for d in inputs]
+    h_colors = [torch.empty(c.numel(), dtype=torch.float32).pin_memory() for c in colors]
+    h2d = sum(t.numel() * t.element_size() for h in host for t in h.values())
+    d2h = sum(c.numel() * 4 for c in colors)
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            for d, h in zip(inputs, host):
+                for k, t in h.items():
+                    d[k].copy_(t, non_blocking=True)
+        b.replay(stream)
+        with torch.cuda.stream(stream):
+            for hc, c in zip(h_colors, colors):
+                hc.copy_(c, non_blocking=True)
+
+    for _ in range(max(3, args.warmup)):
+        e2e_step()
+    stream.synchronize()
+    e2e_total = max_over_ranks(sum(timed(e2e_step, args.steps)), world)
+    e2e_ms = e2e_total / (args.steps * world)
+    assert all(torch.isfinite(h).all() for h in h_colors), "non-finite output"
+
+    # roofline of the dominant stage: algorithmic bytes summed over scenes
+    stats = [ctx.stats(stream) for ctx in b.scenes]
+    alg = [algorithmic_bytes(sc, st, None) for sc, st in zip(scs, stats)]
+    sums = {k: sum(a[k] for a in alg) for k in alg[0]}
+    stage_bytes = {"voxelize_ms": sums["accumulate"],
+                   "mipmap_ms": sums["inject_mark"] + sums["resolve"] + sums["mip_tail"],
+                   "render_ms": sums["trace"]}
+    dom = max(stage_bytes, key=lambda k: stage[k])
+    peaks = load_peaks()
+    achieved = stage_bytes[dom] / (stage[dom] * 1e-3) / 1e9
+    names = {"voxelize_ms": "accumulate (voxelize setup+scan+raster)", "mipmap_ms": "inject_mark+resolve+mip_tail",
+             "render_ms": "trace"}
+    result = {
+        "metric": BATCH_METRIC.replace("32", str(args.batch_scenes)), "value": round(value, 4), "unit": "ms/batch",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value * world, 4),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 math, f16 volumes, u32 accumulators", "data": "synthetic seeded scenes (no dataset)",
+        "config": {"workload": f"batched family: {args.batch_scenes} scenes, triangles log-uniform 1k-200k, grids "
+                               "{64,128,256}^3, G-buffers 320x180..1920x1080, 1-4 lights, 6+1 cones",
+                   "seed": args.seed, "scenes": args.batch_scenes, "triangles": int(sum(sc.ntri for sc in scs)),
+                   "voxels": int(sum(sc.dim ** 3 for sc in scs)),
+                   "pixels": int(sum(sc.gbuffer_size[0] * sc.gbuffer_size[1] for sc in scs)),
+                   "sampler": args.filter, "parallelism": f"replicas x{world}",
+                   "l2": "256 MiB buffer written between timed steps (outside the events)",
+                   "tuning": api.tuning_dict(tuning), "autotune_s": round(tune_s, 2)},
+        "scenes_per_s": round(args.batch_scenes * 1e3 / value, 1),
+        "direct_batch_ms": round(statistics.median(direct_ms), 4),
+        "sequential_ms": {"default_shapes": round(statistics.median(seq_default_ms), 4),
+                          "tuned_shapes": round(statistics.median(seq_tuned_ms), 4)},
+        "speedup_vs_sequential": round(statistics.median(seq_default_ms) / value, 3),
+        "stage_ms": {k: round(v, 4) for k, v in stage.items()},
+        "e2e": {"value": round(e2e_ms, 4), "unit": "ms/batch", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": names[dom], "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                     "peak_source": peaks["source"], "algorithmic_bytes": int(stage_bytes[dom]),
+                     "kernel_ms": round(stage[dom], 4)},
+        "clocks": clk.summary(),
+        "scene_list": [[sc.ntri, sc.dim, list(sc.gbuffer_size), len(sc.lights)] for sc in scs],
+        "scene_gen_s": round(gen_s, 2),
+    }
+    b.close()
+    return result, scs
+
+
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each frame
 # stage, from one ncu --set full capture of the large frame (summarised under
 # profiles/); only meaningful for --config large.
@@ -406,7 +582,37 @@ def cpu_model() -> str:
     return platform.processor() or platform.machine()
 
 
+def run_reference_batch(args, world):
+    """Batched family on the CPU restatement: every scene of the batch per
+    step (full voxelize/normalize/inject/mips, row-sampled trace scaled to the
+    frame), all host threads."""
+    from vct_gb300 import scenes
+
+    nthreads = os.cpu_count() or 1
+    scs = [scenes.batch_scene(seed=args.seed, index=i) for i in range(args.batch_scenes)]
+    times = []
+    for i in range(args.warmup + args.steps):
+        ms = sum(cpu_frame_ms(sc, nthreads, args.cpu_sample_rows)[0] for sc in scs)
+        if i >= args.warmup:
+            times.append(ms)
+    value = sum(times) / len(times)
+    sample = (f"each step: all {len(scs)} scenes, full voxelize/normalize/inject/mips + trace of "
+              f"{args.cpu_sample_rows} evenly spaced rows per scene scaled to the full frame")
+    return {
+        "impl": "reference", "metric": BATCH_METRIC.replace("32", str(args.batch_scenes)), "value": round(value, 2),
+        "unit": "ms/batch", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(value, 2), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 math, f16 volumes, u32 accumulators", "data": "synthetic seeded scenes (no dataset)",
+        "config": {"workload": f"batched family: {args.batch_scenes} scenes", "seed": args.seed},
+        "cpu_baseline": {"value": round(value, 2), "unit": "ms/batch", "cores": nthreads, "kind": "port",
+                         "sample": sample, "cpu": cpu_model()},
+        "e2e": {"value": round(value, 2), "unit": "ms/batch", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 def run_reference(args, rank, world):
+    if args.config == "batch":
+        return run_reference_batch(args, world)
     sc = make_scene(args)
     nthreads = os.cpu_count() or 1
     import oracle as O
@@ -442,6 +648,20 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args, rank, world)), flush=True)
+        return
+    if args.config == "batch":
+        result, scs = run_batch(args, rank, world)
+        if rank == 0 and not args.no_cpu_baseline:
+            # one single-threaded oracle frame of the smallest scene of the batch, row-sampled trace,
+            # scaled by the batch's voxel + pixel work relative to that scene
+            small = min(scs, key=lambda s: s.dim ** 3 + s.gbuffer_size[0] * s.gbuffer_size[1])
+            ms, detail = cpu_frame_ms(small, 1, args.cpu_sample_rows)
+            result["cpu_baseline"] = {"value": round(ms, 2), "unit": "ms/frame of the smallest scene", "cores": 1,
+                                      "kind": "port", "sample": f"scene {small.name}: {small.ntri} tris, "
+                                      f"{small.dim}^3, {small.gbuffer_size[0]}x{small.gbuffer_size[1]}, trace of "
+                                      f"{detail['rows_traced']} rows scaled to the frame", "cpu": cpu_model()}
+        if rank == 0:
+            print(json.dumps(result), flush=True)
         return
     result, sc = run_ours(args, rank, world)
     if result is None:  # --profile-frames

@@ -104,7 +104,7 @@ typedef struct vct_cone_settings {
     float lod_offset;
 } vct_cone_settings;
 
-#define VCT_FILTER_SOFTWARE 0 /* fp32 trilinear from the linear volume (exact GL semantics) */
+#define VCT_FILTER_SOFTWARE 0 /* fp32 trilinear (exact GL semantics) from a bordered fp32 copy of the chain */
 #define VCT_FILTER_HARDWARE 1 /* texture units' trilinear-mip filtering */
 #define VCT_FILTER_HARDWARE_LEVELS 2 /* texture units' trilinear filtering per level, levels blended in fp32 */
 
@@ -205,6 +205,9 @@ const char* vct_last_error(void);
 void vct_struct_sizes(int64_t* light, int64_t* config, int64_t* params,
                       int64_t* triangles, int64_t* gbuffer, int64_t* trace_out,
                       int64_t* shadow_desc, int64_t* stats);
+/* sizeof of a public struct by name ("vct_tuning"), or offsetof of one of its
+ * fields ("vct_scene_desc.eye"); -1 for an unknown name. */
+int64_t vct_struct_layout(const char* name);
 /* Reference defaults (src/Application.h:36-103). */
 void vct_default_params(vct_params* out);
 /* The three per-axis voxelisation matrices of src/Application.cpp:689-692. */
@@ -297,8 +300,43 @@ vct_status vct_batch_frame(vct_batch* batch, const vct_scene_desc* scenes, int32
  * (the descriptors are copied: replays run the captured scenes). */
 vct_status vct_batch_capture(vct_batch* batch, const vct_scene_desc* scenes, int32_t n_scenes, void* stream);
 vct_status vct_batch_replay(vct_batch* batch, void* stream);
-/* The context of one scene (volumes, stats, timers) for reading. */
+/* The context of one scene (volumes, stats) for reading. */
 vct_status vct_batch_context(vct_batch* batch, int32_t scene, vct_ctx** ctx);
+/* CUDA-event stage timers of vct_batch_frame (not of graph replays):
+ * voxelize_ms (all scenes' voxelisation), mipmap_ms (injection, resolve and
+ * mip chains), render_ms (cone tracing), total_ms; radiance_ms is 0. */
+vct_status vct_batch_enable_timers(vct_batch* batch, int32_t enable);
+vct_status vct_batch_get_timers(vct_batch* batch, vct_timers* out);
+
+/* ---- launch shapes and the autotuner ----------------------------------- */
+/* No counterpart in the reference (its launch shapes are fixed by the GL
+ * pipeline and the compute shaders' local sizes).  Every setting gives
+ * bit-identical results; only speed differs. */
+typedef struct vct_tuning {
+    int32_t voxel_unit_pixels;   /* bounding-box pixels per voxeliser work unit: power of two in [32, 8192] (512) */
+    int32_t voxel_blocks_per_sm; /* resident voxeliser raster CTAs per SM: 1..3 (3) */
+    int32_t trace_tile_w;        /* pixel tile of one 256-thread trace CTA, tile_w * tile_h = 256: */
+    int32_t trace_tile_h;        /*   tile_w a power of two in [4, 64] (16 x 16) */
+    int32_t trace_warp_w;        /* pixel tile of one warp: warp_w x 32/warp_w, warp_w a power of two with */
+                                 /*   tile_w/8 <= warp_w <= min(tile_w, 32) (8) */
+} vct_tuning;
+
+void vct_default_tuning(vct_tuning* out);
+vct_status vct_get_tuning(const vct_ctx* ctx, vct_tuning* out);
+vct_status vct_set_tuning(vct_ctx* ctx, const vct_tuning* tuning);
+vct_status vct_batch_get_tuning(const vct_batch* batch, vct_tuning* out);
+vct_status vct_batch_set_tuning(vct_batch* batch, const vct_tuning* tuning);
+/* Times vct_frame under each candidate voxeliser setting and each candidate
+ * trace tile shape (`reps` frames each, median of the stage's CUDA-event
+ * time; the two stages are tuned independently), keeps the fastest as the
+ * context's tuning and returns it in `best` (may be NULL).  Synchronises
+ * `stream`; the frame's outputs are written as by vct_frame. */
+vct_status vct_autotune(vct_ctx* ctx, const vct_triangles* tris, const vct_light* lights, int32_t n_lights,
+                        const vct_shadow_desc* shadow, const float eye[3], const vct_gbuffer* gbuffer,
+                        const vct_trace_out* out, int32_t reps, void* stream, vct_tuning* best);
+/* The same for a batch, timing vct_batch_frame; drops a captured graph. */
+vct_status vct_batch_autotune(vct_batch* batch, const vct_scene_desc* scenes, int32_t n_scenes, int32_t reps,
+                              void* stream, vct_tuning* best);
 
 /* ---- voxelisation without allocation ---------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -122,3 +122,19 @@ def test_static_entry_point_rejects_before_device_work():
                                  None, None)
     # the shadow caster needs a shadow description: rejected first
     assert rc == L.VCT_ERR_INVALID_ARGUMENT
+
+
+def test_default_tuning_and_scene_desc_layout():
+    t = L.vct_tuning()
+    L.load().vct_default_tuning(C.byref(t))
+    assert api.tuning_dict(t) == dict(voxel_unit_pixels=512, voxel_blocks_per_sm=3, trace_tile_w=16, trace_tile_h=16,
+                                      trace_warp_w=8)
+    lib = L.load()
+    for cls in (L.vct_light, L.vct_config, L.vct_cone_settings, L.vct_params, L.vct_triangles, L.vct_gbuffer,
+                L.vct_trace_out, L.vct_shadow_desc, L.vct_stats, L.vct_timers, L.vct_tuning, L.vct_scene_desc):
+        assert lib.vct_struct_layout(cls.__name__.encode()) == C.sizeof(cls), cls.__name__
+    for f in ("lights", "n_lights", "shadow", "eye", "gbuffer", "out"):
+        assert lib.vct_struct_layout(f"vct_scene_desc.{f}".encode()) == getattr(L.vct_scene_desc, f).offset, f
+    assert lib.vct_struct_layout(b"vct_params.trace_filter") == L.vct_params.trace_filter.offset
+    assert lib.vct_struct_layout(b"vct_tuning.trace_warp_w") == L.vct_tuning.trace_warp_w.offset
+    assert lib.vct_struct_layout(b"no_such_struct") == -1

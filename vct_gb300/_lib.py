@@ -103,6 +103,11 @@ class vct_stats(C.Structure):
                 ("max_fragments_per_voxel", C.c_uint32), ("error_flags", C.c_uint32)]
 
 
+class vct_tuning(C.Structure):
+    _fields_ = [("voxel_unit_pixels", C.c_int32), ("voxel_blocks_per_sm", C.c_int32), ("trace_tile_w", C.c_int32),
+                ("trace_tile_h", C.c_int32), ("trace_warp_w", C.c_int32)]
+
+
 class vct_scene_desc(C.Structure):
     _fields_ = [("triangles", vct_triangles), ("lights", C.POINTER(vct_light)), ("n_lights", C.c_int32),
                 ("shadow", vct_shadow_desc), ("eye", C.c_float * 3), ("gbuffer", vct_gbuffer),
@@ -119,6 +124,7 @@ SIGNATURES = {
     "vct_status_string": (C.c_char_p, [st]),
     "vct_last_error": (C.c_char_p, []),
     "vct_struct_sizes": (None, [P(C.c_int64)] * 8),
+    "vct_struct_layout": (C.c_int64, [C.c_char_p]),
     "vct_default_params": (None, [P(vct_params)]),
     "vct_voxel_mvp": (st, [P(vct_config), P(C.c_float)]),
     "vct_create": (st, [P(vct_config), P(vp)]),
@@ -154,6 +160,16 @@ SIGNATURES = {
     "vct_batch_capture": (st, [vp, P(vct_scene_desc), C.c_int32, vp]),
     "vct_batch_replay": (st, [vp, vp]),
     "vct_batch_context": (st, [vp, C.c_int32, P(vp)]),
+    "vct_batch_enable_timers": (st, [vp, C.c_int32]),
+    "vct_batch_get_timers": (st, [vp, P(vct_timers)]),
+    "vct_default_tuning": (None, [P(vct_tuning)]),
+    "vct_get_tuning": (st, [vp, P(vct_tuning)]),
+    "vct_set_tuning": (st, [vp, P(vct_tuning)]),
+    "vct_batch_get_tuning": (st, [vp, P(vct_tuning)]),
+    "vct_batch_set_tuning": (st, [vp, P(vct_tuning)]),
+    "vct_autotune": (st, [vp, P(vct_triangles), P(vct_light), C.c_int32, P(vct_shadow_desc), P(C.c_float),
+                          P(vct_gbuffer), P(vct_trace_out), C.c_int32, vp, P(vct_tuning)]),
+    "vct_batch_autotune": (st, [vp, P(vct_scene_desc), C.c_int32, C.c_int32, vp, P(vct_tuning)]),
 }
 
 _lib = None

@@ -198,6 +198,21 @@ class Context:
     def enable_timers(self, on: bool = True):
         L.check(self._lib.vct_enable_timers(self.handle, int(on)), "vct_enable_timers")
 
+    def tuning(self) -> L.vct_tuning:
+        t = L.vct_tuning()
+        L.check(self._lib.vct_get_tuning(self.handle, C.byref(t)), "vct_get_tuning")
+        return t
+
+    def set_tuning(self, t: L.vct_tuning):
+        L.check(self._lib.vct_set_tuning(self.handle, C.byref(t)), "vct_set_tuning")
+
+    def autotune(self, tris, lights, shadow, eye, gb, out, reps: int = 3, stream=None) -> L.vct_tuning:
+        arr, n = lights
+        t = L.vct_tuning()
+        L.check(self._lib.vct_autotune(self.handle, C.byref(tris), arr, n, C.byref(shadow), f3(eye), C.byref(gb),
+                                       C.byref(out), reps, _stream(stream), C.byref(t)), "vct_autotune")
+        return t
+
     def timers(self) -> dict:
         t = L.vct_timers()
         L.check(self._lib.vct_get_timers(self.handle, C.byref(t)), "vct_get_timers")
@@ -289,6 +304,41 @@ class Batch:
 
     def replay(self, stream=None):
         L.check(self._lib.vct_batch_replay(self.handle, _stream(stream)), "vct_batch_replay")
+
+    def enable_timers(self, on: bool = True):
+        L.check(self._lib.vct_batch_enable_timers(self.handle, int(on)), "vct_batch_enable_timers")
+
+    def timers(self) -> dict:
+        t = L.vct_timers()
+        L.check(self._lib.vct_batch_get_timers(self.handle, C.byref(t)), "vct_batch_get_timers")
+        return {k: getattr(t, k) for k, _ in L.vct_timers._fields_}
+
+    def tuning(self) -> L.vct_tuning:
+        t = L.vct_tuning()
+        L.check(self._lib.vct_batch_get_tuning(self.handle, C.byref(t)), "vct_batch_get_tuning")
+        return t
+
+    def set_tuning(self, t: L.vct_tuning):
+        L.check(self._lib.vct_batch_set_tuning(self.handle, C.byref(t)), "vct_batch_set_tuning")
+
+    def autotune(self, descs, reps: int = 3, stream=None) -> L.vct_tuning:
+        arr, n = self._descs(descs)
+        t = L.vct_tuning()
+        L.check(self._lib.vct_batch_autotune(self.handle, arr, n, reps, _stream(stream), C.byref(t)),
+                "vct_batch_autotune")
+        return t
+
+
+def tuning_dict(t: L.vct_tuning) -> dict:
+    return {k: int(getattr(t, k)) for k, _ in L.vct_tuning._fields_}
+
+
+def tuning_from(d: dict) -> L.vct_tuning:
+    t = L.vct_tuning()
+    L.load().vct_default_tuning(C.byref(t))
+    for k, v in d.items():
+        setattr(t, k, int(v))
+    return t
 
 
 class _CudaArray:

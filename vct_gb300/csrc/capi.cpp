@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <new>
 #include <string>
@@ -42,6 +43,7 @@ struct vct_ctx {
     long long vox_scratch_bytes = 0;
     float4* pchain = nullptr;  // bordered fp32 radiance chain read by the software sampler
     bool pad_ready = false;   // pchain holds the current radiance chain
+    vct_tuning tuning;        // launch shapes (vct_set_tuning / vct_autotune)
 };
 
 namespace vct {
@@ -271,6 +273,8 @@ void fill_accum_inputs(const vct_config& cfg, const vct_params& prm, const float
     P.lighting = prm.voxelize_lighting;
     P.axis_override = prm.axis_override;
     P.nlights = n;
+    P.unit_log2 = 9;
+    P.blocks_per_sm = 3;
     for (int i = 0; i < n; ++i) {
         LightDev& L = P.lights[i];
         L.position = to_f3(lights[i].position);
@@ -300,9 +304,43 @@ void fill_accum_inputs(const vct_config& cfg, const vct_params& prm, const float
 
 namespace {
 
+void default_tuning(vct_tuning& t) {
+    t.voxel_unit_pixels = 512;
+    t.voxel_blocks_per_sm = 3;
+    t.trace_tile_w = 16;
+    t.trace_tile_h = 16;
+    t.trace_warp_w = 8;
+}
+
+vct_status validate_tuning(const vct_tuning* t) {
+    if (!t) return fail(VCT_ERR_INVALID_ARGUMENT, "tuning is NULL");
+    if (!is_pow2(t->voxel_unit_pixels) || t->voxel_unit_pixels < 32 || t->voxel_unit_pixels > 8192)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "voxel_unit_pixels must be a power of two in [32, 8192]");
+    if (t->voxel_blocks_per_sm < 1 || t->voxel_blocks_per_sm > 3)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "voxel_blocks_per_sm must be in [1, 3]");
+    const int tw = t->trace_tile_w, th = t->trace_tile_h, ww = t->trace_warp_w;
+    if (!is_pow2(tw) || tw < 4 || tw > 64 || tw * th != 256)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "trace tile must be tile_w x tile_h = 256 with tile_w in [4, 64]");
+    if (!is_pow2(ww) || ww * 8 < tw || ww > tw || ww > 32)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "trace_warp_w must be a power of two in [tile_w/8, min(tile_w, 32)]");
+    return VCT_OK;
+}
+
+void apply_tuning(const vct_tuning& t, AccumParams& P) {
+    P.unit_log2 = ilog2(t.voxel_unit_pixels);
+    P.blocks_per_sm = t.voxel_blocks_per_sm;
+}
+
+void apply_tuning(const vct_tuning& t, TraceParams& P) {
+    P.tile_w_log2 = ilog2(t.trace_tile_w);
+    P.tile_h_log2 = ilog2(t.trace_tile_h);
+    P.warp_w_log2 = ilog2(t.trace_warp_w);
+}
+
 vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lights, int n,
                       const vct_shadow_desc* sh, AccumParams& P) {
     fill_accum_inputs(ctx->cfg, ctx->params, ctx->mvp, t, lights, n, sh, P);
+    apply_tuning(ctx->tuning, P);
     P.acc = ctx->acc;
     P.occ = ctx->occ;
     P.stats = ctx->stats;
@@ -468,6 +506,7 @@ vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], co
     P.ref_tbn_quirk = pr.ref_tbn_quirk;
     P.filter = pr.trace_filter;
     P.tex = ctx->tex;
+    apply_tuning(ctx->tuning, P);
     for (auto p : {(const void*)g->position_dev, (const void*)g->normal_dev, (const void*)g->albedo_dev,
                    (const void*)out->irradiance_dev, (const void*)out->specular_dev, (const void*)out->color_dev})
         if (reinterpret_cast<uintptr_t>(p) % 16 != 0) return fail(VCT_ERR_INVALID_ARGUMENT, "float4 planes must be 16-byte aligned");
@@ -507,6 +546,29 @@ void vct_struct_sizes(int64_t* light, int64_t* config, int64_t* params, int64_t*
     if (trace_out) *trace_out = sizeof(vct_trace_out);
     if (shadow_desc) *shadow_desc = sizeof(vct_shadow_desc);
     if (stats) *stats = sizeof(vct_stats);
+}
+
+int64_t vct_struct_layout(const char* name) {
+    if (!name) return -1;
+    struct Entry {
+        const char* name;
+        size_t value;
+    };
+#define VCT_SZ(T) {#T, sizeof(T)}
+#define VCT_OFF(T, f) {#T "." #f, offsetof(T, f)}
+    static const Entry table[] = {
+        VCT_SZ(vct_light),  VCT_SZ(vct_config),         VCT_SZ(vct_cone_settings),  VCT_SZ(vct_params),
+        VCT_SZ(vct_triangles), VCT_SZ(vct_gbuffer),     VCT_SZ(vct_trace_out),      VCT_SZ(vct_shadow_desc),
+        VCT_SZ(vct_stats),  VCT_SZ(vct_timers),         VCT_SZ(vct_tuning),         VCT_SZ(vct_scene_desc),
+        VCT_OFF(vct_scene_desc, lights), VCT_OFF(vct_scene_desc, n_lights), VCT_OFF(vct_scene_desc, shadow),
+        VCT_OFF(vct_scene_desc, eye),    VCT_OFF(vct_scene_desc, gbuffer),  VCT_OFF(vct_scene_desc, out),
+        VCT_OFF(vct_params, trace_filter), VCT_OFF(vct_tuning, trace_warp_w),
+    };
+#undef VCT_SZ
+#undef VCT_OFF
+    for (const Entry& e : table)
+        if (std::strcmp(e.name, name) == 0) return (int64_t)e.value;
+    return -1;
 }
 
 void vct_default_params(vct_params* p) {
@@ -560,6 +622,7 @@ vct_status vct_create(const vct_config* cfg, vct_ctx** out) {
     c->dim = cfg->voxel_dim;
     int maxl = ilog2(c->dim) + 1;
     c->levels = cfg->voxel_levels == 0 ? maxl : std::min(std::max(cfg->voxel_levels, 1), maxl);
+    default_tuning(c->tuning);
     c->color_levels = (cfg->flags & VCT_CONFIG_COLOR_MIPS) ? c->levels : 1;
     c->device = cfg->device;
     c->nv = (long long)c->dim * c->dim * c->dim;
@@ -981,6 +1044,10 @@ struct vct_batch {
     long long work_bytes = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    vct_tuning tuning;
+    cudaEvent_t ev[4] = {};  // voxeliser start/end, trace start/end (timers, autotuner)
+    bool timers_on = false, timers_recorded = false;
+    int graph_launches = 0;  // kernels in the captured graph
 };
 
 namespace {
@@ -1016,6 +1083,7 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         const bool hw = filter != VCT_FILTER_SOFTWARE;
         AccumParams A;
         fill_accum_inputs(c->cfg, c->params, c->mvp, &d.triangles, d.lights, d.n_lights, &d.shadow, A);
+        apply_tuning(b->tuning, A);
         A.acc = c->acc;
         A.occ = c->occ;
         A.stats = c->stats;
@@ -1045,6 +1113,7 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         M.first = std::min(4, c->levels - 1);
         TraceParams T;
         if ((s = fill_trace(c, &d.gbuffer, d.eye, &d.out, T)) != VCT_OK) return s;
+        apply_tuning(b->tuning, T);
         std::memcpy(h + b->off_accum + i * sizeof(AccumParams), &A, sizeof A);
         std::memcpy(h + b->off_inject + i * sizeof(InjectParams), &I, sizeof I);
         std::memcpy(h + b->off_resolve + i * sizeof(ResolveParams), &R, sizeof R);
@@ -1058,7 +1127,7 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         tot.texels += (long long)I.nx * I.ny;
         const long long bpa = c->dim / 16;
         tot.bricks += bpa * bpa * bpa;
-        tot.tiles += trace_tiles(d.gbuffer.width, d.gbuffer.height);
+        tot.tiles += trace_tiles(d.gbuffer.width, d.gbuffer.height, T.tile_w_log2, T.tile_h_log2);
     }
     tri_off[n] = tot.tris;
     tex_off[n] = tot.texels;
@@ -1068,6 +1137,11 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
     const long long need = accumulate_scratch_bytes(std::max(tot.tris, 1LL));
     if (need > b->work_bytes) {
         if (!allow_alloc) return fail(VCT_ERR_STATE, "batch work arrays too small for the captured scenes");
+        // A captured graph points at the old arrays: it goes with them.
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
         if (b->work) cudaFree(b->work);
         b->work = nullptr;
         b->work_bytes = 0;
@@ -1082,7 +1156,7 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
 }
 
 // Enqueues one batched frame; `h` holds the staged blob.
-vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cudaStream_t st) {
+vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cudaStream_t st, bool timed = false) {
     const int n = b->n;
     VCT_CUDA(cudaMemcpyAsync(b->d_blob, h, b->blob_bytes, cudaMemcpyHostToDevice, st));
     for (vct_ctx* c : b->ctx) {
@@ -1093,13 +1167,16 @@ vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cu
     AccumParams W0;
     W0.ntri = tot.tris;
     accumulate_bind_scratch(W0, b->work);
-    const VoxWork W = {W0.tri_rec, W0.tri_units, W0.tri_scan, W0.block_off, tot.tris};
+    const VoxWork W = {W0.tri_rec, W0.tri_units, W0.tri_scan, W0.block_off, tot.tris,
+                       ilog2(b->tuning.voxel_unit_pixels)};
+    if (timed) VCT_CUDA(cudaEventRecord(b->ev[0], st));
     if (tot.tris > 0) {
         launch_accumulate_batch(
             SceneBatch<AccumParams>{reinterpret_cast<const AccumParams*>(b->d_blob + b->off_accum), d_tables, n}, W,
-            b->num_sms, st);
+            b->num_sms, b->tuning.voxel_blocks_per_sm, st);
         VCT_CHECK_LAUNCH("batch: accumulate");
     }
+    if (timed) VCT_CUDA(cudaEventRecord(b->ev[1], st));
     launch_inject_mark_batch(
         SceneBatch<InjectParams>{reinterpret_cast<const InjectParams*>(b->d_blob + b->off_inject), d_tables + (n + 1), n},
         tot.texels, st);
@@ -1112,10 +1189,12 @@ vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cu
     launch_mip_tail_batch(SceneBatch<MipLevels>{reinterpret_cast<const MipLevels*>(b->d_blob + b->off_mips), nullptr, n},
                           st);
     VCT_CHECK_LAUNCH("batch: coarse mips");
+    if (timed) VCT_CUDA(cudaEventRecord(b->ev[2], st));
     launch_trace_batch(SceneBatch<TraceParams>{reinterpret_cast<const TraceParams*>(b->d_blob + b->off_trace),
                                               d_tables + 3 * (n + 1), n},
                        b->ctx[0]->params.trace_filter, tot.tiles, st);
     VCT_CHECK_LAUNCH("batch: trace");
+    if (timed) VCT_CUDA(cudaEventRecord(b->ev[3], st));
     const bool hw = b->ctx[0]->params.trace_filter != VCT_FILTER_SOFTWARE;
     for (vct_ctx* c : b->ctx) {
         c->stats_reset_pending = true;
@@ -1145,6 +1224,7 @@ vct_status vct_batch_create(const vct_config* configs, int32_t n, vct_batch** ou
     if (!b) return fail(VCT_ERR_OUT_OF_MEMORY, "host allocation failed");
     b->n = n;
     b->device = configs[0].device;
+    default_tuning(b->tuning);
     for (int i = 0; i < n; ++i) {
         vct_ctx* c = nullptr;
         vct_status s = vct_create(&configs[i], &c);
@@ -1190,6 +1270,8 @@ vct_status vct_batch_destroy(vct_batch* b) {
     DeviceScope ds(b->device);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
+    for (cudaEvent_t e : b->ev)
+        if (e) cudaEventDestroy(e);
     for (vct_ctx* c : b->ctx) vct_destroy(c);
     if (b->d_blob) cudaFree(b->d_blob);
     if (b->h_blob) cudaFreeHost(b->h_blob);
@@ -1220,7 +1302,34 @@ vct_status vct_batch_frame(vct_batch* b, const vct_scene_desc* scenes, int32_t n
     BatchTotals tot;
     vct_status s = batch_stage(b, scenes, n, b->h_blob, tot, true);
     if (s != VCT_OK) return s;
-    return batch_enqueue(b, b->h_blob, tot, st);
+    if ((s = batch_enqueue(b, b->h_blob, tot, st, b->timers_on)) != VCT_OK) return s;
+    b->timers_recorded = b->timers_on;
+    return VCT_OK;
+}
+
+vct_status vct_batch_enable_timers(vct_batch* b, int32_t enable) {
+    if (!b) return fail(VCT_ERR_INVALID_ARGUMENT, "batch is NULL");
+    DeviceScope ds(b->device);
+    VCT_CUDA(ds.err);
+    if (enable && !b->ev[0])
+        for (auto& e : b->ev) VCT_CUDA(cudaEventCreate(&e));
+    b->timers_on = enable != 0;
+    b->timers_recorded = false;
+    return VCT_OK;
+}
+
+vct_status vct_batch_get_timers(vct_batch* b, vct_timers* out) {
+    if (!b || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!b->timers_recorded) return fail(VCT_ERR_STATE, "no timed vct_batch_frame since timers were enabled");
+    DeviceScope ds(b->device);
+    VCT_CUDA(ds.err);
+    VCT_CUDA(cudaEventSynchronize(b->ev[3]));
+    VCT_CUDA(cudaEventElapsedTime(&out->voxelize_ms, b->ev[0], b->ev[1]));
+    VCT_CUDA(cudaEventElapsedTime(&out->mipmap_ms, b->ev[1], b->ev[2]));
+    VCT_CUDA(cudaEventElapsedTime(&out->render_ms, b->ev[2], b->ev[3]));
+    VCT_CUDA(cudaEventElapsedTime(&out->total_ms, b->ev[0], b->ev[3]));
+    out->radiance_ms = 0.0f;
+    return VCT_OK;
 }
 
 vct_status vct_batch_capture(vct_batch* b, const vct_scene_desc* scenes, int32_t n, void* stream) {
@@ -1242,7 +1351,9 @@ vct_status vct_batch_capture(vct_batch* b, const vct_scene_desc* scenes, int32_t
         b->graph = nullptr;
     }
     VCT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const unsigned long long launches0 = g_launches.load();
     s = batch_enqueue(b, b->h_graph_blob, tot, st);
+    b->graph_launches = (int)(g_launches.load() - launches0);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (s != VCT_OK) {
@@ -1261,7 +1372,7 @@ vct_status vct_batch_replay(vct_batch* b, void* stream) {
     DeviceScope ds(b->device);
     VCT_CUDA(ds.err);
     VCT_CUDA(cudaGraphLaunch(b->exec, as_stream(stream)));
-    note_launches(0);
+    note_launches(b->graph_launches);
     return VCT_OK;
 }
 
@@ -1270,6 +1381,201 @@ vct_status vct_batch_context(vct_batch* b, int32_t scene, vct_ctx** ctx) {
     if (scene < 0 || scene >= b->n) return fail(VCT_ERR_INVALID_ARGUMENT, "scene index out of range");
     *ctx = b->ctx[scene];
     return VCT_OK;
+}
+
+
+}  // extern "C"
+
+// ==================================================================== tuning
+namespace {
+
+// Candidate settings of the autotuner.  Voxeliser: work-unit size (smaller
+// units balance scenes of few large triangles, larger ones cut per-unit
+// overhead) x raster CTAs per SM.  Trace: CTA tile and warp sub-tile shapes
+// (the warp's footprint decides how coherent its 32 cones' texel fetches are).
+const int kUnitCand[] = {128, 256, 512, 1024, 2048};
+const int kBpsCand[] = {2, 3};
+const int kTileCand[][3] = {{16, 16, 8}, {16, 16, 4}, {16, 16, 16}, {32, 8, 8}, {32, 8, 4},  {32, 8, 16},
+                            {8, 32, 4},  {8, 32, 8},  {64, 4, 8},   {64, 4, 16}, {64, 4, 32}, {4, 64, 4}};
+
+float median(std::vector<float> v) {
+    std::sort(v.begin(), v.end());
+    return v.empty() ? 0.0f : v[v.size() / 2];
+}
+
+// Runs one timed frame and returns (voxeliser ms, trace ms).
+using TimedFrame = vct_status (*)(void* obj, const void* args, float* vox_ms, float* trace_ms);
+
+vct_status tune(vct_tuning& cur, int reps, void* obj, const void* args, TimedFrame run, vct_tuning* set_into) {
+    reps = std::max(1, std::min(reps, 64));
+    std::vector<float> vox, trc;
+    float v = 0, t = 0;
+    // Voxeliser settings.
+    vct_tuning best = cur;
+    float best_ms = 3.0e38f;
+    for (int u : kUnitCand)
+        for (int bps : kBpsCand) {
+            vct_tuning c = best;
+            c.voxel_unit_pixels = u;
+            c.voxel_blocks_per_sm = bps;
+            *set_into = c;
+            vct_status s = run(obj, args, &v, &t);  // warm-up
+            if (s != VCT_OK) return s;
+            vox.clear();
+            for (int r = 0; r < reps; ++r) {
+                if ((s = run(obj, args, &v, &t)) != VCT_OK) return s;
+                vox.push_back(v);
+            }
+            const float m = median(vox);
+            if (m < best_ms) {
+                best_ms = m;
+                best.voxel_unit_pixels = u;
+                best.voxel_blocks_per_sm = bps;
+            }
+        }
+    // Trace tile shapes.
+    best_ms = 3.0e38f;
+    vct_tuning best2 = best;
+    for (const auto& tc : kTileCand) {
+        vct_tuning c = best;
+        c.trace_tile_w = tc[0];
+        c.trace_tile_h = tc[1];
+        c.trace_warp_w = tc[2];
+        *set_into = c;
+        vct_status s = run(obj, args, &v, &t);
+        if (s != VCT_OK) return s;
+        trc.clear();
+        for (int r = 0; r < reps; ++r) {
+            if ((s = run(obj, args, &v, &t)) != VCT_OK) return s;
+            trc.push_back(t);
+        }
+        const float m = median(trc);
+        if (m < best_ms) {
+            best_ms = m;
+            best2 = c;
+        }
+    }
+    cur = best2;
+    *set_into = best2;
+    return VCT_OK;
+}
+
+struct CtxFrameArgs {
+    const vct_triangles* tris;
+    const vct_light* lights;
+    int32_t n;
+    const vct_shadow_desc* shadow;
+    const float* eye;
+    const vct_gbuffer* g;
+    const vct_trace_out* out;
+    void* stream;
+};
+
+vct_status ctx_timed_frame(void* obj, const void* a, float* vox_ms, float* trace_ms) {
+    vct_ctx* c = static_cast<vct_ctx*>(obj);
+    const CtxFrameArgs& f = *static_cast<const CtxFrameArgs*>(a);
+    vct_status s = vct_frame(c, f.tris, f.lights, f.n, f.shadow, f.eye, f.g, f.out, f.stream);
+    if (s != VCT_OK) return s;
+    vct_timers t;
+    if ((s = vct_get_timers(c, &t)) != VCT_OK) return s;
+    *vox_ms = t.voxelize_ms;
+    *trace_ms = t.render_ms;
+    return VCT_OK;
+}
+
+struct BatchFrameArgs {
+    const vct_scene_desc* scenes;
+    int32_t n;
+    void* stream;
+};
+
+vct_status batch_timed_frame(void* obj, const void* a, float* vox_ms, float* trace_ms) {
+    vct_batch* b = static_cast<vct_batch*>(obj);
+    const BatchFrameArgs& f = *static_cast<const BatchFrameArgs*>(a);
+    cudaStream_t st = as_stream(f.stream);
+    VCT_CUDA(cudaStreamSynchronize(st));
+    BatchTotals tot;
+    vct_status s = batch_stage(b, f.scenes, f.n, b->h_blob, tot, true);
+    if (s != VCT_OK) return s;
+    if ((s = batch_enqueue(b, b->h_blob, tot, st, true)) != VCT_OK) return s;
+    VCT_CUDA(cudaEventSynchronize(b->ev[3]));
+    VCT_CUDA(cudaEventElapsedTime(vox_ms, b->ev[0], b->ev[1]));
+    VCT_CUDA(cudaEventElapsedTime(trace_ms, b->ev[2], b->ev[3]));
+    return VCT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void vct_default_tuning(vct_tuning* out) {
+    if (out) default_tuning(*out);
+}
+
+vct_status vct_get_tuning(const vct_ctx* c, vct_tuning* out) {
+    if (!c || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = c->tuning;
+    return VCT_OK;
+}
+
+vct_status vct_set_tuning(vct_ctx* c, const vct_tuning* t) {
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    vct_status s = validate_tuning(t);
+    if (s != VCT_OK) return s;
+    c->tuning = *t;
+    return VCT_OK;
+}
+
+vct_status vct_batch_get_tuning(const vct_batch* b, vct_tuning* out) {
+    if (!b || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = b->tuning;
+    return VCT_OK;
+}
+
+vct_status vct_batch_set_tuning(vct_batch* b, const vct_tuning* t) {
+    if (!b) return fail(VCT_ERR_INVALID_ARGUMENT, "batch is NULL");
+    vct_status s = validate_tuning(t);
+    if (s != VCT_OK) return s;
+    b->tuning = *t;
+    return VCT_OK;
+}
+
+vct_status vct_autotune(vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n_lights,
+                        const vct_shadow_desc* shadow, const float eye[3], const vct_gbuffer* g,
+                        const vct_trace_out* out, int32_t reps, void* stream, vct_tuning* best) {
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    const bool timers_were_on = c->timers_on;
+    vct_status s = vct_enable_timers(c, 1);
+    if (s != VCT_OK) return s;
+    const CtxFrameArgs args = {tris, lights, n_lights, shadow, eye, g, out, stream};
+    const vct_tuning orig = c->tuning;
+    vct_tuning cur = orig;
+    s = tune(cur, reps, c, &args, ctx_timed_frame, &c->tuning);
+    c->tuning = s == VCT_OK ? cur : orig;
+    vct_enable_timers(c, timers_were_on ? 1 : 0);
+    if (s == VCT_OK && best) *best = c->tuning;
+    return s;
+}
+
+vct_status vct_batch_autotune(vct_batch* b, const vct_scene_desc* scenes, int32_t n, int32_t reps, void* stream,
+                              vct_tuning* best) {
+    if (!b) return fail(VCT_ERR_INVALID_ARGUMENT, "batch is NULL");
+    DeviceScope ds(b->device);
+    VCT_CUDA(ds.err);
+    if (!b->ev[0])
+        for (auto& e : b->ev) VCT_CUDA(cudaEventCreate(&e));
+    b->timers_recorded = false;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    const BatchFrameArgs args = {scenes, n, stream};
+    const vct_tuning orig = b->tuning;
+    vct_tuning cur = orig;
+    vct_status s = tune(cur, reps, b, &args, batch_timed_frame, &b->tuning);
+    b->tuning = s == VCT_OK ? cur : orig;
+    if (s == VCT_OK && best) *best = cur;
+    return s;
 }
 
 }  // extern "C"

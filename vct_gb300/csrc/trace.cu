@@ -145,14 +145,18 @@ __device__ __forceinline__ float4 trace_cone(const TraceParams& P, const int* of
 
 template <int MODE, class Scenes>
 __global__ void __launch_bounds__(256) trace_kernel(const Scenes S) {
-    // One CTA per 16x16 tile, tiles of every scene of the launch in a row.
+    // One CTA per tile of 2^tile_w_log2 x 2^tile_h_log2 = 256 pixels (a
+    // tuning setting; tiles of every scene of the launch in a row), one warp
+    // per 2^warp_w_log2 x 32/2^warp_w_log2 sub-tile.
     long long tile;
     const TraceParams& P = S.get(S.find(blockIdx.x, tile));
-    const int tiles_x = (P.width + 15) / 16;
+    const int twl = P.tile_w_log2, thl = P.tile_h_log2, wwl = P.warp_w_log2;
+    const int tiles_x = (P.width + (1 << twl) - 1) >> twl;
     const int tx = (int)(tile % tiles_x), ty = (int)(tile / tiles_x);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int x = tx * 16 + (wid & 1) * 8 + (lane & 7);
-    const int y = ty * 16 + (wid >> 1) * 4 + (lane >> 3);
+    const int wxl = twl - wwl;  // log2 of warps per tile row
+    const int x = (tx << twl) + ((wid & ((1 << wxl) - 1)) << wwl) + (lane & ((1 << wwl) - 1));
+    const int y = (ty << thl) + ((wid >> wxl) << (5 - wwl)) + (lane >> wwl);
     // Offsets of the bordered levels (32-bit: the chain holds < 2^31 voxels).
     __shared__ int s_off[VCT_MAX_LEVELS];
     if (threadIdx.x < VCT_MAX_LEVELS)
@@ -236,10 +240,14 @@ void launch_trace_set(const Scenes& S, int filter, long long tiles, cudaStream_t
     note_launches(1);
 }
 
-long long trace_tiles(int width, int height) { return (long long)((width + 15) / 16) * ((height + 15) / 16); }
+long long trace_tiles(int width, int height, int tile_w_log2, int tile_h_log2) {
+    const long long tw = 1LL << tile_w_log2, th = 1LL << tile_h_log2;
+    return ((width + tw - 1) / tw) * ((height + th - 1) / th);
+}
 
 void launch_trace(const TraceParams& P, cudaStream_t s) {
-    launch_trace_set(OneScene<TraceParams>{P}, P.filter, trace_tiles(P.width, P.height), s);
+    launch_trace_set(OneScene<TraceParams>{P}, P.filter, trace_tiles(P.width, P.height, P.tile_w_log2, P.tile_h_log2),
+                     s);
 }
 
 void launch_trace_batch(const SceneBatch<TraceParams>& B, int filter, long long tiles, cudaStream_t s) {

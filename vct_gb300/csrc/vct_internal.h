@@ -66,6 +66,8 @@ struct AccumParams {
     uint32_t* occ;  // occupancy bit mask, one bit per voxel
     StatsDev* stats;
     int num_sms;
+    int unit_log2;      // log2 of the bounding-box pixels per work unit
+    int blocks_per_sm;  // raster CTAs per SM (1..3)
     // Work distribution scratch (sized for ntri; see voxelize.cu).
     uint4* tri_rec;          // 3 x uint4 per triangle
     uint32_t* tri_units;     // work units per triangle
@@ -93,6 +95,7 @@ struct VoxWork {
     uint32_t* tri_scan;
     uint32_t* block_off;
     long long ntri;
+    int unit_log2;
 };
 
 constexpr int kSetupThreads = 256;  // triangles per setup block
@@ -184,6 +187,9 @@ struct TraceParams {
     int ref_tbn_quirk;
     int filter;  // VCT_FILTER_*
     cudaTextureObject_t tex;
+    // Pixel tile of one 256-thread CTA (tile_w x tile_h) and of one warp
+    // (warp_w x 32/warp_w), as log2.
+    int tile_w_log2, tile_h_log2, warp_w_log2;
 };
 
 struct ShadowRasterParams {
@@ -237,11 +243,12 @@ void launch_fill_u32(uint32_t* p, uint32_t v, long long n, cudaStream_t s);
 
 // Batched frame stages: one launch covers the work of every scene.
 int accumulate_batch_max_scenes();
-void launch_accumulate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, int num_sms, cudaStream_t s);
+void launch_accumulate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, int num_sms, int blocks_per_sm,
+                             cudaStream_t s);
 void launch_inject_mark_batch(const SceneBatch<InjectParams>& B, long long ntexels, cudaStream_t s);
 void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks, cudaStream_t s);
 void launch_mip_tail_batch(const SceneBatch<MipLevels>& B, cudaStream_t s);
-long long trace_tiles(int width, int height);
+long long trace_tiles(int width, int height, int tile_w_log2, int tile_h_log2);
 void launch_trace_batch(const SceneBatch<TraceParams>& B, int filter, long long tiles, cudaStream_t s);
 // Copies every level of a linear chain into the interior of the bordered chain.
 void launch_pad_copy(const uint2* chain, float4* pchain, int dim, int levels, cudaStream_t s);

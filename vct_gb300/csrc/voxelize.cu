@@ -7,7 +7,8 @@
 //     part (dominant axis from the summed vertex normals, per-axis ortho
 //     projection, snapping to the 1/256 sub-pixel grid, bounding box) into a
 //     48-byte record, and the triangle's share of work: its bounding box in
-//     units of kUnit pixels, with a block-local exclusive scan;
+//     units of 2^unit_log2 pixels (a tuning setting), with a block-local
+//     exclusive scan;
 //  2. voxelize_scan_kernel, one CTA: exclusive scan of the per-block totals;
 //  3. voxelize_raster_kernel, persistent: every warp takes an equal
 //     contiguous range of work units, tests 32 pixel centres at a time for
@@ -28,8 +29,7 @@ namespace {
 
 constexpr int kWarps = 8;
 constexpr int kQueue = 64;
-constexpr int kUnit = 512;  // bounding-box pixels per work unit
-constexpr int kRasterBlocksPerSM = 3;
+constexpr int kRasterBlocksPerSM = 3;  // register budget: up to 3 raster CTAs per SM
 constexpr int kMaxBatchScenes = 256;  // scene id travels in 8 bits of a queue entry
 
 struct FragQueue {
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Sce
                                 (uint32_t)rt.px0 | ((uint32_t)rt.py0 << 11) | ((uint32_t)axis << 22) |
                                     ((uint32_t)rt.perm1 << 24) | (bias << 25),
                                 bw | (bh << 11));
-            units = (bw * bh + kUnit - 1) / kUnit;
+            units = (bw * bh + (1u << W.unit_log2) - 1) >> W.unit_log2;
         }
         W.tri_units[g] = units;
     }
@@ -305,8 +305,8 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
             const int px0 = (int)(r2.z & 0x7ffu), py0 = (int)((r2.z >> 11) & 0x7ffu);
             const int axis = (int)((r2.z >> 22) & 3u), perm1 = (int)((r2.z >> 24) & 1u), bias = (int)(r2.z >> 25);
             const int bw = (int)(r2.w & 0x7ffu), bh = (int)(r2.w >> 11);
-            const int p_begin = (int)(u - start) * kUnit;
-            const int p_end = min(p_begin + kUnit, bw * bh);
+            const int p_begin = (int)(u - start) << W.unit_log2;
+            const int p_end = min(p_begin + (1 << W.unit_log2), bw * bh);
             for (int c = p_begin; c < p_end; c += 32) {
                 const int idx = c + lane;
                 bool cov = false;
@@ -371,12 +371,13 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
 }
 
 template <class Scenes>
-void launch_voxelize(const Scenes& S, const VoxWork& W, int num_sms, cudaStream_t s) {
+void launch_voxelize(const Scenes& S, const VoxWork& W, int num_sms, int blocks_per_sm, cudaStream_t s) {
     if (W.ntri <= 0) return;
     const int nblocks = (int)((W.ntri + kSetupThreads - 1) / kSetupThreads);
     voxelize_setup_kernel<Scenes><<<nblocks, kSetupThreads, 0, s>>>(S, W);
     voxelize_scan_kernel<<<1, 1024, 0, s>>>(W.block_off, nblocks);
-    voxelize_raster_kernel<Scenes><<<num_sms * kRasterBlocksPerSM, kWarps * 32, 0, s>>>(S, W, nblocks);
+    const int bps = blocks_per_sm < 1 ? 1 : (blocks_per_sm > kRasterBlocksPerSM ? kRasterBlocksPerSM : blocks_per_sm);
+    voxelize_raster_kernel<Scenes><<<num_sms * bps, kWarps * 32, 0, s>>>(S, W, nblocks);
     note_launches(3);
 }
 
@@ -395,14 +396,15 @@ void accumulate_bind_scratch(AccumParams& P, void* scratch) {
 }
 
 void launch_accumulate(const AccumParams& P, cudaStream_t s) {
-    const VoxWork W = {P.tri_rec, P.tri_units, P.tri_scan, P.block_off, P.ntri};
-    launch_voxelize(OneScene<AccumParams>{P}, W, P.num_sms, s);
+    const VoxWork W = {P.tri_rec, P.tri_units, P.tri_scan, P.block_off, P.ntri, P.unit_log2};
+    launch_voxelize(OneScene<AccumParams>{P}, W, P.num_sms, P.blocks_per_sm, s);
 }
 
 int accumulate_batch_max_scenes() { return kMaxBatchScenes; }
 
-void launch_accumulate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, int num_sms, cudaStream_t s) {
-    launch_voxelize(ManyScenes<AccumParams>{B}, W, num_sms, s);
+void launch_accumulate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, int num_sms, int blocks_per_sm,
+                             cudaStream_t s) {
+    launch_voxelize(ManyScenes<AccumParams>{B}, W, num_sms, blocks_per_sm, s);
 }
 
 }  // namespace vct
