@@ -38,7 +38,7 @@ CUDA_SOURCES = [
     ("trace.cu", ["--fmad=false"]),
     ("static_scratch.cu", []),
 ]
-CXX_SOURCES = ["capi.cpp"]
+CXX_SOURCES = ["capi.cpp", "batch.cpp"]
 
 
 def nvcc_path() -> str:

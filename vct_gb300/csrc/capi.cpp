@@ -11,47 +11,19 @@
 #include <string>
 #include <vector>
 
-#include "vct_internal.h"
+#include "host.h"
 
 using namespace vct;
+using namespace vct::host;
 
-struct vct_ctx {
-    vct_config cfg;
-    vct_params params;
-    int dim = 0, levels = 0, color_levels = 1, device = 0, num_sms = 0;
-    long long nv = 0;
-    uint32_t* acc = nullptr;  // accumulator records (kAccWords uint32 per voxel)
-    uint32_t* occ = nullptr;  // occupancy bit mask
-    uint32_t* lit = nullptr;
-    uint2* color = nullptr;     // colour chain (color_levels levels)
-    uint2* normal = nullptr;    // one level
-    uint2* radiance = nullptr;  // radiance chain (levels levels)
-    long long level_off[VCT_MAX_LEVELS] = {};
-    StatsDev* stats = nullptr;
-    bool stats_reset_pending = true;
-    bool radiance_ready = false;  // level 0 written since the last accumulate
-    bool mips_ready = false;
-    float mvp[48];
-    cudaMipmappedArray_t tex_array = nullptr;
-    cudaTextureObject_t tex = 0;
-    cudaSurfaceObject_t surf[VCT_MAX_LEVELS] = {};
-    bool tex_ready = false;
-    bool timers_on = false;
-    bool timers_recorded = false;
-    cudaEvent_t ev[5] = {};
-    void* vox_scratch = nullptr;  // voxeliser work-distribution arrays
-    long long vox_scratch_bytes = 0;
-    float4* pchain = nullptr;  // bordered fp32 radiance chain read by the software sampler
-    bool pad_ready = false;   // pchain holds the current radiance chain
-    vct_tuning tuning;        // launch shapes (vct_set_tuning / vct_autotune)
-};
 
 namespace vct {
 static std::atomic<unsigned long long> g_launches{0};
 void note_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 }  // namespace vct
 
-namespace {
+namespace vct {
+namespace host {
 
 thread_local std::string g_err;
 
@@ -60,33 +32,6 @@ vct_status fail(vct_status s, const std::string& msg) {
     return s;
 }
 
-#define VCT_CUDA(expr)                                                                      \
-    do {                                                                                    \
-        cudaError_t e_ = (expr);                                                            \
-        if (e_ != cudaSuccess) return fail(VCT_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
-
-#define VCT_CHECK_LAUNCH(what)                                                               \
-    do {                                                                                     \
-        cudaError_t e_ = cudaGetLastError();                                                 \
-        if (e_ != cudaSuccess) return fail(VCT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
-
-// Makes the context's device current for the duration of a call and
-// restores the caller's device afterwards.
-struct DeviceScope {
-    int prev = -1;
-    cudaError_t err = cudaSuccess;
-    explicit DeviceScope(int dev) {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) err = cudaSetDevice(dev);
-    }
-    ~DeviceScope() {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
-
-inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // ----------------------------------------------------------- glm-style math
 struct hf3 {
@@ -243,7 +188,8 @@ uint2* level_ptr(uint2* chain, const vct_ctx* ctx, int l) { return chain + ctx->
 
 f3 to_f3(const float* p) { return {p[0], p[1], p[2]}; }
 
-}  // namespace
+}  // namespace host
+}  // namespace vct
 
 namespace vct {
 
@@ -302,7 +248,8 @@ void fill_accum_inputs(const vct_config& cfg, const vct_params& prm, const float
 
 }  // namespace vct
 
-namespace {
+namespace vct {
+namespace host {
 
 void default_tuning(vct_tuning& t) {
     t.voxel_unit_pixels = 512;
@@ -513,7 +460,8 @@ vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], co
     return VCT_OK;
 }
 
-}  // namespace
+}  // namespace host
+}  // namespace vct
 
 // ==================================================================== API
 extern "C" {
@@ -1023,559 +971,6 @@ vct_status vct_render_gbuffer(const vct_triangles* tris, const float vp[16], con
     launch_gbuffer_raster(P, as_stream(stream));
     VCT_CHECK_LAUNCH("gbuffer");
     return VCT_OK;
-}
-
-}  // extern "C"
-
-// ==================================================================== batches
-// vct_batch: one context per scene, every frame stage one launch over all
-// scenes.  Per-scene parameter structs and the work-offset tables of the
-// launches travel in one blob: staged in pinned host memory, copied to the
-// device with one stream-ordered copy per frame.
-struct vct_batch {
-    int n = 0, device = 0, num_sms = 0;
-    std::vector<vct_ctx*> ctx;
-    size_t off_accum = 0, off_inject = 0, off_resolve = 0, off_mips = 0, off_trace = 0, off_tables = 0;
-    size_t blob_bytes = 0;
-    char* d_blob = nullptr;
-    char* h_blob = nullptr;        // staging of vct_batch_frame
-    char* h_graph_blob = nullptr;  // staging read by the captured graph
-    void* work = nullptr;          // voxeliser work arrays over all triangles
-    long long work_bytes = 0;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    vct_tuning tuning;
-    cudaEvent_t ev[4] = {};  // voxeliser start/end, trace start/end (timers, autotuner)
-    bool timers_on = false, timers_recorded = false;
-    int graph_launches = 0;  // kernels in the captured graph
-};
-
-namespace {
-
-size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
-
-struct BatchTotals {
-    long long tris = 0, texels = 0, bricks = 0, tiles = 0;
-};
-
-// Validates the scene descriptors and fills the staging blob `h` (parameter
-// structs and prefix tables).  Allocates the voxeliser work arrays when the
-// batch grew (never during a capture: `allow_alloc` false).
-vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, BatchTotals& tot, bool allow_alloc) {
-    if (!sc || n != b->n) return fail(VCT_ERR_INVALID_ARGUMENT, "scene descriptors must match the batch's scene count");
-    const int filter = b->ctx[0]->params.trace_filter;
-    long long* tri_off = reinterpret_cast<long long*>(h + b->off_tables);
-    long long* tex_off = tri_off + (n + 1);
-    long long* brick_off = tex_off + (n + 1);
-    long long* tile_off = brick_off + (n + 1);
-    tot = BatchTotals();
-    for (int i = 0; i < n; ++i) {
-        vct_ctx* c = b->ctx[i];
-        const vct_scene_desc& d = sc[i];
-        vct_status s = validate_tris(&d.triangles);
-        bool need_shadow = false;
-        if (s == VCT_OK) s = validate_lights(d.lights, d.n_lights, &need_shadow);
-        if (s == VCT_OK) s = validate_shadow(&d.shadow, true);
-        if (s == VCT_OK) s = validate_gbuffer(&d.gbuffer);
-        if (s != VCT_OK) return s;
-        if (c->params.trace_filter != filter) return fail(VCT_ERR_INVALID_ARGUMENT, "all scenes of a batch must use the same trace_filter");
-        if (filter != VCT_FILTER_SOFTWARE && (s = ensure_texture(c)) != VCT_OK) return s;
-        const bool hw = filter != VCT_FILTER_SOFTWARE;
-        AccumParams A;
-        fill_accum_inputs(c->cfg, c->params, c->mvp, &d.triangles, d.lights, d.n_lights, &d.shadow, A);
-        apply_tuning(b->tuning, A);
-        A.acc = c->acc;
-        A.occ = c->occ;
-        A.stats = c->stats;
-        A.num_sms = c->num_sms;
-        InjectParams I;
-        fill_inject(c, &d.shadow, I);
-        ResolveParams R;
-        std::memset(&R, 0, sizeof R);
-        fill_norm(c, R.norm);
-        R.fused = 1;
-        R.lighting = c->params.radiance_lighting;
-        R.dilate = c->params.radiance_dilate;
-        R.light_vox = I.light_vox;
-        R.light_int = I.light_int;
-        R.lit = c->lit;
-        R.mip_levels = std::min(4, c->levels - 1);
-        for (int l = 0; l <= R.mip_levels; ++l) {
-            R.radiance_levels[l] = level_ptr(c->radiance, c, l);
-            R.surf[l] = hw ? c->surf[l] : 0;
-            R.pad_levels[l] = hw ? nullptr : c->pchain + padded_level_offset(c->dim, l);
-        }
-        MipLevels M = mip_levels(c, c->radiance, c->levels);
-        for (int l = 0; l < c->levels; ++l) {
-            M.surf[l] = hw ? c->surf[l] : 0;
-            M.pad[l] = hw ? nullptr : c->pchain + padded_level_offset(c->dim, l);
-        }
-        M.first = std::min(4, c->levels - 1);
-        TraceParams T;
-        if ((s = fill_trace(c, &d.gbuffer, d.eye, &d.out, T)) != VCT_OK) return s;
-        apply_tuning(b->tuning, T);
-        std::memcpy(h + b->off_accum + i * sizeof(AccumParams), &A, sizeof A);
-        std::memcpy(h + b->off_inject + i * sizeof(InjectParams), &I, sizeof I);
-        std::memcpy(h + b->off_resolve + i * sizeof(ResolveParams), &R, sizeof R);
-        std::memcpy(h + b->off_mips + i * sizeof(MipLevels), &M, sizeof M);
-        std::memcpy(h + b->off_trace + i * sizeof(TraceParams), &T, sizeof T);
-        tri_off[i] = tot.tris;
-        tex_off[i] = tot.texels;
-        brick_off[i] = tot.bricks;
-        tile_off[i] = tot.tiles;
-        tot.tris += d.triangles.count;
-        tot.texels += (long long)I.nx * I.ny;
-        const long long bpa = c->dim / 16;
-        tot.bricks += bpa * bpa * bpa;
-        tot.tiles += trace_tiles(d.gbuffer.width, d.gbuffer.height, T.tile_w_log2, T.tile_h_log2);
-    }
-    tri_off[n] = tot.tris;
-    tex_off[n] = tot.texels;
-    brick_off[n] = tot.bricks;
-    tile_off[n] = tot.tiles;
-    if (tot.tris > 0x7fffffffLL) return fail(VCT_ERR_INVALID_ARGUMENT, "a batch holds at most 2^31-1 triangles");
-    const long long need = accumulate_scratch_bytes(std::max(tot.tris, 1LL));
-    if (need > b->work_bytes) {
-        if (!allow_alloc) return fail(VCT_ERR_STATE, "batch work arrays too small for the captured scenes");
-        // A captured graph points at the old arrays: it goes with them.
-        if (b->exec) cudaGraphExecDestroy(b->exec);
-        if (b->graph) cudaGraphDestroy(b->graph);
-        b->exec = nullptr;
-        b->graph = nullptr;
-        if (b->work) cudaFree(b->work);
-        b->work = nullptr;
-        b->work_bytes = 0;
-        cudaError_t e = cudaMalloc(&b->work, (size_t)need);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return fail(VCT_ERR_OUT_OF_MEMORY, std::string("batch work arrays: ") + cudaGetErrorString(e));
-        }
-        b->work_bytes = need;
-    }
-    return VCT_OK;
-}
-
-// Enqueues one batched frame; `h` holds the staged blob.
-vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cudaStream_t st, bool timed = false) {
-    const int n = b->n;
-    VCT_CUDA(cudaMemcpyAsync(b->d_blob, h, b->blob_bytes, cudaMemcpyHostToDevice, st));
-    for (vct_ctx* c : b->ctx) {
-        VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
-        VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, st));
-    }
-    const long long* d_tables = reinterpret_cast<const long long*>(b->d_blob + b->off_tables);
-    AccumParams W0;
-    W0.ntri = tot.tris;
-    accumulate_bind_scratch(W0, b->work);
-    const VoxWork W = {W0.tri_rec, W0.tri_units, W0.tri_scan, W0.block_off, tot.tris,
-                       ilog2(b->tuning.voxel_unit_pixels)};
-    if (timed) VCT_CUDA(cudaEventRecord(b->ev[0], st));
-    if (tot.tris > 0) {
-        launch_accumulate_batch(
-            SceneBatch<AccumParams>{reinterpret_cast<const AccumParams*>(b->d_blob + b->off_accum), d_tables, n}, W,
-            b->num_sms, b->tuning.voxel_blocks_per_sm, st);
-        VCT_CHECK_LAUNCH("batch: accumulate");
-    }
-    if (timed) VCT_CUDA(cudaEventRecord(b->ev[1], st));
-    launch_inject_mark_batch(
-        SceneBatch<InjectParams>{reinterpret_cast<const InjectParams*>(b->d_blob + b->off_inject), d_tables + (n + 1), n},
-        tot.texels, st);
-    VCT_CHECK_LAUNCH("batch: inject mark");
-    launch_resolve_batch(SceneBatch<ResolveParams>{reinterpret_cast<const ResolveParams*>(b->d_blob + b->off_resolve),
-                                                  d_tables + 2 * (n + 1), n},
-                         tot.bricks, st);
-    VCT_CHECK_LAUNCH("batch: resolve");
-    for (vct_ctx* c : b->ctx) VCT_CUDA(cudaMemsetAsync(c->occ, 0, (size_t)((c->nv + 31) / 32) * 4, st));
-    launch_mip_tail_batch(SceneBatch<MipLevels>{reinterpret_cast<const MipLevels*>(b->d_blob + b->off_mips), nullptr, n},
-                          st);
-    VCT_CHECK_LAUNCH("batch: coarse mips");
-    if (timed) VCT_CUDA(cudaEventRecord(b->ev[2], st));
-    launch_trace_batch(SceneBatch<TraceParams>{reinterpret_cast<const TraceParams*>(b->d_blob + b->off_trace),
-                                              d_tables + 3 * (n + 1), n},
-                       b->ctx[0]->params.trace_filter, tot.tiles, st);
-    VCT_CHECK_LAUNCH("batch: trace");
-    if (timed) VCT_CUDA(cudaEventRecord(b->ev[3], st));
-    const bool hw = b->ctx[0]->params.trace_filter != VCT_FILTER_SOFTWARE;
-    for (vct_ctx* c : b->ctx) {
-        c->stats_reset_pending = true;
-        c->radiance_ready = c->mips_ready = true;
-        c->tex_ready = hw;
-        c->pad_ready = !hw;
-    }
-    return VCT_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-vct_status vct_batch_create(const vct_config* configs, int32_t n, vct_batch** out) {
-    if (!out) return fail(VCT_ERR_INVALID_ARGUMENT, "out is NULL");
-    *out = nullptr;
-    if (!configs || n < 1 || n > accumulate_batch_max_scenes())
-        return fail(VCT_ERR_INVALID_ARGUMENT, "a batch holds 1..256 scenes");
-    for (int i = 0; i < n; ++i) {
-        vct_status s = validate_config(&configs[i]);
-        if (s != VCT_OK) return s;
-        if (configs[i].voxel_dim > 256) return fail(VCT_ERR_UNSUPPORTED, "batched scenes are limited to 256^3 grids");
-        if (configs[i].device != configs[0].device) return fail(VCT_ERR_INVALID_ARGUMENT, "a batch lives on one device");
-    }
-    vct_batch* b = new (std::nothrow) vct_batch;
-    if (!b) return fail(VCT_ERR_OUT_OF_MEMORY, "host allocation failed");
-    b->n = n;
-    b->device = configs[0].device;
-    default_tuning(b->tuning);
-    for (int i = 0; i < n; ++i) {
-        vct_ctx* c = nullptr;
-        vct_status s = vct_create(&configs[i], &c);
-        if (s != VCT_OK) {
-            std::string msg = g_err;
-            vct_batch_destroy(b);
-            return fail(s, msg);
-        }
-        b->ctx.push_back(c);
-    }
-    b->num_sms = b->ctx[0]->num_sms;
-    size_t off = 0;
-    b->off_accum = off;
-    off = up256(off + sizeof(AccumParams) * n);
-    b->off_inject = off;
-    off = up256(off + sizeof(InjectParams) * n);
-    b->off_resolve = off;
-    off = up256(off + sizeof(ResolveParams) * n);
-    b->off_mips = off;
-    off = up256(off + sizeof(MipLevels) * n);
-    b->off_trace = off;
-    off = up256(off + sizeof(TraceParams) * n);
-    b->off_tables = off;
-    off = up256(off + sizeof(long long) * 4 * (n + 1));
-    b->blob_bytes = off;
-    DeviceScope ds(b->device);
-    cudaError_t e = cudaMalloc(&b->d_blob, off);
-    if (e == cudaSuccess) e = cudaMallocHost(&b->h_blob, off);
-    if (e == cudaSuccess) e = cudaMallocHost(&b->h_graph_blob, off);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        vct_batch_destroy(b);
-        return fail(VCT_ERR_OUT_OF_MEMORY, std::string("batch parameter blob: ") + cudaGetErrorString(e));
-    }
-    std::memset(b->h_blob, 0, off);
-    std::memset(b->h_graph_blob, 0, off);
-    *out = b;
-    return VCT_OK;
-}
-
-vct_status vct_batch_destroy(vct_batch* b) {
-    if (!b) return VCT_OK;
-    DeviceScope ds(b->device);
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    for (cudaEvent_t e : b->ev)
-        if (e) cudaEventDestroy(e);
-    for (vct_ctx* c : b->ctx) vct_destroy(c);
-    if (b->d_blob) cudaFree(b->d_blob);
-    if (b->h_blob) cudaFreeHost(b->h_blob);
-    if (b->h_graph_blob) cudaFreeHost(b->h_graph_blob);
-    if (b->work) cudaFree(b->work);
-    delete b;
-    return VCT_OK;
-}
-
-vct_status vct_batch_set_params(vct_batch* b, int32_t scene, const vct_params* p) {
-    if (!b) return fail(VCT_ERR_INVALID_ARGUMENT, "batch is NULL");
-    if (scene < -1 || scene >= b->n) return fail(VCT_ERR_INVALID_ARGUMENT, "scene index out of range");
-    for (int i = 0; i < b->n; ++i)
-        if (scene == -1 || scene == i) {
-            vct_status s = vct_set_params(b->ctx[i], p);
-            if (s != VCT_OK) return s;
-        }
-    return VCT_OK;
-}
-
-vct_status vct_batch_frame(vct_batch* b, const vct_scene_desc* scenes, int32_t n, void* stream) {
-    if (!b) return fail(VCT_ERR_INVALID_ARGUMENT, "batch is NULL");
-    DeviceScope ds(b->device);
-    VCT_CUDA(ds.err);
-    cudaStream_t st = as_stream(stream);
-    // The staging blob may still be read by the previous frame's copy.
-    VCT_CUDA(cudaStreamSynchronize(st));
-    BatchTotals tot;
-    vct_status s = batch_stage(b, scenes, n, b->h_blob, tot, true);
-    if (s != VCT_OK) return s;
-    if ((s = batch_enqueue(b, b->h_blob, tot, st, b->timers_on)) != VCT_OK) return s;
-    b->timers_recorded = b->timers_on;
-    return VCT_OK;
-}
-
-vct_status vct_batch_enable_timers(vct_batch* b, int32_t enable) {
-    if (!b) return fail(VCT_ERR_INVALID_ARGUMENT, "batch is NULL");
-    DeviceScope ds(b->device);
-    VCT_CUDA(ds.err);
-    if (enable && !b->ev[0])
-        for (auto& e : b->ev) VCT_CUDA(cudaEventCreate(&e));
-    b->timers_on = enable != 0;
-    b->timers_recorded = false;
-    return VCT_OK;
-}
-
-vct_status vct_batch_get_timers(vct_batch* b, vct_timers* out) {
-    if (!b || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (!b->timers_recorded) return fail(VCT_ERR_STATE, "no timed vct_batch_frame since timers were enabled");
-    DeviceScope ds(b->device);
-    VCT_CUDA(ds.err);
-    VCT_CUDA(cudaEventSynchronize(b->ev[3]));
-    VCT_CUDA(cudaEventElapsedTime(&out->voxelize_ms, b->ev[0], b->ev[1]));
-    VCT_CUDA(cudaEventElapsedTime(&out->mipmap_ms, b->ev[1], b->ev[2]));
-    VCT_CUDA(cudaEventElapsedTime(&out->render_ms, b->ev[2], b->ev[3]));
-    VCT_CUDA(cudaEventElapsedTime(&out->total_ms, b->ev[0], b->ev[3]));
-    out->radiance_ms = 0.0f;
-    return VCT_OK;
-}
-
-vct_status vct_batch_capture(vct_batch* b, const vct_scene_desc* scenes, int32_t n, void* stream) {
-    if (!b) return fail(VCT_ERR_INVALID_ARGUMENT, "batch is NULL");
-    if (!stream) return fail(VCT_ERR_INVALID_ARGUMENT, "capture needs a non-default stream");
-    DeviceScope ds(b->device);
-    VCT_CUDA(ds.err);
-    cudaStream_t st = as_stream(stream);
-    VCT_CUDA(cudaStreamSynchronize(st));
-    BatchTotals tot;
-    vct_status s = batch_stage(b, scenes, n, b->h_graph_blob, tot, true);
-    if (s != VCT_OK) return s;
-    if (b->exec) {
-        cudaGraphExecDestroy(b->exec);
-        b->exec = nullptr;
-    }
-    if (b->graph) {
-        cudaGraphDestroy(b->graph);
-        b->graph = nullptr;
-    }
-    VCT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    const unsigned long long launches0 = g_launches.load();
-    s = batch_enqueue(b, b->h_graph_blob, tot, st);
-    b->graph_launches = (int)(g_launches.load() - launches0);
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(st, &g);
-    if (s != VCT_OK) {
-        if (g) cudaGraphDestroy(g);
-        return s;
-    }
-    if (e != cudaSuccess) return fail(VCT_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    b->graph = g;
-    VCT_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
-    return VCT_OK;
-}
-
-vct_status vct_batch_replay(vct_batch* b, void* stream) {
-    if (!b) return fail(VCT_ERR_INVALID_ARGUMENT, "batch is NULL");
-    if (!b->exec) return fail(VCT_ERR_STATE, "no captured graph: call vct_batch_capture first");
-    DeviceScope ds(b->device);
-    VCT_CUDA(ds.err);
-    VCT_CUDA(cudaGraphLaunch(b->exec, as_stream(stream)));
-    note_launches(b->graph_launches);
-    return VCT_OK;
-}
-
-vct_status vct_batch_context(vct_batch* b, int32_t scene, vct_ctx** ctx) {
-    if (!b || !ctx) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (scene < 0 || scene >= b->n) return fail(VCT_ERR_INVALID_ARGUMENT, "scene index out of range");
-    *ctx = b->ctx[scene];
-    return VCT_OK;
-}
-
-
-}  // extern "C"
-
-// ==================================================================== tuning
-namespace {
-
-// Candidate settings of the autotuner.  Voxeliser: work-unit size (smaller
-// units balance scenes of few large triangles, larger ones cut per-unit
-// overhead) x raster CTAs per SM.  Trace: CTA tile and warp sub-tile shapes
-// (the warp's footprint decides how coherent its 32 cones' texel fetches are).
-const int kUnitCand[] = {128, 256, 512, 1024, 2048};
-const int kBpsCand[] = {2, 3};
-const int kTileCand[][3] = {{16, 16, 8}, {16, 16, 4}, {16, 16, 16}, {32, 8, 8}, {32, 8, 4},  {32, 8, 16},
-                            {8, 32, 4},  {8, 32, 8},  {64, 4, 8},   {64, 4, 16}, {64, 4, 32}, {4, 64, 4}};
-
-float median(std::vector<float> v) {
-    std::sort(v.begin(), v.end());
-    return v.empty() ? 0.0f : v[v.size() / 2];
-}
-
-// Runs one timed frame and returns (voxeliser ms, trace ms).
-using TimedFrame = vct_status (*)(void* obj, const void* args, float* vox_ms, float* trace_ms);
-
-vct_status tune(vct_tuning& cur, int reps, void* obj, const void* args, TimedFrame run, vct_tuning* set_into) {
-    reps = std::max(1, std::min(reps, 64));
-    std::vector<float> vox, trc;
-    float v = 0, t = 0;
-    // Voxeliser settings.
-    vct_tuning best = cur;
-    float best_ms = 3.0e38f;
-    for (int u : kUnitCand)
-        for (int bps : kBpsCand) {
-            vct_tuning c = best;
-            c.voxel_unit_pixels = u;
-            c.voxel_blocks_per_sm = bps;
-            *set_into = c;
-            vct_status s = run(obj, args, &v, &t);  // warm-up
-            if (s != VCT_OK) return s;
-            vox.clear();
-            for (int r = 0; r < reps; ++r) {
-                if ((s = run(obj, args, &v, &t)) != VCT_OK) return s;
-                vox.push_back(v);
-            }
-            const float m = median(vox);
-            if (m < best_ms) {
-                best_ms = m;
-                best.voxel_unit_pixels = u;
-                best.voxel_blocks_per_sm = bps;
-            }
-        }
-    // Trace tile shapes.
-    best_ms = 3.0e38f;
-    vct_tuning best2 = best;
-    for (const auto& tc : kTileCand) {
-        vct_tuning c = best;
-        c.trace_tile_w = tc[0];
-        c.trace_tile_h = tc[1];
-        c.trace_warp_w = tc[2];
-        *set_into = c;
-        vct_status s = run(obj, args, &v, &t);
-        if (s != VCT_OK) return s;
-        trc.clear();
-        for (int r = 0; r < reps; ++r) {
-            if ((s = run(obj, args, &v, &t)) != VCT_OK) return s;
-            trc.push_back(t);
-        }
-        const float m = median(trc);
-        if (m < best_ms) {
-            best_ms = m;
-            best2 = c;
-        }
-    }
-    cur = best2;
-    *set_into = best2;
-    return VCT_OK;
-}
-
-struct CtxFrameArgs {
-    const vct_triangles* tris;
-    const vct_light* lights;
-    int32_t n;
-    const vct_shadow_desc* shadow;
-    const float* eye;
-    const vct_gbuffer* g;
-    const vct_trace_out* out;
-    void* stream;
-};
-
-vct_status ctx_timed_frame(void* obj, const void* a, float* vox_ms, float* trace_ms) {
-    vct_ctx* c = static_cast<vct_ctx*>(obj);
-    const CtxFrameArgs& f = *static_cast<const CtxFrameArgs*>(a);
-    vct_status s = vct_frame(c, f.tris, f.lights, f.n, f.shadow, f.eye, f.g, f.out, f.stream);
-    if (s != VCT_OK) return s;
-    vct_timers t;
-    if ((s = vct_get_timers(c, &t)) != VCT_OK) return s;
-    *vox_ms = t.voxelize_ms;
-    *trace_ms = t.render_ms;
-    return VCT_OK;
-}
-
-struct BatchFrameArgs {
-    const vct_scene_desc* scenes;
-    int32_t n;
-    void* stream;
-};
-
-vct_status batch_timed_frame(void* obj, const void* a, float* vox_ms, float* trace_ms) {
-    vct_batch* b = static_cast<vct_batch*>(obj);
-    const BatchFrameArgs& f = *static_cast<const BatchFrameArgs*>(a);
-    cudaStream_t st = as_stream(f.stream);
-    VCT_CUDA(cudaStreamSynchronize(st));
-    BatchTotals tot;
-    vct_status s = batch_stage(b, f.scenes, f.n, b->h_blob, tot, true);
-    if (s != VCT_OK) return s;
-    if ((s = batch_enqueue(b, b->h_blob, tot, st, true)) != VCT_OK) return s;
-    VCT_CUDA(cudaEventSynchronize(b->ev[3]));
-    VCT_CUDA(cudaEventElapsedTime(vox_ms, b->ev[0], b->ev[1]));
-    VCT_CUDA(cudaEventElapsedTime(trace_ms, b->ev[2], b->ev[3]));
-    return VCT_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-void vct_default_tuning(vct_tuning* out) {
-    if (out) default_tuning(*out);
-}
-
-vct_status vct_get_tuning(const vct_ctx* c, vct_tuning* out) {
-    if (!c || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
-    *out = c->tuning;
-    return VCT_OK;
-}
-
-vct_status vct_set_tuning(vct_ctx* c, const vct_tuning* t) {
-    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
-    vct_status s = validate_tuning(t);
-    if (s != VCT_OK) return s;
-    c->tuning = *t;
-    return VCT_OK;
-}
-
-vct_status vct_batch_get_tuning(const vct_batch* b, vct_tuning* out) {
-    if (!b || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
-    *out = b->tuning;
-    return VCT_OK;
-}
-
-vct_status vct_batch_set_tuning(vct_batch* b, const vct_tuning* t) {
-    if (!b) return fail(VCT_ERR_INVALID_ARGUMENT, "batch is NULL");
-    vct_status s = validate_tuning(t);
-    if (s != VCT_OK) return s;
-    b->tuning = *t;
-    return VCT_OK;
-}
-
-vct_status vct_autotune(vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n_lights,
-                        const vct_shadow_desc* shadow, const float eye[3], const vct_gbuffer* g,
-                        const vct_trace_out* out, int32_t reps, void* stream, vct_tuning* best) {
-    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
-    const bool timers_were_on = c->timers_on;
-    vct_status s = vct_enable_timers(c, 1);
-    if (s != VCT_OK) return s;
-    const CtxFrameArgs args = {tris, lights, n_lights, shadow, eye, g, out, stream};
-    const vct_tuning orig = c->tuning;
-    vct_tuning cur = orig;
-    s = tune(cur, reps, c, &args, ctx_timed_frame, &c->tuning);
-    c->tuning = s == VCT_OK ? cur : orig;
-    vct_enable_timers(c, timers_were_on ? 1 : 0);
-    if (s == VCT_OK && best) *best = c->tuning;
-    return s;
-}
-
-vct_status vct_batch_autotune(vct_batch* b, const vct_scene_desc* scenes, int32_t n, int32_t reps, void* stream,
-                              vct_tuning* best) {
-    if (!b) return fail(VCT_ERR_INVALID_ARGUMENT, "batch is NULL");
-    DeviceScope ds(b->device);
-    VCT_CUDA(ds.err);
-    if (!b->ev[0])
-        for (auto& e : b->ev) VCT_CUDA(cudaEventCreate(&e));
-    b->timers_recorded = false;
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    b->exec = nullptr;
-    b->graph = nullptr;
-    const BatchFrameArgs args = {scenes, n, stream};
-    const vct_tuning orig = b->tuning;
-    vct_tuning cur = orig;
-    vct_status s = tune(cur, reps, b, &args, batch_timed_frame, &b->tuning);
-    b->tuning = s == VCT_OK ? cur : orig;
-    if (s == VCT_OK && best) *best = cur;
-    return s;
 }
 
 }  // extern "C"
