@@ -338,6 +338,18 @@ vct_status vct_autotune(vct_ctx* ctx, const vct_triangles* tris, const vct_light
 vct_status vct_batch_autotune(vct_batch* batch, const vct_scene_desc* scenes, int32_t n_scenes, int32_t reps,
                               void* stream, vct_tuning* best);
 
+/* ---- learned path ------------------------------------------------------ */
+/* No counterpart in the reference.  Diagnostic of the tensor-core path the
+ * MLP kernels use: one 128 x n x k BF16 GEMM with FP32 accumulation on the
+ * fifth-generation tensor cores (tcgen05.mma, accumulator in tensor memory):
+ * d_dev (128 x n, row-major fp32) = a_dev (128 x k) * b_dev (n x k)^T, the
+ * operands row-major BF16 bit patterns; k, n in {16, 32, 48, 64}.  variant 1
+ * exchanges the two stride fields of the shared-memory descriptors (a check
+ * of the layout convention: it must NOT reproduce the product).
+ * Synchronises `stream`; VCT_ERR_TIMEOUT if the MMA did not complete. */
+vct_status vct_tensor_core_check(const uint16_t* a_dev, const uint16_t* b_dev, int32_t k, int32_t n,
+                                 int32_t variant, float* d_dev, void* stream);
+
 /* ---- voxelisation without allocation ---------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a host application whose device memory is all reserved up front by its

@@ -162,6 +162,7 @@ SIGNATURES = {
     "vct_batch_context": (st, [vp, C.c_int32, P(vp)]),
     "vct_batch_enable_timers": (st, [vp, C.c_int32]),
     "vct_batch_get_timers": (st, [vp, P(vct_timers)]),
+    "vct_tensor_core_check": (st, [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, vp]),
     "vct_default_tuning": (None, [P(vct_tuning)]),
     "vct_get_tuning": (st, [vp, P(vct_tuning)]),
     "vct_set_tuning": (st, [vp, P(vct_tuning)]),

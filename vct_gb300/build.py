@@ -37,8 +37,9 @@ CUDA_SOURCES = [
     ("raster.cu", ["--fmad=false"]),
     ("trace.cu", ["--fmad=false"]),
     ("static_scratch.cu", []),
+    ("learned.cu", ["--fmad=false"]),
 ]
-CXX_SOURCES = ["capi.cpp", "batch.cpp"]
+CXX_SOURCES = ["capi.cpp", "batch.cpp", "learned_capi.cpp"]
 
 
 def nvcc_path() -> str:

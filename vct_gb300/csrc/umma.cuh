@@ -1,0 +1,141 @@
+// Fifth-generation tensor core (tcgen05) building blocks for sm_103a, as
+// inline PTX: shared-memory matrix and instruction descriptors, the BF16
+// MMA with an FP32 accumulator in tensor memory (TMEM), completion through an
+// mbarrier, TMEM allocation and loads.
+//
+// Operand tiles live in shared memory in the canonical no-swizzle K-major
+// layout: 8 x 8 "core matrices" (8 rows of 16 bytes, 128 contiguous bytes),
+// here stored K-chunk outer:
+//     byte(r, k) = (k / 8) * (R * 16) + (r / 8) * 128 + (r % 8) * 16 + (k % 8) * 2
+// for a tile of R rows.  In the descriptor the leading-dimension byte offset
+// (between core matrices adjacent in K) is R * 16 and the stride-dimension
+// byte offset (between core matrices adjacent in M or N) is 128; one K step of
+// 16 elements advances the start address by 2 * R * 16 bytes.
+//
+// D (M = 128 rows, cta_group::1) occupies TMEM lanes 0..127, one lane per row,
+// and N consecutive 32-bit columns; warp w of the CTA reads lanes
+// 32 (w % 4) .. 32 (w % 4) + 31.
+//
+// Every wait is bounded (one second of %globaltimer): on timeout the caller
+// gets `false`, records an error and still releases its TMEM.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vct {
+namespace umma {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Byte offset of element (r, k) of an R-row operand tile (layout above).
+__host__ __device__ __forceinline__ uint32_t tile_offset(int r, int k, int R) {
+    return (uint32_t)((k >> 3) * (R * 16) + (r >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// Shared-memory descriptor: start address, leading / stride byte offsets,
+// descriptor version 1 (bits 46-48 = 0b001), base offset 0, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Descriptor of an R-row K-major tile at `saddr`, advanced to K step `j`.
+__device__ __forceinline__ uint64_t tile_desc(uint32_t saddr, int R, int j) {
+    return smem_desc(saddr + (uint32_t)(j * 2 * R * 16), (uint32_t)(R * 16), 128u);
+}
+
+// Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits
+// 17-22, M >> 4 in bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A * B^T for one K step of 16; issued by one thread.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+// The mbarrier at `mbar` receives one arrival once every tcgen05.mma this
+// thread issued before has completed.
+__device__ __forceinline__ void commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the completion of the mbarrier phase of parity `parity`, for at
+// most one second.  Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    const uint64_t t0 = global_ns();
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (global_ns() - t0 > 1000000000ull) return false;
+    }
+}
+
+// Generic-proxy shared-memory writes become visible to the tensor core's
+// (async proxy) reads.
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Whole-warp TMEM allocation of `ncols` columns (power of two >= 32); the
+// TMEM address is written to shared memory at `dst`.
+__device__ __forceinline__ void tmem_alloc(uint32_t dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// 16 consecutive 32-bit columns of this thread's TMEM lane (warp-wide; the
+// lane field of `taddr` selects the warp's 32-lane quarter), waited for
+// inside the same statement so the values are valid on return.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// TMEM address of column `col` in the lane quarter of warp `warp`.
+__device__ __forceinline__ uint32_t tmem_addr(uint32_t base, int warp, int col) {
+    return base + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)col;
+}
+
+}  // namespace umma
+}  // namespace vct

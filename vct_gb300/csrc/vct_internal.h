@@ -250,6 +250,9 @@ void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks,
 void launch_mip_tail_batch(const SceneBatch<MipLevels>& B, cudaStream_t s);
 long long trace_tiles(int width, int height, int tile_w_log2, int tile_h_log2);
 void launch_trace_batch(const SceneBatch<TraceParams>& B, int filter, long long tiles, cudaStream_t s);
+// Tensor-core GEMM check: D (128 x n, fp32) = A (128 x k) B^T (n x k), bf16.
+void launch_umma_check(const uint16_t* A, const uint16_t* B, int K, int N, int swap, float* D, uint32_t* status,
+                       cudaStream_t s);
 // Copies every level of a linear chain into the interior of the bordered chain.
 void launch_pad_copy(const uint2* chain, float4* pchain, int dim, int levels, cudaStream_t s);
 
