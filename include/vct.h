@@ -350,6 +350,82 @@ vct_status vct_batch_autotune(vct_batch* batch, const vct_scene_desc* scenes, in
 vct_status vct_tensor_core_check(const uint16_t* a_dev, const uint16_t* b_dev, int32_t k, int32_t n,
                                  int32_t variant, float* d_dev, void* stream);
 
+/* The network: 42 inputs, three hidden layers of 64 with ReLU, 3 linear
+ * outputs (irradiance RGB); BF16 weights and activations, FP32 accumulation
+ * on the tensor cores, FP32 master parameters and Adam state.  Parameters
+ * are packed fp32: W1[64][42] b1[64] W2[64][64] b2[64] W3[64][64] b3[64]
+ * W4[3][64] b4[3] (W[out][in]).  Training minimises the mean squared error
+ * over the n x 3 outputs.  Feature rows: n x 42 fp32, row-major, 8-byte
+ * aligned. */
+#define VCT_MLP_INPUTS 42
+#define VCT_MLP_HIDDEN 64
+#define VCT_MLP_OUTPUTS 3
+#define VCT_MLP_PARAMS 11267
+typedef struct vct_mlp vct_mlp;
+typedef struct vct_adam {
+    float lr, beta1, beta2, eps;
+} vct_adam;
+
+/* He-uniform weights from `seed` (splitmix64), zero biases. */
+vct_status vct_mlp_create(int32_t device, uint64_t seed, vct_mlp** out);
+vct_status vct_mlp_destroy(vct_mlp* mlp);
+/* Host copies of the packed parameters (set also resets the Adam state);
+ * get synchronises `stream` and reports VCT_ERR_TIMEOUT if an earlier
+ * training or inference launch gave up waiting for the tensor core. */
+vct_status vct_mlp_set_params(vct_mlp* mlp, const float* params, int64_t count);
+vct_status vct_mlp_get_params(vct_mlp* mlp, float* params, int64_t count, void* stream);
+/* out_dev (n x 3) = network(rows_dev). */
+vct_status vct_mlp_forward(vct_mlp* mlp, const float* rows_dev, int64_t n, float* out_dev, void* stream);
+/* grad_dev (VCT_MLP_PARAMS fp32) = d loss / d params and loss_dev (1 fp32,
+ * may be NULL) for rows_dev and targets_dev (n x 3); parameters unchanged.
+ * Synchronises `stream`. */
+vct_status vct_mlp_gradients(vct_mlp* mlp, const float* rows_dev, const float* targets_dev, int64_t n,
+                             float* grad_dev, float* loss_dev, void* stream);
+/* One Adam step on the n rows index_dev[0..n) of rows_dev / targets_dev
+ * (index_dev NULL: rows 0..n); loss_dev (may be NULL) receives the step's
+ * loss before the update.  No synchronisation. */
+vct_status vct_mlp_train_step(vct_mlp* mlp, const float* rows_dev, const float* targets_dev, const int32_t* index_dev,
+                              int64_t n, const vct_adam* opt, float* loss_dev, void* stream);
+
+/* Learned trace of a frame whose radiance chain is built (>= 5 levels).
+ * Cheap features: per 4x4 pixel block (ceil(w/4) x ceil(h/4) blocks, row
+ * major), at its first covered pixel, two 90-degree cones along
+ * normalize(N +- T), each marched 8 steps (step s samples mip level s + 1,
+ * 2^s voxels out) and composited front to back; the accumulated RGBA after
+ * levels 2, 4, 6 and 8 are 4 x 4 features per cone: 32 BF16 values, 64 bytes
+ * per block, 16-byte aligned. */
+#define VCT_LEARNED_CHEAP_FEATURES 32
+vct_status vct_learned_features(vct_ctx* ctx, const vct_gbuffer* gbuffer, const float eye[3], uint16_t* features_dev,
+                                void* stream);
+/* Feature rows (n x 42 fp32) of the listed pixels (index y * width + x):
+ * the 32 cheap features of the pixel's block, unit normal N, eye distance /
+ * volume extent, albedo, and the near-field radiance RGB (one trilinear
+ * sample of mip level 1 at position + 2 N / dim, where the diffuse cones
+ * take their first sample; zero outside the volume); all zero for
+ * background.  Every value is BF16-representable. */
+vct_status vct_learned_rows(vct_ctx* ctx, const vct_gbuffer* gbuffer, const float eye[3],
+                            const uint16_t* features_dev, const int32_t* pixels_dev, int64_t n, float* rows_dev,
+                            void* stream);
+/* The plain 16-cone irradiance (the learned path's target and fallback):
+ * 16 cones of equal solid angle (aperture 2 acos(15/16)) on a Fibonacci
+ * hemisphere around the normal, cosine weighted, 24 steps, bias / initial
+ * height / LOD offset of the diffuse cones; float4 per pixel (rgb, 0). */
+vct_status vct_trace_reference16(vct_ctx* ctx, const vct_gbuffer* gbuffer, const float eye[3],
+                                 float* irradiance_dev, void* stream);
+typedef struct vct_learned_stats {
+    int32_t tiles;           /* 16 x 16 pixel tiles */
+    int32_t fallback_tiles;  /* tiles re-traced with the 16-cone reference */
+    float mean_tile_error;   /* mean estimated relative L2 error per tile, each capped at 1 (-1: no probes) */
+    float max_tile_error;
+} vct_learned_stats;
+/* Learned irradiance: cheap features, the network on every pixel, then per
+ * 16 x 16 tile an error estimate (16-cone irradiance at 4 probe pixels vs the
+ * network, relative L2) and the 16-cone trace of every tile whose estimate
+ * exceeds `threshold` (INFINITY: no probes, no fallback).  stats (may be
+ * NULL) synchronises `stream`. */
+vct_status vct_learned_trace(vct_ctx* ctx, vct_mlp* mlp, const vct_gbuffer* gbuffer, const float eye[3],
+                             float threshold, float* irradiance_dev, vct_learned_stats* stats, void* stream);
+
 /* ---- voxelisation without allocation ---------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a host application whose device memory is all reserved up front by its

@@ -252,3 +252,46 @@ def frame(scene, nthreads=1, precision=32, rows=None, row_step=1, shadowmap=None
     stats["total_voxel_fragments"] = total
     return dict(shadowmap=sm, count=count, sums=sums, color=color, normal=normal, chain=chain, gpos=gp, gnrm=gn,
                 galb=ga, irradiance=irr, specular=spec, out=col, samples=ns, stats=stats, nv=nv)
+
+
+# ------------------------------------------------------------ learned path
+def cone_set16() -> np.ndarray:
+    """The learned path's 16-cone reference set, (16, 4) float32: Fibonacci
+    hemisphere directions z_i = 1 - (i + 1/2)/16, azimuth i * golden angle,
+    in the (T, B, N) frame, weights cos(theta) / sum cos(theta)."""
+    golden = np.pi * (3.0 - np.sqrt(5.0))
+    i = np.arange(16, dtype=np.float64)
+    z = 1.0 - (i + 0.5) / 16.0
+    r = np.sqrt(1.0 - z * z)
+    d = np.stack([r * np.cos(golden * i), r * np.sin(golden * i), z, z / z.sum()], 1)
+    return d.astype(np.float32)
+
+
+def reference16_cone(scene) -> orc_cone:
+    """Cone settings of the 16-cone reference: the diffuse cone's bias,
+    initial height and LOD offset, 24 steps, aperture 2 acos(15/16)."""
+    steps, ang, bias, h0, lod = scene.cone["diffuse"]
+    return orc_cone(24, float(np.float32(2.0 * np.arccos(15.0 / 16.0))), float(bias), float(h0), float(lod))
+
+
+def trace_reference16(scene, chain, gpos, gnrm, pixels, precision=64, nthreads=1):
+    """16-cone irradiance (float4) at the listed pixels (y * width + x)."""
+    W, H = scene.gbuffer_size
+    pixels = np.ascontiguousarray(pixels, dtype=np.int32)
+    out = np.zeros((pixels.size, 4), dtype=np.float32)
+    dirs = cone_set16()
+    cone = reference16_cone(scene)
+    samples = C.c_uint64(0)
+    load().orc_trace_cone_set(C.byref(volume(scene)), scene.levels, _p(chain), _p(dirs), 16, C.byref(cone),
+                              C.c_float(float(np.sqrt(3.0))), _p(gpos), _p(gnrm), W, _p(pixels),
+                              C.c_int64(pixels.size), precision, _p(out), C.byref(samples), nthreads)
+    return out, int(samples.value)
+
+
+def learned_features(scene, chain, gpos, gnrm) -> np.ndarray:
+    """Cheap quarter-resolution features (fp32), (ceil(H/4) * ceil(W/4), 32)."""
+    W, H = scene.gbuffer_size
+    wq, hq = (W + 3) // 4, (H + 3) // 4
+    out = np.zeros((hq * wq, 32), dtype=np.float32)
+    load().orc_learned_features(C.byref(volume(scene)), scene.levels, _p(chain), _p(gpos), _p(gnrm), W, H, _p(out))
+    return out

@@ -846,9 +846,128 @@ static void trace_rows(const orc_volume* vol, int levels, const uint16_t* chain,
     if (samples_out) *samples_out += total.load();
 }
 
+// Cone set around the normal of listed pixels: dirs[c] = (x, y, z, weight)
+// in the frame (T, B, N) of the Duff et al. basis; irradiance = sum of
+// weight * cone rgba.  The learned path's 16-cone reference uses it.
+template <typename T>
+static void trace_set_pixels(const orc_volume* vol, int levels, const uint16_t* chain, const float* dirs, int ncones,
+                             const orc_cone& cone, T maxd, const float* gpos, const float* gnrm, int W,
+                             const int32_t* pixels, int64_t npix, float* out, uint64_t* samples_out, int nthreads) {
+    Sampler<T> s;
+    s.init(chain, vol->dim, levels);
+    V<T> vmin = {(T)vol->vmin[0], (T)vol->vmin[1], (T)vol->vmin[2]};
+    V<T> vmax = {(T)vol->vmax[0], (T)vol->vmax[1], (T)vol->vmax[2]};
+    V<T> vc = {(T)vol->vcenter[0], (T)vol->vcenter[1], (T)vol->vcenter[2]};
+    (void)W;
+    std::atomic<uint64_t> total{0};
+    parallel_for(npix, nthreads, [&](int64_t a, int64_t b) {
+        uint64_t ns = 0;
+        for (int64_t i = a; i < b; ++i) {
+            const int64_t p = pixels[i];
+            T acc[4] = {0, 0, 0, 0};
+            if (gpos[4 * p + 3] != 0.0f) {
+                V<T> P = {(T)gpos[4 * p], (T)gpos[4 * p + 1], (T)gpos[4 * p + 2]};
+                V<T> Nn = vnorm(V<T>{(T)gnrm[4 * p], (T)gnrm[4 * p + 1], (T)gnrm[4 * p + 2]});
+                V<T> vp = {((P.x - vc.x) - vmin.x) / (vmax.x - vmin.x), ((P.y - vc.y) - vmin.y) / (vmax.y - vmin.y),
+                           ((P.z - vc.z) - vmin.z) / (vmax.z - vmin.z)};
+                T sgn = Nn.z >= T(0) ? T(1) : T(-1);
+                T ca = T(-1) / (sgn + Nn.z);
+                T cb = Nn.x * Nn.y * ca;
+                V<T> Tg = {T(1) + sgn * Nn.x * Nn.x * ca, sgn * cb, -sgn * Nn.x};
+                V<T> Bt = {cb, sgn + Nn.y * Nn.y * ca, -Nn.y};
+                for (int c = 0; c < ncones; ++c) {
+                    V<T> d = vadd(vadd(vmul(Tg, (T)dirs[4 * c]), vmul(Bt, (T)dirs[4 * c + 1])),
+                                  vmul(Nn, (T)dirs[4 * c + 2]));
+                    T cr[4];
+                    trace_cone(s, vp, Nn, d, cone, maxd, cr, ns);
+                    for (int k = 0; k < 4; ++k) acc[k] += (T)dirs[4 * c + 3] * cr[k];
+                }
+            }
+            for (int k = 0; k < 4; ++k) out[4 * i + k] = (float)acc[k];
+        }
+        total.fetch_add(ns);
+    });
+    if (samples_out) *samples_out += total.load();
+}
+
 }  // namespace
 
 extern "C" {
+
+void orc_trace_cone_set(const orc_volume* vol, int32_t levels, const uint16_t* chain, const float* dirs,
+                        int32_t ncones, const orc_cone* cone, float max_distance, const float* gpos, const float* gnrm,
+                        int32_t width, const int32_t* pixels, int64_t npix, int32_t precision, float* out,
+                        uint64_t* samples, int32_t nthreads) {
+    if (precision == 64)
+        trace_set_pixels<double>(vol, levels, chain, dirs, ncones, *cone, (double)max_distance, gpos, gnrm, width,
+                                 pixels, npix, out, samples, nthreads);
+    else
+        trace_set_pixels<float>(vol, levels, chain, dirs, ncones, *cone, max_distance, gpos, gnrm, width, pixels,
+                                npix, out, samples, nthreads);
+}
+
+// Cheap features of the learned path (fp32): per 4x4 block, at its first
+// covered pixel (order 5, 10, 6, 9, 0, 1, ... of the block, index 4 dy + dx),
+// two cones along normalize(N + T) and normalize(N - T); step s samples mip
+// level min(s + 1, levels - 1) trilinearly at start + dir * 2^s / dim (start
+// = position + N / dim), 8 steps composited front to back (no early out;
+// nothing is added once the cone has left [0,1]^3); the accumulated RGBA
+// after steps 1, 3, 5 and 7 are the cone's 16 features.
+void orc_learned_features(const orc_volume* vol, int32_t levels, const uint16_t* chain, const float* gpos,
+                          const float* gnrm, int32_t W, int32_t H, float* out) {
+    Sampler<float> s;
+    s.init(chain, vol->dim, levels);
+    static const int order[16] = {5, 10, 6, 9, 0, 1, 2, 3, 4, 7, 8, 11, 12, 13, 14, 15};
+    const int wq = (W + 3) / 4, hq = (H + 3) / 4;
+    const float scale = 1.0f / (float)vol->dim;
+    for (int qy = 0; qy < hq; ++qy)
+        for (int qx = 0; qx < wq; ++qx) {
+            float* f = out + ((int64_t)qy * wq + qx) * 32;
+            for (int k = 0; k < 32; ++k) f[k] = 0.0f;
+            int64_t pix = -1;
+            for (int k = 0; k < 16 && pix < 0; ++k) {
+                const int x = 4 * qx + (order[k] & 3), y = 4 * qy + (order[k] >> 2);
+                if (x < W && y < H && gpos[4 * ((int64_t)y * W + x) + 3] != 0.0f) pix = (int64_t)y * W + x;
+            }
+            if (pix < 0) continue;
+            const float* gp = gpos + 4 * pix;
+            const float* gn = gnrm + 4 * pix;
+            V<float> N = vnorm(V<float>{gn[0], gn[1], gn[2]});
+            const float sgn = N.z >= 0.0f ? 1.0f : -1.0f;
+            const float ca = -1.0f / (sgn + N.z);
+            const float cb = N.x * N.y * ca;
+            V<float> Tg = {1.0f + sgn * N.x * N.x * ca, sgn * cb, -sgn * N.x};
+            V<float> vp = {((gp[0] - vol->vcenter[0]) - vol->vmin[0]) / (vol->vmax[0] - vol->vmin[0]),
+                           ((gp[1] - vol->vcenter[1]) - vol->vmin[1]) / (vol->vmax[1] - vol->vmin[1]),
+                           ((gp[2] - vol->vcenter[2]) - vol->vmin[2]) / (vol->vmax[2] - vol->vmin[2])};
+            V<float> start = vadd(vp, vmul(N, scale));
+            for (int c = 0; c < 2; ++c) {
+                V<float> d = vnorm(c == 0 ? vadd(N, Tg) : vsub(N, Tg));
+                float h = 1.0f, alpha = 0.0f, col[3] = {0, 0, 0};
+                bool inside = true;
+                for (int i = 0; i < 8; ++i) {
+                    V<float> sp = vadd(start, vmul(d, h * scale));
+                    inside = inside && sp.x >= 0.f && sp.y >= 0.f && sp.z >= 0.f && sp.x <= 1.f && sp.y <= 1.f &&
+                             sp.z <= 1.f;
+                    if (inside) {
+                        float smp[4];
+                        s.trilinear(std::min(i + 1, levels - 1), sp, smp);
+                        const float a = 1.0f - alpha;
+                        for (int k = 0; k < 3; ++k) col[k] += smp[k] * a;
+                        alpha += a * smp[3];
+                    }
+                    if (i & 1) {
+                        float* o = f + c * 16 + (i >> 1) * 4;
+                        o[0] = col[0];
+                        o[1] = col[1];
+                        o[2] = col[2];
+                        o[3] = alpha;
+                    }
+                    h *= 2.0f;
+                }
+            }
+        }
+}
 
 void orc_trace(const orc_volume* vol, int32_t levels, const uint16_t* chain, const orc_trace_params* tp,
                const float* gpos, const float* gnrm, const float* galb, int32_t width, int32_t height,

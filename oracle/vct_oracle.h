@@ -104,6 +104,18 @@ void orc_trace(const orc_volume* vol, int32_t levels, const uint16_t* chain,
                int32_t row_step, const float eye[3], int32_t precision, float* irradiance,
                float* specular, float* color, uint64_t* samples, int32_t nthreads);
 
+/* Cone set of the learned path's 16-cone reference: for each listed pixel,
+ * sum over cones c of dirs[4c+3] * traceCone(dir = T dirs[4c] + B dirs[4c+1]
+ * + N dirs[4c+2]) in the Duff et al. frame; float4 per listed pixel. */
+void orc_trace_cone_set(const orc_volume* vol, int32_t levels, const uint16_t* chain, const float* dirs,
+                        int32_t ncones, const orc_cone* cone, float max_distance, const float* gpos,
+                        const float* gnrm, int32_t width, const int32_t* pixels, int64_t npix, int32_t precision,
+                        float* out, uint64_t* samples, int32_t nthreads);
+/* Cheap quarter-resolution features of the learned path, fp32,
+ * ceil(W/4) x ceil(H/4) x 32. */
+void orc_learned_features(const orc_volume* vol, int32_t levels, const uint16_t* chain, const float* gpos,
+                          const float* gnrm, int32_t width, int32_t height, float* out);
+
 void orc_render_shadowmap(const float* pos, int64_t ntri, const float ls[16], int32_t w, int32_t h,
                           float* depth, int32_t nthreads);
 void orc_render_gbuffer(const float* pos, const float* nrm, const float* albedo, int64_t ntri,

@@ -131,10 +131,12 @@ def test_default_tuning_and_scene_desc_layout():
                                       trace_warp_w=8)
     lib = L.load()
     for cls in (L.vct_light, L.vct_config, L.vct_cone_settings, L.vct_params, L.vct_triangles, L.vct_gbuffer,
-                L.vct_trace_out, L.vct_shadow_desc, L.vct_stats, L.vct_timers, L.vct_tuning, L.vct_scene_desc):
+                L.vct_trace_out, L.vct_shadow_desc, L.vct_stats, L.vct_timers, L.vct_tuning, L.vct_scene_desc,
+                L.vct_adam, L.vct_learned_stats):
         assert lib.vct_struct_layout(cls.__name__.encode()) == C.sizeof(cls), cls.__name__
     for f in ("lights", "n_lights", "shadow", "eye", "gbuffer", "out"):
         assert lib.vct_struct_layout(f"vct_scene_desc.{f}".encode()) == getattr(L.vct_scene_desc, f).offset, f
     assert lib.vct_struct_layout(b"vct_params.trace_filter") == L.vct_params.trace_filter.offset
     assert lib.vct_struct_layout(b"vct_tuning.trace_warp_w") == L.vct_tuning.trace_warp_w.offset
+    assert lib.vct_struct_layout(b"vct_learned_stats.max_tile_error") == L.vct_learned_stats.max_tile_error.offset
     assert lib.vct_struct_layout(b"no_such_struct") == -1

@@ -108,6 +108,15 @@ class vct_tuning(C.Structure):
                 ("trace_tile_h", C.c_int32), ("trace_warp_w", C.c_int32)]
 
 
+class vct_adam(C.Structure):
+    _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float)]
+
+
+class vct_learned_stats(C.Structure):
+    _fields_ = [("tiles", C.c_int32), ("fallback_tiles", C.c_int32), ("mean_tile_error", C.c_float),
+                ("max_tile_error", C.c_float)]
+
+
 class vct_scene_desc(C.Structure):
     _fields_ = [("triangles", vct_triangles), ("lights", C.POINTER(vct_light)), ("n_lights", C.c_int32),
                 ("shadow", vct_shadow_desc), ("eye", C.c_float * 3), ("gbuffer", vct_gbuffer),
@@ -163,6 +172,17 @@ SIGNATURES = {
     "vct_batch_enable_timers": (st, [vp, C.c_int32]),
     "vct_batch_get_timers": (st, [vp, P(vct_timers)]),
     "vct_tensor_core_check": (st, [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, vp]),
+    "vct_mlp_create": (st, [C.c_int32, C.c_uint64, P(vp)]),
+    "vct_mlp_destroy": (st, [vp]),
+    "vct_mlp_set_params": (st, [vp, P(C.c_float), C.c_int64]),
+    "vct_mlp_get_params": (st, [vp, P(C.c_float), C.c_int64, vp]),
+    "vct_mlp_forward": (st, [vp, vp, C.c_int64, vp, vp]),
+    "vct_mlp_gradients": (st, [vp, vp, vp, C.c_int64, vp, vp, vp]),
+    "vct_mlp_train_step": (st, [vp, vp, vp, vp, C.c_int64, P(vct_adam), vp, vp]),
+    "vct_learned_features": (st, [vp, P(vct_gbuffer), P(C.c_float), vp, vp]),
+    "vct_learned_rows": (st, [vp, P(vct_gbuffer), P(C.c_float), vp, vp, C.c_int64, vp, vp]),
+    "vct_trace_reference16": (st, [vp, P(vct_gbuffer), P(C.c_float), vp, vp]),
+    "vct_learned_trace": (st, [vp, vp, P(vct_gbuffer), P(C.c_float), C.c_float, vp, P(vct_learned_stats), vp]),
     "vct_default_tuning": (None, [P(vct_tuning)]),
     "vct_get_tuning": (st, [vp, P(vct_tuning)]),
     "vct_set_tuning": (st, [vp, P(vct_tuning)]),

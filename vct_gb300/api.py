@@ -329,6 +329,80 @@ class Batch:
         return t
 
 
+class Mlp:
+    """Owns a vct_mlp: the learned path's network (see include/vct.h)."""
+
+    NPARAMS = 11267
+
+    def __init__(self, device: int = 0, seed: int = 0):
+        self._lib = L.load()
+        h = C.c_void_p()
+        L.check(self._lib.vct_mlp_create(device, C.c_uint64(seed), C.byref(h)), "vct_mlp_create")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.vct_mlp_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self, stream=None) -> np.ndarray:
+        out = np.zeros(self.NPARAMS, dtype=np.float32)
+        L.check(self._lib.vct_mlp_get_params(self.handle, out.ctypes.data_as(C.POINTER(C.c_float)), out.size,
+                                             _stream(stream)), "vct_mlp_get_params")
+        return out
+
+    def set_params(self, p):
+        a = np.ascontiguousarray(p, dtype=np.float32)
+        L.check(self._lib.vct_mlp_set_params(self.handle, a.ctypes.data_as(C.POINTER(C.c_float)), a.size),
+                "vct_mlp_set_params")
+
+    def forward(self, rows, out, stream=None):
+        L.check(self._lib.vct_mlp_forward(self.handle, _ptr(rows), int(rows.shape[0]), _ptr(out), _stream(stream)),
+                "vct_mlp_forward")
+
+    def gradients(self, rows, targets, grad, loss=None, stream=None):
+        L.check(self._lib.vct_mlp_gradients(self.handle, _ptr(rows), _ptr(targets), int(rows.shape[0]), _ptr(grad),
+                                            _ptr(loss), _stream(stream)), "vct_mlp_gradients")
+
+    def train_step(self, rows, targets, index, n: int, lr: float, loss=None, beta1=0.9, beta2=0.999, eps=1e-8,
+                   stream=None):
+        opt = L.vct_adam(lr, beta1, beta2, eps)
+        L.check(self._lib.vct_mlp_train_step(self.handle, _ptr(rows), _ptr(targets), _ptr(index), int(n),
+                                             C.byref(opt), _ptr(loss), _stream(stream)), "vct_mlp_train_step")
+
+
+def learned_features(ctx: Context, gb, eye, features, stream=None):
+    L.check(L.load().vct_learned_features(ctx.handle, C.byref(gb), f3(eye), _ptr(features), _stream(stream)),
+            "vct_learned_features")
+
+
+def learned_rows(ctx: Context, gb, eye, features, pixels, rows, stream=None):
+    L.check(L.load().vct_learned_rows(ctx.handle, C.byref(gb), f3(eye), _ptr(features), _ptr(pixels),
+                                      int(pixels.shape[0]), _ptr(rows), _stream(stream)), "vct_learned_rows")
+
+
+def trace_reference16(ctx: Context, gb, eye, irradiance, stream=None):
+    L.check(L.load().vct_trace_reference16(ctx.handle, C.byref(gb), f3(eye), _ptr(irradiance), _stream(stream)),
+            "vct_trace_reference16")
+
+
+def learned_trace(ctx: Context, mlp: Mlp, gb, eye, irradiance, threshold: float = 0.02, want_stats: bool = False,
+                  stream=None):
+    st = L.vct_learned_stats() if want_stats else None
+    L.check(L.load().vct_learned_trace(ctx.handle, mlp.handle, C.byref(gb), f3(eye), C.c_float(threshold),
+                                       _ptr(irradiance), C.byref(st) if st is not None else None, _stream(stream)),
+            "vct_learned_trace")
+    if st is not None:
+        return {k: getattr(st, k) for k, _ in L.vct_learned_stats._fields_}
+    return None
+
+
 def tuning_dict(t: L.vct_tuning) -> dict:
     return {k: int(getattr(t, k)) for k, _ in L.vct_tuning._fields_}
 

@@ -460,6 +460,14 @@ vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], co
     return VCT_OK;
 }
 
+vct_status ensure_padded_chain(vct_ctx* c, cudaStream_t st) {
+    if (c->pad_ready) return VCT_OK;
+    launch_pad_copy(c->radiance, c->pchain, c->dim, c->levels, st);
+    VCT_CHECK_LAUNCH("bordered chain copy");
+    c->pad_ready = true;
+    return VCT_OK;
+}
+
 }  // namespace host
 }  // namespace vct
 
@@ -511,6 +519,7 @@ int64_t vct_struct_layout(const char* name) {
         VCT_OFF(vct_scene_desc, lights), VCT_OFF(vct_scene_desc, n_lights), VCT_OFF(vct_scene_desc, shadow),
         VCT_OFF(vct_scene_desc, eye),    VCT_OFF(vct_scene_desc, gbuffer),  VCT_OFF(vct_scene_desc, out),
         VCT_OFF(vct_params, trace_filter), VCT_OFF(vct_tuning, trace_warp_w),
+        VCT_SZ(vct_adam), VCT_SZ(vct_learned_stats), VCT_OFF(vct_learned_stats, max_tile_error),
     };
 #undef VCT_SZ
 #undef VCT_OFF
@@ -621,7 +630,8 @@ vct_status vct_destroy(vct_ctx* c) {
     if (c->tex_array) cudaFreeMipmappedArray(c->tex_array);
     for (auto sf : c->surf)
         if (sf) cudaDestroySurfaceObject(sf);
-    void* ptrs[] = {c->acc, c->occ, c->lit, c->color, c->normal, c->radiance, c->stats, c->vox_scratch, c->pchain};
+    void* ptrs[] = {c->acc,   c->occ,         c->lit,    c->color,  c->normal,
+                    c->radiance, c->stats, c->vox_scratch, c->pchain, c->learned};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -794,11 +804,7 @@ vct_status vct_trace(vct_ctx* c, const vct_gbuffer* g, const float eye[3], const
     if (c->params.trace_filter != VCT_FILTER_SOFTWARE && !c->tex_ready) {
         if ((s = refresh_texture(c, st)) != VCT_OK) return s;
     }
-    if (c->params.trace_filter == VCT_FILTER_SOFTWARE && !c->pad_ready) {
-        launch_pad_copy(c->radiance, c->pchain, c->dim, c->levels, st);
-        VCT_CHECK_LAUNCH("bordered chain copy");
-        c->pad_ready = true;
-    }
+    if (c->params.trace_filter == VCT_FILTER_SOFTWARE && (s = ensure_padded_chain(c, st)) != VCT_OK) return s;
     TraceParams P;
     if ((s = fill_trace(c, g, eye, out, P)) != VCT_OK) return s;
     launch_trace(P, st);

@@ -36,6 +36,8 @@ struct vct_ctx {
     float4* pchain = nullptr;  // bordered fp32 radiance chain read by the software sampler
     bool pad_ready = false;   // pchain holds the current radiance chain
     vct_tuning tuning;        // launch shapes (vct_set_tuning / vct_autotune)
+    void* learned = nullptr;  // learned-trace scratch (quarter-res features, tile errors, fallback list)
+    size_t learned_bytes = 0;
 };
 
 namespace vct {
@@ -96,6 +98,8 @@ MipLevels mip_levels(vct_ctx* ctx, uint2* chain, int levels);
 vct_status ensure_texture(vct_ctx* ctx);
 vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], const vct_trace_out* out,
                       TraceParams& P);
+// Makes the bordered fp32 chain of the software sampler current.
+vct_status ensure_padded_chain(vct_ctx* ctx, cudaStream_t s);
 
 }  // namespace host
 }  // namespace vct

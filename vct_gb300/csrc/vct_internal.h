@@ -250,6 +250,75 @@ void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks,
 void launch_mip_tail_batch(const SceneBatch<MipLevels>& B, cudaStream_t s);
 long long trace_tiles(int width, int height, int tile_w_log2, int tile_h_log2);
 void launch_trace_batch(const SceneBatch<TraceParams>& B, int filter, long long tiles, cudaStream_t s);
+// ------------------------------------------------------------- learned path
+// MLP 42-64-64-64-3.  Packed fp32 parameters: W1[64][42] b1[64] W2[64][64]
+// b2[64] W3[64][64] b3[64] W4[3][64] b4[3].
+constexpr int kMlpIn = 42, kMlpInPad = 48, kMlpHidden = 64, kMlpOut = 3, kMlpOutPad = 16;
+constexpr int kOffW1 = 0, kOffB1 = 2688, kOffW2 = 2752, kOffB2 = 6848, kOffW3 = 6912, kOffB3 = 11008,
+              kOffW4 = 11072, kOffB4 = 11264, kMlpParams = 11267;
+// BF16 operand images in the tensor core's shared-memory tile layout:
+// forward B operands W1 (64 x 48), W2, W3 (64 x 64), W4 (16 x 64), then the
+// transposes used by the backward pass W4^T (64 x 16), W3^T, W2^T (64 x 64).
+constexpr int kImgW1 = 0, kImgW2 = 6144, kImgW3 = 14336, kImgW4 = 22528, kImgFwd = 24576, kImgW4t = 24576,
+              kImgW3t = 26624, kImgW2t = 34816, kImgAll = 43008;
+// Bias vector padded for the kernels: b1 | b2 | b3 | b4 (16).
+constexpr int kBiasPad = 208;
+// Quarter-resolution cheap trace: 2 cones x 4 levels x RGBA, BF16.
+constexpr int kCheapFeatures = 32;
+// Per-tile error probes of the learned trace and its 16 x 16 tiles.
+constexpr int kProbes = 4, kLearnTile = 16;
+
+struct MlpDev {
+    float* params;  // fp32 master
+    float* grad;
+    float* m;
+    float* v;
+    uint8_t* img;   // kImgAll bytes
+    float* bias;    // kBiasPad floats
+    float* loss;
+};
+
+struct LearnedParams {
+    TraceParams T;             // G-buffer, eye, volume, software sampler chain
+    const uint16_t* qfeat;     // quarter-res features, kCheapFeatures bf16 per quarter pixel
+    int wq, hq;
+    float depth_scale;         // 1 / volume extent
+    float dirs16[16][4];       // 16-cone set in the (T, B, N) frame: xyz + weight
+    vct_cone_settings ref_cone;
+    const uint8_t* img;
+    const float* bias;
+    const float* rows;         // feature rows (vct_mlp_forward), or nullptr: pixels of the frame
+    long long n;               // rows or pixels
+    float* out_rows;           // n x 3
+    float4* out;               // irradiance per pixel
+    const int* pixels;         // rows kernel: pixel indices
+    float* rows_out;           // rows kernel: n x 42
+    float threshold;           // per-tile relative error bound
+    float* tile_err;           // per 16x16 tile
+    uint32_t* list;            // fallback tiles; list[-1] is not used: count at `count`
+    uint32_t* count;
+    uint32_t* status;
+};
+
+struct TrainParams {
+    MlpDev mlp;
+    const float* rows;     // n x 42
+    const float* targets;  // n x 3
+    const int* index;      // optional permutation of rows
+    long long n;
+    float scale;           // 2 / (3 n)
+    uint32_t* status;
+};
+
+void launch_learned_features(const LearnedParams& P, cudaStream_t s);
+void launch_learned_rows(const LearnedParams& P, cudaStream_t s);
+void launch_mlp_infer(const LearnedParams& P, int num_sms, cudaStream_t s);
+void launch_learned_probe(const LearnedParams& P, cudaStream_t s);
+void launch_trace16(const LearnedParams& P, bool listed, int num_sms, cudaStream_t s);
+void launch_mlp_train(const TrainParams& P, int num_sms, cudaStream_t s);
+void launch_mlp_update(const MlpDev& M, int step, float lr, float beta1, float beta2, float eps, int update,
+                       cudaStream_t s);
+
 // Tensor-core GEMM check: D (128 x n, fp32) = A (128 x k) B^T (n x k), bf16.
 void launch_umma_check(const uint16_t* A, const uint16_t* B, int K, int N, int swap, float* D, uint32_t* status,
                        cudaStream_t s);

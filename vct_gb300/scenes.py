@@ -337,6 +337,60 @@ def batch_scene(seed: int = 0, index: int = 0, shadow: int = 1024) -> Scene:
                    np.zeros(3), 55 * DEG, gsize, BASELINE_CONES)
 
 
+def _cylinders(radius, y0, y1, cx, cz, segments):
+    """_cylinder for many columns at once (same triangle order)."""
+    a = np.arange(segments + 1) * (2 * np.pi / segments)
+    x, z = np.cos(a), np.sin(a)
+    C = len(radius)
+    bx = cx[:, None] + radius[:, None] * x[None]
+    bz = cz[:, None] + radius[:, None] * z[None]
+    b = np.stack([bx, np.full_like(bx, y0), bz], -1)
+    t = np.stack([bx, np.full_like(bx, y1), bz], -1)
+    n = np.broadcast_to(np.stack([x, np.zeros_like(x), z], -1), (C, segments + 1, 3))
+    k0, k1 = slice(0, segments), slice(1, segments + 1)
+    tri1 = np.stack([b[:, k0], t[:, k1], b[:, k1]], 2)
+    nrm1 = np.stack([n[:, k0], n[:, k1], n[:, k1]], 2)
+    tri2 = np.stack([b[:, k0], t[:, k0], t[:, k1]], 2)
+    nrm2 = np.stack([n[:, k0], n[:, k0], n[:, k1]], 2)
+    return np.stack([tri1, tri2], 2).reshape(-1, 3, 3), np.stack([nrm1, nrm2], 2).reshape(-1, 3, 3)
+
+
+def large_family(seed: int = 0, dim: int = 256, shadow: int = 2048, gbuffer=(1920, 1080), n_boxes: int = 4096,
+                 n_cyl: int = 64, cyl_segments: int = 1664, orbit: bool = True) -> Scene:
+    """The large plain frame's family, generated with vectorised draws: the
+    same box / column / light distributions as large() (which it does not
+    reproduce draw for draw), and with `orbit` a camera at a random azimuth
+    and height around the volume.  Used for the learned path's training and
+    held-out scenes."""
+    rng = np.random.default_rng((seed, 7))
+    extent = 2.0
+    lo, hi = np.log(0.01 * extent), np.log(0.2 * extent)
+    size = np.exp(rng.uniform(lo, hi, size=(n_boxes, 3)))
+    center = rng.uniform(-0.9, 0.9, size=(n_boxes, 3))
+    yaw = rng.uniform(0, 2 * np.pi, size=n_boxes)
+    bt, bn = _boxes(size, center, yaw)
+    balb = np.repeat(rng.uniform(0, 1, size=(n_boxes, 3)), 12, 0)
+    radius = 0.5 * np.exp(rng.uniform(lo, hi, size=n_cyl))
+    cxz = rng.uniform(-0.9, 0.9, size=(n_cyl, 2))
+    ct, cn = _cylinders(radius, -0.95, 0.95, cxz[:, 0], cxz[:, 1], cyl_segments)
+    calb = np.repeat(rng.uniform(0, 1, size=(n_cyl, 3)), 2 * cyl_segments, 0)
+    light, ls = _directional_light(rng, 1.0)
+    lights = [light]
+    for _ in range(4):
+        lights.append(dict(position=rng.uniform(-0.9, 0.9, size=3), direction=np.array([0.0, -1.0, 0.0]),
+                           color=rng.uniform(0.5, 1.0, size=3), range=float(rng.uniform(0.3, 0.8)), intensity=1.0,
+                           shadow_caster=0, type=0))
+    if orbit:
+        phi = rng.uniform(0, 2 * np.pi)
+        eye = np.array([2.8 * np.sin(phi), rng.uniform(0.2, 1.0), 2.8 * np.cos(phi)])
+    else:
+        eye = np.array([0.0, 0.5, 2.8])
+    levels = int(np.log2(dim)) + 1
+    return _finish(f"family{seed}", np.concatenate([bt, ct]), np.concatenate([bn, cn]), np.concatenate([balb, calb]),
+                   lights, ls, dim, levels, 1.0, (shadow, shadow), eye, np.zeros(3), 55 * DEG, tuple(gbuffer),
+                   BASELINE_CONES)
+
+
 SCENES = {"cornell": cornell, "large": large, "tiny": tiny}
 
 
