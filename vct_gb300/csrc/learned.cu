@@ -47,7 +47,10 @@ __global__ void __launch_bounds__(128) umma_check_kernel(const uint16_t* __restr
         mbar_init(smem_u32(&mbar), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) tmem_alloc(smem_u32(&tmem_base), 64);
+    if (warp == 0) {
+        tmem_alloc(smem_u32(&tmem_base), 64);
+        tmem_relinquish();
+    }
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
@@ -300,41 +303,71 @@ __global__ void __launch_bounds__(256) trace16_kernel(const LearnedParams P, int
 // Per-tile error estimate of the network's output: the 16-cone irradiance at
 // four probe pixels of each 16x16 tile (offsets 4 and 12 on each axis) against
 // the network, relative L2 over the covered probes.  Tiles above the bound
-// are listed for the 16-cone fallback.
-__global__ void __launch_bounds__(128) learned_probe_kernel(const LearnedParams P) {
+// are listed for the 16-cone fallback.  One thread per (tile, probe, cone):
+// a warp holds two probes' 16 cones, two warps a tile.
+constexpr int kProbeThreads = 256;  // 4 tiles per CTA
+
+__global__ void __launch_bounds__(kProbeThreads) learned_probe_kernel(const LearnedParams P) {
     __shared__ int s_off[VCT_MAX_LEVELS];
     __shared__ float s_dirs[16][4];
+    __shared__ float s_part[kProbeThreads / 32][2];
     level_offsets(P.T, s_off);
     load_dirs(P, s_dirs);
     __syncthreads();
     const TraceParams& T = P.T;
     const int tiles_x = (T.width + kLearnTile - 1) / kLearnTile;
     const long long ntiles = (long long)tiles_x * ((T.height + kLearnTile - 1) / kLearnTile);
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long tile = g / kProbes;
-    const int pr = (int)(g % kProbes);
-    float se = 0.0f, st = 0.0f;
+    const long long tile = (long long)blockIdx.x * (kProbeThreads / 64) + (threadIdx.x >> 6);
+    const int pr = (threadIdx.x >> 4) & 3, c = threadIdx.x & 15;
+    float4 rc = make_float4(0.f, 0.f, 0.f, 0.f);
+    long long pix = -1;
     unsigned ns = 0;
     if (tile < ntiles) {
         const int x = (int)(tile % tiles_x) * kLearnTile + ((pr & 1) ? 12 : 4);
         const int y = (int)(tile / tiles_x) * kLearnTile + ((pr & 2) ? 12 : 4);
         if (x < T.width && y < T.height) {
-            const long long pix = (long long)y * T.width + x;
-            const float4 gp = __ldg(T.gpos + pix);
+            const long long p = (long long)y * T.width + x;
+            const float4 gp = __ldg(T.gpos + p);
             if (gp.w != 0.0f) {
-                const float4 r = irradiance16(P, s_off, s_dirs, gp, __ldg(T.gnrm + pix), ns);
-                const float4 o = P.out[pix];
-                const float dx = o.x - r.x, dy = o.y - r.y, dz = o.z - r.z;
-                se = dx * dx + dy * dy + dz * dz;
-                st = r.x * r.x + r.y * r.y + r.z * r.z;
+                pix = p;
+                const float4 gn = __ldg(T.gnrm + p);
+                const f3 N = cone::fnormalize(mk(gn.x, gn.y, gn.z));
+                f3 Tg, Bg;
+                onb(N, Tg, Bg);
+                const f3 vp = volume_coord(T, gp);
+                const f3 d = add(add(mul(Tg, s_dirs[c][0]), mul(Bg, s_dirs[c][1])), mul(N, s_dirs[c][2]));
+                const float4 cr = cone::trace_cone<VCT_FILTER_SOFTWARE>(T, s_off, vp, N, d, P.ref_cone, T.max_distance, ns);
+                const float w = s_dirs[c][3];
+                rc = make_float4(w * cr.x, w * cr.y, w * cr.z, 0.0f);
             }
         }
     }
-    se += __shfl_xor_sync(0xffffffffu, se, 1);
-    se += __shfl_xor_sync(0xffffffffu, se, 2);
-    st += __shfl_xor_sync(0xffffffffu, st, 1);
-    st += __shfl_xor_sync(0xffffffffu, st, 2);
-    if (pr == 0 && tile < ntiles) {
+    // irradiance of the probe: the sum over its 16 lanes (an estimate: the
+    // order differs from the 16-cone trace's sequential accumulation)
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) {
+        rc.x += __shfl_xor_sync(0xffffffffu, rc.x, o);
+        rc.y += __shfl_xor_sync(0xffffffffu, rc.y, o);
+        rc.z += __shfl_xor_sync(0xffffffffu, rc.z, o);
+    }
+    float se = 0.0f, st = 0.0f;
+    if (c == 0 && pix >= 0) {
+        const float4 o = P.out[pix];
+        const float dx = o.x - rc.x, dy = o.y - rc.y, dz = o.z - rc.z;
+        se = dx * dx + dy * dy + dz * dz;
+        st = rc.x * rc.x + rc.y * rc.y + rc.z * rc.z;
+    }
+    se += __shfl_xor_sync(0xffffffffu, se, 16);
+    st += __shfl_xor_sync(0xffffffffu, st, 16);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_part[w][0] = se;
+        s_part[w][1] = st;
+    }
+    __syncthreads();
+    if ((threadIdx.x & 63) == 0 && tile < ntiles) {
+        se = s_part[w][0] + s_part[w + 1][0];
+        st = s_part[w][1] + s_part[w + 1][1];
         const float err = st > 0.0f ? sqrtf(se / st) : (se > 0.0f ? 1.0e30f : 0.0f);
         P.tile_err[tile] = err;
         if (err > P.threshold) P.list[atomicAdd(P.count, 1u)] = (uint32_t)tile;
@@ -342,98 +375,120 @@ __global__ void __launch_bounds__(128) learned_probe_kernel(const LearnedParams 
 }
 
 // ------------------------------------------------------- MLP inference
-// Persistent CTAs of 128 threads; a tile is 128 pixels (or rows), one per
-// thread and per TMEM lane.  Per layer: the features / activations of the
-// tile are the A operand (128 x K, BF16) in shared memory, the layer's weights
-// the B operand, one elected thread issues the K/16 MMAs into a 64-column
-// FP32 accumulator in TMEM and commits to an mbarrier; every thread then
-// loads its row, adds the bias, applies ReLU and writes the BF16 row back as
-// the next layer's A operand.
-constexpr int kInferSmem = kImgFwd + 128 * kMlpHidden * 2;
+// A CTA holds the forward weights once in shared memory and runs kInferGroups
+// independent groups of four warps; a group owns a 128-pixel tile (one pixel
+// per thread and per TMEM lane) and its own 64 TMEM columns, A-operand tile
+// and mbarrier, and synchronises on its own named barrier, so the groups'
+// MMA chains and epilogues interleave on the SM.  Per layer the group's
+// elected thread issues the K/16 MMAs (A = the tile's BF16 activations,
+// B = the layer's weights) into the FP32 accumulator and commits to the
+// group's mbarrier; every thread then loads its row, adds the bias, applies
+// ReLU and writes the BF16 row back as the next layer's A operand.  The
+// features of the group's next tile are gathered while its first MMA runs.
+constexpr int kInferGroups = 2;
+constexpr int kInferThreads = 128 * kInferGroups;
+constexpr int kInferTile = 128 * kMlpHidden * 2;
+constexpr int kInferSmem = kImgFwd + kInferGroups * kInferTile;
 
 template <bool ROWS>
-__global__ void __launch_bounds__(128) mlp_infer_kernel(const LearnedParams P) {
+__device__ __forceinline__ bool gather_features(const LearnedParams& P, long long idx, uint32_t (&f)[24]) {
+#pragma unroll
+    for (int i = 0; i < 24; ++i) f[i] = 0u;
+    if (idx >= P.n) return false;
+    if (ROWS) {
+        const float2* r = reinterpret_cast<const float2*>(P.rows + idx * kMlpIn);
+#pragma unroll
+        for (int i = 0; i < kMlpIn / 2; ++i) {
+            const float2 v = __ldg(r + i);
+            f[i] = bf16x2(v.x, v.y);
+        }
+        return true;
+    }
+    const float4 gp = __ldg(P.T.gpos + idx);
+    if (gp.w == 0.0f) return false;
+    pixel_features(P, idx, gp, f);
+    return true;
+}
+
+template <bool ROWS>
+__global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const LearnedParams P) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ float s_bias[kBiasPad];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[kInferGroups];
     __shared__ uint32_t s_tmem;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    uint8_t* sw = smem;
-    uint8_t* sa = smem + kImgFwd;
-    for (int i = tid; i < kImgFwd / 16; i += 128)
-        reinterpret_cast<uint4*>(sw)[i] = __ldg(reinterpret_cast<const uint4*>(P.img) + i);
-    for (int i = tid; i < kBiasPad; i += 128) s_bias[i] = P.bias[i];
-    if (tid == 0) {
-        mbar_init(smem_u32(&mbar), 1);
-        fence_mbar_init();
+    __shared__ int s_done[kInferGroups];
+    const int tid = threadIdx.x, warp = tid >> 5, grp = warp >> 2, row = tid & 127;
+    for (int i = tid; i < kImgFwd / 16; i += kInferThreads)
+        reinterpret_cast<uint4*>(smem)[i] = __ldg(reinterpret_cast<const uint4*>(P.img) + i);
+    for (int i = tid; i < kBiasPad; i += kInferThreads) s_bias[i] = P.bias[i];
+    if (tid < kInferGroups) mbar_init(smem_u32(&mbar[tid]), 1);
+    if (tid == 0) fence_mbar_init();
+    if (warp == 0) {
+        tmem_alloc(smem_u32(&s_tmem), 64 * kInferGroups);
+        tmem_relinquish();  // lets the SM's other CTAs allocate
     }
-    if (warp == 0) tmem_alloc(smem_u32(&s_tmem), 64);
     fence_async_smem();
     tc_sync();
-    const uint32_t tm = s_tmem, a0 = smem_u32(sa), w0 = smem_u32(sw), mb = smem_u32(&mbar);
+    uint8_t* sa = smem + kImgFwd + grp * kInferTile;
+    const uint32_t tm = s_tmem + 64u * grp, a0 = smem_u32(sa), w0 = smem_u32(smem), mb = smem_u32(&mbar[grp]);
+    const int bar = 1 + grp;
+    const bool leader = row == 0;
+    auto group_sync = [&]() {
+        fence_before_sync();
+        named_sync(bar, 128);
+        fence_after_sync();
+    };
     const long long ntiles = (P.n + 127) / 128;
+    const long long stride = (long long)gridDim.x * kInferGroups;
     uint32_t phase = 0;
     int ok = 1;
-    for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        const long long idx = t * 128 + tid;
-        const bool valid = idx < P.n;
-        bool covered = false;
-        uint32_t f[24];
-#pragma unroll
-        for (int i = 0; i < 24; ++i) f[i] = 0u;
-        if (valid) {
-            if (ROWS) {
-                const float2* r = reinterpret_cast<const float2*>(P.rows + idx * kMlpIn);
-#pragma unroll
-                for (int i = 0; i < kMlpIn / 2; ++i) {
-                    const float2 v = __ldg(r + i);
-                    f[i] = bf16x2(v.x, v.y);
-                }
-                covered = true;
-            } else {
-                const float4 gp = __ldg(P.T.gpos + idx);
-                covered = gp.w != 0.0f;
-                if (covered) pixel_features(P, idx, gp, f);
-            }
-        }
+    long long t = (long long)blockIdx.x * kInferGroups + grp;
+    uint32_t f[24];
+    bool covered = gather_features<ROWS>(P, t * 128 + row, f);
+    for (; t < ntiles && ok; t += stride) {
+        const long long idx = t * 128 + row;
+        const bool valid = idx < P.n, cov = covered;
 #pragma unroll
         for (int c = 0; c < 6; ++c)
-            *reinterpret_cast<uint4*>(sa + tile_offset(tid, 8 * c, 128)) =
+            *reinterpret_cast<uint4*>(sa + tile_offset(row, 8 * c, 128)) =
                 make_uint4(f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3]);
         fence_async_smem();
-        tc_sync();
+        group_sync();
         float o0 = 0.f, o1 = 0.f, o2 = 0.f;
 #pragma unroll 1
         for (int layer = 0; layer < 4; ++layer) {
             const int K = layer == 0 ? kMlpInPad : kMlpHidden;
             const int N = layer == 3 ? kMlpOutPad : kMlpHidden;
             const uint32_t b = w0 + (layer == 0 ? kImgW1 : layer == 1 ? kImgW2 : layer == 2 ? kImgW3 : kImgW4);
-            int done = 1;
-            if (tid == 0) {
+            if (leader) {
                 const uint32_t id = idesc_bf16_f32(128, N);
                 for (int j = 0; j < K / 16; ++j) mma_bf16(tm, tile_desc(a0, 128, j), tile_desc(b, N, j), id, j > 0);
                 commit(mb);
-                done = mbar_wait(mb, phase) ? 1 : 0;
             }
+            // the next tile's features load while the first layer runs
+            if (layer == 0) covered = gather_features<ROWS>(P, (t + stride) * 128 + row, f);
+            if (leader) s_done[grp] = mbar_wait(mb, phase) ? 1 : 0;
             phase ^= 1u;
-            ok = __syncthreads_and(done);
-            fence_after_sync();
+            group_sync();
+            ok = s_done[grp];
             if (!ok) break;
             if (layer < 3) {
                 const float* bb = s_bias + kMlpHidden * layer;
 #pragma unroll
-                for (int c = 0; c < kMlpHidden; c += 16) {
-                    float v[16];
-                    tmem_ld16(tmem_addr(tm, warp, c), v);
-                    uint32_t pk[8];
+                for (int c = 0; c < kMlpHidden; c += 32) {
+                    float v[32];
+                    tmem_ld32(tmem_addr(tm, warp, c), v);
+                    uint32_t pk[16];
 #pragma unroll
-                    for (int i = 0; i < 8; ++i)
+                    for (int i = 0; i < 16; ++i)
                         pk[i] = bf16x2(fmaxf(v[2 * i] + bb[c + 2 * i], 0.0f), fmaxf(v[2 * i + 1] + bb[c + 2 * i + 1], 0.0f));
-                    *reinterpret_cast<uint4*>(sa + tile_offset(tid, c, 128)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                    *reinterpret_cast<uint4*>(sa + tile_offset(tid, c + 8, 128)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        *reinterpret_cast<uint4*>(sa + tile_offset(row, c + 8 * q, 128)) =
+                            make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
                 }
                 fence_async_smem();
-                tc_sync();
+                group_sync();
             } else {
                 float v[16];
                 tmem_ld16(tmem_addr(tm, warp, 0), v);
@@ -449,13 +504,13 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const LearnedParams P) {
                 P.out_rows[idx * 3 + 1] = o1;
                 P.out_rows[idx * 3 + 2] = o2;
             } else {
-                P.out[idx] = covered ? make_float4(o0, o1, o2, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+                P.out[idx] = cov ? make_float4(o0, o1, o2, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
     }
-    if (!ok && tid == 0) atomicOr(P.status, 1u);
+    if (!ok && leader) atomicOr(P.status, 1u);
     tc_sync();
-    if (warp == 0) tmem_dealloc(tm, 64);
+    if (warp == 0) tmem_dealloc(s_tmem, 64 * kInferGroups);
 }
 
 // ------------------------------------------------------- MLP training
@@ -514,7 +569,10 @@ __global__ void __launch_bounds__(128, 1) mlp_train_kernel(const TrainParams P) 
         mbar_init(smem_u32(&mbar), 1);
         fence_mbar_init();
     }
-    if (warp == 0) tmem_alloc(smem_u32(&s_tmem), 512);
+    if (warp == 0) {
+        tmem_alloc(smem_u32(&s_tmem), 512);
+        tmem_relinquish();
+    }
     fence_async_smem();
     tc_sync();
     const uint32_t tm = s_tmem, mb = smem_u32(&mbar), w0 = smem_u32(smem + kTrW);
@@ -774,14 +832,15 @@ void launch_learned_rows(const LearnedParams& P, cudaStream_t s) {
 void launch_mlp_infer(const LearnedParams& P, int num_sms, cudaStream_t s) {
     if (P.n <= 0) return;
     const long long tiles = (P.n + 127) / 128;
-    // Up to four 40 KB CTAs per SM (4 x 64 TMEM columns).
-    const long long grid = tiles < (long long)num_sms * 4 ? tiles : (long long)num_sms * 4;
+    // Three CTAs per SM (3 x 57 KB of shared memory, 3 x 128 TMEM columns).
+    const long long groups = (long long)num_sms * 3 * kInferGroups;
+    const long long grid = (tiles < groups ? tiles + kInferGroups - 1 : groups) / kInferGroups;
     if (P.rows) {
         cudaFuncSetAttribute(mlp_infer_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem);
-        mlp_infer_kernel<true><<<(unsigned)grid, 128, kInferSmem, s>>>(P);
+        mlp_infer_kernel<true><<<(unsigned)grid, kInferThreads, kInferSmem, s>>>(P);
     } else {
         cudaFuncSetAttribute(mlp_infer_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem);
-        mlp_infer_kernel<false><<<(unsigned)grid, 128, kInferSmem, s>>>(P);
+        mlp_infer_kernel<false><<<(unsigned)grid, kInferThreads, kInferSmem, s>>>(P);
     }
     note_launches(1);
 }
@@ -789,15 +848,16 @@ void launch_mlp_infer(const LearnedParams& P, int num_sms, cudaStream_t s) {
 void launch_learned_probe(const LearnedParams& P, cudaStream_t s) {
     const long long tiles = (long long)((P.T.width + kLearnTile - 1) / kLearnTile) *
                             ((P.T.height + kLearnTile - 1) / kLearnTile);
-    learned_probe_kernel<<<(unsigned)((tiles * kProbes + 127) / 128), 128, 0, s>>>(P);
+    learned_probe_kernel<<<(unsigned)((tiles + kProbeThreads / 64 - 1) / (kProbeThreads / 64)), kProbeThreads, 0, s>>>(P);
     note_launches(1);
 }
 
 void launch_trace16(const LearnedParams& P, bool listed, int num_sms, cudaStream_t s) {
     const long long tiles = (long long)((P.T.width + kLearnTile - 1) / kLearnTile) *
                             ((P.T.height + kLearnTile - 1) / kLearnTile);
-    const long long cap = (long long)num_sms * 3;
-    const long long grid = listed ? cap : (tiles < cap * 8 ? tiles : cap * 8);
+    // Persistent over the listed tiles: as many CTAs as fit (8 per SM).
+    const long long cap = (long long)num_sms * 8;
+    const long long grid = listed ? cap : (tiles < cap * 4 ? tiles : cap * 4);
     trace16_kernel<<<(unsigned)(grid > 0 ? grid : 1), 256, 0, s>>>(P, listed ? 1 : 0);
     note_launches(1);
 }
