@@ -172,16 +172,18 @@ def algorithmic_bytes(sc, stats, launches_per_frame):
     SW, SH = sc.shadow_size
     F = stats["total_voxel_fragments"]
     U = stats["unique_voxels"]
-    mip_tail = sum((N >> l) ** 3 for l in range(5, sc.levels))
+    lv = lambda a, b: sum((N >> l) ** 3 for l in range(a, min(b, sc.levels)))  # noqa: E731
     return {
-        # triangles in (pos, normal, albedo), 7 x 4 B accumulator read-modify-write per fragment
+        # triangles in (positions, normals, albedo); 7 accumulator words read-modify-written per fragment
         "accumulate": T * (36 + 36 + 12) + F * 7 * 4 * 2,
-        # shadow map read, lit bit set per texel (bit mask write once)
+        # shadow map read, lit bit set per texel (bit mask written once)
         "inject_mark": SW * SH * 4 + nv // 8,
-        # counts read; sums read+cleared for occupied voxels; colour, normal, radiance L0 written; lit mask read;
-        # levels 1..4 written
-        "resolve": nv * 4 + U * 7 * 4 * 2 + nv * 8 * 3 + nv // 8 + sum((N >> l) ** 3 for l in range(1, 5)) * 8,
-        "mip_tail": (N >> 4) ** 3 * 8 + mip_tail * 8,
+        # occupancy and lit masks read; records of occupied voxels read and zeroed; colour, normal,
+        # radiance level 0 written (RGBA16F); radiance levels 1-4 written; the software sampler's
+        # bordered fp32 copy of levels 0-4 written (interiors)
+        "resolve": nv // 8 * 2 + U * 32 * 2 + nv * 8 * 3 + lv(1, 5) * 8 + lv(0, 5) * 16,
+        # level 4 read, levels 5.. written (RGBA16F and the bordered fp32 copy)
+        "mip_tail": (N >> 4) ** 3 * 8 + lv(5, 99) * (8 + 16),
         # G-buffer (3 float4) read, composite float4 written
         "trace": P * (48 + 16),
     }
@@ -641,9 +643,10 @@ def run_learned(args, rank, world):
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each frame
-# stage, from one ncu --set full capture of the large frame (summarised under
-# profiles/); only meaningful for --config large.
-NCU_TRAFFIC = {"accumulate": 504.0e6, "resolve+mips": 1001.8e6, "trace": 88.4e6}
+# stage, from one ncu capture of the large frame (profiles/kernels_large_frame.md):
+# accumulate = setup + raster, resolve+mips = resolve + tail; only for --config large.
+NCU_TRAFFIC = {"accumulate": 18.9e6 + 556.1e6, "resolve+mips": 1156.6e6 + 0.05e6, "inject_mark": 18.2e6,
+               "trace": 95.8e6}
 
 
 def load_peaks() -> dict:
