@@ -108,6 +108,23 @@ typedef struct vct_cone_settings {
 #define VCT_FILTER_HARDWARE 1 /* texture units' trilinear-mip filtering */
 #define VCT_FILTER_HARDWARE_LEVELS 2 /* texture units' trilinear filtering per level, levels blended in fp32 */
 
+/* Voxel warping: positions in [0,1]^3 volume coordinates are remapped before
+ * they index or sample the grid, in the voxeliser (voxelize.frag:100-106),
+ * injection (getVoxelPosition) and the cone tracer (phong.frag:150-157).
+ *  - ANALYTIC (warpVoxels): voxelWarp about the eye, a cubic per axis
+ *    (common.glsl:11-31).
+ *  - TEXTURE (warpTexture): a 32^3 warp map built every voxelisation from a
+ *    32^3 occupancy voxelisation of the same triangles: per axis, occupied
+ *    warp cells get warp_high_resolution and empty ones a resolution that
+ *    keeps each row's total (Application.cpp:346-371), the weights stored as
+ *    binary16 (the RGBA16F weight textures), cell centres warped by the
+ *    prefix sums of the widths (generateWarpmap.frag), stored RGBA16 unorm
+ *    and read with trilinear filtering and clamp-to-edge. */
+#define VCT_WARP_NONE 0
+#define VCT_WARP_ANALYTIC 1
+#define VCT_WARP_TEXTURE 2
+#define VCT_WARP_DIM 32
+
 /* Every hot-path uniform of the reference, with vct_default_params giving the
  * reference defaults of src/Application.h:36-103. */
 typedef struct vct_params {
@@ -133,6 +150,10 @@ typedef struct vct_params {
     float max_distance;          /* cone length limit in texture units; <= 0: grid diagonal */
     int32_t ref_tbn_quirk;       /* 1: map the cone set's y axis to the bitangent as phong.vert's TBN does */
     int32_t trace_filter;        /* VCT_FILTER_* */
+    /* voxel warping (common.glsl:11-64, generateWarpmap.frag, Application.cpp:300-580) */
+    int32_t warp_mode;           /* VCT_WARP_* (warpVoxels / warpTexture; default none) */
+    float warp_high_resolution;  /* warpTextureHighResolution (2.0) */
+    float warp_low_resolution;   /* warpTextureLowResolution (0.5) */
 } vct_params;
 
 /* Caller-owned triangle soup on the device. */
@@ -268,6 +289,10 @@ vct_status vct_get_stats(vct_ctx* ctx, vct_stats* out, void* stream);
 vct_status vct_enable_timers(vct_ctx* ctx, int32_t enable);
 /* Waits for the last timed vct_frame and returns its stage times. */
 vct_status vct_get_timers(vct_ctx* ctx, vct_timers* out);
+/* The warp map of the last voxelisation with VCT_WARP_TEXTURE: 32^3 texels,
+ * x fastest, RGBA16 unorm (xyz = warped coordinate * 65535, w = the packed
+ * cell information of generateWarpmap.frag). */
+vct_status vct_warpmap(const vct_ctx* ctx, const uint16_t** map_dev);
 /* Number of kernels this library has launched since it was loaded. */
 uint64_t vct_launch_count(void);
 

@@ -47,6 +47,10 @@ class orc_trace_params(C.Structure):
                 ("ref_tbn_quirk", C.c_int32)]
 
 
+class orc_warp(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("map", C.c_void_p), ("eye_tc", C.c_float * 3)]
+
+
 class orc_stats(C.Structure):
     _fields_ = [("total_voxel_fragments", C.c_uint32), ("unique_voxels", C.c_uint32),
                 ("max_fragments_per_voxel", C.c_uint32), ("error_flags", C.c_uint32)]
@@ -134,8 +138,38 @@ def voxel_mvp(scene) -> np.ndarray:
     return out
 
 
+def warp(scene, mode: int = 0, warpmap: np.ndarray | None = None):
+    """orc_warp of a scene: mode 1 warps about the eye (warpVoxels), mode 2
+    reads `warpmap` (32^3 x 4 uint16, from warpmap()).  The struct keeps a
+    reference to the map."""
+    w = orc_warp()
+    w.mode = int(mode)
+    if warpmap is not None:
+        w._map = np.ascontiguousarray(warpmap, dtype=np.uint16)
+        w.map = w._map.ctypes.data
+    # voxelLinearPosition(eye) in fp32: ((eye - center) - min) / (max - min)
+    e = np.asarray(scene.eye, dtype=np.float32)
+    vmin, ext = np.float32(-scene.vmax), np.float32(2 * scene.vmax)
+    w.eye_tc = _f([((e[k] - np.float32(0.0)) - vmin) / ext for k in range(3)], 3)
+    return w
+
+
+def warpmap(occupancy: np.ndarray, high: float = 2.0, low: float = 0.5) -> np.ndarray:
+    """The 32^3 warp map (32^3 x 4 uint16) of a 32^3 occupancy grid."""
+    occ = np.ascontiguousarray(np.asarray(occupancy).reshape(-1) != 0, dtype=np.uint8)
+    out = np.zeros(32 ** 3 * 4, dtype=np.uint16)
+    load().orc_warpmap(_p(occ), C.c_float(high), C.c_float(low), _p(out))
+    return out
+
+
+def warp_occupancy(scene, shadowmap: np.ndarray, nthreads: int = 1) -> np.ndarray:
+    """The 32^3 occupancy voxelisation of the scene (bool per cell)."""
+    count, _, _ = voxelize(scene, shadowmap, lighting=0, nthreads=nthreads, dim=32)
+    return count > 0
+
+
 def voxelize(scene, shadowmap: np.ndarray, lighting: int = 1, axis_override: int = -1, nthreads: int = 1,
-             positions=None, normals=None, albedo=None, dim: int | None = None):
+             positions=None, normals=None, albedo=None, dim: int | None = None, warp=None):
     """Returns (count[N^3] u32, sums[6*N^3] u32, total_fragments)."""
     N = int(dim or scene.dim)
     pos = np.ascontiguousarray(scene.positions if positions is None else positions, dtype=np.float32)
@@ -150,7 +184,7 @@ def voxelize(scene, shadowmap: np.ndarray, lighting: int = 1, axis_override: int
     sw, sh = scene.shadow_size
     load().orc_voxelize(C.byref(v), _p(pos), _p(nrm), _p(alb), C.c_int64(pos.shape[0]), arr, n, lighting,
                         axis_override, _p(sm), sw, sh, _f(scene.ls, 16), _p(count), _p(sums), C.byref(total),
-                        nthreads)
+                        nthreads, C.byref(warp) if warp is not None else None)
     return count, sums, int(total.value)
 
 
@@ -172,13 +206,14 @@ def normalize(scene, count, sums, opacity=0.5, temporal=0, decay=0.8, radiance=N
     return color, normal, rad, stats
 
 
-def inject(scene, shadowmap, color, normal, radiance, lighting=0, dilate=0, nthreads=1, dim=None):
+def inject(scene, shadowmap, color, normal, radiance, lighting=0, dilate=0, nthreads=1, dim=None, warp=None):
     N = int(dim or scene.dim)
     v = volume(scene, N)
     sw, sh = scene.shadow_size
     sm = np.ascontiguousarray(shadowmap, dtype=np.float32)
     load().orc_inject(C.byref(v), _p(sm), sw, sh, _f(scene.ls_inverse, 16), _f(scene.light_pos, 3),
-                      _f(scene.light_int, 3), lighting, dilate, _p(color), _p(normal), _p(radiance), nthreads)
+                      _f(scene.light_int, 3), lighting, dilate, _p(color), _p(normal), _p(radiance), nthreads,
+                      C.byref(warp) if warp is not None else None)
     return radiance
 
 
@@ -200,7 +235,8 @@ def build_mips(dim: int, levels: int, chain: np.ndarray, nthreads: int = 1) -> n
 
 
 def trace(scene, chain, gpos, gnrm, galb, precision=32, rows=None, row_step=1, nthreads=1, want=("irr", "spec",
-                                                                                                  "color"), **over):
+                                                                                                  "color"), warp=None,
+          **over):
     W, H = scene.gbuffer_size
     r0, r1 = rows if rows is not None else (0, H)
     tp = trace_params(scene, **over)
@@ -210,7 +246,8 @@ def trace(scene, chain, gpos, gnrm, galb, precision=32, rows=None, row_step=1, n
     col = np.zeros((H * W * 4,), dtype=np.float32) if "color" in want else None
     samples = C.c_uint64(0)
     load().orc_trace(C.byref(v), scene.levels, _p(chain), C.byref(tp), _p(gpos), _p(gnrm), _p(galb), W, H, r0, r1,
-                     row_step, _f(scene.eye, 3), precision, _p(irr), _p(spec), _p(col), C.byref(samples), nthreads)
+                     row_step, _f(scene.eye, 3), precision, _p(irr), _p(spec), _p(col), C.byref(samples), nthreads,
+                     C.byref(warp) if warp is not None else None)
     return irr, spec, col, int(samples.value)
 
 
@@ -236,22 +273,30 @@ def f16_to_f32(h: np.ndarray) -> np.ndarray:
     return np.asarray(h, dtype=np.uint16).view(np.float16).astype(np.float32)
 
 
-def frame(scene, nthreads=1, precision=32, rows=None, row_step=1, shadowmap=None, gbuf=None, **trace_over):
+def frame(scene, nthreads=1, precision=32, rows=None, row_step=1, shadowmap=None, gbuf=None, warp_mode=0,
+          warp_high=2.0, warp_low=0.5, **trace_over):
     """The whole reference pipeline on the CPU (voxelize, normalise, inject,
-    mips, trace).  Returns a dict of every intermediate."""
+    mips, trace), optionally warped (warp_mode 1: about the eye; 2: through
+    the warp map of the scene's 32^3 occupancy).  Returns a dict of every
+    intermediate."""
     sm = render_shadowmap(scene, nthreads) if shadowmap is None else shadowmap
-    count, sums, total = voxelize(scene, sm, nthreads=nthreads)
+    wmap = None
+    if warp_mode == 2:
+        wmap = warpmap(warp_occupancy(scene, sm, nthreads), warp_high, warp_low)
+    w = warp(scene, warp_mode, wmap) if warp_mode else None
+    count, sums, total = voxelize(scene, sm, nthreads=nthreads, warp=w)
     nv = scene.dim ** 3
     chain = np.zeros(4 * chain_voxels(scene.dim, scene.levels), dtype=np.uint16)
     color, normal, _, stats = normalize(scene, count, sums, radiance=chain, nthreads=nthreads)
-    inject(scene, sm, color, normal, chain, nthreads=nthreads)
+    inject(scene, sm, color, normal, chain, nthreads=nthreads, warp=w)
     build_mips(scene.dim, scene.levels, chain, nthreads)
     gp, gn, ga = render_gbuffer(scene) if gbuf is None else gbuf
     irr, spec, col, ns = trace(scene, chain, gp, gn, ga, precision=precision, rows=rows, row_step=row_step,
-                               nthreads=nthreads, **trace_over)
+                               nthreads=nthreads, warp=w, **trace_over)
     stats["total_voxel_fragments"] = total
     return dict(shadowmap=sm, count=count, sums=sums, color=color, normal=normal, chain=chain, gpos=gp, gnrm=gn,
-                galb=ga, irradiance=irr, specular=spec, out=col, samples=ns, stats=stats, nv=nv)
+                galb=ga, irradiance=irr, specular=spec, out=col, samples=ns, stats=stats, nv=nv, warpmap=wmap,
+                warp=w)
 
 
 # ------------------------------------------------------------ learned path
@@ -284,7 +329,7 @@ def trace_reference16(scene, chain, gpos, gnrm, pixels, precision=64, nthreads=1
     samples = C.c_uint64(0)
     load().orc_trace_cone_set(C.byref(volume(scene)), scene.levels, _p(chain), _p(dirs), 16, C.byref(cone),
                               C.c_float(float(np.sqrt(3.0))), _p(gpos), _p(gnrm), W, _p(pixels),
-                              C.c_int64(pixels.size), precision, _p(out), C.byref(samples), nthreads)
+                              C.c_int64(pixels.size), precision, _p(out), C.byref(samples), nthreads, None)
     return out, int(samples.value)
 
 
@@ -293,5 +338,6 @@ def learned_features(scene, chain, gpos, gnrm) -> np.ndarray:
     W, H = scene.gbuffer_size
     wq, hq = (W + 3) // 4, (H + 3) // 4
     out = np.zeros((hq * wq, 32), dtype=np.float32)
-    load().orc_learned_features(C.byref(volume(scene)), scene.levels, _p(chain), _p(gpos), _p(gnrm), W, H, _p(out))
+    load().orc_learned_features(C.byref(volume(scene)), scene.levels, _p(chain), _p(gpos), _p(gnrm), W, H, _p(out),
+                                None)
     return out

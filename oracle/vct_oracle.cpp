@@ -307,6 +307,67 @@ static float shadow_factor(const float* sm, int W, int H, const float ls[16], f3
 
 static inline uint32_t quant16(float x) { return (uint32_t)std::rint(clampf(x, 0.0f, 1.0f) * 65535.0f); }
 
+// ------------------------------------------------------------------- warping
+// voxelWarpFn (common.glsl:11-18), alpha = 0.25, in the GLSL's order.
+template <typename T>
+static inline T warp_fn(T x) {
+    T y = (T(0.25) * x + T(2.25) * x * x) + T(-1.5) * x * x * x;
+    return std::min(std::max(y, T(0)), T(1));
+}
+// voxelWarp (common.glsl:20-27).
+template <typename T>
+static inline void voxel_warp(const T p[3], const float c[3], T out[3]) {
+    for (int k = 0; k < 3; ++k) {
+        T off = p[k] - (T)c[k];
+        off = T(0.5) * off + T(0.5);
+        off = warp_fn(off);
+        off = T(2) * off - T(1);
+        out[k] = (T)c[k] + off;
+    }
+}
+// texture(warpmap, p).xyz: GL_LINEAR, clamp-to-edge, texel c / 65535.
+template <typename T>
+static inline void warp_lookup(const uint16_t* map, const T p[3], T out[3]) {
+    const int D = 32;
+    T f[3], a[3];
+    int i0[3], i1[3];
+    for (int k = 0; k < 3; ++k) {
+        T u = p[k] * (T)D - T(0.5);
+        f[k] = std::floor(u);
+        a[k] = u - f[k];
+        int i = (int)f[k];
+        i0[k] = std::min(std::max(i, 0), D - 1);
+        i1[k] = std::min(std::max(i + 1, 0), D - 1);
+    }
+    T t[8][3];
+    for (int n = 0; n < 8; ++n) {
+        int x = (n & 1) ? i1[0] : i0[0], y = ((n >> 1) & 1) ? i1[1] : i0[1], z = (n >> 2) ? i1[2] : i0[2];
+        const uint16_t* q = map + 4 * (((int64_t)z * D + y) * D + x);
+        for (int c = 0; c < 3; ++c) t[n][c] = (T)q[c] / (T)65535;
+    }
+    for (int c = 0; c < 3; ++c) {
+        T x00 = t[0][c] * (T(1) - a[0]) + t[1][c] * a[0];
+        T x10 = t[2][c] * (T(1) - a[0]) + t[3][c] * a[0];
+        T x01 = t[4][c] * (T(1) - a[0]) + t[5][c] * a[0];
+        T x11 = t[6][c] * (T(1) - a[0]) + t[7][c] * a[0];
+        T y0 = x00 * (T(1) - a[1]) + x10 * a[1];
+        T y1 = x01 * (T(1) - a[1]) + x11 * a[1];
+        out[c] = y0 * (T(1) - a[2]) + y1 * a[2];
+    }
+}
+template <typename T>
+static inline void apply_warp(const orc_warp* w, T p[3]) {
+    if (!w || w->mode == 0) return;
+    T o[3];
+    if (w->mode == 1)
+        voxel_warp(p, w->eye_tc, o);
+    else
+        warp_lookup(w->map, p, o);
+    p[0] = o[0];
+    p[1] = o[1];
+    p[2] = o[2];
+}
+
 }  // namespace
 
 // ================================================================ C API
@@ -339,7 +400,9 @@ void orc_mat4_mul(const float a[16], const float b[16], float out[16]) { matmul(
 void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, const float* albedo,
                   int64_t ntri, const orc_light* lights, int32_t nlights, int32_t lighting,
                   int32_t axis_override, const float* sm, int32_t sw, int32_t sh, const float ls[16],
-                  uint32_t* count, uint32_t* sums, uint32_t* total_fragments, int32_t nthreads) {
+                  uint32_t* count, uint32_t* sums, uint32_t* total_fragments, int32_t nthreads,
+                  const orc_warp* warp) {
+    const bool warped = warp && warp->mode != 0;
     const int N = vol->dim;
     const int64_t NV = (int64_t)N * N * N;
     float mvp[48];
@@ -429,7 +492,25 @@ void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, con
                     float dz = (float)N * (1.0f - uz);
                     int iz = (int)dz;
                     int vx, vy, vz;
-                    if (axis == 0) {
+                    if (warped) {
+                        // the fragment's volume coordinate: pixel centre, depth,
+                        // swizzled, z flipped, warped, scaled
+                        const float fN = (float)N;
+                        const float ux = ((float)px + 0.5f) / fN, uy = ((float)py + 0.5f) / fN;
+                        float u[3];
+                        if (axis == 0) {
+                            u[0] = 1.0f - uz; u[1] = uy; u[2] = ux;
+                        } else if (axis == 1) {
+                            u[0] = ux; u[1] = 1.0f - uz; u[2] = uy;
+                        } else {
+                            u[0] = ux; u[1] = uy; u[2] = uz;
+                        }
+                        u[2] = 1.0f - u[2];
+                        apply_warp(warp, u);
+                        vx = (int)(fN * u[0]);
+                        vy = (int)(fN * u[1]);
+                        vz = (int)(fN * u[2]);
+                    } else if (axis == 0) {
                         vx = iz;
                         vy = py;
                         vz = N - 1 - px;
@@ -518,7 +599,8 @@ void orc_normalize(const orc_volume* vol, float opacity, int32_t temporal, float
 // each thread writes through relaxed atomics to stay well defined.
 void orc_inject(const orc_volume* vol, const float* sm, int32_t sw, int32_t sh, const float li[16],
                 const float lpos[3], const float lint[3], int32_t lighting, int32_t dilate,
-                const uint16_t* color, const uint16_t* normal, uint16_t* radiance, int32_t nthreads) {
+                const uint16_t* color, const uint16_t* normal, uint16_t* radiance, int32_t nthreads,
+                const orc_warp* warp) {
     const int N = vol->dim;
     // The dispatch covers ceil(size/16)*16 threads and the bounds test is
     // `>`: thread index == size also runs when size is not a multiple of 16.
@@ -527,8 +609,10 @@ void orc_inject(const orc_volume* vol, const float* sm, int32_t sw, int32_t sh, 
     f3 vmin = ld3(vol->vmin), vmax = ld3(vol->vmax), vc = ld3(vol->vcenter);
     f3 ext = sub(vmax, vmin);
     auto vindex = [&](f3 w) {
-        f3 tc = mk(((w.x - vc.x) - vmin.x) / ext.x, ((w.y - vc.y) - vmin.y) / ext.y, ((w.z - vc.z) - vmin.z) / ext.z);
-        return mul(tc, (float)N);
+        float tc[3] = {((w.x - vc.x) - vmin.x) / ext.x, ((w.y - vc.y) - vmin.y) / ext.y,
+                       ((w.z - vc.z) - vmin.z) / ext.z};
+        apply_warp(warp, tc);  // getVoxelPosition (common.glsl:44-60)
+        return mk((float)N * tc[0], (float)N * tc[1], (float)N * tc[2]);
     };
     f3 lvox = vindex(ld3(lpos));
     auto store = [&](int x, int y, int z, const uint16_t v[4]) {
@@ -718,7 +802,7 @@ struct Sampler {
 // phong.frag:135-180 plus a length limit `maxd` in texture units.
 template <typename T>
 static void trace_cone(const Sampler<T>& s, V<T> pos, V<T> n, V<T> dir, const orc_cone& c, T maxd, T out[4],
-                       uint64_t& samples) {
+                       uint64_t& samples, const orc_warp* warp) {
     dir = vnorm(dir);
     T col[3] = {0, 0, 0};
     T alpha = 0;
@@ -734,6 +818,11 @@ static void trace_cone(const Sampler<T>& s, V<T> pos, V<T> n, V<T> dir, const or
         if (!(sp.x >= T(0) && sp.y >= T(0) && sp.z >= T(0) && sp.x <= T(1) && sp.y <= T(1) && sp.z <= T(1))) break;
         if (h * scale > maxd) break;
         T sc[4];
+        if (warp && warp->mode != 0) {  // phong.frag:150-157
+            T q[3] = {sp.x, sp.y, sp.z};
+            apply_warp(warp, q);
+            sp = {q[0], q[1], q[2]};
+        }
         s.sample(sp, lod + (T)c.lod_offset, sc);
         ++samples;
         T a = T(1) - alpha;
@@ -760,7 +849,7 @@ template <typename T>
 static void trace_rows(const orc_volume* vol, int levels, const uint16_t* chain, const orc_trace_params* tp,
                        const float* gpos, const float* gnrm, const float* galb, int W, int H, int row0, int row1,
                        int row_step, const float eye[3], float* irr, float* spec, float* colr, uint64_t* samples_out,
-                       int nthreads) {
+                       int nthreads, const orc_warp* warp) {
     Sampler<T> s;
     s.init(chain, vol->dim, levels);
     V<T> vmin = {(T)vol->vmin[0], (T)vol->vmin[1], (T)vol->vmin[2]};
@@ -803,7 +892,7 @@ static void trace_rows(const orc_volume* vol, int levels, const uint16_t* chain,
                                 d = vsub(vadd(vmul(Tg, dx), vmul(Nn, dy)), vmul(Bt, dz));
                             d = vnorm(d);
                             T cr[4];
-                            trace_cone(s, vp, Nn, d, tp->diffuse, maxd, cr, ns);
+                            trace_cone(s, vp, Nn, d, tp->diffuse, maxd, cr, ns, warp);
                             T w = (T)kConeWeights[c];
                             for (int k = 0; k < 4; ++k) ind[k] += w * cr[k];
                         }
@@ -814,7 +903,7 @@ static void trace_rows(const orc_volume* vol, int levels, const uint16_t* chain,
                             V<T> I = vsub(P, E);
                             V<T> R = vsub(I, vmul(Nn, T(2) * vdot(Nn, I)));
                             T sr[4];
-                            trace_cone(s, vp, Nn, R, tp->specular, maxd, sr, ns);
+                            trace_cone(s, vp, Nn, R, tp->specular, maxd, sr, ns, warp);
                             for (int k = 0; k < 4; ++k) sp[k] = (float)sr[k];
                             rgb = vadd(rgb, vmul(V<T>{sr[0], sr[1], sr[2]}, (T)tp->reflect_scale));
                         }
@@ -852,7 +941,8 @@ static void trace_rows(const orc_volume* vol, int levels, const uint16_t* chain,
 template <typename T>
 static void trace_set_pixels(const orc_volume* vol, int levels, const uint16_t* chain, const float* dirs, int ncones,
                              const orc_cone& cone, T maxd, const float* gpos, const float* gnrm, int W,
-                             const int32_t* pixels, int64_t npix, float* out, uint64_t* samples_out, int nthreads) {
+                             const int32_t* pixels, int64_t npix, float* out, uint64_t* samples_out, int nthreads,
+                             const orc_warp* warp) {
     Sampler<T> s;
     s.init(chain, vol->dim, levels);
     V<T> vmin = {(T)vol->vmin[0], (T)vol->vmin[1], (T)vol->vmin[2]};
@@ -879,7 +969,7 @@ static void trace_set_pixels(const orc_volume* vol, int levels, const uint16_t* 
                     V<T> d = vadd(vadd(vmul(Tg, (T)dirs[4 * c]), vmul(Bt, (T)dirs[4 * c + 1])),
                                   vmul(Nn, (T)dirs[4 * c + 2]));
                     T cr[4];
-                    trace_cone(s, vp, Nn, d, cone, maxd, cr, ns);
+                    trace_cone(s, vp, Nn, d, cone, maxd, cr, ns, warp);
                     for (int k = 0; k < 4; ++k) acc[k] += (T)dirs[4 * c + 3] * cr[k];
                 }
             }
@@ -897,13 +987,13 @@ extern "C" {
 void orc_trace_cone_set(const orc_volume* vol, int32_t levels, const uint16_t* chain, const float* dirs,
                         int32_t ncones, const orc_cone* cone, float max_distance, const float* gpos, const float* gnrm,
                         int32_t width, const int32_t* pixels, int64_t npix, int32_t precision, float* out,
-                        uint64_t* samples, int32_t nthreads) {
+                        uint64_t* samples, int32_t nthreads, const orc_warp* warp) {
     if (precision == 64)
         trace_set_pixels<double>(vol, levels, chain, dirs, ncones, *cone, (double)max_distance, gpos, gnrm, width,
-                                 pixels, npix, out, samples, nthreads);
+                                 pixels, npix, out, samples, nthreads, warp);
     else
         trace_set_pixels<float>(vol, levels, chain, dirs, ncones, *cone, max_distance, gpos, gnrm, width, pixels,
-                                npix, out, samples, nthreads);
+                                npix, out, samples, nthreads, warp);
 }
 
 // Cheap features of the learned path (fp32): per 4x4 block, at its first
@@ -914,7 +1004,7 @@ void orc_trace_cone_set(const orc_volume* vol, int32_t levels, const uint16_t* c
 // nothing is added once the cone has left [0,1]^3); the accumulated RGBA
 // after steps 1, 3, 5 and 7 are the cone's 16 features.
 void orc_learned_features(const orc_volume* vol, int32_t levels, const uint16_t* chain, const float* gpos,
-                          const float* gnrm, int32_t W, int32_t H, float* out) {
+                          const float* gnrm, int32_t W, int32_t H, float* out, const orc_warp* warp) {
     Sampler<float> s;
     s.init(chain, vol->dim, levels);
     static const int order[16] = {5, 10, 6, 9, 0, 1, 2, 3, 4, 7, 8, 11, 12, 13, 14, 15};
@@ -951,7 +1041,9 @@ void orc_learned_features(const orc_volume* vol, int32_t levels, const uint16_t*
                              sp.z <= 1.f;
                     if (inside) {
                         float smp[4];
-                        s.trilinear(std::min(i + 1, levels - 1), sp, smp);
+                        float q[3] = {sp.x, sp.y, sp.z};
+                        apply_warp(warp, q);
+                        s.trilinear(std::min(i + 1, levels - 1), V<float>{q[0], q[1], q[2]}, smp);
                         const float a = 1.0f - alpha;
                         for (int k = 0; k < 3; ++k) col[k] += smp[k] * a;
                         alpha += a * smp[3];
@@ -972,15 +1064,75 @@ void orc_learned_features(const orc_volume* vol, int32_t levels, const uint16_t*
 void orc_trace(const orc_volume* vol, int32_t levels, const uint16_t* chain, const orc_trace_params* tp,
                const float* gpos, const float* gnrm, const float* galb, int32_t width, int32_t height,
                int32_t row0, int32_t row1, int32_t row_step, const float eye[3], int32_t precision, float* irradiance,
-               float* specular, float* color, uint64_t* samples, int32_t nthreads) {
+               float* specular, float* color, uint64_t* samples, int32_t nthreads, const orc_warp* warp) {
     row0 = std::max(0, row0);
     row1 = std::min(height, row1);
     if (precision == 64)
         trace_rows<double>(vol, levels, chain, tp, gpos, gnrm, galb, width, height, row0, row1, row_step, eye,
-                           irradiance, specular, color, samples, nthreads);
+                           irradiance, specular, color, samples, nthreads, warp);
     else
         trace_rows<float>(vol, levels, chain, tp, gpos, gnrm, galb, width, height, row0, row1, row_step, eye,
-                          irradiance, specular, color, samples, nthreads);
+                          irradiance, specular, color, samples, nthreads, warp);
+}
+
+void orc_warpmap(const uint8_t* occ, float high, float low, uint16_t* map) {
+    const int D = 32;
+    // Application.cpp:313-344: inclusive prefix sums of the occupancy along x, y, z
+    std::vector<int> px(D * D * D), py(D * D * D), pz(D * D * D);
+    auto at = [&](int x, int y, int z) { return (z * D + y) * D + x; };
+    for (int z = 0; z < D; ++z)
+        for (int y = 0; y < D; ++y) {
+            int sx = 0;
+            for (int x = 0; x < D; ++x) px[at(x, y, z)] = (sx += occ[at(x, y, z)] ? 1 : 0);
+        }
+    for (int z = 0; z < D; ++z)
+        for (int x = 0; x < D; ++x) {
+            int sy = 0;
+            for (int y = 0; y < D; ++y) py[at(x, y, z)] = (sy += occ[at(x, y, z)] ? 1 : 0);
+        }
+    for (int y = 0; y < D; ++y)
+        for (int x = 0; x < D; ++x) {
+            int sz = 0;
+            for (int z = 0; z < D; ++z) pz[at(x, y, z)] = (sz += occ[at(x, y, z)] ? 1 : 0);
+        }
+    // Application.cpp:346-371: per occupied count, the low and high cell
+    // widths; generateWarpmapWeights.frag stores them in RGBA16F targets.
+    float wl[D + 1], wh[D + 1];
+    for (int o = 0; o <= D; ++o) {
+        float l = 1.0f, h = 1.0f;
+        if (o != 0 && o != D) {
+            const int occupied = o, empty = D - o, total = D;
+            h = high;
+            l = (total - h * occupied) / (float)empty;
+            if (l < low) {
+                l = low;
+                h = (total - l * empty) / (float)occupied;
+            }
+        }
+        wl[o] = h2f(f2h(l));
+        wh[o] = h2f(f2h(h));
+    }
+    // generateWarpmap.frag at the texel centres
+    for (int z = 0; z < D; ++z)
+        for (int y = 0; y < D; ++y)
+            for (int x = 0; x < D; ++x) {
+                const int i = at(x, y, z);
+                const bool o = occ[i] != 0;
+                const int idx[3] = {x, y, z};
+                const int tot[3] = {px[at(D - 1, y, z)], py[at(x, D - 1, z)], pz[at(x, y, D - 1)]};
+                const int part[3] = {px[i], py[i], pz[i]};
+                uint16_t* t = map + 4 * (int64_t)i;
+                for (int k = 0; k < 3; ++k) {
+                    const float lo = wl[tot[k]], hi = wh[tot[k]];
+                    const float res = o ? hi : lo;
+                    const float prev = (float)(o ? part[k] - 1 : part[k]);
+                    const float offset = lo * ((float)idx[k] - prev) + hi * prev;
+                    const float inner = 0.5f * res;
+                    const float w = (offset + inner) / (float)D;
+                    t[k] = (uint16_t)std::rint(clampf(w, 0.0f, 1.0f) * 65535.0f);
+                }
+                t[3] = (uint16_t)((tot[0] & 0x1F) | ((tot[1] & 0x1F) << 5) | ((tot[2] & 0x1F) << 10) | ((o ? 1 : 0) << 15));
+            }
 }
 
 // ------------------------------------------------------------ set-up passes

@@ -38,6 +38,14 @@ typedef struct orc_volume {
     float vmin[3], vmax[3], vcenter[3];
 } orc_volume;
 
+/* Voxel warping: mode 0 none, 1 voxelWarp about eye_tc (warpVoxels),
+ * 2 the 32^3 RGBA16 unorm warp map (warpTexture). */
+typedef struct orc_warp {
+    int32_t mode;
+    const uint16_t* map;
+    float eye_tc[3];
+} orc_warp;
+
 /* Same layout as vct_light (80 bytes). */
 typedef struct orc_light {
     float position[3], _p0;
@@ -79,7 +87,7 @@ void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, con
                   int64_t ntri, const orc_light* lights, int32_t nlights, int32_t lighting,
                   int32_t axis_override, const float* shadowmap, int32_t sw, int32_t sh,
                   const float ls[16], uint32_t* count, uint32_t* sums, uint32_t* total_fragments,
-                  int32_t nthreads);
+                  int32_t nthreads, const orc_warp* warp);
 
 /* transferVoxels.comp; radiance/colour/normal are dim^3 RGBA16F (uint16 x4). */
 void orc_normalize(const orc_volume* vol, float voxel_set_opacity, int32_t temporal_filter,
@@ -90,7 +98,7 @@ void orc_normalize(const orc_volume* vol, float voxel_set_opacity, int32_t tempo
 void orc_inject(const orc_volume* vol, const float* shadowmap, int32_t sw, int32_t sh,
                 const float ls_inverse[16], const float light_pos[3], const float light_int[3],
                 int32_t radiance_lighting, int32_t radiance_dilate, const uint16_t* color,
-                const uint16_t* normal, uint16_t* radiance, int32_t nthreads);
+                const uint16_t* normal, uint16_t* radiance, int32_t nthreads, const orc_warp* warp);
 
 /* chain: all `levels` levels contiguous; level 0 is read, 1.. are written. */
 void orc_build_mips(int32_t dim, int32_t levels, uint16_t* chain, int32_t nthreads);
@@ -102,7 +110,7 @@ void orc_trace(const orc_volume* vol, int32_t levels, const uint16_t* chain,
                const orc_trace_params* tp, const float* gpos, const float* gnrm,
                const float* galb, int32_t width, int32_t height, int32_t row0, int32_t row1,
                int32_t row_step, const float eye[3], int32_t precision, float* irradiance,
-               float* specular, float* color, uint64_t* samples, int32_t nthreads);
+               float* specular, float* color, uint64_t* samples, int32_t nthreads, const orc_warp* warp);
 
 /* Cone set of the learned path's 16-cone reference: for each listed pixel,
  * sum over cones c of dirs[4c+3] * traceCone(dir = T dirs[4c] + B dirs[4c+1]
@@ -110,11 +118,15 @@ void orc_trace(const orc_volume* vol, int32_t levels, const uint16_t* chain,
 void orc_trace_cone_set(const orc_volume* vol, int32_t levels, const uint16_t* chain, const float* dirs,
                         int32_t ncones, const orc_cone* cone, float max_distance, const float* gpos,
                         const float* gnrm, int32_t width, const int32_t* pixels, int64_t npix, int32_t precision,
-                        float* out, uint64_t* samples, int32_t nthreads);
+                        float* out, uint64_t* samples, int32_t nthreads, const orc_warp* warp);
 /* Cheap quarter-resolution features of the learned path, fp32,
  * ceil(W/4) x ceil(H/4) x 32. */
 void orc_learned_features(const orc_volume* vol, int32_t levels, const uint16_t* chain, const float* gpos,
-                          const float* gnrm, int32_t width, int32_t height, float* out);
+                          const float* gnrm, int32_t width, int32_t height, float* out, const orc_warp* warp);
+/* The 32^3 warp map (RGBA16 unorm, x fastest) from a 32^3 occupancy grid
+ * (bytes, nonzero = occupied): Application.cpp:313-371, generateWarpmapWeights.frag
+ * (weights stored binary16), generateWarpmap.frag. */
+void orc_warpmap(const uint8_t* occupancy, float high, float low, uint16_t* map);
 
 void orc_render_shadowmap(const float* pos, int64_t ntri, const float ls[16], int32_t w, int32_t h,
                           float* depth, int32_t nthreads);

@@ -1,0 +1,132 @@
+"""Voxel warping against the oracle: the 32^3 warp map (warpTexture) and the
+analytic warp about the eye (warpVoxels) through voxelisation, injection,
+the mip chain and the cone trace.  Integer and binary16 results are
+bit-exact; irradiance within the trace tolerances."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import GpuScene, read_chain, rel_l2, rgb, split_records, u16
+from vct_gb300 import _lib as L
+from vct_gb300 import api, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", params=[L.VCT_WARP_ANALYTIC, L.VCT_WARP_TEXTURE], ids=["analytic", "texture"])
+def warped(request):
+    import torch
+
+    mode = request.param
+    if mode == L.VCT_WARP_ANALYTIC:
+        # voxelWarp magnifies the volume around the eye and pushes what lies
+        # farther than ~0.42 of the extent out of the grid: boxes near the
+        # centre, warped (and reflected) about the volume's centre
+        sc = scenes.tiny(seed=3, dim=64, shadow=512, gbuffer=(320, 180), n_boxes=12)
+        g = GpuScene(sc)  # shadow map and G-buffer from the scene's camera
+        sc.eye = np.array([0.0, 0.0, 0.0], np.float32)
+    else:
+        sc = scenes.cornell(seed=6)
+        g = GpuScene(sc)
+    sm, gbuf = g.host_inputs()
+    ref = O.frame(sc, shadowmap=sm, gbuf=gbuf, warp_mode=mode, nthreads=8)
+    ref64 = O.trace(sc, ref["chain"], *gbuf, precision=64, want=("irr",), warp=ref["warp"], nthreads=8)
+    ctx = api.Context(api.config_for(sc))
+    ctx.set_params(api.scene_params(sc, warp_mode=mode))
+    ctx.voxelize_accumulate(g.tris, g.lights, g.shadow, sc.eye)
+    torch.cuda.synchronize()
+    cnt, sums, occ, _ = split_records(*ctx.read_accumulators())
+    wmap = ctx.read_warpmap().cpu().numpy().view(np.uint16) if mode == L.VCT_WARP_TEXTURE else None
+    ctx.normalize()
+    ctx.inject(g.shadow, sc.eye)
+    ctx.build_mips()
+    irr, spec, col, samples = g.new_outputs()
+    ctx.trace(g.gb, sc.eye, api.trace_out(irr, spec, col, samples))
+    torch.cuda.synchronize()
+    stages = dict(count=cnt, sums=sums, occ=occ, wmap=wmap, chain=read_chain(ctx), irr=irr.cpu().numpy(),
+                  stats=ctx.stats())
+    # the fused frame on a second context
+    ctx2 = api.Context(api.config_for(sc))
+    ctx2.set_params(api.scene_params(sc, warp_mode=mode))
+    irr2, spec2, col2, samples2 = g.new_outputs()
+    ctx2.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(irr2, spec2, col2, samples2))
+    torch.cuda.synchronize()
+    fused = dict(chain=read_chain(ctx2), irr=irr2.cpu().numpy(), stats=ctx2.stats())
+    return mode, sc, ref, ref64, stages, fused
+
+
+def test_warpmap_bitexact(warped):
+    mode, sc, ref, _, st, _ = warped
+    if mode != L.VCT_WARP_TEXTURE:
+        pytest.skip("analytic warp has no map")
+    assert np.array_equal(st["wmap"], ref["warpmap"])
+    # the map is not the identity for this scene
+    D = 32
+    idx = np.arange(D)
+    ident = np.rint((idx + 0.5) / D * 65535).astype(np.uint16)
+    assert not np.array_equal(st["wmap"].reshape(D, D, D, 4)[..., 0], np.broadcast_to(ident, (D, D, D)))
+
+
+def test_warped_accumulators_bitexact(warped):
+    mode, sc, ref, _, st, _ = warped
+    assert ref["count"].sum() > 100
+    assert np.array_equal(st["count"], ref["count"])
+    assert np.array_equal(st["sums"], ref["sums"])
+    assert np.array_equal(st["occ"], ref["count"] > 0)
+    # warping moved voxels relative to the plain voxelisation
+    plain, _, _ = O.voxelize(sc, O.render_shadowmap(sc), nthreads=8)
+    assert not np.array_equal(plain > 0, ref["count"] > 0)
+
+
+def test_warped_chain_bitexact_stage_and_fused(warped):
+    mode, sc, ref, _, st, fused = warped
+    assert np.array_equal(st["chain"], ref["chain"])
+    assert np.array_equal(fused["chain"], ref["chain"])
+    for k in ("total_voxel_fragments", "unique_voxels", "max_fragments_per_voxel"):
+        assert st["stats"][k] == ref["stats"][k] == fused["stats"][k], k
+
+
+def test_warped_trace_matches_oracles(warped):
+    mode, sc, ref, ref64, st, fused = warped
+    irr = rgb(st["irr"])
+    assert np.abs(irr).sum() > 0
+    assert rel_l2(irr, rgb(ref["irradiance"])) <= 1e-5
+    e64 = rel_l2(irr, rgb(ref64[0]))
+    print(f"warp mode {mode}: irradiance rel L2 vs fp64 {e64:.2e}")
+    assert e64 <= 1e-3
+    assert np.array_equal(st["irr"].view(np.uint32), fused["irr"].view(np.uint32))
+
+
+def test_batch_with_analytic_warp_equals_single_frames():
+    import torch
+
+    scs = [scenes.batch_scene(seed=5, index=i) for i in range(3)]
+    gs = [GpuScene(sc) for sc in scs]
+    for sc in scs:
+        sc.eye = np.array([0.0, 0.0, 0.0], np.float32)  # warp about the centre
+    ref = []
+    for sc, g in zip(scs, gs):
+        ctx = api.Context(api.config_for(sc))
+        ctx.set_params(api.scene_params(sc, warp_mode=L.VCT_WARP_ANALYTIC))
+        o = g.new_outputs()
+        ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
+        torch.cuda.synchronize()
+        ref.append((read_chain(ctx), o[0].cpu().numpy()))
+    b = api.Batch([api.config_for(sc) for sc in scs])
+    for i, sc in enumerate(scs):
+        b.set_params(api.scene_params(sc, warp_mode=L.VCT_WARP_ANALYTIC), i)
+    outs = [g.new_outputs() for g in gs]
+    b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
+             for sc, g, o in zip(scs, gs, outs)])
+    torch.cuda.synchronize()
+    for i in range(len(scs)):
+        assert np.array_equal(read_chain(b.scenes[i]), ref[i][0])
+        assert np.array_equal(outs[i][0].cpu().numpy().view(np.uint32), ref[i][1].view(np.uint32))
+    # the texture warp is rejected by batches
+    b.set_params(api.scene_params(scs[0], warp_mode=L.VCT_WARP_TEXTURE), 0)
+    with pytest.raises(L.VctError):
+        b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
+                 for sc, g, o in zip(scs, gs, outs)])

@@ -27,6 +27,10 @@ VCT_CONFIG_COLOR_MIPS = 1
 VCT_FILTER_SOFTWARE = 0
 VCT_FILTER_HARDWARE = 1
 VCT_FILTER_HARDWARE_LEVELS = 2
+VCT_WARP_NONE = 0
+VCT_WARP_ANALYTIC = 1
+VCT_WARP_TEXTURE = 2
+VCT_WARP_DIM = 32
 VCT_VOLUME_COLOR = 0
 VCT_VOLUME_NORMAL = 1
 VCT_VOLUME_RADIANCE = 2
@@ -70,6 +74,7 @@ class vct_params(C.Structure):
         ("draw_occlusion", C.c_int32), ("enable_postprocess", C.c_int32),
         ("ambient_scale", C.c_float), ("reflect_scale", C.c_float), ("max_distance", C.c_float),
         ("ref_tbn_quirk", C.c_int32), ("trace_filter", C.c_int32),
+        ("warp_mode", C.c_int32), ("warp_high_resolution", C.c_float), ("warp_low_resolution", C.c_float),
     ]
 
 
@@ -157,6 +162,7 @@ SIGNATURES = {
     "vct_enable_timers": (st, [vp, C.c_int32]),
     "vct_get_timers": (st, [vp, P(vct_timers)]),
     "vct_launch_count": (C.c_uint64, []),
+    "vct_warpmap": (st, [vp, P(vp)]),
     "vct_voxelize_static": (st, [P(vct_config), P(vct_params), P(vct_triangles), P(vct_light), C.c_int32,
                                  P(vct_shadow_desc), vp, vp, vp, P(vct_stats), vp]),
     "vct_render_shadowmap": (st, [P(vct_triangles), P(C.c_float), vp, C.c_int32, C.c_int32, vp]),

@@ -235,6 +235,13 @@ class Context:
         L.check(self._lib.vct_accumulators(self.handle, C.byref(a), C.byref(b)), "vct_accumulators")
         return int(a.value), int(b.value)
 
+    def read_warpmap(self):
+        """Copy of the warp map of the last VCT_WARP_TEXTURE voxelisation:
+        (32^3 * 4,) int16 tensor (RGBA16 unorm bit patterns, x fastest)."""
+        p = C.c_void_p()
+        L.check(self._lib.vct_warpmap(self.handle, C.byref(p)), "vct_warpmap")
+        return device_view(int(p.value), (32 ** 3 * 4,), "<i2").clone()
+
     # -- copies of device state into torch tensors (test helpers)
     def read_volume(self, volume: int, level: int = 0):
         """Copy of one volume level as an int16 tensor (binary16 bit patterns)."""

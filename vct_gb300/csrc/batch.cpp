@@ -65,15 +65,18 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         if (c->params.trace_filter != filter) return fail(VCT_ERR_INVALID_ARGUMENT, "all scenes of a batch must use the same trace_filter");
         if (filter != VCT_FILTER_SOFTWARE && (s = ensure_texture(c)) != VCT_OK) return s;
         const bool hw = filter != VCT_FILTER_SOFTWARE;
+        if (c->params.warp_mode == VCT_WARP_TEXTURE)
+            return fail(VCT_ERR_UNSUPPORTED, "batches do not build warp maps: use VCT_WARP_NONE or VCT_WARP_ANALYTIC");
         AccumParams A;
         fill_accum_inputs(c->cfg, c->params, c->mvp, &d.triangles, d.lights, d.n_lights, &d.shadow, A);
+        A.warp = warp_dev(c, d.eye);
         apply_tuning(b->tuning, A);
         A.acc = c->acc;
         A.occ = c->occ;
         A.stats = c->stats;
         A.num_sms = c->num_sms;
         InjectParams I;
-        fill_inject(c, &d.shadow, I);
+        fill_inject(c, &d.shadow, d.eye, I);
         ResolveParams R;
         std::memset(&R, 0, sizeof R);
         fill_norm(c, R.norm);
@@ -82,6 +85,8 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         R.dilate = c->params.radiance_dilate;
         R.light_vox = I.light_vox;
         R.light_int = I.light_int;
+        R.warp = I.warp;
+        R.light_tc = I.light_tc;
         R.lit = c->lit;
         R.mip_levels = std::min(4, c->levels - 1);
         for (int l = 0; l <= R.mip_levels; ++l) {

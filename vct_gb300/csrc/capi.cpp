@@ -145,6 +145,11 @@ vct_status validate_params(const vct_params* p) {
     if (p->axis_override < -1 || p->axis_override > 2) return fail(VCT_ERR_INVALID_ARGUMENT, "axis_override in [-1, 2]");
     if (!std::isfinite(p->voxel_set_opacity) || !std::isfinite(p->temporal_decay))
         return fail(VCT_ERR_INVALID_ARGUMENT, "opacity/decay must be finite");
+    if (p->warp_mode < VCT_WARP_NONE || p->warp_mode > VCT_WARP_TEXTURE)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "warp_mode must be one of VCT_WARP_*");
+    if (!(p->warp_high_resolution > 0.0f && p->warp_high_resolution <= 32.0f) ||
+        !(p->warp_low_resolution > 0.0f && p->warp_low_resolution <= 32.0f))
+        return fail(VCT_ERR_INVALID_ARGUMENT, "warp resolutions must be in (0, 32]");
     return VCT_OK;
 }
 
@@ -284,9 +289,43 @@ void apply_tuning(const vct_tuning& t, TraceParams& P) {
     P.warp_w_log2 = ilog2(t.trace_warp_w);
 }
 
+WarpDev warp_dev(const vct_ctx* ctx, const float* eye) {
+    WarpDev W;
+    std::memset(&W, 0, sizeof W);
+    W.mode = ctx->params.warp_mode;
+    W.map = ctx->warpmap;
+    if (eye) {  // voxelLinearPosition(eye) (common.glsl:6-9)
+        float tc[3];
+        for (int k = 0; k < 3; ++k)
+            tc[k] = ((eye[k] - ctx->cfg.voxel_center[k]) - ctx->cfg.voxel_min[k]) /
+                    (ctx->cfg.voxel_max[k] - ctx->cfg.voxel_min[k]);
+        W.eye_tc = {tc[0], tc[1], tc[2]};
+    }
+    return W;
+}
+
+vct_status build_warpmap(vct_ctx* ctx, const AccumParams& A, cudaStream_t st) {
+    // voxelize.frag:187-192 into the 32^3 occupancy grid (Application.cpp:
+    // 235-285): the same rasteriser at a 32^2 viewport, unwarped.
+    AccumParams O = A;
+    O.dim = VCT_WARP_DIM;
+    O.occ = ctx->occ32;
+    O.acc = nullptr;
+    O.stats = nullptr;
+    O.occupancy_only = 1;
+    O.warp.mode = VCT_WARP_NONE;
+    VCT_CUDA(cudaMemsetAsync(ctx->occ32, 0, (VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM / 32) * 4, st));
+    launch_accumulate(O, st);
+    VCT_CHECK_LAUNCH("warp occupancy");
+    launch_warpmap(ctx->occ32, ctx->params.warp_high_resolution, ctx->params.warp_low_resolution, ctx->warpmap, st);
+    VCT_CHECK_LAUNCH("warp map");
+    return VCT_OK;
+}
+
 vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lights, int n,
-                      const vct_shadow_desc* sh, AccumParams& P) {
+                      const vct_shadow_desc* sh, const float* eye, AccumParams& P) {
     fill_accum_inputs(ctx->cfg, ctx->params, ctx->mvp, t, lights, n, sh, P);
+    P.warp = warp_dev(ctx, eye);
     apply_tuning(ctx->tuning, P);
     P.acc = ctx->acc;
     P.occ = ctx->occ;
@@ -333,8 +372,12 @@ f3 voxel_index_host(const vct_config& c, int dim, const float* p) {
     return {out[0], out[1], out[2]};
 }
 
-void fill_inject(vct_ctx* ctx, const vct_shadow_desc* s, InjectParams& P) {
+void fill_inject(vct_ctx* ctx, const vct_shadow_desc* s, const float* eye, InjectParams& P) {
     std::memset(&P, 0, sizeof P);
+    P.warp = warp_dev(ctx, eye);
+    for (int k = 0; k < 3; ++k)  // voxelLinearPosition(lightPos)
+        (&P.light_tc.x)[k] = ((s->light_pos[k] - ctx->cfg.voxel_center[k]) - ctx->cfg.voxel_min[k]) /
+                             (ctx->cfg.voxel_max[k] - ctx->cfg.voxel_min[k]);
     P.dim = ctx->dim;
     P.shadowmap = s->shadowmap_dev;
     P.sw = s->width;
@@ -453,6 +496,7 @@ vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], co
     P.ref_tbn_quirk = pr.ref_tbn_quirk;
     P.filter = pr.trace_filter;
     P.tex = ctx->tex;
+    P.warp = warp_dev(ctx, eye);
     apply_tuning(ctx->tuning, P);
     for (auto p : {(const void*)g->position_dev, (const void*)g->normal_dev, (const void*)g->albedo_dev,
                    (const void*)out->irradiance_dev, (const void*)out->specular_dev, (const void*)out->color_dev})
@@ -550,6 +594,9 @@ void vct_default_params(vct_params* p) {
     p->max_distance = 0.0f;
     p->ref_tbn_quirk = 0;
     p->trace_filter = VCT_FILTER_SOFTWARE;
+    p->warp_mode = VCT_WARP_NONE;
+    p->warp_high_resolution = 2.0f;  // src/Application.h:81-82
+    p->warp_low_resolution = 0.5f;
 }
 
 vct_status vct_voxel_mvp(const vct_config* cfg, float mvp_xyz[48]) {
@@ -606,6 +653,8 @@ vct_status vct_create(const vct_config* cfg, vct_ctx** out) {
         {(void**)&c->radiance, (size_t)chain_vox * 8},
         {(void**)&c->stats, sizeof(StatsDev)},
         {(void**)&c->pchain, (size_t)padded_level_offset(c->dim, c->levels) * 16},
+        {(void**)&c->occ32, (size_t)(VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM / 32) * 4},
+        {(void**)&c->warpmap, (size_t)VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM * 8},
     };
     for (auto& a : allocs) {
         cudaError_t e = cudaMalloc(a.p, a.bytes);
@@ -630,8 +679,8 @@ vct_status vct_destroy(vct_ctx* c) {
     if (c->tex_array) cudaFreeMipmappedArray(c->tex_array);
     for (auto sf : c->surf)
         if (sf) cudaDestroySurfaceObject(sf);
-    void* ptrs[] = {c->acc,   c->occ,         c->lit,    c->color,  c->normal,
-                    c->radiance, c->stats, c->vox_scratch, c->pchain, c->learned};
+    void* ptrs[] = {c->acc,    c->occ,   c->lit,         c->color,  c->normal,  c->radiance,
+                    c->stats,  c->vox_scratch, c->pchain, c->learned, c->occ32, c->warpmap};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -684,8 +733,9 @@ vct_status vct_accumulators(const vct_ctx* c, const uint32_t** records, const ui
 
 vct_status vct_voxelize_accumulate(vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n,
                                    const vct_shadow_desc* shadow, const float eye[3], void* stream) {
-    (void)eye;  // only used by the warped-voxel modes
     if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (!eye && c->params.warp_mode == VCT_WARP_ANALYTIC)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "the analytic warp needs the eye position");
     vct_status s = validate_tris(tris);
     if (s != VCT_OK) return s;
     bool need_shadow = false;
@@ -700,7 +750,8 @@ vct_status vct_voxelize_accumulate(vct_ctx* c, const vct_triangles* tris, const 
         c->stats_reset_pending = false;
     }
     AccumParams P;
-    if ((s = fill_accum(c, tris, lights, n, need_shadow ? shadow : nullptr, P)) != VCT_OK) return s;
+    if ((s = fill_accum(c, tris, lights, n, need_shadow ? shadow : nullptr, eye, P)) != VCT_OK) return s;
+    if (c->params.warp_mode == VCT_WARP_TEXTURE && (s = build_warpmap(c, P, st)) != VCT_OK) return s;
     launch_accumulate(P, st);
     VCT_CHECK_LAUNCH("voxelize accumulate");
     c->radiance_ready = false;
@@ -750,14 +801,15 @@ vct_status vct_voxelize(vct_ctx* c, const vct_triangles* tris, const vct_light* 
 }
 
 vct_status vct_inject(vct_ctx* c, const vct_shadow_desc* shadow, const float eye[3], void* stream) {
-    (void)eye;
     if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (!eye && c->params.warp_mode == VCT_WARP_ANALYTIC)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "the analytic warp needs the eye position");
     vct_status s = validate_shadow(shadow, true);
     if (s != VCT_OK) return s;
     DeviceScope ds(c->device);
     VCT_CUDA(ds.err);
     InjectParams P;
-    fill_inject(c, shadow, P);
+    fill_inject(c, shadow, eye, P);
     launch_inject(P, as_stream(stream));
     VCT_CHECK_LAUNCH("inject");
     c->mips_ready = false;
@@ -830,12 +882,13 @@ vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lig
     VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
     VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, st));
     AccumParams A;
-    if ((s = fill_accum(c, tris, lights, n, shadow, A)) != VCT_OK) return s;
+    if ((s = fill_accum(c, tris, lights, n, shadow, eye, A)) != VCT_OK) return s;
+    if (c->params.warp_mode == VCT_WARP_TEXTURE && (s = build_warpmap(c, A, st)) != VCT_OK) return s;
     launch_accumulate(A, st);
     VCT_CHECK_LAUNCH("frame: accumulate");
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[1], st));
     InjectParams I;
-    fill_inject(c, shadow, I);
+    fill_inject(c, shadow, eye, I);
     launch_inject_mark(I, st);
     VCT_CHECK_LAUNCH("frame: inject mark");
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[2], st));
@@ -849,6 +902,8 @@ vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lig
     R.dilate = c->params.radiance_dilate;
     R.light_vox = I.light_vox;
     R.light_int = I.light_int;
+    R.warp = I.warp;
+    R.light_tc = I.light_tc;
     R.lit = c->lit;
     R.mip_levels = std::min(4, c->levels - 1);
     // The sampler's own copy of the chain is written by the same kernels:
@@ -912,6 +967,12 @@ vct_status vct_get_timers(vct_ctx* c, vct_timers* out) {
 }
 
 uint64_t vct_launch_count(void) { return g_launches.load(); }
+
+vct_status vct_warpmap(const vct_ctx* c, const uint16_t** map) {
+    if (!c || !map) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *map = c->warpmap;
+    return VCT_OK;
+}
 
 vct_status vct_get_stats(vct_ctx* c, vct_stats* out, void* stream) {
     if (!c || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");

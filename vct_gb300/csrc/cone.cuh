@@ -50,10 +50,18 @@ __device__ __forceinline__ float4 to_float4(rgba2 v) { return make_float4(v.rg.x
 // chain: for a position in [0,1]^3 the footprint's lower corner is in
 // [-1, S-1]^3, i.e. [0, S]^3 of the (S+2)^3 bordered level, so the eight
 // texels are plain loads at constant offsets with no bounds tests.
-__device__ __forceinline__ rgba2 trilinear2(const TraceParams& P, const int* __restrict__ off, int l, f3 p) {
+//
+// With `guard` (positions warped about an eye outside the volume can leave
+// [0,1]^3) the footprint is checked first: the bordered level holds texel
+// indices -1..S, i.e. u = p S - 1/2 in [-1, S); outside that every texel of
+// the footprint is border and the sample is (0,0,0,0).
+__device__ __forceinline__ rgba2 trilinear2(const TraceParams& P, const int* __restrict__ off, int l, f3 p,
+                                            bool guard = false) {
     const int S = P.dim >> l, Pd = S + 2;
     const float4* base = P.pchain + off[l];
     const float u = fmaf(p.x, (float)S, -0.5f), v = fmaf(p.y, (float)S, -0.5f), w = fmaf(p.z, (float)S, -0.5f);
+    if (guard && !(u >= -1.0f && v >= -1.0f && w >= -1.0f && u < (float)S && v < (float)S && w < (float)S))
+        return {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
     const float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     const float a = u - fu, b = v - fv, c = w - fw;
     const int i = (int)fu + 1, j = (int)fv + 1, k = (int)fw + 1;
@@ -67,8 +75,8 @@ __device__ __forceinline__ rgba2 trilinear2(const TraceParams& P, const int* __r
     return lerp2(lerp2(x00, x10, b), lerp2(x01, x11, b), c);
 }
 
-__device__ __forceinline__ float4 trilinear(const TraceParams& P, const int* off, int l, f3 p) {
-    return to_float4(trilinear2(P, off, l, p));
+__device__ __forceinline__ float4 trilinear(const TraceParams& P, const int* off, int l, f3 p, bool guard = false) {
+    return to_float4(trilinear2(P, off, l, p, guard));
 }
 
 template <int MODE>
@@ -88,10 +96,12 @@ __device__ __forceinline__ float4 sample_lod(const TraceParams& P, const int* of
         const int S = P.dim;
         return texel(P.chain, S, (int)floorf(p.x * S), (int)floorf(p.y * S), (int)floorf(p.z * S));
     }
-    if (lambda >= (float)q) return trilinear(P, off, q, p);
+    const bool guard = P.warp.mode == VCT_WARP_ANALYTIC;
+    if (lambda >= (float)q) return trilinear(P, off, q, p, guard);
     float fl = floorf(lambda);
     int d1 = (int)fl;
     float f = lambda - fl;
+    if (guard) return to_float4(lerp2(trilinear2(P, off, d1, p, true), trilinear2(P, off, d1 + 1, p, true), f));
     return to_float4(lerp2(trilinear2(P, off, d1, p), trilinear2(P, off, d1 + 1, p), f));
 }
 
@@ -114,7 +124,7 @@ __device__ __forceinline__ float4 trace_cone(const TraceParams& P, const int* of
         // any(notEqual(p, clamp(p, 0, 1))): outside, or NaN
         if (!(sp.x >= 0.f && sp.y >= 0.f && sp.z >= 0.f && sp.x <= 1.f && sp.y <= 1.f && sp.z <= 1.f)) break;
         if (h * scale > maxd) break;
-        float4 s = sample_lod<MODE>(P, off, sp, lod + c.lod_offset);
+        float4 s = sample_lod<MODE>(P, off, P.warp.mode ? apply_warp(P.warp, sp) : sp, lod + c.lod_offset);
         ++ns;
         float a = 1.0f - alpha;
         col = mk(fmaf(s.x, a, col.x), fmaf(s.y, a, col.y), fmaf(s.z, a, col.z));

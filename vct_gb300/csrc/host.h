@@ -38,6 +38,8 @@ struct vct_ctx {
     vct_tuning tuning;        // launch shapes (vct_set_tuning / vct_autotune)
     void* learned = nullptr;  // learned-trace scratch (quarter-res features, tile errors, fallback list)
     size_t learned_bytes = 0;
+    uint32_t* occ32 = nullptr;   // VCT_WARP_TEXTURE: 32^3 occupancy bit mask
+    uint16_t* warpmap = nullptr; // VCT_WARP_TEXTURE: 32^3 RGBA16 unorm warp map
 };
 
 namespace vct {
@@ -91,9 +93,15 @@ void apply_tuning(const vct_tuning& t, AccumParams& P);
 void apply_tuning(const vct_tuning& t, TraceParams& P);
 
 vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lights, int n,
-                      const vct_shadow_desc* sh, AccumParams& P);
+                      const vct_shadow_desc* sh, const float* eye, AccumParams& P);
 void fill_norm(vct_ctx* ctx, NormalizeParams& P);
-void fill_inject(vct_ctx* ctx, const vct_shadow_desc* s, InjectParams& P);
+void fill_inject(vct_ctx* ctx, const vct_shadow_desc* s, const float* eye, InjectParams& P);
+// Warp state of the context's parameters for an eye position (may be NULL
+// unless the mode is VCT_WARP_ANALYTIC).
+WarpDev warp_dev(const vct_ctx* ctx, const float* eye);
+// VCT_WARP_TEXTURE: the 32^3 occupancy voxelisation of `A`'s triangles and
+// the warp map built from it (A: the main pass's parameters, scratch bound).
+vct_status build_warpmap(vct_ctx* ctx, const AccumParams& A, cudaStream_t s);
 MipLevels mip_levels(vct_ctx* ctx, uint2* chain, int levels);
 vct_status ensure_texture(vct_ctx* ctx);
 vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], const vct_trace_out* out,

@@ -12,6 +12,7 @@
 #include <stdint.h>
 
 #include "vct_internal.h"
+#include "warp.cuh"
 
 namespace vct {
 

@@ -29,6 +29,14 @@ VCT_HD inline long long padded_level_offset(int N, int l) {
     return (n * n * n - s * s * s) / 7 * 8 + 8 * (n * n - s * s) + 24 * (n - s) + 8LL * l;
 }
 
+// Voxel warping (VCT_WARP_*): the texture mode's map is 32^3 RGBA16 unorm
+// texels, x fastest; the analytic mode warps about the eye's volume coordinate.
+struct WarpDev {
+    int mode;
+    const uint16_t* map;
+    f3 eye_tc;
+};
+
 struct LightDev {
     f3 position;
     f3 direction;
@@ -68,6 +76,8 @@ struct AccumParams {
     int num_sms;
     int unit_log2;      // log2 of the bounding-box pixels per work unit
     int blocks_per_sm;  // raster CTAs per SM (1..3)
+    WarpDev warp;
+    int occupancy_only;  // only set occupancy bits (the warp map's occupancy voxelisation)
     // Work distribution scratch (sized for ntri; see voxelize.cu).
     uint4* tri_rec;          // 3 x uint4 per triangle
     uint32_t* tri_units;     // work units per triangle
@@ -144,6 +154,8 @@ struct InjectParams {
     const uint2* normal;
     uint2* radiance;
     uint32_t* lit;  // fused path: bit mask of voxels the shader would store to
+    WarpDev warp;
+    f3 light_tc;    // voxelLinearPosition(lightPos): light_vox is warped on the device when warping
 };
 
 // Fused normalisation + injection resolve + first mip levels (vct_frame).
@@ -157,6 +169,8 @@ struct ResolveParams {
     int mip_levels;             // number of levels below 0 to write from the brick (<= 4)
     cudaSurfaceObject_t surf[5];  // texture-unit copy of levels 0..4 (0 = none)
     float4* pad_levels[5];        // bordered fp32 copy of levels 0..4 (nullptr = none)
+    WarpDev warp;
+    f3 light_tc;
 };
 
 struct MipLevels {
@@ -190,6 +204,7 @@ struct TraceParams {
     // Pixel tile of one 256-thread CTA (tile_w x tile_h) and of one warp
     // (warp_w x 32/warp_w), as log2.
     int tile_w_log2, tile_h_log2, warp_w_log2;
+    WarpDev warp;
 };
 
 struct ShadowRasterParams {
@@ -318,6 +333,9 @@ void launch_trace16(const LearnedParams& P, bool listed, int num_sms, cudaStream
 void launch_mlp_train(const TrainParams& P, int num_sms, cudaStream_t s);
 void launch_mlp_update(const MlpDev& M, int step, float lr, float beta1, float beta2, float eps, int update,
                        cudaStream_t s);
+
+// Warp map of VCT_WARP_TEXTURE from a 32^3 occupancy bit mask.
+void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, cudaStream_t s);
 
 // Tensor-core GEMM check: D (128 x n, fp32) = A (128 x k) B^T (n x k), bf16.
 void launch_umma_check(const uint16_t* A, const uint16_t* B, int K, int N, int swap, float* D, uint32_t* status,

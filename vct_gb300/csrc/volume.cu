@@ -63,6 +63,14 @@ __device__ __forceinline__ uint2 light_voxel(f3 light_vox, f3 light_int, uint2 c
     return pack_h4((diff * light_int.x) * c.x, (diff * light_int.y) * c.y, (diff * light_int.z) * c.z, c.w);
 }
 
+// voxelIndex(lightPos) (injectRadiance.comp:80): computed on the host without
+// warping, on the device with it (the warp map lives on the device).
+__device__ __forceinline__ f3 light_voxel_index(const WarpDev& W, f3 light_vox, f3 light_tc, int N) {
+    if (W.mode == VCT_WARP_NONE) return light_vox;
+    const f3 t = apply_warp(W, light_tc);
+    return mk((float)N * t.x, (float)N * t.y, (float)N * t.z);
+}
+
 // -------------------------------------------------------------------- mips
 // filterRadiance.comp BOX2: fp32 sum over the children in the shader's order
 // (z fastest, then y, then x), times 0.125, rounded to binary16.
@@ -156,6 +164,7 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
     const int N = P.dim;
     const int bpa = N / kBrick;
     const int bx = (int)(brick % bpa), by = (int)((brick / bpa) % bpa), bz = (int)(brick / (bpa * bpa));
+    const f3 lvox = FUSED ? light_voxel_index(R.warp, R.light_vox, R.light_tc, N) : R.light_vox;
     uint32_t uniq = 0, mx = 0, flags = 0;
 #pragma unroll 1
     for (int it = 0; it < kBrickVox / 4 / kThreads; ++it) {
@@ -218,7 +227,7 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
                 rad[j] = ((ob >> j) & 1u) ? pack_h4(0.0f, 0.0f, 0.0f, alpha) : make_uint2(0u, 0u);
             }
             if (FUSED && ((lb >> j) & 1u))
-                rad[j] = (R.lighting && !R.dilate) ? light_voxel(R.light_vox, R.light_int, col[j], nrm[j], x + j, y, z)
+                rad[j] = (R.lighting && !R.dilate) ? light_voxel(lvox, R.light_int, col[j], nrm[j], x + j, y, z)
                                                    : col[j];
         }
         store4(P.color + v0, col);
@@ -254,6 +263,12 @@ __device__ __forceinline__ bool inject_voxel(const InjectParams& P, int x, int y
     float tx = __fdiv_rn((w[0] - P.vcenter.x) - P.vmin.x, ext.x);
     float ty = __fdiv_rn((w[1] - P.vcenter.y) - P.vmin.y, ext.y);
     float tz = __fdiv_rn((w[2] - P.vcenter.z) - P.vmin.z, ext.z);
+    if (P.warp.mode != VCT_WARP_NONE) {  // getVoxelPosition (common.glsl:44-60)
+        const f3 t = apply_warp(P.warp, mk(tx, ty, tz));
+        tx = t.x;
+        ty = t.y;
+        tz = t.z;
+    }
     ix = __float2int_rz(tx * N);
     iy = __float2int_rz(ty * N);
     iz = __float2int_rz(tz * N);
@@ -281,7 +296,8 @@ __global__ void __launch_bounds__(kThreads) inject_kernel(const InjectParams P) 
     }
     long long v = ((long long)iz * N + iy) * N + ix;
     if (P.lighting)
-        P.radiance[v] = light_voxel(P.light_vox, P.light_int, P.color[v], P.normal[v], ix, iy, iz);
+        P.radiance[v] = light_voxel(light_voxel_index(P.warp, P.light_vox, P.light_tc, N), P.light_int, P.color[v],
+                                    P.normal[v], ix, iy, iz);
     else
         P.radiance[v] = P.color[v];
 }
@@ -365,7 +381,88 @@ __global__ void fill_u32_kernel(uint32_t* p, uint32_t v, long long n) {
         p[i] = v;
 }
 
+// ------------------------------------------------------------- warp map
+// Application.cpp:300-371 + generateWarpmapWeights.frag + generateWarpmap.frag
+// for the 32^3 warp map, in one CTA: per-axis inclusive prefix sums of the
+// occupancy, the per-row resolution weights (high for occupied cells, low for
+// empty ones, keeping each row's total of 32; stored as binary16 by the
+// weight textures), and per texel the warped coordinate of its cell centre,
+// stored RGBA16 unorm.
+struct WarpmapArgs {
+    const uint32_t* occ;  // 32^3 bit mask
+    float high, low;
+    uint16_t* map;
+};
+
+__global__ void __launch_bounds__(1024) warpmap_kernel(const WarpmapArgs A) {
+    constexpr int D = kWarpDim;
+    __shared__ uint8_t occ[D * D * D];
+    __shared__ uint8_t part[3][D * D * D];  // inclusive prefix sums along x, y, z
+    __shared__ float wts[2][D + 1];          // binary16-rounded low / high weights per occupied count
+    const int t = threadIdx.x;
+    for (int i = t; i < D * D * D; i += blockDim.x) occ[i] = (uint8_t)((A.occ[i >> 5] >> (i & 31)) & 1u);
+    if (t <= D) {
+        float l = 1.0f, h = 1.0f;
+        if (t != 0 && t != D) {
+            const int occupied = t, empty = D - t, total = D;
+            h = A.high;
+            l = ((float)total - h * (float)occupied) / (float)empty;
+            if (l < A.low) {
+                l = A.low;
+                h = ((float)total - l * (float)empty) / (float)occupied;
+            }
+        }
+        wts[0][t] = __half2float(__float2half_rn(l));
+        wts[1][t] = __half2float(__float2half_rn(h));
+    }
+    __syncthreads();
+    {
+        const int a = t & (D - 1), b = t >> 5;
+        int sx = 0, sy = 0, sz = 0;
+        for (int k = 0; k < D; ++k) {
+            const int ix = (b * D + a) * D + k;  // x = k, y = a, z = b
+            const int iy = (b * D + k) * D + a;  // x = a, y = k, z = b
+            const int iz = (k * D + b) * D + a;  // x = a, y = b, z = k
+            sx += occ[ix];
+            part[0][ix] = (uint8_t)sx;
+            sy += occ[iy];
+            part[1][iy] = (uint8_t)sy;
+            sz += occ[iz];
+            part[2][iz] = (uint8_t)sz;
+        }
+    }
+    __syncthreads();
+    for (int i = t; i < D * D * D; i += blockDim.x) {
+        const int x = i & (D - 1), y = (i >> 5) & (D - 1), z = i >> 10;
+        const bool o = occ[i] != 0;
+        const int idx[3] = {x, y, z};
+        const int tot[3] = {part[0][(z * D + y) * D + D - 1], part[1][(z * D + D - 1) * D + x],
+                            part[2][((D - 1) * D + y) * D + x]};
+        uint16_t out[4];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float lo = wts[0][tot[k]], hi = wts[1][tot[k]];
+            const float res = o ? hi : lo;
+            const int ps = part[k][i];
+            const float prev = (float)(o ? ps - 1 : ps);
+            const float offset = lo * ((float)idx[k] - prev) + hi * prev;
+            const float inner = 0.5f * res;
+            const float w = (offset + inner) / (float)D;
+            out[k] = (uint16_t)__float2uint_rn(fminf(fmaxf(w, 0.0f), 1.0f) * 65535.0f);
+        }
+        // packCellInfo: totals (5 bits each) and the cell's occupancy
+        out[3] = (uint16_t)((tot[0] & 0x1F) | ((tot[1] & 0x1F) << 5) | ((tot[2] & 0x1F) << 10) | ((o ? 1 : 0) << 15));
+        reinterpret_cast<uint2*>(A.map)[i] =
+            make_uint2((uint32_t)out[0] | ((uint32_t)out[1] << 16), (uint32_t)out[2] | ((uint32_t)out[3] << 16));
+    }
+}
+
 }  // namespace
+
+void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, cudaStream_t s) {
+    warpmap_kernel<<<1, 1024, 0, s>>>(WarpmapArgs{occ32, high, low, map});
+    note_launches(1);
+}
 
 void launch_normalize(const NormalizeParams& P, cudaStream_t s) {
     ResolveParams R;

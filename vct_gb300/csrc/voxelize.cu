@@ -161,13 +161,57 @@ __global__ void __launch_bounds__(1024) voxelize_scan_kernel(uint32_t* block_off
 }
 
 // ------------------------------------------------------------- 3. raster
+// Voxel of a fragment: voxelize.frag:79-108.  Without warping the axis
+// swizzle resolves to integers: the projected coordinates are the pixel
+// indices and the depth axis is trunc(N * (1 - u.z)).  With warping the
+// fragment's volume coordinate (pixel centre (p + 0.5) / N, depth
+// (z + 1) / 2, swizzled, z flipped) is warped and scaled, as the shader does.
+__device__ __forceinline__ bool fragment_voxel(const AccumParams& P, int px, int py, int axis, float zf, int& vx,
+                                               int& vy, int& vz) {
+    const int N = P.dim;
+    const float uz = (zf + 1.0f) * 0.5f;
+    if (P.warp.mode == VCT_WARP_NONE) {
+        const int iz = __float2int_rz((float)N * (1.0f - uz));
+        if (axis == 0) {
+            vx = iz;
+            vy = py;
+            vz = N - 1 - px;
+        } else if (axis == 1) {
+            vx = px;
+            vy = iz;
+            vz = N - 1 - py;
+        } else {
+            vx = px;
+            vy = py;
+            vz = iz;
+        }
+    } else {
+        const float fN = (float)N;
+        const float ux = __fdiv_rn((float)px + 0.5f, fN), uy = __fdiv_rn((float)py + 0.5f, fN);
+        f3 u = axis == 0 ? mk(1.0f - uz, uy, ux) : axis == 1 ? mk(ux, 1.0f - uz, uy) : mk(ux, uy, uz);
+        u.z = 1.0f - u.z;
+        u = apply_warp(P.warp, u);
+        vx = __float2int_rz(fN * u.x);
+        vy = __float2int_rz(fN * u.y);
+        vz = __float2int_rz(fN * u.z);
+    }
+    return !(vx < 0 || vy < 0 || vz < 0 || vx >= N || vy >= N || vz >= N);
+}
+
 // voxelize.frag:186-280 for one queued fragment.
 __device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQueue& q, int e) {
     const long long t = q.tri[e];
     const uint32_t pix = q.pix[e];
     const int px = (int)(pix & 0x7ffu), py = (int)((pix >> 11) & 0x7ffu), axis = (int)((pix >> 22) & 3u);
+    int vx, vy, vz;
+    if (!fragment_voxel(P, px, py, axis, q.z[e], vx, vy, vz)) return;
+    const int N = P.dim;
+    const long long v = ((long long)vz * N + vy) * N + vx;
+    if (P.occupancy_only) {  // voxelize.frag:187-192
+        atomicOr(P.occ + (v >> 5), 1u << (v & 31));
+        return;
+    }
     const float l[3] = {q.l0[e], q.l1[e], q.l2[e]};
-    const float zf = q.z[e];
     const float* Pp = P.pos + t * 9;
     const float* Pn = P.nrm + t * 9;
     const f3 p0 = ld3(Pp), p1 = ld3(Pp + 3), p2 = ld3(Pp + 6);
@@ -198,27 +242,6 @@ __device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQ
         color = mk(clampf(fin.x, 0.0f, 1.0f), clampf(fin.y, 0.0f, 1.0f), clampf(fin.z, 0.0f, 1.0f));
     }
     const f3 n01 = mk((Nf.x + 1.0f) * 0.5f, (Nf.y + 1.0f) * 0.5f, (Nf.z + 1.0f) * 0.5f);
-    // voxelize.frag:79-108 with the axis swizzle resolved: the projected
-    // coordinates are the pixel indices, the depth axis is trunc(N*(1-u.z)).
-    const int N = P.dim;
-    const float uz = (zf + 1.0f) * 0.5f;
-    const int iz = __float2int_rz((float)N * (1.0f - uz));
-    int vx, vy, vz;
-    if (axis == 0) {
-        vx = iz;
-        vy = py;
-        vz = N - 1 - px;
-    } else if (axis == 1) {
-        vx = px;
-        vy = iz;
-        vz = N - 1 - py;
-    } else {
-        vx = px;
-        vy = py;
-        vz = iz;
-    }
-    if (vx < 0 || vy < 0 || vz < 0 || vx >= N || vy >= N || vz >= N) return;
-    const long long v = ((long long)vz * N + vy) * N + vx;
     unsigned long long* rec = reinterpret_cast<unsigned long long*>(P.acc + (long long)kAccWords * v);
     const unsigned long long qr = quant16(color.x), qg = quant16(color.y), qb = quant16(color.z);
     const unsigned long long qx = quant16(n01.x), qy = quant16(n01.y), qz = quant16(n01.z);
@@ -258,9 +281,10 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
         __syncwarp();
         if (lane < nact) {
             const int s = (int)(q.pix[lane] >> 24);
-            shade_fragment(S.get(s), q, lane);
+            const AccumParams& P = S.get(s);
+            shade_fragment(P, q, lane);
             const unsigned same = __match_any_sync(__activemask(), s);
-            if (lane == __ffs(same) - 1) atomicAdd(&frag_count[s], (unsigned)__popc(same));
+            if (lane == __ffs(same) - 1 && !P.occupancy_only) atomicAdd(&frag_count[s], (unsigned)__popc(same));
         }
         __syncwarp();
     };
