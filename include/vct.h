@@ -289,6 +289,28 @@ vct_status vct_get_stats(vct_ctx* ctx, vct_stats* out, void* stream);
 vct_status vct_enable_timers(vct_ctx* ctx, int32_t enable);
 /* Waits for the last timed vct_frame and returns its stage times. */
 vct_status vct_get_timers(vct_ctx* ctx, vct_timers* out);
+/* temporalRadianceFilter.comp: radiance level 0 *= temporal_decay (every
+ * voxel, RGBA16F rounded).  The coarser levels are stale until the next
+ * vct_build_mips. */
+vct_status vct_decay_radiance(vct_ctx* ctx, void* stream);
+
+/* ---- rigid actors (src/Actor.h, src/Transform.h, voxelize.vert) --------- */
+/* Triangles [first_triangle, first_triangle + triangle_count) of `local`
+ * move with `model` (column-major): positions = model * p, normals =
+ * mat3(transpose(inverse(model))) * n (computed here from the upper 3x3's
+ * cofactors and determinant), written to the same triangle indices of
+ * positions_dev / normals_dev (count * 9 floats each; other triangles are
+ * not written).  Ranges ascending and non-overlapping, at most
+ * VCT_MAX_ACTORS per call. */
+#define VCT_MAX_ACTORS 64 /* = the kernel's per-launch table */
+typedef struct vct_actor {
+    int64_t first_triangle;
+    int64_t triangle_count;
+    float model[16];
+} vct_actor;
+vct_status vct_transform_actors(const vct_triangles* local, const vct_actor* actors, int32_t n_actors,
+                                float* positions_dev, float* normals_dev, void* stream);
+
 /* The warp map of the last voxelisation with VCT_WARP_TEXTURE: 32^3 texels,
  * x fastest, RGBA16 unorm (xyz = warped coordinate * 65535, w = the packed
  * cell information of generateWarpmap.frag). */

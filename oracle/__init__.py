@@ -206,14 +206,15 @@ def normalize(scene, count, sums, opacity=0.5, temporal=0, decay=0.8, radiance=N
     return color, normal, rad, stats
 
 
-def inject(scene, shadowmap, color, normal, radiance, lighting=0, dilate=0, nthreads=1, dim=None, warp=None):
+def inject(scene, shadowmap, color, normal, radiance, lighting=0, dilate=0, nthreads=1, dim=None, warp=None,
+           temporal=0, decay=0.8):
     N = int(dim or scene.dim)
     v = volume(scene, N)
     sw, sh = scene.shadow_size
     sm = np.ascontiguousarray(shadowmap, dtype=np.float32)
     load().orc_inject(C.byref(v), _p(sm), sw, sh, _f(scene.ls_inverse, 16), _f(scene.light_pos, 3),
                       _f(scene.light_int, 3), lighting, dilate, _p(color), _p(normal), _p(radiance), nthreads,
-                      C.byref(warp) if warp is not None else None)
+                      C.byref(warp) if warp is not None else None, int(temporal), C.c_float(decay))
     return radiance
 
 
@@ -341,3 +342,30 @@ def learned_features(scene, chain, gpos, gnrm) -> np.ndarray:
     load().orc_learned_features(C.byref(volume(scene)), scene.levels, _p(chain), _p(gpos), _p(gnrm), W, H, _p(out),
                                 None)
     return out
+
+
+# ----------------------------------------------------- dynamic scenes
+def decay_radiance(radiance: np.ndarray, decay: float) -> np.ndarray:
+    """temporalRadianceFilter.comp on a level-0 radiance array (in place)."""
+    load().orc_decay_radiance(_p(radiance), C.c_int64(radiance.size // 4), C.c_float(decay))
+    return radiance
+
+
+def normal_matrix(model: np.ndarray) -> np.ndarray:
+    out = np.zeros(9, dtype=np.float32)
+    load().orc_normal_matrix(_f(np.asarray(model, np.float32).reshape(16), 16), _p(out))
+    return out
+
+
+def transform_actors(positions, normals, first, count, models):
+    """World-space copies of positions / normals (T x 9 float32) with the
+    listed triangle ranges transformed by their column-major models."""
+    pos = np.ascontiguousarray(positions, dtype=np.float32).copy()
+    nrm = np.ascontiguousarray(normals, dtype=np.float32).copy()
+    f = np.ascontiguousarray(first, dtype=np.int64)
+    c = np.ascontiguousarray(count, dtype=np.int64)
+    m = np.ascontiguousarray(models, dtype=np.float32).reshape(-1, 16)
+    load().orc_transform_actors(_p(np.ascontiguousarray(positions, dtype=np.float32)),
+                                _p(np.ascontiguousarray(normals, dtype=np.float32)), _p(f), _p(c), _p(m), len(f),
+                                _p(pos), _p(nrm))
+    return pos, nrm

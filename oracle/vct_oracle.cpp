@@ -600,8 +600,13 @@ void orc_normalize(const orc_volume* vol, float opacity, int32_t temporal, float
 void orc_inject(const orc_volume* vol, const float* sm, int32_t sw, int32_t sh, const float li[16],
                 const float lpos[3], const float lint[3], int32_t lighting, int32_t dilate,
                 const uint16_t* color, const uint16_t* normal, uint16_t* radiance, int32_t nthreads,
-                const orc_warp* warp) {
+                const orc_warp* warp, int32_t temporal, float decay) {
     const int N = vol->dim;
+    // With the temporal filter the relit colour mixes with the radiance
+    // transferVoxels seeded this frame (injectRadiance.comp:86-93); every
+    // store reads that seeded value (a snapshot), so racing stores agree.
+    std::vector<uint16_t> seeded;
+    if (temporal && lighting && !dilate) seeded.assign(radiance, radiance + 4 * (int64_t)N * N * N);
     // The dispatch covers ceil(size/16)*16 threads and the bounds test is
     // `>`: thread index == size also runs when size is not a multiple of 16.
     const int nx = std::min(((sw + 15) / 16) * 16, sw + 1);
@@ -656,9 +661,16 @@ void orc_inject(const orc_volume* vol, const float* sm, int32_t sw, int32_t sh, 
                         f3 n = mk(2.0f * h2f(Nn[0]) - 1.0f, 2.0f * h2f(Nn[1]) - 1.0f, 2.0f * h2f(Nn[2]) - 1.0f);
                         f3 L = normalize(sub(lvox, mk((float)ix, (float)iy, (float)iz)));
                         float diff = std::fmax(dot(n, L), 0.0f);
+                        float rgb[3];
+                        for (int k = 0; k < 3; ++k) rgb[k] = (diff * lint[k]) * h2f(c[k]);
                         uint16_t o[4];
-                        for (int k = 0; k < 3; ++k) o[k] = f2h((diff * lint[k]) * h2f(c[k]));
                         o[3] = c[3];
+                        if (!seeded.empty()) {
+                            const uint16_t* p = seeded.data() + 4 * (((int64_t)iz * N + iy) * N + ix);
+                            for (int k = 0; k < 3; ++k) rgb[k] = (1.0f - decay) * rgb[k] + decay * h2f(p[k]);
+                            o[3] = p[3];
+                        }
+                        for (int k = 0; k < 3; ++k) o[k] = f2h(rgb[k]);
                         store(ix, iy, iz, o);
                     } else {
                         store(ix, iy, iz, c);
@@ -1073,6 +1085,52 @@ void orc_trace(const orc_volume* vol, int32_t levels, const uint16_t* chain, con
     else
         trace_rows<float>(vol, levels, chain, tp, gpos, gnrm, galb, width, height, row0, row1, row_step, eye,
                           irradiance, specular, color, samples, nthreads, warp);
+}
+
+// temporalRadianceFilter.comp: every voxel of level 0 scaled by decay.
+void orc_decay_radiance(uint16_t* radiance, int64_t nv, float decay) {
+    for (int64_t i = 0; i < 4 * nv; ++i) radiance[i] = f2h(h2f(radiance[i]) * decay);
+}
+
+// Normal matrix mat3(transpose(inverse(model))) of an affine model matrix:
+// the transposed inverse of its upper 3x3, i.e. its cofactors / determinant.
+void orc_normal_matrix(const float m[16], float out[9]) {
+    float a[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) a[r][c] = m[c * 4 + r];
+    float C[3][3];
+    C[0][0] = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+    C[0][1] = -(a[1][0] * a[2][2] - a[1][2] * a[2][0]);
+    C[0][2] = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+    C[1][0] = -(a[0][1] * a[2][2] - a[0][2] * a[2][1]);
+    C[1][1] = a[0][0] * a[2][2] - a[0][2] * a[2][0];
+    C[1][2] = -(a[0][0] * a[2][1] - a[0][1] * a[2][0]);
+    C[2][0] = a[0][1] * a[1][2] - a[0][2] * a[1][1];
+    C[2][1] = -(a[0][0] * a[1][2] - a[0][2] * a[1][0]);
+    C[2][2] = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+    const float det = a[0][0] * C[0][0] + a[0][1] * C[0][1] + a[0][2] * C[0][2];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) out[c * 3 + r] = C[r][c] / det;
+}
+
+// voxelize.vert:15-22 for rigid actors: triangles [first, first + count) of
+// actor k transformed by model k (positions) and its normal matrix (normals).
+void orc_transform_actors(const float* src_pos, const float* src_nrm, const int64_t* first, const int64_t* count,
+                          const float* models, int32_t n, float* dst_pos, float* dst_nrm) {
+    for (int k = 0; k < n; ++k) {
+        const float* M = models + 16 * k;
+        float Nm[9];
+        orc_normal_matrix(M, Nm);
+        for (int64_t t = first[k]; t < first[k] + count[k]; ++t)
+            for (int v = 0; v < 3; ++v) {
+                const float* p = src_pos + t * 9 + 3 * v;
+                const float* q = src_nrm + t * 9 + 3 * v;
+                float o[4];
+                mat_vec(M, p[0], p[1], p[2], 1.0f, o);
+                for (int r = 0; r < 3; ++r) dst_pos[t * 9 + 3 * v + r] = o[r];
+                for (int r = 0; r < 3; ++r) dst_nrm[t * 9 + 3 * v + r] = Nm[0 + r] * q[0] + Nm[3 + r] * q[1] + Nm[6 + r] * q[2];
+            }
+    }
 }
 
 void orc_warpmap(const uint8_t* occ, float high, float low, uint16_t* map) {

@@ -98,7 +98,15 @@ void orc_normalize(const orc_volume* vol, float voxel_set_opacity, int32_t tempo
 void orc_inject(const orc_volume* vol, const float* shadowmap, int32_t sw, int32_t sh,
                 const float ls_inverse[16], const float light_pos[3], const float light_int[3],
                 int32_t radiance_lighting, int32_t radiance_dilate, const uint16_t* color,
-                const uint16_t* normal, uint16_t* radiance, int32_t nthreads, const orc_warp* warp);
+                const uint16_t* normal, uint16_t* radiance, int32_t nthreads, const orc_warp* warp,
+                int32_t temporal, float decay);
+/* temporalRadianceFilter.comp: radiance (nv RGBA16F voxels) *= decay. */
+void orc_decay_radiance(uint16_t* radiance, int64_t nv, float decay);
+/* mat3(transpose(inverse(model))) of an affine model (column-major in and out). */
+void orc_normal_matrix(const float model[16], float out[9]);
+/* Rigid actors: triangles [first[k], first[k] + count[k]) transformed by model k. */
+void orc_transform_actors(const float* src_pos, const float* src_nrm, const int64_t* first, const int64_t* count,
+                          const float* models, int32_t n, float* dst_pos, float* dst_nrm);
 
 /* chain: all `levels` levels contiguous; level 0 is read, 1.. are written. */
 void orc_build_mips(int32_t dim, int32_t levels, uint16_t* chain, int32_t nthreads);

@@ -31,6 +31,7 @@ VCT_WARP_NONE = 0
 VCT_WARP_ANALYTIC = 1
 VCT_WARP_TEXTURE = 2
 VCT_WARP_DIM = 32
+VCT_MAX_ACTORS = 64
 VCT_VOLUME_COLOR = 0
 VCT_VOLUME_NORMAL = 1
 VCT_VOLUME_RADIANCE = 2
@@ -113,6 +114,10 @@ class vct_tuning(C.Structure):
                 ("trace_tile_h", C.c_int32), ("trace_warp_w", C.c_int32)]
 
 
+class vct_actor(C.Structure):
+    _fields_ = [("first_triangle", C.c_int64), ("triangle_count", C.c_int64), ("model", C.c_float * 16)]
+
+
 class vct_adam(C.Structure):
     _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float)]
 
@@ -163,6 +168,8 @@ SIGNATURES = {
     "vct_get_timers": (st, [vp, P(vct_timers)]),
     "vct_launch_count": (C.c_uint64, []),
     "vct_warpmap": (st, [vp, P(vp)]),
+    "vct_decay_radiance": (st, [vp, vp]),
+    "vct_transform_actors": (st, [P(vct_triangles), P(vct_actor), C.c_int32, vp, vp, vp]),
     "vct_voxelize_static": (st, [P(vct_config), P(vct_params), P(vct_triangles), P(vct_light), C.c_int32,
                                  P(vct_shadow_desc), vp, vp, vp, P(vct_stats), vp]),
     "vct_render_shadowmap": (st, [P(vct_triangles), P(C.c_float), vp, C.c_int32, C.c_int32, vp]),

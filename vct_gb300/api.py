@@ -235,6 +235,9 @@ class Context:
         L.check(self._lib.vct_accumulators(self.handle, C.byref(a), C.byref(b)), "vct_accumulators")
         return int(a.value), int(b.value)
 
+    def decay_radiance(self, stream=None):
+        L.check(self._lib.vct_decay_radiance(self.handle, _stream(stream)), "vct_decay_radiance")
+
     def read_warpmap(self):
         """Copy of the warp map of the last VCT_WARP_TEXTURE voxelisation:
         (32^3 * 4,) int16 tensor (RGBA16 unorm bit patterns, x fastest)."""
@@ -408,6 +411,24 @@ def learned_trace(ctx: Context, mlp: Mlp, gb, eye, irradiance, threshold: float 
     if st is not None:
         return {k: getattr(st, k) for k, _ in L.vct_learned_stats._fields_}
     return None
+
+
+def actor_array(actors) -> tuple:
+    """actors: iterable of (first_triangle, triangle_count, model) with model a
+    4x4 row-major numpy matrix (stored column-major, as glm does)."""
+    actors = list(actors)
+    arr = (L.vct_actor * max(1, len(actors)))()
+    for i, (first, count, model) in enumerate(actors):
+        arr[i].first_triangle = int(first)
+        arr[i].triangle_count = int(count)
+        arr[i].model = f16(np.asarray(model, dtype=np.float64).T.reshape(16))
+    return arr, len(actors)
+
+
+def transform_actors(local_tris, actors, positions, normals, stream=None):
+    arr, n = actors if isinstance(actors, tuple) else actor_array(actors)
+    L.check(L.load().vct_transform_actors(C.byref(local_tris), arr, n, _ptr(positions), _ptr(normals),
+                                          _stream(stream)), "vct_transform_actors")
 
 
 def tuning_dict(t: L.vct_tuning) -> dict:

@@ -395,6 +395,8 @@ void fill_inject(vct_ctx* ctx, const vct_shadow_desc* s, const float* eye, Injec
     P.light_int = to_f3(s->light_int);
     P.lighting = ctx->params.radiance_lighting;
     P.dilate = ctx->params.radiance_dilate;
+    P.temporal = ctx->params.temporal_filter;
+    P.decay = ctx->params.temporal_decay;
     P.color = ctx->color;
     P.normal = ctx->normal;
     P.radiance = ctx->radiance;
@@ -810,7 +812,15 @@ vct_status vct_inject(vct_ctx* c, const vct_shadow_desc* shadow, const float eye
     VCT_CUDA(ds.err);
     InjectParams P;
     fill_inject(c, shadow, eye, P);
-    launch_inject(P, as_stream(stream));
+    cudaStream_t st = as_stream(stream);
+    if (P.temporal && P.lighting && !P.dilate) {
+        // the relit stores read the seeded radiance: one store per marked voxel
+        VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, st));
+        launch_inject_mark(P, st);
+        launch_inject_apply(P, st);
+    } else {
+        launch_inject(P, st);
+    }
     VCT_CHECK_LAUNCH("inject");
     c->mips_ready = false;
     c->pad_ready = false;
@@ -967,6 +977,69 @@ vct_status vct_get_timers(vct_ctx* c, vct_timers* out) {
 }
 
 uint64_t vct_launch_count(void) { return g_launches.load(); }
+
+vct_status vct_decay_radiance(vct_ctx* c, void* stream) {
+    if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    launch_decay(c->radiance, c->nv, c->params.temporal_decay, as_stream(stream));
+    VCT_CHECK_LAUNCH("decay radiance");
+    c->mips_ready = false;
+    c->pad_ready = false;
+    c->tex_ready = false;
+    return VCT_OK;
+}
+
+// mat3(transpose(inverse(model))) from the upper 3x3's cofactors / determinant.
+static void normal_matrix(const float m[16], float out[9]) {
+    float a[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) a[r][c] = m[c * 4 + r];
+    float C[3][3];
+    C[0][0] = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+    C[0][1] = -(a[1][0] * a[2][2] - a[1][2] * a[2][0]);
+    C[0][2] = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+    C[1][0] = -(a[0][1] * a[2][2] - a[0][2] * a[2][1]);
+    C[1][1] = a[0][0] * a[2][2] - a[0][2] * a[2][0];
+    C[1][2] = -(a[0][0] * a[2][1] - a[0][1] * a[2][0]);
+    C[2][0] = a[0][1] * a[1][2] - a[0][2] * a[1][1];
+    C[2][1] = -(a[0][0] * a[1][2] - a[0][2] * a[1][0]);
+    C[2][2] = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+    const float det = a[0][0] * C[0][0] + a[0][1] * C[0][1] + a[0][2] * C[0][2];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) out[c * 3 + r] = C[r][c] / det;
+}
+
+vct_status vct_transform_actors(const vct_triangles* local, const vct_actor* actors, int32_t n, float* pos, float* nrm,
+                                void* stream) {
+    vct_status s = validate_tris(local);
+    if (s != VCT_OK) return s;
+    if (!actors || !pos || !nrm) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n < 0 || n > VCT_MAX_ACTORS) return fail(VCT_ERR_INVALID_ARGUMENT, "n_actors must be in [0, VCT_MAX_ACTORS]");
+    ActorsDev A;
+    std::memset(&A, 0, sizeof A);
+    A.src_pos = local->positions_dev;
+    A.src_nrm = local->normals_dev;
+    A.dst_pos = pos;
+    A.dst_nrm = nrm;
+    A.n = n;
+    long long prev_end = 0;
+    for (int k = 0; k < n; ++k) {
+        const vct_actor& a = actors[k];
+        if (a.first_triangle < prev_end || a.triangle_count < 0 || a.first_triangle + a.triangle_count > local->count)
+            return fail(VCT_ERR_INVALID_ARGUMENT, "actor triangle ranges must be ascending, disjoint and inside the triangles");
+        for (float v : a.model)
+            if (!std::isfinite(v)) return fail(VCT_ERR_INVALID_ARGUMENT, "actor models must be finite");
+        A.start[k] = a.first_triangle;
+        A.end[k] = a.first_triangle + a.triangle_count;
+        prev_end = A.end[k];
+        std::memcpy(A.model[k], a.model, sizeof a.model);
+        normal_matrix(a.model, A.normal[k]);
+    }
+    launch_transform_actors(A, as_stream(stream));
+    VCT_CHECK_LAUNCH("transform actors");
+    return VCT_OK;
+}
 
 vct_status vct_warpmap(const vct_ctx* c, const uint16_t** map) {
     if (!c || !map) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");

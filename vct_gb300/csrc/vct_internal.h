@@ -156,6 +156,8 @@ struct InjectParams {
     uint32_t* lit;  // fused path: bit mask of voxels the shader would store to
     WarpDev warp;
     f3 light_tc;    // voxelLinearPosition(lightPos): light_vox is warped on the device when warping
+    int temporal;   // temporalFilterRadiance: relit voxels mix with the radiance seeded this frame
+    float decay;
 };
 
 // Fused normalisation + injection resolve + first mip levels (vct_frame).
@@ -333,6 +335,27 @@ void launch_trace16(const LearnedParams& P, bool listed, int num_sms, cudaStream
 void launch_mlp_train(const TrainParams& P, int num_sms, cudaStream_t s);
 void launch_mlp_update(const MlpDev& M, int step, float lr, float beta1, float beta2, float eps, int update,
                        cudaStream_t s);
+
+// Injection through the lit mask (marked by launch_inject_mark): every marked
+// voxel's store computed once from the radiance seeded this frame.
+void launch_inject_apply(const InjectParams& P, cudaStream_t s);
+// temporalRadianceFilter.comp: radiance level 0 *= decay.
+void launch_decay(uint2* radiance, long long nv, float decay, cudaStream_t s);
+
+// Rigid actors: world = model * local for positions, mat3(transpose(inverse(
+// model))) * local for normals (voxelize.vert), per triangle range.
+constexpr int kMaxActors = 64;
+struct ActorsDev {
+    const float* src_pos;
+    const float* src_nrm;
+    float* dst_pos;
+    float* dst_nrm;
+    long long start[kMaxActors], end[kMaxActors];  // ascending, non-overlapping triangle ranges
+    float model[kMaxActors][16];                    // column-major
+    float normal[kMaxActors][9];      // column-major 3x3
+    int n;
+};
+void launch_transform_actors(const ActorsDev& A, cudaStream_t s);
 
 // Warp map of VCT_WARP_TEXTURE from a 32^3 occupancy bit mask.
 void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, cudaStream_t s);

@@ -52,15 +52,28 @@ __device__ __forceinline__ bool in_grid(int x, int y, int z, int N) {
     return x >= 0 && y >= 0 && z >= 0 && x < N && y < N && z < N;
 }
 
-// radianceLighting branch (injectRadiance.comp:222-230).
+// radianceLighting branch (injectRadiance.comp:74-98).  With the temporal
+// filter the relit colour mixes with `prev`, the radiance transferVoxels
+// seeded this frame: rgb = (1 - decay) rgb + decay prev.rgb, alpha = prev.a.
+// (The shader's stores race when several shadow texels reach one voxel; here
+// every store reads the seeded value, which makes the result deterministic.)
 __device__ __forceinline__ uint2 light_voxel(f3 light_vox, f3 light_int, uint2 color, uint2 normal, int x, int y,
-                                             int z) {
+                                             int z, bool temporal = false, float decay = 0.0f,
+                                             uint2 prev = make_uint2(0u, 0u)) {
     float4 c = unpack_h4(color);
     float4 nn = unpack_h4(normal);
     f3 n = mk(2.0f * nn.x - 1.0f, 2.0f * nn.y - 1.0f, 2.0f * nn.z - 1.0f);
     f3 L = normalize(sub(light_vox, mk((float)x, (float)y, (float)z)));
     float diff = fmaxf(dot(n, L), 0.0f);
-    return pack_h4((diff * light_int.x) * c.x, (diff * light_int.y) * c.y, (diff * light_int.z) * c.z, c.w);
+    float r = (diff * light_int.x) * c.x, g = (diff * light_int.y) * c.y, b = (diff * light_int.z) * c.z, a = c.w;
+    if (temporal) {
+        const float4 p = unpack_h4(prev);
+        r = (1.0f - decay) * r + decay * p.x;
+        g = (1.0f - decay) * g + decay * p.y;
+        b = (1.0f - decay) * b + decay * p.z;
+        a = p.w;
+    }
+    return pack_h4(r, g, b, a);
 }
 
 // voxelIndex(lightPos) (injectRadiance.comp:80): computed on the host without
@@ -227,7 +240,8 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
                 rad[j] = ((ob >> j) & 1u) ? pack_h4(0.0f, 0.0f, 0.0f, alpha) : make_uint2(0u, 0u);
             }
             if (FUSED && ((lb >> j) & 1u))
-                rad[j] = (R.lighting && !R.dilate) ? light_voxel(lvox, R.light_int, col[j], nrm[j], x + j, y, z)
+                rad[j] = (R.lighting && !R.dilate) ? light_voxel(lvox, R.light_int, col[j], nrm[j], x + j, y, z,
+                                                                 P.temporal != 0, P.decay, rad[j])
                                                    : col[j];
         }
         store4(P.color + v0, col);
@@ -381,6 +395,64 @@ __global__ void fill_u32_kernel(uint32_t* p, uint32_t v, long long n) {
         p[i] = v;
 }
 
+// Stage-path injection through the lit mask: one thread per 4 voxels along x.
+__global__ void __launch_bounds__(kThreads) inject_apply_kernel(const InjectParams P) {
+    const int N = P.dim;
+    const long long nq = (long long)N * N * N / 4;
+    const f3 lvox = light_voxel_index(P.warp, P.light_vox, P.light_tc, N);
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x) {
+        const long long v0 = q * 4;
+        const uint32_t lb = (__ldg(P.lit + (v0 >> 5)) >> (v0 & 31)) & 15u;
+        if (!lb) continue;
+        const int x = (int)(v0 % N), y = (int)((v0 / N) % N), z = (int)(v0 / ((long long)N * N));
+        for (int j = 0; j < 4; ++j) {
+            if (!((lb >> j) & 1u)) continue;
+            const long long v = v0 + j;
+            P.radiance[v] = (P.lighting && !P.dilate) ? light_voxel(lvox, P.light_int, P.color[v], P.normal[v], x + j,
+                                                                     y, z, P.temporal != 0, P.decay, P.radiance[v])
+                                                      : P.color[v];
+        }
+    }
+}
+
+__global__ void decay_kernel(uint2* radiance, long long nv, float decay) {
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x) {
+        const float4 c = unpack_h4(radiance[v]);
+        radiance[v] = pack_h4(c.x * decay, c.y * decay, c.z * decay, c.w * decay);
+    }
+}
+
+// voxelize.vert:15-22 for rigid actors: one thread per triangle.
+__global__ void transform_actors_kernel(const ActorsDev A) {
+    const long long t0 = A.start[0], t1 = A.end[A.n - 1];
+    for (long long t = t0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; t < t1;
+         t += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = A.n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (A.start[mid] <= t)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        if (t >= A.end[lo]) continue;  // between two actors' ranges
+        const float* M = A.model[lo];
+        const float* Nm = A.normal[lo];
+        for (int k = 0; k < 3; ++k) {
+            const float* p = A.src_pos + t * 9 + 3 * k;
+            const float* n = A.src_nrm + t * 9 + 3 * k;
+            float o[4];
+            mat_vec(M, p[0], p[1], p[2], 1.0f, o);
+            float* dp = A.dst_pos + t * 9 + 3 * k;
+            dp[0] = o[0];
+            dp[1] = o[1];
+            dp[2] = o[2];
+            float* dn = A.dst_nrm + t * 9 + 3 * k;
+            for (int r = 0; r < 3; ++r) dn[r] = Nm[0 + r] * n[0] + Nm[3 + r] * n[1] + Nm[6 + r] * n[2];
+        }
+    }
+}
+
 // ------------------------------------------------------------- warp map
 // Application.cpp:300-371 + generateWarpmapWeights.frag + generateWarpmap.frag
 // for the 32^3 warp map, in one CTA: per-axis inclusive prefix sums of the
@@ -476,6 +548,31 @@ void launch_normalize(const NormalizeParams& P, cudaStream_t s) {
 void launch_inject(const InjectParams& P, cudaStream_t s) {
     dim3 grid((P.nx + 15) / 16, (P.ny + 15) / 16);
     inject_kernel<<<grid, kThreads, 0, s>>>(P);
+    note_launches(1);
+}
+
+void launch_inject_apply(const InjectParams& P, cudaStream_t s) {
+    const long long nq = (long long)P.dim * P.dim * P.dim / 4;
+    long long blocks = (nq + kThreads - 1) / kThreads;
+    if (blocks > 8192) blocks = 8192;
+    inject_apply_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(P);
+    note_launches(1);
+}
+
+void launch_decay(uint2* radiance, long long nv, float decay, cudaStream_t s) {
+    long long blocks = (nv + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    decay_kernel<<<(unsigned)blocks, 256, 0, s>>>(radiance, nv, decay);
+    note_launches(1);
+}
+
+void launch_transform_actors(const ActorsDev& A, cudaStream_t s) {
+    if (A.n <= 0) return;
+    const long long total = A.end[A.n - 1] - A.start[0];
+    if (total <= 0) return;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    transform_actors_kernel<<<(unsigned)blocks, 256, 0, s>>>(A);
     note_launches(1);
 }
 

@@ -391,6 +391,88 @@ def large_family(seed: int = 0, dim: int = 256, shadow: int = 2048, gbuffer=(192
                    BASELINE_CONES)
 
 
+# Dynamic family: rigid actors (cylinders of 1k-4k segments, 2k-8k triangles)
+# with random linear and angular velocities in a static environment of the
+# large frame's family (4,096 boxes and 45 columns: 198,912 triangles).
+@dataclass
+class Actors:
+    first: np.ndarray      # (A,) first triangle of each actor in the scene's arrays
+    count: np.ndarray      # (A,) triangles per actor
+    p0: np.ndarray         # (A, 3) initial positions
+    vel: np.ndarray        # (A, 3) linear velocities (units / s)
+    axis: np.ndarray       # (A, 3) unit rotation axes
+    omega: np.ndarray      # (A,) angular speeds (rad / s)
+
+    def model(self, k: int, t: float) -> np.ndarray:
+        """Row-major 4x4 model of actor k at time t: translate(p(t)) * rotate(axis, omega t);
+        positions bounce inside [-0.8, 0.8]^3."""
+        p = self.p0[k] + self.vel[k] * t
+        p = 0.8 - np.abs(np.mod(p + 0.8, 3.2) - 1.6)  # triangle wave in [-0.8, 0.8]
+        a = self.axis[k]
+        ang = self.omega[k] * t
+        c, s_ = np.cos(ang), np.sin(ang)
+        K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+        R = np.eye(3) + s_ * K + (1 - c) * (K @ K)
+        M = np.eye(4)
+        M[:3, :3] = R
+        M[:3, 3] = p
+        return M
+
+    def models(self, t: float) -> list:
+        return [(int(self.first[k]), int(self.count[k]), self.model(k, t)) for k in range(len(self.first))]
+
+
+def dynamic_scene(seed: int = 0, n_actors: int = 64, dim: int = 256, shadow: int = 2048, gbuffer=(1280, 720),
+                  static_boxes: int = 4096, static_cyl: int = 45) -> tuple:
+    """(scene, actors): the scene's triangle arrays hold the static environment
+    followed by every actor's mesh in its local frame (centred at the
+    origin); actors.model(k, t) places actor k at time t."""
+    env = large_family(seed, dim=dim, shadow=shadow, gbuffer=gbuffer, n_boxes=static_boxes, n_cyl=static_cyl,
+                       orbit=False)
+    rng = np.random.default_rng((seed, 11))
+    tris, nrms, albs = [env.positions.reshape(-1, 3, 3)], [env.normals.reshape(-1, 3, 3)], [env.albedo]
+    first, count = [], []
+    t0 = env.ntri
+    for _ in range(n_actors):
+        seg = int(rng.integers(1000, 4001))
+        r = float(rng.uniform(0.03, 0.1))
+        h = float(rng.uniform(0.1, 0.4))
+        t, n = _cylinders(np.array([r]), -h / 2, h / 2, np.zeros(1), np.zeros(1), seg)
+        tris.append(t)
+        nrms.append(n)
+        albs.append(np.repeat(rng.uniform(0, 1, size=(1, 3)), t.shape[0], 0))
+        first.append(t0)
+        count.append(t.shape[0])
+        t0 += t.shape[0]
+    A = len(first)
+    axis = rng.normal(size=(A, 3))
+    axis /= np.linalg.norm(axis, axis=1, keepdims=True)
+    actors = Actors(first=np.array(first, np.int64), count=np.array(count, np.int64),
+                    p0=rng.uniform(-0.8, 0.8, size=(A, 3)), vel=rng.uniform(-0.4, 0.4, size=(A, 3)), axis=axis,
+                    omega=rng.uniform(-2.0, 2.0, size=A))
+    sc = _finish(f"dynamic{seed}", np.concatenate(tris).astype(np.float64), np.concatenate(nrms).astype(np.float64),
+                 np.concatenate(albs), env.lights, np.eye(4), dim, env.levels, 1.0, env.shadow_size,
+                 np.array([0.0, 0.5, 2.8]), np.zeros(3), 55 * DEG, tuple(gbuffer), BASELINE_CONES)
+    # keep the environment's light-space matrices
+    sc.ls, sc.ls_inverse = env.ls, env.ls_inverse
+    return sc, actors
+
+
+def viewpoint(sc: Scene, k: int, n: int = 8, radius: float = 2.8) -> Scene:
+    """The scene seen from the k-th of n cameras on a circle around the volume."""
+    import copy
+
+    v = copy.copy(sc)
+    phi = 2 * np.pi * k / n
+    eye = np.array([radius * np.sin(phi), 0.5, radius * np.cos(phi)])
+    W, H = sc.gbuffer_size
+    vpm = perspective(55 * DEG, W / H, 0.1, 20.0) @ look_at(eye, np.zeros(3), (0, 1, 0))
+    v.eye = eye.astype(np.float32)
+    v.view_proj = colmajor(vpm)
+    v.inv_view_proj = colmajor(np.linalg.inv(vpm))
+    return v
+
+
 SCENES = {"cornell": cornell, "large": large, "tiny": tiny}
 
 
