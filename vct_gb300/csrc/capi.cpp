@@ -293,7 +293,7 @@ WarpDev warp_dev(const vct_ctx* ctx, const float* eye) {
     WarpDev W;
     std::memset(&W, 0, sizeof W);
     W.mode = ctx->params.warp_mode;
-    W.map = ctx->warpmap;
+    W.mapf = ctx->warpmap_f;
     if (eye) {  // voxelLinearPosition(eye) (common.glsl:6-9)
         float tc[3];
         for (int k = 0; k < 3; ++k)
@@ -317,7 +317,8 @@ vct_status build_warpmap(vct_ctx* ctx, const AccumParams& A, cudaStream_t st) {
     VCT_CUDA(cudaMemsetAsync(ctx->occ32, 0, (VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM / 32) * 4, st));
     launch_accumulate(O, st);
     VCT_CHECK_LAUNCH("warp occupancy");
-    launch_warpmap(ctx->occ32, ctx->params.warp_high_resolution, ctx->params.warp_low_resolution, ctx->warpmap, st);
+    launch_warpmap(ctx->occ32, ctx->params.warp_high_resolution, ctx->params.warp_low_resolution, ctx->warpmap,
+                   ctx->warpmap_f, st);
     VCT_CHECK_LAUNCH("warp map");
     return VCT_OK;
 }
@@ -657,6 +658,7 @@ vct_status vct_create(const vct_config* cfg, vct_ctx** out) {
         {(void**)&c->pchain, (size_t)padded_level_offset(c->dim, c->levels) * 16},
         {(void**)&c->occ32, (size_t)(VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM / 32) * 4},
         {(void**)&c->warpmap, (size_t)VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM * 8},
+        {(void**)&c->warpmap_f, (size_t)VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM * 16},
     };
     for (auto& a : allocs) {
         cudaError_t e = cudaMalloc(a.p, a.bytes);
@@ -682,7 +684,7 @@ vct_status vct_destroy(vct_ctx* c) {
     for (auto sf : c->surf)
         if (sf) cudaDestroySurfaceObject(sf);
     void* ptrs[] = {c->acc,    c->occ,   c->lit,         c->color,  c->normal,  c->radiance,
-                    c->stats,  c->vox_scratch, c->pchain, c->learned, c->occ32, c->warpmap};
+                    c->stats,  c->vox_scratch, c->pchain, c->learned, c->occ32, c->warpmap, c->warpmap_f};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete c;

@@ -40,6 +40,7 @@ struct vct_ctx {
     size_t learned_bytes = 0;
     uint32_t* occ32 = nullptr;   // VCT_WARP_TEXTURE: 32^3 occupancy bit mask
     uint16_t* warpmap = nullptr; // VCT_WARP_TEXTURE: 32^3 RGBA16 unorm warp map
+    float4* warpmap_f = nullptr; // its fp32 copy read by the lookups
 };
 
 namespace vct {

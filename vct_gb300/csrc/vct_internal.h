@@ -30,10 +30,11 @@ VCT_HD inline long long padded_level_offset(int N, int l) {
 }
 
 // Voxel warping (VCT_WARP_*): the texture mode's map is 32^3 RGBA16 unorm
-// texels, x fastest; the analytic mode warps about the eye's volume coordinate.
+// texels, x fastest, read through its fp32 copy (c / 65535 per channel); the
+// analytic mode warps about the eye's volume coordinate.
 struct WarpDev {
     int mode;
-    const uint16_t* map;
+    const float4* mapf;
     f3 eye_tc;
 };
 
@@ -358,7 +359,7 @@ struct ActorsDev {
 void launch_transform_actors(const ActorsDev& A, cudaStream_t s);
 
 // Warp map of VCT_WARP_TEXTURE from a 32^3 occupancy bit mask.
-void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, cudaStream_t s);
+void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, float4* mapf, cudaStream_t s);
 
 // Tensor-core GEMM check: D (128 x n, fp32) = A (128 x k) B^T (n x k), bf16.
 void launch_umma_check(const uint16_t* A, const uint16_t* B, int K, int N, int swap, float* D, uint32_t* status,

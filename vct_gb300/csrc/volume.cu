@@ -464,6 +464,7 @@ struct WarpmapArgs {
     const uint32_t* occ;  // 32^3 bit mask
     float high, low;
     uint16_t* map;
+    float4* mapf;  // fp32 copy read by the lookups
 };
 
 __global__ void __launch_bounds__(1024) warpmap_kernel(const WarpmapArgs A) {
@@ -526,13 +527,15 @@ __global__ void __launch_bounds__(1024) warpmap_kernel(const WarpmapArgs A) {
         out[3] = (uint16_t)((tot[0] & 0x1F) | ((tot[1] & 0x1F) << 5) | ((tot[2] & 0x1F) << 10) | ((o ? 1 : 0) << 15));
         reinterpret_cast<uint2*>(A.map)[i] =
             make_uint2((uint32_t)out[0] | ((uint32_t)out[1] << 16), (uint32_t)out[2] | ((uint32_t)out[3] << 16));
+        A.mapf[i] = make_float4(__fdiv_rn((float)out[0], 65535.0f), __fdiv_rn((float)out[1], 65535.0f),
+                                __fdiv_rn((float)out[2], 65535.0f), __fdiv_rn((float)out[3], 65535.0f));
     }
 }
 
 }  // namespace
 
-void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, cudaStream_t s) {
-    warpmap_kernel<<<1, 1024, 0, s>>>(WarpmapArgs{occ32, high, low, map});
+void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, float4* mapf, cudaStream_t s) {
+    warpmap_kernel<<<1, 1024, 0, s>>>(WarpmapArgs{occ32, high, low, map, mapf});
     note_launches(1);
 }
 

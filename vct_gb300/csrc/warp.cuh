@@ -38,8 +38,9 @@ __device__ __forceinline__ f3 voxel_warp(f3 p, f3 c) {
 }
 
 // texture(warpmap, p).xyz: GL_LINEAR with clamp-to-edge over the 32^3 RGBA16
-// unorm map (texel value c / 65535), lerped along x, then y, then z.
-__device__ __forceinline__ f3 warp_lookup(const uint16_t* __restrict__ map, f3 p) {
+// unorm map, read through its fp32 copy (texel value c / 65535), lerped
+// along x, then y, then z.
+__device__ __forceinline__ f3 warp_lookup(const float4* __restrict__ mapf, f3 p) {
     const float u = p.x * (float)kWarpDim - 0.5f, v = p.y * (float)kWarpDim - 0.5f, w = p.z * (float)kWarpDim - 0.5f;
     const float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     const float a = u - fu, b = v - fv, c = w - fw;
@@ -50,11 +51,10 @@ __device__ __forceinline__ f3 warp_lookup(const uint16_t* __restrict__ map, f3 p
     float t[8][3];
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
-        const uint2 q = __ldg(reinterpret_cast<const uint2*>(map) +
-                              ((iz[n >> 2] * kWarpDim + iy[(n >> 1) & 1]) * kWarpDim + ix[n & 1]));
-        t[n][0] = __fdiv_rn((float)(q.x & 0xFFFFu), 65535.0f);
-        t[n][1] = __fdiv_rn((float)(q.x >> 16), 65535.0f);
-        t[n][2] = __fdiv_rn((float)(q.y & 0xFFFFu), 65535.0f);
+        const float4 q = __ldg(mapf + ((iz[n >> 2] * kWarpDim + iy[(n >> 1) & 1]) * kWarpDim + ix[n & 1]));
+        t[n][0] = q.x;
+        t[n][1] = q.y;
+        t[n][2] = q.z;
     }
     float o[3];
 #pragma unroll
@@ -76,7 +76,7 @@ __device__ __forceinline__ f3 warp_lookup(const uint16_t* __restrict__ map, f3 p
 
 __device__ __forceinline__ f3 apply_warp(const WarpDev& W, f3 p) {
     if (W.mode == VCT_WARP_ANALYTIC) return voxel_warp(p, W.eye_tc);
-    if (W.mode == VCT_WARP_TEXTURE) return warp_lookup(W.map, p);
+    if (W.mode == VCT_WARP_TEXTURE) return warp_lookup(W.mapf, p);
     return p;
 }
 
