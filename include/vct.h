@@ -154,6 +154,13 @@ typedef struct vct_params {
     int32_t warp_mode;           /* VCT_WARP_* (warpVoxels / warpTexture; default none) */
     float warp_high_resolution;  /* warpTextureHighResolution (2.0) */
     float warp_low_resolution;   /* warpTextureLowResolution (0.5) */
+    /* direct lighting of vct_shade (phong.frag:183-344) */
+    int32_t cooktorrance;        /* cooktorrance (1): GGX Cook-Torrance, else Blinn-Phong */
+    int32_t enable_diffuse;      /* enableDiffuse (1) */
+    int32_t enable_specular;     /* enableSpecular (1) */
+    float roughness;             /* 0.5: phong.frag's value without a roughness map */
+    float metallic;              /* 0.0: without a metallic map */
+    float shininess;             /* material.shininess (32, src/Graphics/Mesh.h:29) */
 } vct_params;
 
 /* Caller-owned triangle soup on the device. */
@@ -289,6 +296,19 @@ vct_status vct_get_stats(vct_ctx* ctx, vct_stats* out, void* stream);
 vct_status vct_enable_timers(vct_ctx* ctx, int32_t enable);
 /* Waits for the last timed vct_frame and returns its stage times. */
 vct_status vct_get_timers(vct_ctx* ctx, vct_timers* out);
+/* phong.frag's full composite (main, 430-520) for a G-buffer: direct
+ * lighting of every enabled light (Cook-Torrance with GGX and Schlick-GGX, or
+ * Blinn-Phong; point-light range and smoothstep attenuation; 5-tap PCF for
+ * shadow casters, phong.frag:183-207) plus the indirect term from a previous
+ * vct_trace: color = (irradiance.rgb + specular.rgb * reflect_scale) *
+ * ambient_scale * albedo + diffuse + specular, times the occlusion
+ * 1 - clamp(irradiance.a) with draw_occlusion; without irradiance (NULL, or
+ * enable_indirect 0): ambient_scale * albedo + diffuse + specular; then the
+ * tone map and gamma with enable_postprocess.  color_dev: float4 per pixel. */
+vct_status vct_shade(vct_ctx* ctx, const vct_gbuffer* gbuffer, const float eye[3], const vct_light* lights,
+                     int32_t n_lights, const vct_shadow_desc* shadow, const float* irradiance_dev,
+                     const float* specular_dev, float* color_dev, void* stream);
+
 /* temporalRadianceFilter.comp: radiance level 0 *= temporal_decay (every
  * voxel, RGBA16F rounded).  The coarser levels are stale until the next
  * vct_build_mips. */

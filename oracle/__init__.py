@@ -51,6 +51,12 @@ class orc_warp(C.Structure):
     _fields_ = [("mode", C.c_int32), ("map", C.c_void_p), ("eye_tc", C.c_float * 3)]
 
 
+class orc_shade_params(C.Structure):
+    _fields_ = [(k, C.c_int32) for k in ("cooktorrance", "enable_diffuse", "enable_specular", "enable_indirect",
+                                         "enable_reflections", "draw_occlusion", "enable_postprocess")] + \
+               [(k, C.c_float) for k in ("roughness", "metallic", "shininess", "ambient_scale", "reflect_scale")]
+
+
 class orc_stats(C.Structure):
     _fields_ = [("total_voxel_fragments", C.c_uint32), ("unique_voxels", C.c_uint32),
                 ("max_fragments_per_voxel", C.c_uint32), ("error_flags", C.c_uint32)]
@@ -369,3 +375,26 @@ def transform_actors(positions, normals, first, count, models):
                                 _p(np.ascontiguousarray(normals, dtype=np.float32)), _p(f), _p(c), _p(m), len(f),
                                 _p(pos), _p(nrm))
     return pos, nrm
+
+
+def shade(scene, gbuf, shadowmap, irradiance=None, specular=None, eye=None, **params):
+    """phong.frag's composite with direct lighting; params: the
+    orc_shade_params fields (defaults: Cook-Torrance, roughness 0.5,
+    metallic 0, shininess 32, the trace's composite switches on, ambient and
+    reflect scale 1)."""
+    W, H = scene.gbuffer_size
+    d = dict(cooktorrance=1, enable_diffuse=1, enable_specular=1, enable_indirect=1, enable_reflections=1,
+             draw_occlusion=1, enable_postprocess=1, roughness=0.5, metallic=0.0, shininess=32.0, ambient_scale=1.0,
+             reflect_scale=1.0)
+    d.update(params)
+    sp = orc_shade_params(**d)
+    gp, gn, ga = (np.ascontiguousarray(a, dtype=np.float32) for a in gbuf)
+    arr, n = lights(scene)
+    sw, sh = scene.shadow_size
+    out = np.zeros(W * H * 4, dtype=np.float32)
+    ir = None if irradiance is None else np.ascontiguousarray(irradiance, dtype=np.float32)
+    spc = None if specular is None else np.ascontiguousarray(specular, dtype=np.float32)
+    load().orc_shade(_p(gp), _p(gn), _p(ga), W, H, _f(scene.eye if eye is None else eye, 3), arr, n,
+                     _p(np.ascontiguousarray(shadowmap, dtype=np.float32)), sw, sh, _f(scene.ls, 16), _p(ir), _p(spc),
+                     C.byref(sp), _p(out))
+    return out

@@ -1087,6 +1087,134 @@ void orc_trace(const orc_volume* vol, int32_t levels, const uint16_t* chain, con
                           irradiance, specular, color, samples, nthreads, warp);
 }
 
+// ------------------------------------------------------------------ shade
+// phong.frag:183-344 (direct lighting: Cook-Torrance with GGX / Schlick-GGX /
+// Schlick, or Blinn-Phong; point-light range and attenuation; PCF) and the
+// composite of main (430-520).
+namespace {
+const float kPiRef = 3.1415982f;  // common.glsl:1 (sic)
+struct Lit {
+    f3 d, s;
+};
+inline float sq(float x) { return x * x; }
+Lit cook_torrance(f3 dc, f3 lc, f3 N, f3 V, f3 L, f3 H, float r, float m) {
+    const float n_dot_l = std::fmax(0.0f, dot(N, L));
+    const float n_dot_v = std::fmax(0.0f, dot(N, V));
+    const float n_dot_h = std::fmax(0.0f, dot(N, H));
+    const float h_dot_v = std::fmax(0.0f, dot(H, V));
+    const f3 fl = mk(dc.x / kPiRef, dc.y / kPiRef, dc.z / kPiRef);
+    const float alpha2 = sq(r);
+    const float D = alpha2 / (kPiRef * sq(sq(n_dot_h) * (alpha2 - 1.0f) + 1.0f));
+    const float k = sq(r + 1.0f) / 8.0f;
+    const float g1v = n_dot_v / (n_dot_v * (1.0f - k) + k);
+    const float g1l = n_dot_l / (n_dot_l * (1.0f - k) + k);
+    const float G = g1v * g1l;
+    const float f0[3] = {0.04f * (1.0f - m) + dc.x * m, 0.04f * (1.0f - m) + dc.y * m, 0.04f * (1.0f - m) + dc.z * m};
+    const float p5 = std::pow(1.0f - h_dot_v, 5.0f);
+    float F[3], fct[3], kd[3];
+    const float den = std::fmax(4.0f * n_dot_l * n_dot_v, 0.001f);
+    for (int c = 0; c < 3; ++c) {
+        F[c] = f0[c] + (1.0f - f0[c]) * p5;
+        fct[c] = D * G * F[c] / den;
+        kd[c] = (1.0f - F[c]) * (1.0f - m);
+    }
+    const float lcv[3] = {lc.x, lc.y, lc.z}, flv[3] = {fl.x, fl.y, fl.z};
+    float d[3], sp[3];
+    for (int c = 0; c < 3; ++c) {
+        d[c] = lcv[c] * n_dot_l * kd[c] * flv[c];
+        sp[c] = lcv[c] * n_dot_l * fct[c];
+    }
+    return {mk(d[0], d[1], d[2]), mk(sp[0], sp[1], sp[2])};
+}
+Lit blinn_phong(f3 dc, const orc_light& Lt, f3 N, f3 V, f3 L, float shininess, float att) {
+    const float diff = std::fmax(dot(N, L), 0.0f);
+    const f3 H = normalize(add(V, L));
+    const float spec = std::pow(std::fmax(dot(N, H), 0.0f), shininess);
+    const float lc[3] = {Lt.color[0], Lt.color[1], Lt.color[2]}, d[3] = {dc.x, dc.y, dc.z};
+    float a[3], b[3];
+    for (int c = 0; c < 3; ++c) {
+        a[c] = diff * att * lc[c] * Lt.intensity * d[c];
+        b[c] = spec * att * lc[c] * Lt.intensity * d[c];
+    }
+    return {mk(a[0], a[1], a[2]), mk(b[0], b[1], b[2])};
+}
+}  // namespace
+
+void orc_shade(const float* gpos, const float* gnrm, const float* galb, int32_t W, int32_t H, const float eye[3],
+               const orc_light* lights, int32_t nl, const float* sm, int32_t sw, int32_t sh, const float ls[16],
+               const float* irr, const float* spec, const orc_shade_params* sp, float* color) {
+    const f3 E = ld3(eye);
+    for (int64_t p = 0; p < (int64_t)W * H; ++p) {
+        float* out = color + 4 * p;
+        if (gpos[4 * p + 3] == 0.0f) {
+            out[0] = out[1] = out[2] = out[3] = 0.0f;
+            continue;
+        }
+        const f3 Pw = ld3(gpos + 4 * p);
+        const f3 N = normalize(ld3(gnrm + 4 * p));
+        const f3 dc = ld3(galb + 4 * p);
+        const f3 V = normalize(sub(E, Pw));
+        f3 dsum = mk(0, 0, 0), ssum = mk(0, 0, 0);
+        for (int i = 0; i < nl; ++i) {
+            const orc_light& Lt = lights[i];
+            if (!Lt.enabled) continue;
+            Lit lg = {mk(0, 0, 0), mk(0, 0, 0)};
+            if (Lt.type == 0u) {
+                const f3 lp = ld3(Lt.position);
+                const float dist = length(sub(lp, Pw));
+                if (dist > Lt.range) continue;
+                const float att = 1.0f - smoothstep(0.75f * Lt.range, Lt.range, dist);
+                const f3 L = normalize(sub(lp, Pw));
+                if (sp->cooktorrance) {
+                    lg = cook_torrance(dc, ld3(Lt.color), N, V, L, normalize(add(V, L)), sp->roughness, sp->metallic);
+                    lg.d = mul(lg.d, att);
+                    lg.s = mul(lg.s, att);
+                } else {
+                    lg = blinn_phong(dc, Lt, N, V, L, sp->shininess, att);
+                }
+            } else if (Lt.type == 1u) {
+                const f3 dir = ld3(Lt.direction);
+                const f3 L = normalize(mk(-dir.x, -dir.y, -dir.z));
+                if (sp->cooktorrance)
+                    lg = cook_torrance(dc, ld3(Lt.color), N, V, L, normalize(add(V, L)), sp->roughness, sp->metallic);
+                else
+                    lg = blinn_phong(dc, Lt, N, V, L, sp->shininess, 1.0f);
+            }
+            if (Lt.shadow_caster) {
+                const float sf = 1.0f - shadow_factor(sm, sw, sh, ls, Pw);
+                lg.d = mul(lg.d, sf);
+                lg.s = mul(lg.s, sf);
+            }
+            dsum = add(dsum, lg.d);
+            ssum = add(ssum, lg.s);
+        }
+        const f3 dl = sp->enable_diffuse ? dsum : mk(0, 0, 0);
+        const f3 sl = sp->enable_specular ? ssum : mk(0, 0, 0);
+        f3 rgb;
+        if (sp->enable_indirect && irr) {
+            const float* ir = irr + 4 * p;
+            const float occ = 1.0f - clampf(ir[3], 0.0f, 1.0f);
+            f3 ind = ld3(ir);
+            if (sp->enable_reflections && spec) ind = add(ind, mul(ld3(spec + 4 * p), sp->reflect_scale));
+            const float as = sp->ambient_scale;
+            ind = mk(ind.x * (as * dc.x), ind.y * (as * dc.y), ind.z * (as * dc.z));
+            rgb = add(add(ind, dl), sl);
+            if (sp->draw_occlusion) rgb = mul(rgb, occ);
+        } else {
+            rgb = add(add(mul(dc, sp->ambient_scale), dl), sl);
+        }
+        if (sp->enable_postprocess) {
+            const float g = 1.0f / 2.2f;
+            rgb = mk(std::pow(rgb.x / (rgb.x + 1.0f), g), std::pow(rgb.y / (rgb.y + 1.0f), g),
+                     std::pow(rgb.z / (rgb.z + 1.0f), g));
+        }
+        out[0] = rgb.x;
+        out[1] = rgb.y;
+        out[2] = rgb.z;
+        out[3] = 1.0f;
+    }
+}
+
 // temporalRadianceFilter.comp: every voxel of level 0 scaled by decay.
 void orc_decay_radiance(uint16_t* radiance, int64_t nv, float decay) {
     for (int64_t i = 0; i < 4 * nv; ++i) radiance[i] = f2h(h2f(radiance[i]) * decay);

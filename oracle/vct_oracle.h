@@ -100,6 +100,16 @@ void orc_inject(const orc_volume* vol, const float* shadowmap, int32_t sw, int32
                 int32_t radiance_lighting, int32_t radiance_dilate, const uint16_t* color,
                 const uint16_t* normal, uint16_t* radiance, int32_t nthreads, const orc_warp* warp,
                 int32_t temporal, float decay);
+/* phong.frag's composite with direct lighting (see vct_shade). */
+typedef struct orc_shade_params {
+    int32_t cooktorrance, enable_diffuse, enable_specular, enable_indirect, enable_reflections, draw_occlusion,
+        enable_postprocess;
+    float roughness, metallic, shininess, ambient_scale, reflect_scale;
+} orc_shade_params;
+void orc_shade(const float* gpos, const float* gnrm, const float* galb, int32_t width, int32_t height,
+               const float eye[3], const orc_light* lights, int32_t nlights, const float* shadowmap, int32_t sw,
+               int32_t sh, const float ls[16], const float* irradiance, const float* specular,
+               const orc_shade_params* sp, float* color);
 /* temporalRadianceFilter.comp: radiance (nv RGBA16F voxels) *= decay. */
 void orc_decay_radiance(uint16_t* radiance, int64_t nv, float decay);
 /* mat3(transpose(inverse(model))) of an affine model (column-major in and out). */

@@ -76,6 +76,8 @@ class vct_params(C.Structure):
         ("ambient_scale", C.c_float), ("reflect_scale", C.c_float), ("max_distance", C.c_float),
         ("ref_tbn_quirk", C.c_int32), ("trace_filter", C.c_int32),
         ("warp_mode", C.c_int32), ("warp_high_resolution", C.c_float), ("warp_low_resolution", C.c_float),
+        ("cooktorrance", C.c_int32), ("enable_diffuse", C.c_int32), ("enable_specular", C.c_int32),
+        ("roughness", C.c_float), ("metallic", C.c_float), ("shininess", C.c_float),
     ]
 
 
@@ -169,6 +171,8 @@ SIGNATURES = {
     "vct_launch_count": (C.c_uint64, []),
     "vct_warpmap": (st, [vp, P(vp)]),
     "vct_decay_radiance": (st, [vp, vp]),
+    "vct_shade": (st, [vp, P(vct_gbuffer), P(C.c_float), P(vct_light), C.c_int32, P(vct_shadow_desc), vp, vp, vp,
+                       vp]),
     "vct_transform_actors": (st, [P(vct_triangles), P(vct_actor), C.c_int32, vp, vp, vp]),
     "vct_voxelize_static": (st, [P(vct_config), P(vct_params), P(vct_triangles), P(vct_light), C.c_int32,
                                  P(vct_shadow_desc), vp, vp, vp, P(vct_stats), vp]),

@@ -235,6 +235,11 @@ class Context:
         L.check(self._lib.vct_accumulators(self.handle, C.byref(a), C.byref(b)), "vct_accumulators")
         return int(a.value), int(b.value)
 
+    def shade(self, gb, eye, lights, shadow, color, irradiance=None, specular=None, stream=None):
+        arr, n = lights
+        L.check(self._lib.vct_shade(self.handle, C.byref(gb), f3(eye), arr, n, C.byref(shadow), _ptr(irradiance),
+                                    _ptr(specular), _ptr(color), _stream(stream)), "vct_shade")
+
     def decay_radiance(self, stream=None):
         L.check(self._lib.vct_decay_radiance(self.handle, _stream(stream)), "vct_decay_radiance")
 

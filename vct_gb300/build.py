@@ -38,6 +38,7 @@ CUDA_SOURCES = [
     ("trace.cu", ["--fmad=false"]),
     ("static_scratch.cu", []),
     ("learned.cu", ["--fmad=false"]),
+    ("shade.cu", ["--fmad=false"]),
 ]
 CXX_SOURCES = ["capi.cpp", "batch.cpp", "learned_capi.cpp"]
 

@@ -147,6 +147,8 @@ vct_status validate_params(const vct_params* p) {
         return fail(VCT_ERR_INVALID_ARGUMENT, "opacity/decay must be finite");
     if (p->warp_mode < VCT_WARP_NONE || p->warp_mode > VCT_WARP_TEXTURE)
         return fail(VCT_ERR_INVALID_ARGUMENT, "warp_mode must be one of VCT_WARP_*");
+    if (!std::isfinite(p->roughness) || !std::isfinite(p->metallic) || !std::isfinite(p->shininess))
+        return fail(VCT_ERR_INVALID_ARGUMENT, "roughness, metallic and shininess must be finite");
     if (!(p->warp_high_resolution > 0.0f && p->warp_high_resolution <= 32.0f) ||
         !(p->warp_low_resolution > 0.0f && p->warp_low_resolution <= 32.0f))
         return fail(VCT_ERR_INVALID_ARGUMENT, "warp resolutions must be in (0, 32]");
@@ -600,6 +602,12 @@ void vct_default_params(vct_params* p) {
     p->warp_mode = VCT_WARP_NONE;
     p->warp_high_resolution = 2.0f;  // src/Application.h:81-82
     p->warp_low_resolution = 0.5f;
+    p->cooktorrance = 1;  // src/Application.h:60-68
+    p->enable_diffuse = 1;
+    p->enable_specular = 1;
+    p->roughness = 0.5f;  // phong.frag:310 without a roughness map
+    p->metallic = 0.0f;
+    p->shininess = 32.0f;  // src/Graphics/Mesh.h:29
 }
 
 vct_status vct_voxel_mvp(const vct_config* cfg, float mvp_xyz[48]) {
@@ -979,6 +987,58 @@ vct_status vct_get_timers(vct_ctx* c, vct_timers* out) {
 }
 
 uint64_t vct_launch_count(void) { return g_launches.load(); }
+
+vct_status vct_shade(vct_ctx* c, const vct_gbuffer* g, const float eye[3], const vct_light* lights, int32_t n,
+                     const vct_shadow_desc* shadow, const float* irradiance, const float* specular, float* color,
+                     void* stream) {
+    if (!c || !eye || !color) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    vct_status s = validate_gbuffer(g);
+    if (s != VCT_OK) return s;
+    bool need_shadow = false;
+    if ((s = validate_lights(lights, n, &need_shadow)) != VCT_OK) return s;
+    if ((s = validate_shadow(shadow, need_shadow)) != VCT_OK) return s;
+    for (const void* p : {(const void*)irradiance, (const void*)specular, (const void*)color})
+        if (reinterpret_cast<uintptr_t>(p) % 16 != 0) return fail(VCT_ERR_INVALID_ARGUMENT, "float4 planes must be 16-byte aligned");
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    // the lights as the voxeliser holds them (neg_dir_n = normalize(-direction))
+    AccumParams A;
+    vct_triangles none = {};
+    fill_accum_inputs(c->cfg, c->params, c->mvp, &none, lights, n, need_shadow ? shadow : nullptr, A);
+    ShadeParams P;
+    std::memset(&P, 0, sizeof P);
+    P.gpos = reinterpret_cast<const float4*>(g->position_dev);
+    P.gnrm = reinterpret_cast<const float4*>(g->normal_dev);
+    P.galb = reinterpret_cast<const float4*>(g->albedo_dev);
+    P.irradiance = reinterpret_cast<const float4*>(irradiance);
+    P.specular = reinterpret_cast<const float4*>(specular);
+    P.color = reinterpret_cast<float4*>(color);
+    P.width = g->width;
+    P.height = g->height;
+    P.eye = to_f3(eye);
+    P.nlights = n;
+    std::memcpy(P.lights, A.lights, sizeof P.lights);
+    P.shadowmap = A.shadowmap;
+    P.sw = A.sw;
+    P.sh = A.sh;
+    std::memcpy(P.ls, A.ls, sizeof P.ls);
+    const vct_params& pr = c->params;
+    P.cooktorrance = pr.cooktorrance;
+    P.enable_diffuse = pr.enable_diffuse;
+    P.enable_specular = pr.enable_specular;
+    P.enable_indirect = pr.enable_indirect;
+    P.enable_reflections = pr.enable_reflections;
+    P.draw_occlusion = pr.draw_occlusion;
+    P.enable_postprocess = pr.enable_postprocess;
+    P.roughness = pr.roughness;
+    P.metallic = pr.metallic;
+    P.shininess = pr.shininess;
+    P.ambient_scale = pr.ambient_scale;
+    P.reflect_scale = pr.reflect_scale;
+    launch_shade(P, as_stream(stream));
+    VCT_CHECK_LAUNCH("shade");
+    return VCT_OK;
+}
 
 vct_status vct_decay_radiance(vct_ctx* c, void* stream) {
     if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");

@@ -178,6 +178,31 @@ __device__ __forceinline__ float shadow_bilinear(const float* __restrict__ sm, i
     return bot * (1.0f - b) + top * b;
 }
 
+// calcShadowFactor (voxelize.frag:160-184 = phong.frag:183-207): 5-tap PCF of
+// the bilinear light-space depth with bias 0.01; 0 beyond the far plane.
+__device__ __forceinline__ float pcf5(const float* __restrict__ sm, int sw, int sh, const float* ls, f3 wp) {
+    float c[4];
+    mat_vec(ls, wp.x, wp.y, wp.z, 1.0f, c);
+    // x / 1 == x exactly: skip the divide for an orthographic light.
+    if (c[3] != 1.0f) {
+        c[0] = __fdiv_rn(c[0], c[3]);
+        c[1] = __fdiv_rn(c[1], c[3]);
+        c[2] = __fdiv_rn(c[2], c[3]);
+    }
+    float sx = (c[0] + 1.0f) * 0.5f;
+    float sy = (c[1] + 1.0f) * 0.5f;
+    float sz = (c[2] + 1.0f) * 0.5f;
+    float frag = sz - 0.01f;
+    if (frag > 1.0f) return 0.0f;
+    const int ox[5] = {0, 1, 0, -1, 0};
+    const int oy[5] = {0, 0, 1, 0, -1};
+    float f = 0.0f;
+#pragma unroll
+    for (int s = 0; s < 5; ++s)
+        if (frag > shadow_bilinear(sm, sw, sh, sx, sy, ox[s], oy[s])) f += 1.0f;
+    return __fdiv_rn(f, 5.0f);
+}
+
 __device__ __forceinline__ uint32_t quant16(float x) { return __float2uint_rn(clampf(x, 0.0f, 1.0f) * 65535.0f); }
 
 // ------------------------------------------------------------ scene sets

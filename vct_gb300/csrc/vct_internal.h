@@ -358,6 +358,27 @@ struct ActorsDev {
 };
 void launch_transform_actors(const ActorsDev& A, cudaStream_t s);
 
+// phong.frag's composite with direct lighting (vct_shade).
+struct ShadeParams {
+    const float4* gpos;
+    const float4* gnrm;
+    const float4* galb;
+    const float4* irradiance;  // nullptr: no indirect term
+    const float4* specular;
+    float4* color;
+    int width, height;
+    f3 eye;
+    int nlights;
+    LightDev lights[VCT_MAX_LIGHTS];
+    const float* shadowmap;
+    int sw, sh;
+    float ls[16];
+    int cooktorrance, enable_diffuse, enable_specular, enable_indirect, enable_reflections, draw_occlusion,
+        enable_postprocess;
+    float roughness, metallic, shininess, ambient_scale, reflect_scale;
+};
+void launch_shade(const ShadeParams& P, cudaStream_t s);
+
 // Warp map of VCT_WARP_TEXTURE from a 32^3 occupancy bit mask.
 void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, float4* mapf, cudaStream_t s);
 

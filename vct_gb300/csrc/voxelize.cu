@@ -39,26 +39,7 @@ struct FragQueue {
 };
 
 __device__ __forceinline__ float shadow_factor(const AccumParams& P, f3 wp) {
-    float c[4];
-    mat_vec(P.ls, wp.x, wp.y, wp.z, 1.0f, c);
-    // x / 1 == x exactly: skip the divide for an orthographic light.
-    if (c[3] != 1.0f) {
-        c[0] = __fdiv_rn(c[0], c[3]);
-        c[1] = __fdiv_rn(c[1], c[3]);
-        c[2] = __fdiv_rn(c[2], c[3]);
-    }
-    float sx = (c[0] + 1.0f) * 0.5f;
-    float sy = (c[1] + 1.0f) * 0.5f;
-    float sz = (c[2] + 1.0f) * 0.5f;
-    float frag = sz - 0.01f;
-    if (frag > 1.0f) return 0.0f;
-    const int ox[5] = {0, 1, 0, -1, 0};
-    const int oy[5] = {0, 0, 1, 0, -1};
-    float f = 0.0f;
-#pragma unroll
-    for (int s = 0; s < 5; ++s)
-        if (frag > shadow_bilinear(P.shadowmap, P.sw, P.sh, sx, sy, ox[s], oy[s])) f += 1.0f;
-    return __fdiv_rn(f, 5.0f);
+    return pcf5(P.shadowmap, P.sw, P.sh, P.ls, wp);
 }
 
 // ------------------------------------------------------------- 1. setup
