@@ -61,6 +61,11 @@ def parse():
     ap.add_argument("--filter", default="software", choices=["software", "levels", "hardware"],
                     help="cone sampler: fp32 trilinear (exact), texture units per level + fp32 level blend, "
                          "or texture units' trilinear-mip")
+    ap.add_argument("--voxelizer", default="raster", choices=["raster", "tess"],
+                    help="rasterising voxeliser (voxelize.geom/.frag, the benchmark frame's) or the "
+                         "tessellation voxeliser (testTesselation.tesc/.tese)")
+    ap.add_argument("--warp", default="none", choices=["none", "perspective"],
+                    help="perspective: the voxelizeTesselationWarp froxel grid over the camera frustum")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-rows", type=int, default=24, help="rows of the frame traced by the CPU baseline")
@@ -224,6 +229,8 @@ def run_ours(args, rank, world):
     params = api.scene_params(sc)
     params.trace_filter = {"software": L.VCT_FILTER_SOFTWARE, "levels": L.VCT_FILTER_HARDWARE_LEVELS,
                            "hardware": L.VCT_FILTER_HARDWARE}[args.filter]
+    params.voxelize_tesselation = int(args.voxelizer == "tess")
+    params.warp_mode = L.VCT_WARP_PERSPECTIVE if args.warp == "perspective" else L.VCT_WARP_NONE
     ctx.set_params(params)
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -315,6 +322,10 @@ def run_ours(args, rank, world):
 
     # ---- roofline of the dominant kernel
     alg = algorithmic_bytes(sc, stats, None)
+    if args.voxelizer == "tess":
+        # triangles read once; the record of every occupied voxel read and written once (points that
+        # land in one voxel are summed before they reach memory)
+        alg["accumulate"] = sc.ntri * (36 + 36 + 12) + stats["unique_voxels"] * 32 * 2
     kernel_ms = {"accumulate": stage["voxelize_ms"], "inject_mark": stage["radiance_ms"],
                  "resolve+mips": stage["mipmap_ms"], "trace": stage["render_ms"]}
     dom = max(kernel_ms, key=kernel_ms.get)
@@ -324,12 +335,17 @@ def run_ours(args, rank, world):
     else:
         bytes_dom = alg[dom]
     achieved = bytes_dom / (kernel_ms[dom] * 1e-3) / 1e9
-    traffic = NCU_TRAFFIC.get(dom) if args.config == "large" else None
+    headline = args.config == "large" and args.voxelizer == "raster" and args.warp == "none"
+    traffic = NCU_TRAFFIC.get(dom) if headline else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
                 "traffic_source": "ncu dram read+write per launch, one capture of this workload",
                 "peak_source": peaks["source"], "algorithmic_bytes": int(bytes_dom),
                 "kernel_ms": round(kernel_ms[dom], 4)}
+    if dom == "accumulate" and args.voxelizer == "tess":
+        roofline["points_per_s"] = round(stats["total_voxel_fragments"] / (kernel_ms[dom] * 1e-3), 1)
+        roofline["note"] = ("the tessellation voxeliser is bound by its point rate (every point interpolated, "
+                            "mapped and summed into its voxel), not by HBM")
     if dom == "trace":
         roofline["samples_per_s"] = round(n_samples / (kernel_ms[dom] * 1e-3), 1)
         roofline["note"] = ("cone tracing is gather-bound (L1/L2 trilinear samples), not HBM-bound: its HBM "
@@ -340,8 +356,10 @@ def run_ours(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_frame * world, 4),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32 math, f16 volumes, u32 accumulators",
         "data": "synthetic seeded scene (no dataset); inputs resident in HBM",
-        "config": {"workload": WORKLOAD if args.config == "large" else f"{args.config} scene",
-                   "scene": args.config, "seed": args.seed, "triangles": sc.ntri, "grid": sc.dim, "levels": sc.levels,
+        "config": {"workload": WORKLOAD if headline else f"{args.config} scene, {args.voxelizer} voxeliser, "
+                                                             f"{args.warp} warp",
+                   "scene": args.config, "voxelizer": args.voxelizer, "warp": args.warp,
+                   "seed": args.seed, "triangles": sc.ntri, "grid": sc.dim, "levels": sc.levels,
                    "shadow_map": list(sc.shadow_size), "gbuffer": list(sc.gbuffer_size), "cones": "6x60deg + 1x10deg",
                    "sampler": args.filter, "parallelism": f"replicas x{world}",
                    "l2": "256 MiB buffer written between timed frames (outside the events)"},
@@ -763,7 +781,8 @@ def load_peaks() -> dict:
 
 
 # ----------------------------------------------------------- CPU side
-def cpu_frame_ms(sc, nthreads: int, sample_rows: int, shadowmap=None, gbuf=None) -> tuple[float, dict]:
+def cpu_frame_ms(sc, nthreads: int, sample_rows: int, shadowmap=None, gbuf=None, tesselation=False,
+                 warp_mode=0) -> tuple[float, dict]:
     """One CPU-oracle frame: full voxelize/normalize/inject/mips, trace of
     `sample_rows` evenly spaced rows, extrapolated to the full frame."""
     import oracle as O
@@ -771,19 +790,24 @@ def cpu_frame_ms(sc, nthreads: int, sample_rows: int, shadowmap=None, gbuf=None)
     W, H = sc.gbuffer_size
     sm = O.render_shadowmap(sc, nthreads) if shadowmap is None else shadowmap
     gp, gn, ga = O.render_gbuffer(sc) if gbuf is None else gbuf
+    w = O.warp(sc, warp_mode) if warp_mode else None
     t = {}
     t0 = time.perf_counter()
-    count, sums, total = O.voxelize(sc, sm, nthreads=nthreads)
+    if tesselation:
+        count, sums, total = O.voxelize_tess(sc, nthreads=nthreads, warp=w)
+    else:
+        count, sums, total = O.voxelize(sc, sm, nthreads=nthreads, warp=w)
     t1 = time.perf_counter()
     chain = np.zeros(4 * O.chain_voxels(sc.dim, sc.levels), dtype=np.uint16)
     color, normal, _, _ = O.normalize(sc, count, sums, radiance=chain, nthreads=nthreads)
     t2 = time.perf_counter()
-    O.inject(sc, sm, color, normal, chain, nthreads=nthreads)
+    O.inject(sc, sm, color, normal, chain, nthreads=nthreads, warp=w)
     t3 = time.perf_counter()
     O.build_mips(sc.dim, sc.levels, chain, nthreads)
     t4 = time.perf_counter()
     step = max(1, H // max(1, sample_rows))
-    O.trace(sc, chain, gp, gn, ga, precision=32, rows=(0, H), row_step=step, nthreads=nthreads, want=("color",))
+    O.trace(sc, chain, gp, gn, ga, precision=32, rows=(0, H), row_step=step, nthreads=nthreads, want=("color",),
+            warp=w)
     t5 = time.perf_counter()
     rows_traced = len(range(0, H, step))
     t = {"voxelize_ms": (t1 - t0) * 1e3, "normalize_ms": (t2 - t1) * 1e3, "inject_ms": (t3 - t2) * 1e3,
@@ -897,11 +921,14 @@ def main():
     if result is None:  # --profile-frames
         return
     if rank == 0 and not args.no_cpu_baseline:
-        ms, detail = cpu_frame_ms(sc, 1, args.cpu_sample_rows)
-        result["cpu_baseline"] = {"value": round(ms, 2), "unit": "ms/frame", "cores": 1, "kind": "port",
+        # the tessellation voxeliser's hundreds of millions of points take minutes on one core: all cores
+        cores = 1 if args.voxelizer == "raster" else (os.cpu_count() or 1)
+        ms, detail = cpu_frame_ms(sc, cores, args.cpu_sample_rows, tesselation=args.voxelizer == "tess",
+                                  warp_mode=3 if args.warp == "perspective" else 0)
+        result["cpu_baseline"] = {"value": round(ms, 2), "unit": "ms/frame", "cores": cores, "kind": "port",
                                   "sample": f"one frame: full voxelize/normalize/inject/mips + trace of "
                                             f"{detail['rows_traced']} evenly spaced rows scaled to the full frame, "
-                                            f"single thread", "cpu": cpu_model(), "nproc": os.cpu_count(),
+                                            f"{cores} thread(s)", "cpu": cpu_model(), "nproc": os.cpu_count(),
                                   "stage_ms": {k: round(v, 1) for k, v in detail.items()}}
     if rank == 0:
         print(json.dumps(result), flush=True)

@@ -8,6 +8,9 @@
  *
  *   reference program / call site                         entry point here
  *   voxelize.vert/.geom/.frag   src/Application.cpp:666-754   vct_voxelize_accumulate
+ *   simpleTesselated.vert, testTesselation.tesc/.tese
+ *                               src/Application.cpp:585-662   vct_voxelize_accumulate with
+ *                                                             params.voxelize_tesselation
  *   transferVoxels.comp         src/Application.cpp:757-785   vct_normalize
  *   (both, back to back)                                      vct_voxelize
  *   injectRadiance.comp         src/Application.cpp:788-837   vct_inject
@@ -120,10 +123,36 @@ typedef struct vct_cone_settings {
  *    binary16 (the RGBA16F weight textures), cell centres warped by the
  *    prefix sums of the widths (generateWarpmap.frag), stored RGBA16 unorm
  *    and read with trilinear filtering and clamp-to-edge. */
+/*  - PERSPECTIVE (voxelizeTesselationWarp): the grid is laid over the camera
+ *    frustum of `pv`; a world position maps to (pv p).xyz / (pv p).w * 0.5
+ *    + 0.5 (common.glsl:37-42).  Injection and the cone tracer use it as the
+ *    reference does (getVoxelPosition, phong.frag:158-160), and so does the
+ *    tessellation voxeliser; the rasterising voxeliser ignores it, as
+ *    voxelize.frag does.  Projected coordinates outside [-1, 2] (all of them
+ *    off the grid) are replaced by -1 so that points on or behind the camera
+ *    plane stay well defined. */
 #define VCT_WARP_NONE 0
 #define VCT_WARP_ANALYTIC 1
 #define VCT_WARP_TEXTURE 2
+#define VCT_WARP_PERSPECTIVE 3
 #define VCT_WARP_DIM 32
+
+/* Tessellation voxeliser (voxelizeTesselation: simpleTesselated.vert,
+ * testTesselation.tesc/.tese; Application.cpp:585-662).  Every triangle is a
+ * patch whose tessellation levels follow the control shader (each outer
+ * level the edge length in voxels along the edge direction, the inner level
+ * the longest altitude in voxels, all at least 1; a triangle whose three
+ * vertices truncate to one voxel is discarded), tessellated as GL's
+ * triangle primitive generator does in point mode with equal spacing (levels
+ * clamped to [1, max_tess_level] and rounded up; concentric inner rings built
+ * from the perpendiculars of the inner subdivision, OpenGL 4.6 section
+ * 11.2.2.1).  Every generated point stores the triangle's albedo and its
+ * interpolated normal into the voxel that contains it, unlit, like the
+ * evaluation shader.  The rasterising voxeliser stays the default of
+ * vct_default_params because the benchmark frame is defined on its
+ * pixel-centre rule; the reference's own default is the tessellation one
+ * (Application.h:100). */
+#define VCT_MAX_TESS_LEVEL 64 /* GL_MAX_TESS_GEN_LEVEL of the reference's GL implementation */
 
 /* Every hot-path uniform of the reference, with vct_default_params giving the
  * reference defaults of src/Application.h:36-103. */
@@ -161,6 +190,10 @@ typedef struct vct_params {
     float roughness;             /* 0.5: phong.frag's value without a roughness map */
     float metallic;              /* 0.0: without a metallic map */
     float shininess;             /* material.shininess (32, src/Graphics/Mesh.h:29) */
+    /* tessellation voxeliser and the perspective warp (Application.cpp:202,585-662) */
+    int32_t voxelize_tesselation; /* voxelizeTesselation (0 here; see VCT_MAX_TESS_LEVEL) */
+    float max_tess_level;         /* GL_MAX_TESS_GEN_LEVEL, in [1, VCT_MAX_TESS_LEVEL] (64) */
+    float pv[16];                 /* 'pv' = perspective(fov, aspect, 1, 20) * view, column-major */
 } vct_params;
 
 /* Caller-owned triangle soup on the device. */
@@ -260,7 +293,10 @@ vct_status vct_accumulators(const vct_ctx* ctx, const uint32_t** records_dev,
 
 /* ---- stages ----------------------------------------------------------- */
 /* voxelize.geom/.frag: rasterise every triangle along its dominant axis and
- * add colour, normal and count of each fragment into the accumulators. */
+ * add colour, normal and count of each fragment into the accumulators.  With
+ * params.voxelize_tesselation the triangles are tessellated into points
+ * instead (testTesselation.tesc/.tese) and lights and shadow map are not
+ * read; total_voxel_fragments then counts the generated points. */
 vct_status vct_voxelize_accumulate(vct_ctx* ctx, const vct_triangles* tris,
                                    const vct_light* lights, int32_t n_lights,
                                    const vct_shadow_desc* shadow, const float eye[3],

@@ -48,7 +48,8 @@ class orc_trace_params(C.Structure):
 
 
 class orc_warp(C.Structure):
-    _fields_ = [("mode", C.c_int32), ("map", C.c_void_p), ("eye_tc", C.c_float * 3)]
+    _fields_ = [("mode", C.c_int32), ("map", C.c_void_p), ("eye_tc", C.c_float * 3), ("pv", C.c_float * 16),
+                ("vmin", C.c_float * 3), ("vcenter", C.c_float * 3), ("ext", C.c_float * 3)]
 
 
 class orc_shade_params(C.Structure):
@@ -146,10 +147,16 @@ def voxel_mvp(scene) -> np.ndarray:
 
 def warp(scene, mode: int = 0, warpmap: np.ndarray | None = None):
     """orc_warp of a scene: mode 1 warps about the eye (warpVoxels), mode 2
-    reads `warpmap` (32^3 x 4 uint16, from warpmap()).  The struct keeps a
-    reference to the map."""
+    reads `warpmap` (32^3 x 4 uint16, from warpmap()), mode 3 projects with
+    the scene's `pv` (voxelizeTesselationWarp).  The struct keeps a reference
+    to the map."""
     w = orc_warp()
     w.mode = int(mode)
+    if getattr(scene, "pv", None) is not None:
+        w.pv = _f(scene.pv, 16)
+    w.vmin = _f([-scene.vmax] * 3, 3)
+    w.vcenter = _f([0, 0, 0], 3)
+    w.ext = _f([np.float32(scene.vmax) - np.float32(-scene.vmax)] * 3, 3)
     if warpmap is not None:
         w._map = np.ascontiguousarray(warpmap, dtype=np.uint16)
         w.map = w._map.ctypes.data
@@ -191,6 +198,44 @@ def voxelize(scene, shadowmap: np.ndarray, lighting: int = 1, axis_override: int
     load().orc_voxelize(C.byref(v), _p(pos), _p(nrm), _p(alb), C.c_int64(pos.shape[0]), arr, n, lighting,
                         axis_override, _p(sm), sw, sh, _f(scene.ls, 16), _p(count), _p(sums), C.byref(total),
                         nthreads, C.byref(warp) if warp is not None else None)
+    return count, sums, int(total.value)
+
+
+def tess_levels(scene, tri, max_level: float = 64.0, dim: int | None = None):
+    """Tessellation levels (inner, outer0, outer1, outer2) of one triangle
+    (9 floats), or None when the control shader discards it."""
+    v = volume(scene, dim)
+    t = np.ascontiguousarray(tri, dtype=np.float32).reshape(9)
+    out = np.zeros(4, dtype=np.int32)
+    ok = load().orc_tess_levels(C.byref(v), _p(t), C.c_float(max_level), _p(out))
+    return tuple(int(x) for x in out) if ok else None
+
+
+def tess_coords(levels) -> np.ndarray:
+    """gl_TessCoord of every point GL's triangle tessellation generates in
+    point mode for (inner, outer0, outer1, outer2), (npoints, 3) float32."""
+    lv = np.ascontiguousarray(levels, dtype=np.int32)
+    lib = load()
+    n = lib.orc_tess_point_count(_p(lv))
+    out = np.zeros((n, 3), dtype=np.float32)
+    lib.orc_tess_coords(_p(lv), _p(out))
+    return out
+
+
+def voxelize_tess(scene, max_level: float = 64.0, nthreads: int = 1, positions=None, normals=None, albedo=None,
+                  dim: int | None = None, warp=None):
+    """The tessellation voxeliser: (count[N^3], sums[6*N^3], total_points)."""
+    N = int(dim or scene.dim)
+    pos = np.ascontiguousarray(scene.positions if positions is None else positions, dtype=np.float32)
+    nrm = np.ascontiguousarray(scene.normals if normals is None else normals, dtype=np.float32)
+    alb = np.ascontiguousarray(scene.albedo if albedo is None else albedo, dtype=np.float32)
+    count = np.zeros(N ** 3, dtype=np.uint32)
+    sums = np.zeros(6 * N ** 3, dtype=np.uint32)
+    total = C.c_uint64(0)
+    v = volume(scene, N)
+    load().orc_voxelize_tess(C.byref(v), _p(pos), _p(nrm), _p(alb), C.c_int64(pos.shape[0]), C.c_float(max_level),
+                             C.byref(warp) if warp is not None else None, _p(count), _p(sums), C.byref(total),
+                             nthreads)
     return count, sums, int(total.value)
 
 
@@ -281,17 +326,21 @@ def f16_to_f32(h: np.ndarray) -> np.ndarray:
 
 
 def frame(scene, nthreads=1, precision=32, rows=None, row_step=1, shadowmap=None, gbuf=None, warp_mode=0,
-          warp_high=2.0, warp_low=0.5, **trace_over):
+          warp_high=2.0, warp_low=0.5, tesselation=False, max_tess_level=64.0, **trace_over):
     """The whole reference pipeline on the CPU (voxelize, normalise, inject,
     mips, trace), optionally warped (warp_mode 1: about the eye; 2: through
-    the warp map of the scene's 32^3 occupancy).  Returns a dict of every
-    intermediate."""
+    the warp map of the scene's 32^3 occupancy; 3: the perspective warp),
+    with the rasterising or (tesselation=True) the tessellation voxeliser.
+    Returns a dict of every intermediate."""
     sm = render_shadowmap(scene, nthreads) if shadowmap is None else shadowmap
     wmap = None
     if warp_mode == 2:
         wmap = warpmap(warp_occupancy(scene, sm, nthreads), warp_high, warp_low)
     w = warp(scene, warp_mode, wmap) if warp_mode else None
-    count, sums, total = voxelize(scene, sm, nthreads=nthreads, warp=w)
+    if tesselation:
+        count, sums, total = voxelize_tess(scene, max_tess_level, nthreads=nthreads, warp=w)
+    else:
+        count, sums, total = voxelize(scene, sm, nthreads=nthreads, warp=w)
     nv = scene.dim ** 3
     chain = np.zeros(4 * chain_voxels(scene.dim, scene.levels), dtype=np.uint16)
     color, normal, _, stats = normalize(scene, count, sums, radiance=chain, nthreads=nthreads)

@@ -355,14 +355,36 @@ static inline void warp_lookup(const uint16_t* map, const T p[3], T out[3]) {
         out[c] = y0 * (T(1) - a[2]) + y1 * a[2];
     }
 }
+// voxelTesselationWarpedPosition (common.glsl:37-42) of a world position:
+// (pv (p, 1)).xyz / w * 0.5 + 0.5.  Results outside [-1, 2] (off the grid for
+// every consumer), infinities and NaN become -1.
+template <typename T>
+static inline void perspective_tc(const orc_warp* w, const T p[3], T out[3]) {
+    const float* m = w->pv;
+    T c[4];
+    for (int r = 0; r < 4; ++r)
+        c[r] = (((T)m[r] * p[0] + (T)m[4 + r] * p[1]) + (T)m[8 + r] * p[2]) + (T)m[12 + r] * T(1);
+    bool inside = true;
+    for (int k = 0; k < 3; ++k) {
+        out[k] = c[k] / c[3] * T(0.5) + T(0.5);
+        inside = inside && out[k] >= T(-1) && out[k] <= T(2);
+    }
+    if (!inside) out[0] = out[1] = out[2] = T(-1);
+}
 template <typename T>
 static inline void apply_warp(const orc_warp* w, T p[3]) {
     if (!w || w->mode == 0) return;
     T o[3];
-    if (w->mode == 1)
+    if (w->mode == 1) {
         voxel_warp(p, w->eye_tc, o);
-    else
+    } else if (w->mode == 3) {
+        // phong.frag:159: back to world space, then projected
+        T wp[3];
+        for (int k = 0; k < 3; ++k) wp[k] = (p[k] * (T)w->ext[k] + (T)w->vcenter[k]) + (T)w->vmin[k];
+        perspective_tc(w, wp, o);
+    } else {
         warp_lookup(w->map, p, o);
+    }
     p[0] = o[0];
     p[1] = o[1];
     p[2] = o[2];
@@ -402,7 +424,9 @@ void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, con
                   int32_t axis_override, const float* sm, int32_t sw, int32_t sh, const float ls[16],
                   uint32_t* count, uint32_t* sums, uint32_t* total_fragments, int32_t nthreads,
                   const orc_warp* warp) {
-    const bool warped = warp && warp->mode != 0;
+    // voxelize.frag reads warpVoxels and warpTexture; voxelizeTesselationWarp
+    // (mode 3) leaves the rasterised grid linear.
+    const bool warped = warp && warp->mode != 0 && warp->mode != 3;
     const int N = vol->dim;
     const int64_t NV = (int64_t)N * N * N;
     float mvp[48];
@@ -540,6 +564,194 @@ void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, con
     if (total_fragments) *total_fragments += (uint32_t)total.load();
 }
 
+// ------------------------------------------------- tessellation voxeliser
+// simpleTesselated.vert -> testTesselation.tesc -> GL's triangle primitive
+// generator (point_mode, equal_spacing) -> testTesselation.tese.
+
+// ivec3(x): truncation toward zero; NaN gives 0 and values beyond the int
+// range saturate, as the GPU's conversion does.
+static inline int trunc_sat(float x) {
+    if (!(x == x)) return 0;
+    if (x >= 2147483648.0f) return 2147483647;
+    if (x <= -2147483648.0f) return (-2147483647 - 1);
+    return (int)x;
+}
+
+// Level after clamping to [1, max] and rounding up (equal_spacing).
+static inline int round_level(float level, float max_level) {
+    return (int)std::ceil(std::fmin(std::fmax(level, 1.0f), max_level));
+}
+
+int32_t orc_tess_levels(const orc_volume* vol, const float* tri, float max_level, int32_t out[4]) {
+    const f3 vmin = ld3(vol->vmin), vmax = ld3(vol->vmax), vc = ld3(vol->vcenter);
+    const f3 ext = sub(vmax, vmin);
+    const float fN = (float)vol->dim;
+    const f3 a = ld3(tri), b = ld3(tri + 3), c = ld3(tri + 6);
+    // testTesselation.tesc:15-21,42-43: ivec3(voxelDim * getVoxelPosition(p))
+    auto vox = [&](f3 p, int v[3]) {
+        v[0] = trunc_sat(fN * (((p.x - vc.x) - vmin.x) / ext.x));
+        v[1] = trunc_sat(fN * (((p.y - vc.y) - vmin.y) / ext.y));
+        v[2] = trunc_sat(fN * (((p.z - vc.z) - vmin.z) / ext.z));
+    };
+    int va[3], vb[3], vcc[3];
+    vox(a, va);
+    vox(b, vb);
+    vox(c, vcc);
+    if (va[0] == vb[0] && va[1] == vb[1] && va[2] == vb[2] && va[0] == vcc[0] && va[1] == vcc[1] &&
+        va[2] == vcc[2])
+        return 0;  // all levels 0: the patch is discarded
+    // :51-71, edges opposite each vertex, Heron's area, altitudes
+    const f3 A = sub(c, b), B = sub(c, a), C = sub(b, a);
+    const float la = length(A), lb = length(B), lc = length(C);
+    const float s = ((la + lb) + lc) * 0.5f;
+    const float area = std::sqrt(((s * (s - la)) * (s - lb)) * (s - lc));
+    const float alt[3] = {2.0f * area / la, 2.0f * area / lb, 2.0f * area / lc};
+    const float max_alt = std::fmax(alt[0], std::fmax(alt[1], alt[2]));  // GLSL max: a NaN operand loses
+    const f3 vs = mk(ext.x / fN, ext.y / fN, ext.z / fN);
+    auto div_factor = [&](f3 e) { return std::fabs(length(mulv(normalize(e), vs))); };
+    const float outer[3] = {std::fmax(1.0f, la / div_factor(A)), std::fmax(1.0f, lb / div_factor(B)),
+                            std::fmax(1.0f, lc / div_factor(C))};
+    const float inner = std::fmax(1.0f, max_alt / vs.x);
+    // :73-76: TessLevelOuter[0] = outer.z, [1] = outer.x, [2] = outer.y
+    int n = round_level(inner, max_level);
+    const int m0 = round_level(outer[2], max_level), m1 = round_level(outer[0], max_level),
+              m2 = round_level(outer[1], max_level);
+    // An inner level of 1 with any outer level above 1 counts as 1 + epsilon.
+    if (n == 1 && (m0 > 1 || m1 > 1 || m2 > 1)) n = 2;
+    out[0] = n;
+    out[1] = m0;
+    out[2] = m1;
+    out[3] = m2;
+    return 1;
+}
+
+int32_t orc_tess_point_count(const int32_t lv[4]) {
+    int32_t total = lv[1] + lv[2] + lv[3];  // outer ring: corners + (m - 1) per edge
+    for (int q = lv[0] - 2; q >= 0; q -= 2) total += q > 0 ? 3 * q : 1;  // inner rings
+    return total;
+}
+
+// OpenGL 4.6 section 11.2.2.1, point mode.  Order: the corners (1,0,0),
+// (0,1,0), (0,0,1); the inner points of the u = 0 edge (outer[0], from
+// vertex 1 to vertex 2), of the v = 0 edge (outer[1], vertex 2 to 0) and of
+// the w = 0 edge (outer[2], vertex 0 to 1), at j/m; then the inner rings from
+// the outside in.  In the equilateral domain the inner subdivision has n
+// segments per edge; ring k's corner next to vertex 0 is where the
+// perpendiculars to the two adjacent edges through their subdivision points
+// at distance k/n from ring k-1's corners meet, which in barycentric
+// coordinates is (1 - 2t, t, t) with t = 2k / (3n).  Its edges keep the
+// spacing 1/n: n - 2k segments, 3 (n - 2k) points, and a single centre point
+// when n - 2k = 0.
+void orc_tess_coords(const int32_t lv[4], float* out) {
+    const int n = lv[0];
+    int64_t o = 0;
+    auto put = [&](float u, float v, float w) {
+        out[o++] = u;
+        out[o++] = v;
+        out[o++] = w;
+    };
+    put(1.0f, 0.0f, 0.0f);
+    put(0.0f, 1.0f, 0.0f);
+    put(0.0f, 0.0f, 1.0f);
+    for (int j = 1; j < lv[1]; ++j) {
+        const float s = (float)j / (float)lv[1];
+        put(0.0f, 1.0f - s, s);
+    }
+    for (int j = 1; j < lv[2]; ++j) {
+        const float s = (float)j / (float)lv[2];
+        put(s, 0.0f, 1.0f - s);
+    }
+    for (int j = 1; j < lv[3]; ++j) {
+        const float s = (float)j / (float)lv[3];
+        put(1.0f - s, s, 0.0f);
+    }
+    for (int k = 1; n - 2 * k >= 0; ++k) {
+        const int q = n - 2 * k;
+        if (q == 0) {
+            const float third = 1.0f / 3.0f;
+            put(third, third, third);
+            break;
+        }
+        const float t = (float)(2 * k) / (float)(3 * n);
+        const float h = 1.0f - 2.0f * t;
+        const float corner[3][3] = {{h, t, t}, {t, h, t}, {t, t, h}};
+        for (int e = 0; e < 3; ++e) {
+            const float* p0 = corner[e];
+            const float* p1 = corner[(e + 1) % 3];
+            for (int j = 0; j < q; ++j) {
+                const float s = (float)j / (float)q;
+                put(p0[0] + s * (p1[0] - p0[0]), p0[1] + s * (p1[1] - p0[1]), p0[2] + s * (p1[2] - p0[2]));
+            }
+        }
+    }
+}
+
+void orc_voxelize_tess(const orc_volume* vol, const float* pos, const float* nrm, const float* albedo,
+                       int64_t ntri, float max_level, const orc_warp* warp, uint32_t* count, uint32_t* sums,
+                       uint64_t* total_points, int32_t nthreads) {
+    const int N = vol->dim;
+    const int64_t NV = (int64_t)N * N * N;
+    const f3 vmin = ld3(vol->vmin), vmax = ld3(vol->vmax), vc = ld3(vol->vcenter);
+    const f3 ext = sub(vmax, vmin);
+    const bool persp = warp && warp->mode == 3;  // the other warps are off in the evaluation shader
+    std::atomic<uint64_t> total{0};
+    const bool atomic = nthreads > 1;
+    auto addu = [atomic](uint32_t* p, uint32_t v) {
+        if (atomic)
+            __atomic_fetch_add(p, v, __ATOMIC_RELAXED);
+        else
+            *p += v;
+    };
+    parallel_for(ntri, nthreads, [&](int64_t t0, int64_t t1) {
+        uint64_t local = 0;
+        std::vector<float> bc;
+        for (int64_t t = t0; t < t1; ++t) {
+            int32_t lv[4];
+            if (!orc_tess_levels(vol, pos + t * 9, max_level, lv)) continue;
+            const int32_t np = orc_tess_point_count(lv);
+            bc.resize((size_t)np * 3);
+            orc_tess_coords(lv, bc.data());
+            local += (uint64_t)np;
+            const float* P = pos + t * 9;
+            const float* Nn = nrm + t * 9;
+            const f3 p0 = ld3(P), p1 = ld3(P + 3), p2 = ld3(P + 6);
+            const f3 n0 = ld3(Nn), n1 = ld3(Nn + 3), n2 = ld3(Nn + 6);
+            const f3 col = ld3(albedo + t * 3);
+            const uint32_t qc[3] = {quant16(col.x), quant16(col.y), quant16(col.z)};
+            for (int32_t i = 0; i < np; ++i) {
+                const float u = bc[3 * i], v = bc[3 * i + 1], w = bc[3 * i + 2];
+                // testTesselation.tese:102-110: u P0 + v P1 + w P2
+                const f3 p = add(add(mul(p0, u), mul(p1, v)), mul(p2, w));
+                const f3 nn = add(add(mul(n0, u), mul(n1, v)), mul(n2, w));
+                float tc[3];
+                if (persp) {
+                    const float wp[3] = {p.x, p.y, p.z};
+                    perspective_tc(warp, wp, tc);
+                } else {
+                    tc[0] = ((p.x - vc.x) - vmin.x) / ext.x;
+                    tc[1] = ((p.y - vc.y) - vmin.y) / ext.y;
+                    tc[2] = ((p.z - vc.z) - vmin.z) / ext.z;
+                }
+                const int x = trunc_sat((float)N * tc[0]), y = trunc_sat((float)N * tc[1]),
+                          z = trunc_sat((float)N * tc[2]);
+                if (x < 0 || y < 0 || z < 0 || x >= N || y >= N || z >= N) continue;
+                const int64_t vi = ((int64_t)z * N + y) * N + x;
+                // voxelStore: normal = normalize(normal) * 0.5 + 0.5
+                const f3 Nf = normalize(nn);
+                addu(count + vi, 1u);
+                addu(sums + 0 * NV + vi, qc[0]);
+                addu(sums + 1 * NV + vi, qc[1]);
+                addu(sums + 2 * NV + vi, qc[2]);
+                addu(sums + 3 * NV + vi, quant16(Nf.x * 0.5f + 0.5f));
+                addu(sums + 4 * NV + vi, quant16(Nf.y * 0.5f + 0.5f));
+                addu(sums + 5 * NV + vi, quant16(Nf.z * 0.5f + 0.5f));
+            }
+        }
+        total.fetch_add(local);
+    });
+    if (total_points) *total_points += total.load();
+}
+
 // --------------------------------------------------------------- normalize
 void orc_normalize(const orc_volume* vol, float opacity, int32_t temporal, float decay,
                    const uint32_t* count, const uint32_t* sums, uint16_t* color, uint16_t* normal,
@@ -616,7 +828,12 @@ void orc_inject(const orc_volume* vol, const float* sm, int32_t sw, int32_t sh, 
     auto vindex = [&](f3 w) {
         float tc[3] = {((w.x - vc.x) - vmin.x) / ext.x, ((w.y - vc.y) - vmin.y) / ext.y,
                        ((w.z - vc.z) - vmin.z) / ext.z};
-        apply_warp(warp, tc);  // getVoxelPosition (common.glsl:44-60)
+        if (warp && warp->mode == 3) {  // getVoxelPosition projects the world position
+            const float wp[3] = {w.x, w.y, w.z};
+            perspective_tc(warp, wp, tc);
+        } else {
+            apply_warp(warp, tc);  // getVoxelPosition (common.glsl:44-60)
+        }
         return mk((float)N * tc[0], (float)N * tc[1], (float)N * tc[2]);
     };
     f3 lvox = vindex(ld3(lpos));

@@ -7,6 +7,7 @@
  *   shaders/common.glsl:1-64          voxel coordinate mapping
  *   shaders/voxelize.geom:25-73       dominant-axis projection
  *   shaders/voxelize.frag:75-108,159-280  fragment lighting, PCF, accumulation
+ *   shaders/testTesselation.tesc/.tese    the tessellation voxeliser
  *   shaders/transferVoxels.comp:29-70 normalisation / opacity / radiance seed
  *   shaders/injectRadiance.comp:40-103 shadow-map injection
  *   shaders/filterRadiance.comp:14-65 2x2x2 box mip
@@ -39,11 +40,15 @@ typedef struct orc_volume {
 } orc_volume;
 
 /* Voxel warping: mode 0 none, 1 voxelWarp about eye_tc (warpVoxels),
- * 2 the 32^3 RGBA16 unorm warp map (warpTexture). */
+ * 2 the 32^3 RGBA16 unorm warp map (warpTexture), 3 the perspective
+ * projection pv of voxelizeTesselationWarp (common.glsl:37-42; volume
+ * coordinates go back to world space through vmin, vcenter, ext). */
 typedef struct orc_warp {
     int32_t mode;
     const uint16_t* map;
     float eye_tc[3];
+    float pv[16];
+    float vmin[3], vcenter[3], ext[3];
 } orc_warp;
 
 /* Same layout as vct_light (80 bytes). */
@@ -88,6 +93,22 @@ void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, con
                   int32_t axis_override, const float* shadowmap, int32_t sw, int32_t sh,
                   const float ls[16], uint32_t* count, uint32_t* sums, uint32_t* total_fragments,
                   int32_t nthreads, const orc_warp* warp);
+
+/* Tessellation voxeliser (testTesselation.tesc/.tese): levels of one
+ * triangle (9 floats) after GL's equal_spacing rounding, out = {inner,
+ * outer0, outer1, outer2}; returns 0 when the control shader discards the
+ * patch (all three vertices in one voxel). */
+int32_t orc_tess_levels(const orc_volume* vol, const float* tri, float max_level, int32_t out[4]);
+/* Number of points of GL's triangle tessellation in point mode, and their
+ * gl_TessCoord (3 floats each) in this oracle's enumeration order. */
+int32_t orc_tess_point_count(const int32_t levels[4]);
+void orc_tess_coords(const int32_t levels[4], float* out);
+/* Every generated point stores the triangle's albedo and its normal into
+ * the voxel holding it (linear mapping, or warp mode 3).  count/sums as for
+ * orc_voxelize; total_points counts the generated points. */
+void orc_voxelize_tess(const orc_volume* vol, const float* pos, const float* nrm, const float* albedo,
+                       int64_t ntri, float max_level, const orc_warp* warp, uint32_t* count, uint32_t* sums,
+                       uint64_t* total_points, int32_t nthreads);
 
 /* transferVoxels.comp; radiance/colour/normal are dim^3 RGBA16F (uint16 x4). */
 void orc_normalize(const orc_volume* vol, float voxel_set_opacity, int32_t temporal_filter,

@@ -1,0 +1,156 @@
+"""The tessellation voxeliser (testTesselation.tesc/.tese) and the
+perspective warp (voxelizeTesselationWarp) against the oracle: accumulators
+bit-exact with and without the warp, the whole frame with either voxeliser
+under the perspective warp (volumes bit-exact, irradiance within the trace
+tolerances), and the batch's refusal."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import GpuScene, read_chain, rel_l2, rgb, split_records
+from vct_gb300 import _lib as L
+from vct_gb300 import api, scenes
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    # walls span the grid (levels near the 64 limit), a sphere of small triangles (many discarded)
+    "cornell": lambda: scenes.cornell(seed=2),
+    # boxes and slivers of the large frame's family: columns of 256 segments put many points in one voxel
+    "family": lambda: scenes.large_family(seed=3, dim=128, shadow=1024, gbuffer=(320, 180), n_boxes=512, n_cyl=8,
+                                          cyl_segments=256),
+}
+
+
+@pytest.fixture(scope="module", params=[(c, w) for c in CASES for w in (L.VCT_WARP_NONE, L.VCT_WARP_PERSPECTIVE)],
+                ids=lambda p: f"{p[0]}-{'persp' if p[1] else 'linear'}")
+def tess(request):
+    import torch
+
+    name, mode = request.param
+    sc = CASES[name]()
+    g = GpuScene(sc)
+    w = O.warp(sc, mode) if mode else None
+    ref = O.voxelize_tess(sc, nthreads=8, warp=w)
+    ctx = api.Context(api.config_for(sc))
+    ctx.set_params(api.scene_params(sc, voxelize_tesselation=1, warp_mode=mode))
+    ctx.voxelize_accumulate(g.tris, g.lights, g.shadow, sc.eye)
+    torch.cuda.synchronize()
+    got = split_records(*ctx.read_accumulators())
+    ctx.normalize()
+    torch.cuda.synchronize()
+    return name, mode, sc, ref, got, ctx.stats()
+
+
+def test_tess_accumulators_bitexact(tess):
+    name, mode, sc, (count, sums, total), (gc, gs, gocc, pad), stats = tess
+    assert count.sum() > 1000
+    assert np.array_equal(gc, count)
+    assert np.array_equal(gs, sums)
+    assert np.array_equal(gocc, count > 0)
+    assert np.all(pad == 0)
+    assert stats["total_voxel_fragments"] == total
+    assert stats["unique_voxels"] == int((count > 0).sum())
+    assert stats["max_fragments_per_voxel"] == int(count.max())
+    print(f"{name}: {total} points, {int((count > 0).sum())} voxels, max {int(count.max())} per voxel")
+
+
+def test_tess_differs_from_rasterising(tess):
+    name, mode, sc, (count, _, _), _, _ = tess
+    if mode:
+        pytest.skip("compared unwarped")
+    raster, _, _ = O.voxelize(sc, O.render_shadowmap(sc), nthreads=8)
+    assert not np.array_equal(raster > 0, count > 0)
+    # the same surfaces: most occupied voxels agree
+    both = np.logical_and(raster > 0, count > 0).sum()
+    assert both > 0.5 * (count > 0).sum()
+
+
+def test_slivers_exercise_the_aggregated_stores():
+    """Columns of thin triangles put several points of one warp into one
+    voxel; the summed stores equal one store per point (the oracle)."""
+    import torch
+
+    sc = scenes.large_family(seed=5, dim=64, shadow=512, gbuffer=(64, 36), n_boxes=4, n_cyl=6, cyl_segments=1024)
+    g = GpuScene(sc)
+    count, sums, total = O.voxelize_tess(sc, nthreads=8)
+    assert count.max() >= 32
+    ctx = api.Context(api.config_for(sc))
+    ctx.set_params(api.scene_params(sc, voxelize_tesselation=1))
+    ctx.voxelize_accumulate(g.tris, g.lights, g.shadow, sc.eye)
+    torch.cuda.synchronize()
+    gc, gs, _, _ = split_records(*ctx.read_accumulators())
+    assert np.array_equal(gc, count) and np.array_equal(gs, sums)
+
+
+@pytest.fixture(scope="module", params=[True, False], ids=["tess", "raster"])
+def persp_frame(request):
+    import torch
+
+    tesselation = request.param
+    sc = scenes.cornell(seed=7, gbuffer=(320, 180))
+    g = GpuScene(sc)
+    sm, gbuf = g.host_inputs()
+    ref = O.frame(sc, shadowmap=sm, gbuf=gbuf, warp_mode=L.VCT_WARP_PERSPECTIVE, tesselation=tesselation,
+                  nthreads=8)
+    ref64 = O.trace(sc, ref["chain"], *gbuf, precision=64, want=("irr",), warp=ref["warp"], nthreads=8)
+    prm = api.scene_params(sc, warp_mode=L.VCT_WARP_PERSPECTIVE, voxelize_tesselation=int(tesselation))
+    # stage by stage
+    ctx = api.Context(api.config_for(sc))
+    ctx.set_params(prm)
+    ctx.voxelize(g.tris, g.lights, g.shadow, sc.eye)
+    ctx.inject(g.shadow, sc.eye)
+    ctx.build_mips()
+    irr, spec, col, samples = g.new_outputs()
+    ctx.trace(g.gb, sc.eye, api.trace_out(irr, spec, col, samples))
+    torch.cuda.synchronize()
+    stage = dict(chain=read_chain(ctx), irr=irr.cpu().numpy())
+    # fused
+    ctx2 = api.Context(api.config_for(sc))
+    ctx2.set_params(prm)
+    irr2, spec2, col2, samples2 = g.new_outputs()
+    ctx2.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(irr2, spec2, col2, samples2))
+    torch.cuda.synchronize()
+    fused = dict(chain=read_chain(ctx2), irr=irr2.cpu().numpy(), stats=ctx2.stats())
+    return tesselation, sc, ref, ref64, stage, fused
+
+
+def test_perspective_frame_chain_bitexact(persp_frame):
+    tesselation, sc, ref, _, stage, fused = persp_frame
+    assert np.count_nonzero(ref["chain"]) > 1000
+    assert np.array_equal(stage["chain"], ref["chain"])
+    assert np.array_equal(fused["chain"], ref["chain"])
+    assert fused["stats"]["total_voxel_fragments"] == ref["stats"]["total_voxel_fragments"]
+    lin = O.frame(sc, shadowmap=ref["shadowmap"], gbuf=(ref["gpos"], ref["gnrm"], ref["galb"]),
+                  tesselation=tesselation, nthreads=8, rows=(0, 1))
+    if tesselation:  # the froxel grid differs from the linear one
+        assert not np.array_equal(lin["count"] > 0, ref["count"] > 0)
+    else:  # voxelize.frag ignores voxelizeTesselationWarp; injection and the trace do not
+        assert np.array_equal(lin["count"], ref["count"])
+        assert not np.array_equal(lin["chain"], ref["chain"])
+
+
+def test_perspective_frame_trace(persp_frame):
+    tesselation, sc, ref, ref64, stage, fused = persp_frame
+    irr = rgb(stage["irr"])
+    assert np.abs(irr).sum() > 0
+    assert rel_l2(irr, rgb(ref["irradiance"])) <= 1e-5
+    e64 = rel_l2(irr, rgb(ref64[0]))
+    print(f"perspective warp ({'tess' if tesselation else 'raster'}): irradiance rel L2 vs fp64 {e64:.2e}")
+    assert e64 <= 1e-3
+    assert np.array_equal(stage["irr"].view(np.uint32), fused["irr"].view(np.uint32))
+
+
+def test_batch_refuses_tesselation_and_perspective():
+    sc = scenes.batch_scene(seed=1, index=0)
+    g = GpuScene(sc)
+    b = api.Batch([api.config_for(sc)])
+    for over in (dict(voxelize_tesselation=1), dict(warp_mode=L.VCT_WARP_PERSPECTIVE)):
+        b.set_params(api.scene_params(sc, **over), 0)
+        o = g.new_outputs()
+        with pytest.raises(L.VctError) as e:
+            b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))])
+        assert e.value.status == L.VCT_ERR_UNSUPPORTED

@@ -30,7 +30,9 @@ VCT_FILTER_HARDWARE_LEVELS = 2
 VCT_WARP_NONE = 0
 VCT_WARP_ANALYTIC = 1
 VCT_WARP_TEXTURE = 2
+VCT_WARP_PERSPECTIVE = 3
 VCT_WARP_DIM = 32
+VCT_MAX_TESS_LEVEL = 64
 VCT_MAX_ACTORS = 64
 VCT_VOLUME_COLOR = 0
 VCT_VOLUME_NORMAL = 1
@@ -78,6 +80,7 @@ class vct_params(C.Structure):
         ("warp_mode", C.c_int32), ("warp_high_resolution", C.c_float), ("warp_low_resolution", C.c_float),
         ("cooktorrance", C.c_int32), ("enable_diffuse", C.c_int32), ("enable_specular", C.c_int32),
         ("roughness", C.c_float), ("metallic", C.c_float), ("shininess", C.c_float),
+        ("voxelize_tesselation", C.c_int32), ("max_tess_level", C.c_float), ("pv", f16),
     ]
 
 

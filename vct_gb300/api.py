@@ -58,6 +58,8 @@ def scene_params(scene, **overrides) -> L.vct_params:
             steps, ang, bias, h0, lod = scene.cone[key]
             setattr(p, name, L.vct_cone_settings(int(steps), float(ang), float(bias), float(h0), float(lod)))
     p.max_distance = float(np.sqrt(3.0))  # grid diagonal in texture units
+    if getattr(scene, "pv", None) is not None:
+        p.pv = (C.c_float * 16)(*np.asarray(scene.pv, dtype=np.float32).tolist())
     for k, v in overrides.items():
         setattr(p, k, v)
     return p

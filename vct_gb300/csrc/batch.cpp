@@ -65,8 +65,10 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         if (c->params.trace_filter != filter) return fail(VCT_ERR_INVALID_ARGUMENT, "all scenes of a batch must use the same trace_filter");
         if (filter != VCT_FILTER_SOFTWARE && (s = ensure_texture(c)) != VCT_OK) return s;
         const bool hw = filter != VCT_FILTER_SOFTWARE;
-        if (c->params.warp_mode == VCT_WARP_TEXTURE)
-            return fail(VCT_ERR_UNSUPPORTED, "batches do not build warp maps: use VCT_WARP_NONE or VCT_WARP_ANALYTIC");
+        if (c->params.warp_mode == VCT_WARP_TEXTURE || c->params.warp_mode == VCT_WARP_PERSPECTIVE)
+            return fail(VCT_ERR_UNSUPPORTED, "batches support VCT_WARP_NONE and VCT_WARP_ANALYTIC only");
+        if (c->params.voxelize_tesselation)
+            return fail(VCT_ERR_UNSUPPORTED, "batches use the rasterising voxeliser (voxelize_tesselation = 0)");
         AccumParams A;
         fill_accum_inputs(c->cfg, c->params, c->mvp, &d.triangles, d.lights, d.n_lights, &d.shadow, A);
         A.warp = warp_dev(c, d.eye);
@@ -87,6 +89,7 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         R.light_int = I.light_int;
         R.warp = I.warp;
         R.light_tc = I.light_tc;
+        R.light_pos = I.light_pos;
         R.lit = c->lit;
         R.mip_levels = std::min(4, c->levels - 1);
         for (int l = 0; l <= R.mip_levels; ++l) {

@@ -145,8 +145,14 @@ vct_status validate_params(const vct_params* p) {
     if (p->axis_override < -1 || p->axis_override > 2) return fail(VCT_ERR_INVALID_ARGUMENT, "axis_override in [-1, 2]");
     if (!std::isfinite(p->voxel_set_opacity) || !std::isfinite(p->temporal_decay))
         return fail(VCT_ERR_INVALID_ARGUMENT, "opacity/decay must be finite");
-    if (p->warp_mode < VCT_WARP_NONE || p->warp_mode > VCT_WARP_TEXTURE)
+    if (p->warp_mode < VCT_WARP_NONE || p->warp_mode > VCT_WARP_PERSPECTIVE)
         return fail(VCT_ERR_INVALID_ARGUMENT, "warp_mode must be one of VCT_WARP_*");
+    if (p->voxelize_tesselation != 0 && p->voxelize_tesselation != 1)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "voxelize_tesselation must be 0 or 1");
+    if (!(p->max_tess_level >= 1.0f && p->max_tess_level <= (float)VCT_MAX_TESS_LEVEL))
+        return fail(VCT_ERR_INVALID_ARGUMENT, "max_tess_level must be in [1, VCT_MAX_TESS_LEVEL]");
+    for (int i = 0; i < 16; ++i)
+        if (!std::isfinite(p->pv[i])) return fail(VCT_ERR_INVALID_ARGUMENT, "pv must be finite");
     if (!std::isfinite(p->roughness) || !std::isfinite(p->metallic) || !std::isfinite(p->shininess))
         return fail(VCT_ERR_INVALID_ARGUMENT, "roughness, metallic and shininess must be finite");
     if (!(p->warp_high_resolution > 0.0f && p->warp_high_resolution <= 32.0f) ||
@@ -245,6 +251,11 @@ void fill_accum_inputs(const vct_config& cfg, const vct_params& prm, const float
         L.range075 = 0.75f * lights[i].range;
     }
     std::memcpy(P.mvp, mvp, sizeof P.mvp);
+    P.vmin = to_f3(cfg.voxel_min);
+    P.vcenter = to_f3(cfg.voxel_center);
+    P.ext = {cfg.voxel_max[0] - cfg.voxel_min[0], cfg.voxel_max[1] - cfg.voxel_min[1],
+             cfg.voxel_max[2] - cfg.voxel_min[2]};
+    P.max_tess_level = prm.max_tess_level;
     if (sh) {
         std::memcpy(P.ls, sh->ls, sizeof P.ls);
         P.shadowmap = sh->shadowmap_dev;
@@ -296,6 +307,11 @@ WarpDev warp_dev(const vct_ctx* ctx, const float* eye) {
     std::memset(&W, 0, sizeof W);
     W.mode = ctx->params.warp_mode;
     W.mapf = ctx->warpmap_f;
+    std::memcpy(W.pv, ctx->params.pv, sizeof W.pv);
+    W.vmin = to_f3(ctx->cfg.voxel_min);
+    W.vcenter = to_f3(ctx->cfg.voxel_center);
+    W.ext = {ctx->cfg.voxel_max[0] - ctx->cfg.voxel_min[0], ctx->cfg.voxel_max[1] - ctx->cfg.voxel_min[1],
+             ctx->cfg.voxel_max[2] - ctx->cfg.voxel_min[2]};
     if (eye) {  // voxelLinearPosition(eye) (common.glsl:6-9)
         float tc[3];
         for (int k = 0; k < 3; ++k)
@@ -325,8 +341,19 @@ vct_status build_warpmap(vct_ctx* ctx, const AccumParams& A, cudaStream_t st) {
     return VCT_OK;
 }
 
+// The voxeliser the parameters select: rasterising (voxelize.geom/.frag) or
+// tessellating (testTesselation.tesc/.tese).
+void launch_voxelizer(const vct_ctx* ctx, const AccumParams& P, cudaStream_t st) {
+    if (ctx->params.voxelize_tesselation)
+        launch_tesselate(P, st);
+    else
+        launch_accumulate(P, st);
+}
+
 vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lights, int n,
                       const vct_shadow_desc* sh, const float* eye, AccumParams& P) {
+    if (ctx->params.voxelize_tesselation && t->count > (1LL << 24))
+        return fail(VCT_ERR_UNSUPPORTED, "the tessellation voxeliser takes at most 2^24 triangles per call");
     fill_accum_inputs(ctx->cfg, ctx->params, ctx->mvp, t, lights, n, sh, P);
     P.warp = warp_dev(ctx, eye);
     apply_tuning(ctx->tuning, P);
@@ -381,6 +408,7 @@ void fill_inject(vct_ctx* ctx, const vct_shadow_desc* s, const float* eye, Injec
     for (int k = 0; k < 3; ++k)  // voxelLinearPosition(lightPos)
         (&P.light_tc.x)[k] = ((s->light_pos[k] - ctx->cfg.voxel_center[k]) - ctx->cfg.voxel_min[k]) /
                              (ctx->cfg.voxel_max[k] - ctx->cfg.voxel_min[k]);
+    P.light_pos = to_f3(s->light_pos);
     P.dim = ctx->dim;
     P.shadowmap = s->shadowmap_dev;
     P.sw = s->width;
@@ -567,7 +595,7 @@ int64_t vct_struct_layout(const char* name) {
         VCT_SZ(vct_stats),  VCT_SZ(vct_timers),         VCT_SZ(vct_tuning),         VCT_SZ(vct_scene_desc),
         VCT_OFF(vct_scene_desc, lights), VCT_OFF(vct_scene_desc, n_lights), VCT_OFF(vct_scene_desc, shadow),
         VCT_OFF(vct_scene_desc, eye),    VCT_OFF(vct_scene_desc, gbuffer),  VCT_OFF(vct_scene_desc, out),
-        VCT_OFF(vct_params, trace_filter), VCT_OFF(vct_tuning, trace_warp_w),
+        VCT_OFF(vct_params, trace_filter), VCT_OFF(vct_params, pv), VCT_OFF(vct_tuning, trace_warp_w),
         VCT_SZ(vct_adam), VCT_SZ(vct_learned_stats), VCT_OFF(vct_learned_stats, max_tile_error),
     };
 #undef VCT_SZ
@@ -608,6 +636,9 @@ void vct_default_params(vct_params* p) {
     p->roughness = 0.5f;  // phong.frag:310 without a roughness map
     p->metallic = 0.0f;
     p->shininess = 32.0f;  // src/Graphics/Mesh.h:29
+    p->voxelize_tesselation = 0;  // the reference's default is 1 (Application.h:100); see vct.h
+    p->max_tess_level = (float)VCT_MAX_TESS_LEVEL;
+    for (int i = 0; i < 16; ++i) p->pv[i] = (i % 5 == 0) ? 1.0f : 0.0f;
 }
 
 vct_status vct_voxel_mvp(const vct_config* cfg, float mvp_xyz[48]) {
@@ -764,7 +795,7 @@ vct_status vct_voxelize_accumulate(vct_ctx* c, const vct_triangles* tris, const 
     AccumParams P;
     if ((s = fill_accum(c, tris, lights, n, need_shadow ? shadow : nullptr, eye, P)) != VCT_OK) return s;
     if (c->params.warp_mode == VCT_WARP_TEXTURE && (s = build_warpmap(c, P, st)) != VCT_OK) return s;
-    launch_accumulate(P, st);
+    launch_voxelizer(c, P, st);
     VCT_CHECK_LAUNCH("voxelize accumulate");
     c->radiance_ready = false;
     c->mips_ready = false;
@@ -904,7 +935,7 @@ vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lig
     AccumParams A;
     if ((s = fill_accum(c, tris, lights, n, shadow, eye, A)) != VCT_OK) return s;
     if (c->params.warp_mode == VCT_WARP_TEXTURE && (s = build_warpmap(c, A, st)) != VCT_OK) return s;
-    launch_accumulate(A, st);
+    launch_voxelizer(c, A, st);
     VCT_CHECK_LAUNCH("frame: accumulate");
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[1], st));
     InjectParams I;
@@ -924,6 +955,7 @@ vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lig
     R.light_int = I.light_int;
     R.warp = I.warp;
     R.light_tc = I.light_tc;
+    R.light_pos = I.light_pos;
     R.lit = c->lit;
     R.mip_levels = std::min(4, c->levels - 1);
     // The sampler's own copy of the chain is written by the same kernels:

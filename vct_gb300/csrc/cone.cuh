@@ -51,8 +51,9 @@ __device__ __forceinline__ float4 to_float4(rgba2 v) { return make_float4(v.rg.x
 // [-1, S-1]^3, i.e. [0, S]^3 of the (S+2)^3 bordered level, so the eight
 // texels are plain loads at constant offsets with no bounds tests.
 //
-// With `guard` (positions warped about an eye outside the volume can leave
-// [0,1]^3) the footprint is checked first: the bordered level holds texel
+// With `guard` (positions warped about an eye outside the volume, or
+// projected by the perspective warp, can leave [0,1]^3) the footprint is
+// checked first: the bordered level holds texel
 // indices -1..S, i.e. u = p S - 1/2 in [-1, S); outside that every texel of
 // the footprint is border and the sample is (0,0,0,0).
 __device__ __forceinline__ rgba2 trilinear2(const TraceParams& P, const int* __restrict__ off, int l, f3 p,
@@ -96,7 +97,7 @@ __device__ __forceinline__ float4 sample_lod(const TraceParams& P, const int* of
         const int S = P.dim;
         return texel(P.chain, S, (int)floorf(p.x * S), (int)floorf(p.y * S), (int)floorf(p.z * S));
     }
-    const bool guard = P.warp.mode == VCT_WARP_ANALYTIC;
+    const bool guard = warp_leaves_volume(P.warp.mode);
     if (lambda >= (float)q) return trilinear(P, off, q, p, guard);
     float fl = floorf(lambda);
     int d1 = (int)fl;

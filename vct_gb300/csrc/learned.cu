@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(256) learned_features_kernel(const LearnedPara
                 if (inside) {
                     const f3 wp = T.warp.mode ? apply_warp(T.warp, sp) : sp;
                     const float4 smp =
-                        cone::trilinear(T, s_off, min(i + 1, T.levels - 1), wp, T.warp.mode == VCT_WARP_ANALYTIC);
+                        cone::trilinear(T, s_off, min(i + 1, T.levels - 1), wp, warp_leaves_volume(T.warp.mode));
                     const float a = 1.0f - alpha;
                     col = mk(fmaf(smp.x, a, col.x), fmaf(smp.y, a, col.y), fmaf(smp.z, a, col.z));
                     alpha = fmaf(a, smp.w, alpha);
@@ -225,7 +225,7 @@ __device__ __forceinline__ void pixel_features(const LearnedParams& P, long long
     float4 near = make_float4(0.f, 0.f, 0.f, 0.f);
     if (sp.x >= 0.f && sp.y >= 0.f && sp.z >= 0.f && sp.x <= 1.f && sp.y <= 1.f && sp.z <= 1.f) {
         const int off[2] = {0, (int)padded_level_offset(T.dim, 1)};
-        near = cone::trilinear(T, off, 1, T.warp.mode ? apply_warp(T.warp, sp) : sp, T.warp.mode == VCT_WARP_ANALYTIC);
+        near = cone::trilinear(T, off, 1, T.warp.mode ? apply_warp(T.warp, sp) : sp, warp_leaves_volume(T.warp.mode));
     }
     f[16] = bf16x2(N.x, N.y);
     f[17] = bf16x2(N.z, dist * P.depth_scale);

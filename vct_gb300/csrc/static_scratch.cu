@@ -71,6 +71,8 @@ extern "C" vct_status vct_voxelize_static(const vct_config* cfg, const vct_param
     if (s != VCT_OK) return s;
     if (params->warp_mode != VCT_WARP_NONE)
         return set_error(VCT_ERR_UNSUPPORTED, "vct_voxelize_static: voxel warping needs a context (vct_voxelize)");
+    if (params->voxelize_tesselation)
+        return set_error(VCT_ERR_UNSUPPORTED, "vct_voxelize_static: the tessellation voxeliser needs a context");
     if (cfg->voxel_dim > VCT_STATIC_MAX_DIM)
         return set_error(VCT_ERR_INVALID_ARGUMENT, "vct_voxelize_static: voxel_dim exceeds VCT_STATIC_MAX_DIM (64)");
     if (tris->count > VCT_STATIC_MAX_TRIANGLES)

@@ -31,11 +31,15 @@ VCT_HD inline long long padded_level_offset(int N, int l) {
 
 // Voxel warping (VCT_WARP_*): the texture mode's map is 32^3 RGBA16 unorm
 // texels, x fastest, read through its fp32 copy (c / 65535 per channel); the
-// analytic mode warps about the eye's volume coordinate.
+// analytic mode warps about the eye's volume coordinate; the perspective mode
+// projects world positions with `pv` (volume coordinates are first mapped
+// back to world space with vmin, vcenter and ext = vmax - vmin).
 struct WarpDev {
     int mode;
     const float4* mapf;
     f3 eye_tc;
+    float pv[16];
+    f3 vmin, vcenter, ext;
 };
 
 struct LightDev {
@@ -79,6 +83,8 @@ struct AccumParams {
     int blocks_per_sm;  // raster CTAs per SM (1..3)
     WarpDev warp;
     int occupancy_only;  // only set occupancy bits (the warp map's occupancy voxelisation)
+    f3 vmin, vcenter, ext;  // voxelLinearPosition of the tessellation voxeliser
+    float max_tess_level;   // GL_MAX_TESS_GEN_LEVEL
     // Work distribution scratch (sized for ntri; see voxelize.cu).
     uint4* tri_rec;          // 3 x uint4 per triangle
     uint32_t* tri_units;     // work units per triangle
@@ -157,6 +163,7 @@ struct InjectParams {
     uint32_t* lit;  // fused path: bit mask of voxels the shader would store to
     WarpDev warp;
     f3 light_tc;    // voxelLinearPosition(lightPos): light_vox is warped on the device when warping
+    f3 light_pos;   // lightPos (the perspective warp projects the world position)
     int temporal;   // temporalFilterRadiance: relit voxels mix with the radiance seeded this frame
     float decay;
 };
@@ -174,6 +181,7 @@ struct ResolveParams {
     float4* pad_levels[5];        // bordered fp32 copy of levels 0..4 (nullptr = none)
     WarpDev warp;
     f3 light_tc;
+    f3 light_pos;
 };
 
 struct MipLevels {
@@ -248,6 +256,8 @@ void fill_accum_inputs(const vct_config& cfg, const vct_params& prm, const float
                        const vct_light* lights, int n, const vct_shadow_desc* sh, AccumParams& P);
 
 void launch_accumulate(const AccumParams& P, cudaStream_t s);
+// The tessellation voxeliser into the same accumulators (testTesselation.tesc/.tese).
+void launch_tesselate(const AccumParams& P, cudaStream_t s);
 void launch_normalize(const NormalizeParams& P, cudaStream_t s);
 void launch_inject(const InjectParams& P, cudaStream_t s);
 void launch_inject_mark(const InjectParams& P, cudaStream_t s);

@@ -78,9 +78,9 @@ __device__ __forceinline__ uint2 light_voxel(f3 light_vox, f3 light_int, uint2 c
 
 // voxelIndex(lightPos) (injectRadiance.comp:80): computed on the host without
 // warping, on the device with it (the warp map lives on the device).
-__device__ __forceinline__ f3 light_voxel_index(const WarpDev& W, f3 light_vox, f3 light_tc, int N) {
+__device__ __forceinline__ f3 light_voxel_index(const WarpDev& W, f3 light_vox, f3 light_tc, f3 light_pos, int N) {
     if (W.mode == VCT_WARP_NONE) return light_vox;
-    const f3 t = apply_warp(W, light_tc);
+    const f3 t = W.mode == VCT_WARP_PERSPECTIVE ? perspective_tc(W, light_pos) : apply_warp(W, light_tc);
     return mk((float)N * t.x, (float)N * t.y, (float)N * t.z);
 }
 
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
     const int N = P.dim;
     const int bpa = N / kBrick;
     const int bx = (int)(brick % bpa), by = (int)((brick / bpa) % bpa), bz = (int)(brick / (bpa * bpa));
-    const f3 lvox = FUSED ? light_voxel_index(R.warp, R.light_vox, R.light_tc, N) : R.light_vox;
+    const f3 lvox = FUSED ? light_voxel_index(R.warp, R.light_vox, R.light_tc, R.light_pos, N) : R.light_vox;
     uint32_t uniq = 0, mx = 0, flags = 0;
 #pragma unroll 1
     for (int it = 0; it < kBrickVox / 4 / kThreads; ++it) {
@@ -278,7 +278,8 @@ __device__ __forceinline__ bool inject_voxel(const InjectParams& P, int x, int y
     float ty = __fdiv_rn((w[1] - P.vcenter.y) - P.vmin.y, ext.y);
     float tz = __fdiv_rn((w[2] - P.vcenter.z) - P.vmin.z, ext.z);
     if (P.warp.mode != VCT_WARP_NONE) {  // getVoxelPosition (common.glsl:44-60)
-        const f3 t = apply_warp(P.warp, mk(tx, ty, tz));
+        const f3 t = P.warp.mode == VCT_WARP_PERSPECTIVE ? perspective_tc(P.warp, mk(w[0], w[1], w[2]))
+                                                         : apply_warp(P.warp, mk(tx, ty, tz));
         tx = t.x;
         ty = t.y;
         tz = t.z;
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(kThreads) inject_kernel(const InjectParams P) 
     }
     long long v = ((long long)iz * N + iy) * N + ix;
     if (P.lighting)
-        P.radiance[v] = light_voxel(light_voxel_index(P.warp, P.light_vox, P.light_tc, N), P.light_int, P.color[v],
+        P.radiance[v] = light_voxel(light_voxel_index(P.warp, P.light_vox, P.light_tc, P.light_pos, N), P.light_int, P.color[v],
                                     P.normal[v], ix, iy, iz);
     else
         P.radiance[v] = P.color[v];
@@ -399,7 +400,7 @@ __global__ void fill_u32_kernel(uint32_t* p, uint32_t v, long long n) {
 __global__ void __launch_bounds__(kThreads) inject_apply_kernel(const InjectParams P) {
     const int N = P.dim;
     const long long nq = (long long)N * N * N / 4;
-    const f3 lvox = light_voxel_index(P.warp, P.light_vox, P.light_tc, N);
+    const f3 lvox = light_voxel_index(P.warp, P.light_vox, P.light_tc, P.light_pos, N);
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x) {
         const long long v0 = q * 4;
         const uint32_t lb = (__ldg(P.lit + (v0 >> 5)) >> (v0 & 31)) & 15u;

@@ -42,6 +42,29 @@ __device__ __forceinline__ float shadow_factor(const AccumParams& P, f3 wp) {
     return pcf5(P.shadowmap, P.sw, P.sh, P.ls, wp);
 }
 
+// Block-local exclusive scan of the per-triangle unit counts of one setup
+// block into tri_scan, and the block's total into block_off[blockIdx.x].
+__device__ __forceinline__ void block_scan_units(const VoxWork& W, long long g, uint32_t units) {
+    __shared__ uint32_t warp_tot[kSetupThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t incl = units;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kSetupThreads / 32; ++w) {
+        before += (w < wid) ? warp_tot[w] : 0u;
+        total += warp_tot[w];
+    }
+    if (g < W.ntri) W.tri_scan[g] = before + incl - units;
+    if (threadIdx.x == 0) W.block_off[blockIdx.x] = total;
+}
+
 // ------------------------------------------------------------- 1. setup
 template <class Scenes>
 __global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Scenes S, const VoxWork W) {
@@ -89,25 +112,7 @@ __global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Sce
         }
         W.tri_units[g] = units;
     }
-    // Block-local exclusive scan of the unit counts.
-    __shared__ uint32_t warp_tot[kSetupThreads / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    uint32_t incl = units;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    if (lane == 31) warp_tot[wid] = incl;
-    __syncthreads();
-    uint32_t before = 0, total = 0;
-#pragma unroll
-    for (int w = 0; w < kSetupThreads / 32; ++w) {
-        before += (w < wid) ? warp_tot[w] : 0u;
-        total += warp_tot[w];
-    }
-    if (g < W.ntri) W.tri_scan[g] = before + incl - units;
-    if (threadIdx.x == 0) W.block_off[blockIdx.x] = total;
+    block_scan_units(W, g, units);
 }
 
 // --------------------------------------------------------------- 2. scan
@@ -151,7 +156,9 @@ __device__ __forceinline__ bool fragment_voxel(const AccumParams& P, int px, int
                                                int& vy, int& vz) {
     const int N = P.dim;
     const float uz = (zf + 1.0f) * 0.5f;
-    if (P.warp.mode == VCT_WARP_NONE) {
+    // voxelize.frag reads warpVoxels and warpTexture only: the perspective
+    // warp (voxelizeTesselationWarp) leaves the rasterised grid linear.
+    if (P.warp.mode == VCT_WARP_NONE || P.warp.mode == VCT_WARP_PERSPECTIVE) {
         const int iz = __float2int_rz((float)N * (1.0f - uz));
         if (axis == 0) {
             vx = iz;
@@ -386,7 +393,284 @@ void launch_voxelize(const Scenes& S, const VoxWork& W, int num_sms, int blocks_
     note_launches(3);
 }
 
+// ====================================================== tessellation voxeliser
+// testTesselation.tesc/.tese (Application.cpp:585-662) in three launches of
+// the same shape as the rasteriser's: per-triangle tessellation levels and
+// point counts (tess_setup_kernel), the scan of the block totals, and a
+// persistent kernel in which every warp takes an equal range of 32-point
+// work units, queues the points of its units and stores 32 at a time.
+//
+// Tessellation levels after GL's equal_spacing rounding, packed 7 bits each:
+// inner n | outer[0] << 7 | outer[1] << 14 | outer[2] << 21 (1..64 each).
+constexpr int kTessUnit = 32;
+
+// Float-to-int truncation of ivec3(): NaN -> 0, saturating (cvt.rzi.s32.f32).
+__device__ __forceinline__ int trunc_sat(float x) { return __float2int_rz(x); }
+
+// equal_spacing: clamp to [1, max], round up (OpenGL 4.6, 11.2.2).
+__device__ __forceinline__ int tess_round(float level, float max_level) {
+    return (int)ceilf(fminf(fmaxf(level, 1.0f), max_level));
+}
+
+// Points of the triangle primitive generator in point mode for inner level
+// n and outer levels m0..m2: the outer ring (3 corners and m - 1 points per
+// edge) plus the concentric inner rings k = 1.. of n - 2k segments each
+// (3 (n - 2k) points, or the centre when n - 2k = 0).
+__device__ __forceinline__ uint32_t tess_point_count(int n, int m0, int m1, int m2) {
+    uint32_t c = (uint32_t)(m0 + m1 + m2);
+    if (n >= 2) {
+        const int K = (n & 1) ? (n - 1) / 2 : n / 2 - 1;
+        c += 3u * (uint32_t)(K * n - K * (K + 1)) + ((n & 1) ? 0u : 1u);
+    }
+    return c;
+}
+
+// testTesselation.tesc:33-78: levels of one triangle; false if discarded
+// (all three vertices truncate to one voxel: levels 0).
+__device__ __forceinline__ bool tess_levels(const AccumParams& P, const float* Pp, uint32_t& packed, uint32_t& npts) {
+    const f3 a = ld3(Pp), b = ld3(Pp + 3), c = ld3(Pp + 6);
+    const float fN = (float)P.dim;
+    const f3 vtx[3] = {a, b, c};
+    int vi[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {  // ivec3(voxelDim * getVoxelPosition(p)), the shader's own linear mapping
+        vi[k][0] = trunc_sat(fN * __fdiv_rn((vtx[k].x - P.vcenter.x) - P.vmin.x, P.ext.x));
+        vi[k][1] = trunc_sat(fN * __fdiv_rn((vtx[k].y - P.vcenter.y) - P.vmin.y, P.ext.y));
+        vi[k][2] = trunc_sat(fN * __fdiv_rn((vtx[k].z - P.vcenter.z) - P.vmin.z, P.ext.z));
+    }
+    if (vi[0][0] == vi[1][0] && vi[0][1] == vi[1][1] && vi[0][2] == vi[1][2] && vi[0][0] == vi[2][0] &&
+        vi[0][1] == vi[2][1] && vi[0][2] == vi[2][2])
+        return false;
+    const f3 A = sub(c, b), B = sub(c, a), C = sub(b, a);
+    const float lx = length(A), ly = length(B), lz = length(C);
+    const float sp = ((lx + ly) + lz) * 0.5f;  // semiperimeter
+    const float area = __fsqrt_rn(((sp * (sp - lx)) * (sp - ly)) * (sp - lz));  // Heron
+    const float ax = __fdiv_rn(2.0f * area, lx), ay = __fdiv_rn(2.0f * area, ly), az = __fdiv_rn(2.0f * area, lz);
+    const float max_alt = fmaxf(ax, fmaxf(ay, az));
+    const f3 vs = mk(__fdiv_rn(P.ext.x, fN), __fdiv_rn(P.ext.y, fN), __fdiv_rn(P.ext.z, fN));
+    const float dx = fabsf(length(mulv(normalize(A), vs))), dy = fabsf(length(mulv(normalize(B), vs))),
+                dz = fabsf(length(mulv(normalize(C), vs)));
+    const float ox = fmaxf(1.0f, __fdiv_rn(lx, dx)), oy = fmaxf(1.0f, __fdiv_rn(ly, dy)),
+                oz = fmaxf(1.0f, __fdiv_rn(lz, dz));
+    const float inner = fmaxf(1.0f, __fdiv_rn(max_alt, vs.x));
+    // gl_TessLevelOuter[0] = outer.z, [1] = outer.x, [2] = outer.y
+    const int m0 = tess_round(oz, P.max_tess_level), m1 = tess_round(ox, P.max_tess_level),
+              m2 = tess_round(oy, P.max_tess_level);
+    int n = tess_round(inner, P.max_tess_level);
+    if (n == 1 && (m0 > 1 || m1 > 1 || m2 > 1)) n = 2;  // inner 1 + epsilon
+    packed = (uint32_t)n | ((uint32_t)m0 << 7) | ((uint32_t)m1 << 14) | ((uint32_t)m2 << 21);
+    npts = tess_point_count(n, m0, m1, m2);
+    return true;
+}
+
+// gl_TessCoord of point `i` in the order of tess_point_count.  The outer
+// edges are u = 0 (from vertex 1 to 2, outer[0]), v = 0 (2 to 0, outer[1]),
+// w = 0 (0 to 1, outer[2]), at j / m.  Ring k's corners lie where the
+// perpendiculars through the inner subdivision points nearest each corner
+// meet: (1 - 2t, t, t) and rotations, t = 2k / (3n); its edges are split
+// into n - 2k equal segments.
+__device__ __forceinline__ f3 tess_coord(uint32_t packed, int i) {
+    const int n = (int)(packed & 127u), m0 = (int)((packed >> 7) & 127u), m1 = (int)((packed >> 14) & 127u),
+              m2 = (int)((packed >> 21) & 127u);
+    if (i < 3) return i == 0 ? mk(1.0f, 0.0f, 0.0f) : i == 1 ? mk(0.0f, 1.0f, 0.0f) : mk(0.0f, 0.0f, 1.0f);
+    i -= 3;
+    if (i < m0 - 1) {
+        const float s = __fdiv_rn((float)(i + 1), (float)m0);
+        return mk(0.0f, 1.0f - s, s);
+    }
+    i -= m0 - 1;
+    if (i < m1 - 1) {
+        const float s = __fdiv_rn((float)(i + 1), (float)m1);
+        return mk(s, 0.0f, 1.0f - s);
+    }
+    i -= m1 - 1;
+    if (i < m2 - 1) {
+        const float s = __fdiv_rn((float)(i + 1), (float)m2);
+        return mk(1.0f - s, s, 0.0f);
+    }
+    i -= m2 - 1;
+    int k = 1, q = n - 2;
+    while (q > 0 && i >= 3 * q) {
+        i -= 3 * q;
+        ++k;
+        q -= 2;
+    }
+    if (q <= 0) {  // the centre of an even inner level
+        const float third = __fdiv_rn(1.0f, 3.0f);
+        return mk(third, third, third);
+    }
+    const float t = __fdiv_rn((float)(2 * k), (float)(3 * n));
+    const float h = 1.0f - 2.0f * t;
+    const int e = i / q, j = i - e * q;
+    const float s = __fdiv_rn((float)j, (float)q);
+    // corners c_e and c_{e+1} of the ring: c0 = (h,t,t), c1 = (t,h,t), c2 = (t,t,h)
+    const float c[3][3] = {{h, t, t}, {t, h, t}, {t, t, h}};
+    const float* p0 = c[e];
+    const float* p1 = c[e == 2 ? 0 : e + 1];
+    return mk(p0[0] + s * (p1[0] - p0[0]), p0[1] + s * (p1[1] - p0[1]), p0[2] + s * (p1[2] - p0[2]));
+}
+
+__global__ void __launch_bounds__(kSetupThreads) tess_setup_kernel(const AccumParams P, const VoxWork W) {
+    const long long g = (long long)blockIdx.x * kSetupThreads + threadIdx.x;
+    uint32_t units = 0;
+    if (g < W.ntri) {
+        uint32_t packed = 0, npts = 0;
+        if (!tess_levels(P, P.pos + g * 9, packed, npts)) npts = 0;
+        W.tri_rec[3 * g] = make_uint4(packed, npts, 0u, 0u);
+        units = (npts + kTessUnit - 1) / kTessUnit;
+        W.tri_units[g] = units;
+    }
+    block_scan_units(W, g, units);
+}
+
+struct TessQueue {
+    int tri[2 * kTessUnit];
+    uint32_t pt[2 * kTessUnit];   // point index within the triangle
+    uint32_t lev[2 * kTessUnit];  // packed levels
+};
+
+// testTesselation.tese:101-133 for the queued points, one per lane (lanes
+// >= nact idle), with the stores of lanes that hit the same voxel summed in
+// registers first: the sums are integers, so the records are the same as
+// with one atomic per point.
+__device__ __forceinline__ void tess_store32(const AccumParams& P, const TessQueue& q, int nact, int lane) {
+    bool valid = false;
+    uint32_t v = 0, qr = 0, qg = 0, qb = 0, qx = 0, qy = 0, qz = 0;
+    if (lane < nact) {
+        const long long t = q.tri[lane];
+        const f3 bc = tess_coord(q.lev[lane], (int)q.pt[lane]);
+        const float* Pp = P.pos + t * 9;
+        const float* Pn = P.nrm + t * 9;
+        const f3 p0 = ld3(Pp), p1 = ld3(Pp + 3), p2 = ld3(Pp + 6);
+        const f3 n0 = ld3(Pn), n1 = ld3(Pn + 3), n2 = ld3(Pn + 6);
+        const f3 pos = add(add(mul(p0, bc.x), mul(p1, bc.y)), mul(p2, bc.z));
+        const f3 nrm = add(add(mul(n0, bc.x), mul(n1, bc.y)), mul(n2, bc.z));
+        const int N = P.dim;
+        const float fN = (float)N;
+        f3 tc;
+        if (P.warp.mode == VCT_WARP_PERSPECTIVE) {  // voxelTesselationWarpedPosition
+            tc = perspective_tc(P.warp, pos);
+        } else {  // voxelLinearPosition (the evaluation shader passes warpVoxels = false)
+            tc = mk(__fdiv_rn((pos.x - P.vcenter.x) - P.vmin.x, P.ext.x),
+                    __fdiv_rn((pos.y - P.vcenter.y) - P.vmin.y, P.ext.y),
+                    __fdiv_rn((pos.z - P.vcenter.z) - P.vmin.z, P.ext.z));
+        }
+        const int vx = trunc_sat(fN * tc.x), vy = trunc_sat(fN * tc.y), vz = trunc_sat(fN * tc.z);
+        if (!(vx < 0 || vy < 0 || vz < 0 || vx >= N || vy >= N || vz >= N)) {
+            valid = true;
+            v = (uint32_t)(((long long)vz * N + vy) * N + vx);
+            const f3 Nf = normalize(nrm);  // voxelStore: normalize(normal) * 0.5 + 0.5
+            const f3 col = ld3(P.albedo + t * 3);
+            qr = quant16(col.x);
+            qg = quant16(col.y);
+            qb = quant16(col.z);
+            qx = quant16(Nf.x * 0.5f + 0.5f);
+            qy = quant16(Nf.y * 0.5f + 0.5f);
+            qz = quant16(Nf.z * 0.5f + 0.5f);
+        }
+    }
+    const unsigned act = __ballot_sync(0xffffffffu, valid);
+    if (!valid) return;
+    const unsigned peers = __match_any_sync(act, v);
+    uint32_t cnt = 1;
+    if (!__all_sync(act, peers == (1u << lane))) {
+        cnt = (uint32_t)__popc(peers);
+        qr = __reduce_add_sync(peers, qr);
+        qg = __reduce_add_sync(peers, qg);
+        qb = __reduce_add_sync(peers, qb);
+        qx = __reduce_add_sync(peers, qx);
+        qy = __reduce_add_sync(peers, qy);
+        qz = __reduce_add_sync(peers, qz);
+    }
+    if (lane == __ffs(peers) - 1) {
+        unsigned long long* rec = reinterpret_cast<unsigned long long*>(P.acc + (long long)kAccWords * v);
+        atomicAdd(rec + 0, (unsigned long long)cnt | ((unsigned long long)qr << 32));
+        atomicAdd(rec + 1, (unsigned long long)qg | ((unsigned long long)qb << 32));
+        atomicAdd(rec + 2, (unsigned long long)qx | ((unsigned long long)qy << 32));
+        atomicAdd(rec + 3, (unsigned long long)qz);
+        atomicOr(P.occ + (v >> 5), 1u << (v & 31));
+    }
+}
+
+__global__ void __launch_bounds__(kWarps * 32, 4) tess_points_kernel(const AccumParams P, const VoxWork W, int nblocks) {
+    __shared__ TessQueue queues[kWarps];
+    const int lane = threadIdx.x & 31;
+    TessQueue& q = queues[threadIdx.x >> 5];
+    const long long nw = (long long)gridDim.x * kWarps;
+    const long long w = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const long long total = W.block_off[nblocks];
+    const long long u0 = total * w / nw, u1 = total * (w + 1) / nw;
+    int qn = 0;                // queued points (warp-uniform)
+    unsigned long long generated = 0;
+    if (u0 < u1) {
+        int lo = 0, hi = nblocks - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((long long)W.block_off[mid] <= u0)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        long long glo = (long long)lo * kSetupThreads;
+        long long ghi = min(glo + kSetupThreads, W.ntri) - 1;
+        while (glo < ghi) {
+            const long long mid = (glo + ghi + 1) >> 1;
+            if (unit_start<OneScene<AccumParams>>(W, mid) <= u0)
+                glo = mid;
+            else
+                ghi = mid - 1;
+        }
+        long long g = glo;
+        long long start = unit_start<OneScene<AccumParams>>(W, g);
+        uint32_t nunits = W.tri_units[g];
+        for (long long u = u0; u < u1; ++u) {
+            while (u >= start + nunits) {
+                ++g;
+                start = unit_start<OneScene<AccumParams>>(W, g);
+                nunits = W.tri_units[g];
+            }
+            const uint4 r = __ldg(W.tri_rec + 3 * g);
+            const int base = (int)(u - start) * kTessUnit;
+            const int cnt = min(kTessUnit, (int)r.y - base);
+            if (lane < cnt) {
+                q.tri[qn + lane] = (int)g;
+                q.pt[qn + lane] = (uint32_t)(base + lane);
+                q.lev[qn + lane] = r.x;
+            }
+            __syncwarp();
+            qn += cnt;
+            generated += (unsigned long long)cnt;
+            if (qn >= kTessUnit) {
+                tess_store32(P, q, kTessUnit, lane);
+                __syncwarp();
+                if (lane < qn - kTessUnit) {
+                    q.tri[lane] = q.tri[kTessUnit + lane];
+                    q.pt[lane] = q.pt[kTessUnit + lane];
+                    q.lev[lane] = q.lev[kTessUnit + lane];
+                }
+                __syncwarp();
+                qn -= kTessUnit;
+            }
+        }
+    }
+    tess_store32(P, q, qn, lane);
+    if (lane == 0 && generated && P.stats)
+        atomicAdd(&P.stats->total_voxel_fragments, (unsigned)generated);
+}
+
 }  // namespace
+
+// The tessellation voxeliser: setup, scan, points (the same scratch as the
+// rasteriser's).
+void launch_tesselate(const AccumParams& P, cudaStream_t s) {
+    if (P.ntri <= 0) return;
+    const VoxWork W = {P.tri_rec, P.tri_units, P.tri_scan, P.block_off, P.ntri, 0};
+    const int nblocks = (int)((P.ntri + kSetupThreads - 1) / kSetupThreads);
+    tess_setup_kernel<<<nblocks, kSetupThreads, 0, s>>>(P, W);
+    voxelize_scan_kernel<<<1, 1024, 0, s>>>(W.block_off, nblocks);
+    tess_points_kernel<<<P.num_sms * 4, kWarps * 32, 0, s>>>(P, W, nblocks);
+    note_launches(3);
+}
 
 void accumulate_bind_scratch(AccumParams& P, void* scratch) {
     char* p = static_cast<char*>(scratch);

@@ -74,9 +74,44 @@ __device__ __forceinline__ f3 warp_lookup(const float4* __restrict__ mapf, f3 p)
     return r;
 }
 
+// voxelTesselationWarpedPosition (common.glsl:37-42): pv * (p, 1), divided
+// by w, mapped from [-1,1] to [0,1].  Every consumer drops (voxeliser,
+// injection) or reads as border (cone tracer) a coordinate outside [-1, 2],
+// so such results, infinities and NaN (points on or behind the camera plane)
+// are replaced by -1, which keeps the float-to-int truncations defined.
+__device__ __forceinline__ f3 perspective_tc(const WarpDev& W, f3 p) {
+    const float* m = W.pv;
+    float c[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) c[r] = ((m[r] * p.x + m[4 + r] * p.y) + m[8 + r] * p.z) + m[12 + r] * 1.0f;
+    f3 q;
+    q.x = __fdiv_rn(c[0], c[3]) * 0.5f + 0.5f;
+    q.y = __fdiv_rn(c[1], c[3]) * 0.5f + 0.5f;
+    q.z = __fdiv_rn(c[2], c[3]) * 0.5f + 0.5f;
+    if (!(q.x >= -1.0f && q.x <= 2.0f && q.y >= -1.0f && q.y <= 2.0f && q.z >= -1.0f && q.z <= 2.0f))
+        q.x = q.y = q.z = -1.0f;
+    return q;
+}
+
+// Volume coordinate -> world (phong.frag:159: p * (max - min) + center + min)
+// -> perspective coordinate.
+__device__ __forceinline__ f3 perspective_from_tc(const WarpDev& W, f3 t) {
+    f3 w;
+    w.x = (t.x * W.ext.x + W.vcenter.x) + W.vmin.x;
+    w.y = (t.y * W.ext.y + W.vcenter.y) + W.vmin.y;
+    w.z = (t.z * W.ext.z + W.vcenter.z) + W.vmin.z;
+    return perspective_tc(W, w);
+}
+
+// Warps that can move a position off [0,1]^3 (the samplers check the footprint).
+__device__ __forceinline__ bool warp_leaves_volume(int mode) {
+    return mode == VCT_WARP_ANALYTIC || mode == VCT_WARP_PERSPECTIVE;
+}
+
 __device__ __forceinline__ f3 apply_warp(const WarpDev& W, f3 p) {
     if (W.mode == VCT_WARP_ANALYTIC) return voxel_warp(p, W.eye_tc);
     if (W.mode == VCT_WARP_TEXTURE) return warp_lookup(W.mapf, p);
+    if (W.mode == VCT_WARP_PERSPECTIVE) return perspective_from_tc(W, p);
     return p;
 }
 

@@ -98,6 +98,9 @@ class Scene:
     inv_view_proj: np.ndarray
     gbuffer_size: tuple
     cone: dict = field(default_factory=dict)  # trace settings (radians)
+    # 'pv' of the perspective warp: perspective(fov, aspect, 1, 20) * view
+    # (src/Application.cpp:202), column-major
+    pv: np.ndarray | None = None
 
     @property
     def ntri(self) -> int:
@@ -214,7 +217,8 @@ def _finish(name, tris, nrms, alb, lights, ls, dim, levels, vmax, shadow_size, e
         light_pos=np.asarray(main["position"], dtype=np.float32),
         light_int=np.asarray(main["color"], dtype=np.float32),
         eye=np.asarray(eye, dtype=np.float32), view_proj=colmajor(vpm), inv_view_proj=colmajor(np.linalg.inv(vpm)),
-        gbuffer_size=gsize, cone=cone)
+        gbuffer_size=gsize, cone=cone,
+        pv=colmajor(perspective(fovy, W / H, 1.0, 20.0) @ look_at(eye, target, (0, 1, 0))))
 
 
 BASELINE_CONES = dict(diffuse=(16, 60 * DEG, 1.0, 1.0, 0.5), specular=(32, 10 * DEG, 1.7, 0.5, 0.1))
@@ -470,6 +474,7 @@ def viewpoint(sc: Scene, k: int, n: int = 8, radius: float = 2.8) -> Scene:
     v.eye = eye.astype(np.float32)
     v.view_proj = colmajor(vpm)
     v.inv_view_proj = colmajor(np.linalg.inv(vpm))
+    v.pv = colmajor(perspective(55 * DEG, W / H, 1.0, 20.0) @ look_at(eye, np.zeros(3), (0, 1, 0)))
     return v
 
 
