@@ -14,6 +14,9 @@ numpy only (deterministic for a given seed):
              log-uniform in 0.01-0.2 of the scene extent, albedo in [0,1]^3
              per instance; 256^3 grid, 9 levels; one directional light plus
              4 point lights; 2048^2 shadow map; 1920x1080 G-buffer.
+  obj      - an OBJ mesh (parse_obj / obj_scene: the reference's
+             resources/*.obj loaded as its tinyobjloader does) inside the
+             Cornell walls.
 
 Matrices follow glm's formulas (column-major float32, flattened
 column by column as GLSL stores them).
@@ -476,6 +479,107 @@ def viewpoint(sc: Scene, k: int, n: int = 8, radius: float = 2.8) -> Scene:
     v.inv_view_proj = colmajor(np.linalg.inv(vpm))
     v.pv = colmajor(perspective(55 * DEG, W / H, 1.0, 20.0) @ look_at(eye, np.zeros(3), (0, 1, 0)))
     return v
+
+
+# ------------------------------------------------------------ OBJ meshes
+def parse_obj(text: str):
+    """Triangles of a Wavefront OBJ text as the reference's loader reads
+    them (tinyobjloader with triangulation, src/Graphics/Mesh.cpp:41-190):
+    `v` and `vn` records, faces of `v`, `v/vt`, `v//vn` or `v/vt/vn` indices
+    (1-based, negative = relative to the end), polygons split into a fan
+    (0, i, i+1) around their first vertex, and a zero normal for a face
+    corner without one (the loader's zero-initialised vertex).  Returns
+    positions (T, 3, 3), normals (T, 3, 3) and the face's object index
+    (T,) counting `o`/`g` records."""
+    vs, vns, tris, nrms, groups = [], [], [], [], []
+    group = 0
+    seen_face = False
+    for line in text.splitlines():
+        parts = line.split()
+        if not parts or parts[0].startswith("#"):
+            continue
+        tag = parts[0]
+        if tag == "v":
+            vs.append([float(x) for x in parts[1:4]])
+        elif tag == "vn":
+            vns.append([float(x) for x in parts[1:4]])
+        elif tag in ("o", "g"):
+            if seen_face:
+                group += 1
+                seen_face = False
+        elif tag == "f":
+            corners = []
+            for c in parts[1:]:
+                f = c.split("/")
+                vi = int(f[0])
+                vi = vi - 1 if vi > 0 else len(vs) + vi
+                ni = None
+                if len(f) >= 3 and f[2]:
+                    ni = int(f[2])
+                    ni = ni - 1 if ni > 0 else len(vns) + ni
+                corners.append((vi, ni))
+            for i in range(1, len(corners) - 1):
+                tri = (corners[0], corners[i], corners[i + 1])
+                tris.append([vs[k] for k, _ in tri])
+                nrms.append([vns[n] if n is not None else [0.0, 0.0, 0.0] for _, n in tri])
+                groups.append(group)
+            seen_face = True
+    return (np.asarray(tris, dtype=np.float64).reshape(-1, 3, 3), np.asarray(nrms, dtype=np.float64).reshape(-1, 3, 3),
+            np.asarray(groups, dtype=np.int64))
+
+
+def load_obj(path: str):
+    with open(path) as f:
+        return parse_obj(f.read())
+
+
+def obj_scene(text: str, seed: int = 0, dim: int = 64, shadow: int = 512, gbuffer=(640, 360), size: float = 0.7,
+              walls: bool = True) -> Scene:
+    """A parity scene around an OBJ mesh (the reference's resources/*.obj):
+    the mesh scaled uniformly so its bounding box spans `size` of the volume
+    [-1, 1]^3 and centred, inside the Cornell walls; one albedo per OBJ
+    object; the Cornell box's camera and light."""
+    rng = np.random.default_rng(seed)
+    tris, nrms, groups = parse_obj(text)
+    lo, hi = tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)
+    scale = 2.0 * size / max(float((hi - lo).max()), 1e-12)
+    tris = (tris - 0.5 * (lo + hi)) * scale
+    alb_groups = rng.uniform(0.1, 0.9, size=(int(groups.max()) + 1 if len(groups) else 1, 3))
+    alb = alb_groups[groups]
+    parts_t, parts_n, parts_a = [tris], [nrms], [alb]
+    if walls:
+        base = cornell(seed=seed, dim=dim)
+        k = 10  # the five wall quads
+        parts_t.insert(0, base.positions[:k].reshape(-1, 3, 3).astype(np.float64))
+        parts_n.insert(0, base.normals[:k].reshape(-1, 3, 3).astype(np.float64))
+        parts_a.insert(0, base.albedo[:k].astype(np.float64))
+    light, ls = _directional_light(rng, 1.0)
+    levels = int(np.log2(dim)) + 1
+    return _finish("obj", np.concatenate(parts_t), np.concatenate(parts_n), np.concatenate(parts_a), [light], ls, dim,
+                   levels, 1.0, (shadow, shadow), np.array([0.0, 1.6, 2.6]), np.array([0.0, -0.4, 0.0]), 50 * DEG,
+                   tuple(gbuffer), BASELINE_CONES)
+
+
+def obj_text(tris: np.ndarray, normals: np.ndarray | None = None, quads: bool = False) -> str:
+    """OBJ text of a triangle soup (F, 3, 3), with `vn` records when normals
+    are given; with `quads` consecutive triangle pairs (p0,p1,p2), (p0,p2,p3)
+    are written as one quad face.  Used to build OBJ inputs for the loader."""
+    lines = ["# generated"]
+    v = tris.reshape(-1, 3)
+    lines += [f"v {a:.9g} {b:.9g} {c:.9g}" for a, b, c in v]
+    if normals is not None:
+        lines += [f"vn {a:.9g} {b:.9g} {c:.9g}" for a, b, c in normals.reshape(-1, 3)]
+    fmt = (lambda i: f"{i}//{i}") if normals is not None else (lambda i: f"{i}")
+    F = tris.shape[0]
+    if quads:
+        for t in range(0, F - 1, 2):
+            i = 3 * t + 1
+            lines.append("f " + " ".join(fmt(k) for k in (i, i + 1, i + 2, i + 5)))
+    else:
+        for t in range(F):
+            i = 3 * t + 1
+            lines.append("f " + " ".join(fmt(k) for k in (i, i + 1, i + 2)))
+    return "\n".join(lines) + "\n"
 
 
 SCENES = {"cornell": cornell, "large": large, "tiny": tiny}
