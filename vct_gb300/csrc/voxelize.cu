@@ -224,7 +224,11 @@ __device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQ
                 float ndl = fmaxf(0.0f, dot(Nf, L.neg_dir_n));
                 lit = mul(mul(mulv(color, L.color), L.intensity), ndl);
             }
-            if (L.shadow_caster) lit = mul(lit, 1.0f - shadow_factor(P, wp));
+            // lit *= 1 - shadow: when lit is exactly zero (the surface faces away, or the
+            // light is out of range) the product is +-0 and adding it leaves `fin`
+            // unchanged (1 - shadow is finite), so the PCF is not evaluated.
+            if (L.shadow_caster && (lit.x != 0.0f || lit.y != 0.0f || lit.z != 0.0f))
+                lit = mul(lit, 1.0f - shadow_factor(P, wp));
             fin = add(fin, lit);
         }
         color = mk(clampf(fin.x, 0.0f, 1.0f), clampf(fin.y, 0.0f, 1.0f), clampf(fin.z, 0.0f, 1.0f));
@@ -261,16 +265,19 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
     const long long w = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
     const long long total = W.block_off[nblocks];
     const long long u0 = total * w / nw, u1 = total * (w + 1) / nw;
-    int qn = 0;  // queued fragments (warp-uniform)
+    // The queue is a ring of kQueue entries: fragments [head, head + qn).
+    int qn = 0, head = 0;  // warp-uniform
 
-    // Shades the first 32 queued fragments, one per lane, and counts them
-    // per scene (one shared-memory atomic per distinct scene in the warp).
+    // Shades the 32 oldest queued fragments (or `nact`), one per lane, and
+    // counts them per scene (one shared-memory atomic per distinct scene in
+    // the warp).
     auto shade32 = [&](int nact) {
         __syncwarp();
         if (lane < nact) {
-            const int s = (int)(q.pix[lane] >> 24);
+            const int e = (head + lane) & (kQueue - 1);
+            const int s = (int)(q.pix[e] >> 24);
             const AccumParams& P = S.get(s);
-            shade_fragment(P, q, lane);
+            shade_fragment(P, q, e);
             const unsigned same = __match_any_sync(__activemask(), s);
             if (lane == __ffs(same) - 1 && !P.occupancy_only) atomicAdd(&frag_count[s], (unsigned)__popc(same));
         }
@@ -319,22 +326,36 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
             const int bw = (int)(r2.w & 0x7ffu), bh = (int)(r2.w >> 11);
             const int p_begin = (int)(u - start) << W.unit_log2;
             const int p_end = min(p_begin + (1 << W.unit_log2), bw * bh);
+            // Edge k runs from vertex a = k+1 to b = k+2; its function at a pixel
+            // centre is dX (sy - Ya) - dY (sx - Xa), every factor within 32 bits
+            // (|snapped coordinates| <= 2^28), each product exact in 64.
+            int dX[3], dY[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                dX[k] = X[(k + 2) % 3] - X[(k + 1) % 3];
+                dY[k] = Y[(k + 2) % 3] - Y[(k + 1) % 3];
+            }
+            const float rbw = 1.0f / (float)bw;  // row = idx / bw, corrected below
             for (int c = p_begin; c < p_end; c += 32) {
                 const int idx = c + lane;
                 bool cov = false;
                 float l[3] = {0.f, 0.f, 0.f}, zf = 0.f;
                 int px = 0, py = 0;
                 if (idx < p_end) {
-                    const int row = idx / bw;
+                    int row = (int)((float)idx * rbw);
+                    if (row * bw > idx)
+                        --row;
+                    else if ((row + 1) * bw <= idx)
+                        ++row;
                     py = py0 + row;
                     px = px0 + (idx - row * bw);
-                    const long long sx = (long long)px * kSub + kSub / 2, sy = (long long)py * kSub + kSub / 2;
+                    const int sx = px * (int)kSub + (int)kSub / 2, sy = py * (int)kSub + (int)kSub / 2;
                     long long e[3];
                     cov = true;
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        const int a = (k + 1) % 3, b = (k + 2) % 3;
-                        e[k] = (long long)(X[b] - X[a]) * (sy - Y[a]) - (long long)(Y[b] - Y[a]) * (sx - X[a]);
+                        const int a = (k + 1) % 3;
+                        e[k] = (long long)dX[k] * (long long)(sy - Y[a]) - (long long)dY[k] * (long long)(sx - X[a]);
                         cov = cov && (e[k] - ((bias >> k) & 1) >= 0);
                     }
                     if (cov) {
@@ -349,7 +370,7 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
                 }
                 const unsigned m = __ballot_sync(FULL, cov);
                 if (cov) {
-                    const int slot = qn + __popc(m & ((1u << lane) - 1u));
+                    const int slot = (head + qn + __popc(m & ((1u << lane) - 1u))) & (kQueue - 1);
                     q.tri[slot] = (int)tl;
                     q.pix[slot] = (uint32_t)px | ((uint32_t)py << 11) | ((uint32_t)axis << 22) |
                                   ((uint32_t)scene << 24);
@@ -361,16 +382,7 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
                 qn += __popc(m);
                 if (qn >= 32) {
                     shade32(32);
-                    if (lane < qn - 32) {
-                        const int src = 32 + lane;
-                        q.tri[lane] = q.tri[src];
-                        q.pix[lane] = q.pix[src];
-                        q.l0[lane] = q.l0[src];
-                        q.l1[lane] = q.l1[src];
-                        q.l2[lane] = q.l2[src];
-                        q.z[lane] = q.z[src];
-                    }
-                    __syncwarp();
+                    head = (head + 32) & (kQueue - 1);
                     qn -= 32;
                 }
             }
@@ -504,10 +516,10 @@ __device__ __forceinline__ f3 tess_coord(uint32_t packed, int i) {
     const int e = i / q, j = i - e * q;
     const float s = __fdiv_rn((float)j, (float)q);
     // corners c_e and c_{e+1} of the ring: c0 = (h,t,t), c1 = (t,h,t), c2 = (t,t,h)
-    const float c[3][3] = {{h, t, t}, {t, h, t}, {t, t, h}};
-    const float* p0 = c[e];
-    const float* p1 = c[e == 2 ? 0 : e + 1];
-    return mk(p0[0] + s * (p1[0] - p0[0]), p0[1] + s * (p1[1] - p0[1]), p0[2] + s * (p1[2] - p0[2]));
+    const int e1 = e == 2 ? 0 : e + 1;
+    const float a0 = e == 0 ? h : t, a1 = e == 1 ? h : t, a2 = e == 2 ? h : t;
+    const float b0 = e1 == 0 ? h : t, b1 = e1 == 1 ? h : t, b2 = e1 == 2 ? h : t;
+    return mk(a0 + s * (b0 - a0), a1 + s * (b1 - a1), a2 + s * (b2 - a2));
 }
 
 __global__ void __launch_bounds__(kSetupThreads) tess_setup_kernel(const AccumParams P, const VoxWork W) {
