@@ -118,10 +118,11 @@ struct VoxWork {
 constexpr int kSetupThreads = 256;  // triangles per setup block
 constexpr long long align256(long long b) { return (b + 255) & ~255LL; }
 // Scratch bytes the voxeliser needs for `ntri` triangles: a 48-byte setup
-// record, a unit count and a scan entry per triangle, one offset per block.
+// record, a unit count and a scan entry per triangle, one offset per block
+// (+ the total), then an 8-byte work counter.
 constexpr long long accumulate_scratch_bytes(long long ntri) {
     return align256(ntri * 48) + align256(ntri * 4) * 2 +
-           align256(((ntri + kSetupThreads - 1) / kSetupThreads + 1) * 4);
+           align256(((ntri + kSetupThreads - 1) / kSetupThreads + 2) * 4 + 8);
 }
 // Carves the scratch buffer into the AccumParams work arrays.
 void accumulate_bind_scratch(AccumParams& P, void* scratch);

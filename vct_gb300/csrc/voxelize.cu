@@ -31,6 +31,14 @@ constexpr int kWarps = 8;
 constexpr int kQueue = 64;
 constexpr int kRasterBlocksPerSM = 3;  // register budget: up to 3 raster CTAs per SM
 constexpr int kMaxBatchScenes = 256;  // scene id travels in 8 bits of a queue entry
+constexpr int kGrabUnits = 2;          // work units a warp takes from the shared counter at a time
+constexpr int kStagedBlocks = 4096;    // setup-block offsets copied to shared memory when they fit
+
+// The raster warps' shared work counter: 8 bytes after block_off[nblocks]
+// (zeroed by the setup kernel).
+__device__ __forceinline__ unsigned long long* grab_counter(const VoxWork& W, int nblocks) {
+    return reinterpret_cast<unsigned long long*>(W.block_off + (((long long)nblocks + 2) & ~1LL));
+}
 
 struct FragQueue {
     int tri[kQueue];       // triangle index within its scene
@@ -112,6 +120,7 @@ __global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Sce
         }
         W.tri_units[g] = units;
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *grab_counter(W, gridDim.x) = 0ull;
     block_scan_units(W, g, units);
 }
 
@@ -255,16 +264,19 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
     voxelize_raster_kernel(const Scenes S, const VoxWork W, int nblocks) {
     __shared__ FragQueue queues[kWarps];
     __shared__ unsigned frag_count[kMaxBatchScenes];  // VoxelizeInfo.totalVoxelFragments per scene
+    __shared__ uint32_t s_boff[kStagedBlocks + 1];
     const int lane = threadIdx.x & 31;
     FragQueue& q = queues[threadIdx.x >> 5];
     const unsigned FULL = 0xffffffffu;
     const int nscenes = S.count();
     for (int i = threadIdx.x; i < nscenes; i += blockDim.x) frag_count[i] = 0;
+    const bool staged = nblocks <= kStagedBlocks;
+    if (staged)
+        for (int i = threadIdx.x; i <= nblocks; i += blockDim.x) s_boff[i] = W.block_off[i];
     __syncthreads();
-    const long long nw = (long long)gridDim.x * kWarps;
-    const long long w = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
-    const long long total = W.block_off[nblocks];
-    const long long u0 = total * w / nw, u1 = total * (w + 1) / nw;
+    auto boff = [&](long long b) -> long long { return staged ? s_boff[b] : W.block_off[b]; };
+    const long long total = boff(nblocks);
+    unsigned long long* grab = grab_counter(W, nblocks);
     // The queue is a ring of kQueue entries: fragments [head, head + qn).
     int qn = 0, head = 0;  // warp-uniform
 
@@ -284,33 +296,45 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
         __syncwarp();
     };
 
-    if (u0 < u1) {
+    // Warps take kGrabUnits work units at a time from a shared counter until
+    // none are left, so that every warp ends at about the same time whatever
+    // the units cost (their pixel counts and coverage vary by orders of
+    // magnitude).  Fragments are summed as integers, so the order in which
+    // warps take the units does not change the result.
+    for (;;) {
+        unsigned long long gu = 0;
+        if (lane == 0) gu = atomicAdd(grab, (unsigned long long)kGrabUnits);
+        gu = __shfl_sync(FULL, gu, 0);
+        if ((long long)gu >= total) break;
+        const long long u0 = (long long)gu, u1 = min(u0 + (long long)kGrabUnits, total);
         // Triangle owning unit u0: binary search over the block offsets, then
-        // over the block-local scan.
+        // the block-local scan, 8 entries per lane: the number of entries <=
+        // u0 is one past the last triangle starting at or before u0.
         int lo = 0, hi = nblocks - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if ((long long)W.block_off[mid] <= u0)
+            if (boff(mid) <= u0)
                 lo = mid;
             else
                 hi = mid - 1;
         }
-        long long glo = (long long)lo * kSetupThreads;
-        long long ghi = min(glo + kSetupThreads, W.ntri) - 1;
-        while (glo < ghi) {
-            const long long mid = (glo + ghi + 1) >> 1;
-            if (unit_start<Scenes>(W, mid) <= u0)
-                glo = mid;
-            else
-                ghi = mid - 1;
+        const long long gbase = (long long)lo * kSetupThreads;
+        const int in_block = (int)min((long long)kSetupThreads, W.ntri - gbase);
+        const uint32_t rel = (uint32_t)(u0 - boff(lo));
+        int below = 0;
+#pragma unroll
+        for (int j = 0; j < kSetupThreads / 32; ++j) {
+            const int k = lane * (kSetupThreads / 32) + j;
+            below += (k < in_block && __ldg(W.tri_scan + gbase + k) <= rel) ? 1 : 0;
         }
-        long long g = glo;
-        long long start = unit_start<Scenes>(W, g);
+        below = __reduce_add_sync(FULL, below);
+        long long g = gbase + max(below - 1, 0);
+        long long start = boff(lo) + W.tri_scan[g];
         uint32_t nunits = W.tri_units[g];
         for (long long u = u0; u < u1; ++u) {
             while (u >= start + nunits) {
                 ++g;
-                start = unit_start<Scenes>(W, g);
+                start = boff(g / kSetupThreads) + W.tri_scan[g];
                 nunits = W.tri_units[g];
             }
             long long tl;
