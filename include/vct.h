@@ -324,6 +324,14 @@ vct_status vct_trace(vct_ctx* ctx, const vct_gbuffer* gbuffer, const float eye[3
 vct_status vct_frame(vct_ctx* ctx, const vct_triangles* tris, const vct_light* lights,
                      int32_t n_lights, const vct_shadow_desc* shadow, const float eye[3],
                      const vct_gbuffer* gbuffer, const vct_trace_out* out, void* stream);
+/* The volume half of vct_frame (voxelise, inject, mips; the reference's
+ * passes before phong.frag), for callers that overlap the upload of the
+ * G-buffer with it: vct_frame = vct_frame_volume + vct_trace, with the same
+ * results.  With timers enabled, the next vct_trace records the render
+ * stage. */
+vct_status vct_frame_volume(vct_ctx* ctx, const vct_triangles* tris, const vct_light* lights,
+                            int32_t n_lights, const vct_shadow_desc* shadow, const float eye[3],
+                            void* stream);
 /* Synchronises `stream` and returns the VoxelizeInfo counters of the last
  * vct_normalize / vct_frame. */
 vct_status vct_get_stats(vct_ctx* ctx, vct_stats* out, void* stream);

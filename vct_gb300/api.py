@@ -197,6 +197,11 @@ class Context:
         L.check(self._lib.vct_frame(self.handle, C.byref(tris), arr, n, C.byref(shadow), f3(eye), C.byref(gb),
                                     C.byref(out), _stream(stream)), "vct_frame")
 
+    def frame_volume(self, tris, lights, shadow, eye, stream=None):
+        arr, n = lights
+        L.check(self._lib.vct_frame_volume(self.handle, C.byref(tris), arr, n, C.byref(shadow), f3(eye),
+                                           _stream(stream)), "vct_frame_volume")
+
     def enable_timers(self, on: bool = True):
         L.check(self._lib.vct_enable_timers(self.handle, int(on)), "vct_enable_timers")
 

@@ -912,23 +912,22 @@ vct_status vct_trace(vct_ctx* c, const vct_gbuffer* g, const float eye[3], const
     if ((s = fill_trace(c, g, eye, out, P)) != VCT_OK) return s;
     launch_trace(P, st);
     VCT_CHECK_LAUNCH("trace");
+    if (c->timers_on && c->volume_timed) {  // render stage of a timed vct_frame_volume
+        VCT_CUDA(cudaEventRecord(c->ev[4], st));
+        c->timers_recorded = true;
+    }
     return VCT_OK;
 }
 
-vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n,
-                     const vct_shadow_desc* shadow, const float eye[3], const vct_gbuffer* g,
-                     const vct_trace_out* out, void* stream) {
-    if (!c || !eye || !out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
-    vct_status s = validate_tris(tris);
-    if (s != VCT_OK) return s;
-    bool need_shadow = false;
-    if ((s = validate_lights(lights, n, &need_shadow)) != VCT_OK) return s;
-    if ((s = validate_shadow(shadow, true)) != VCT_OK) return s;
-    if ((s = validate_gbuffer(g)) != VCT_OK) return s;
-    DeviceScope ds(c->device);
-    VCT_CUDA(ds.err);
-    cudaStream_t st = as_stream(stream);
+namespace {
+
+// The volume pass of vct_frame: voxelise, inject (marked), normalise +
+// inject resolve + mips.  Inputs are validated by the callers.
+vct_status frame_volume(vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n,
+                        const vct_shadow_desc* shadow, const float eye[3], cudaStream_t st) {
+    vct_status s = VCT_OK;
     const bool timed = c->timers_on;
+    c->volume_timed = false;
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[0], st));
     VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
     VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, st));
@@ -983,11 +982,47 @@ vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lig
     c->radiance_ready = true;
     c->mips_ready = true;
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[3], st));
+    c->volume_timed = timed;
+    return VCT_OK;
+}
+
+vct_status validate_volume_inputs(const vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n,
+                                  const vct_shadow_desc* shadow, const float* eye) {
+    if (!c || !eye) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    vct_status s = validate_tris(tris);
+    if (s != VCT_OK) return s;
+    bool need_shadow = false;
+    if ((s = validate_lights(lights, n, &need_shadow)) != VCT_OK) return s;
+    return validate_shadow(shadow, true);
+}
+
+}  // namespace
+
+vct_status vct_frame_volume(vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n,
+                            const vct_shadow_desc* shadow, const float eye[3], void* stream) {
+    vct_status s = validate_volume_inputs(c, tris, lights, n, shadow, eye);
+    if (s != VCT_OK) return s;
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    return frame_volume(c, tris, lights, n, shadow, eye, as_stream(stream));
+}
+
+vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lights, int32_t n,
+                     const vct_shadow_desc* shadow, const float eye[3], const vct_gbuffer* g,
+                     const vct_trace_out* out, void* stream) {
+    vct_status s = validate_volume_inputs(c, tris, lights, n, shadow, eye);
+    if (s != VCT_OK) return s;
+    if (!out) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if ((s = validate_gbuffer(g)) != VCT_OK) return s;
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    cudaStream_t st = as_stream(stream);
+    if ((s = frame_volume(c, tris, lights, n, shadow, eye, st)) != VCT_OK) return s;
     TraceParams T;
     if ((s = fill_trace(c, g, eye, out, T)) != VCT_OK) return s;
     launch_trace(T, st);
     VCT_CHECK_LAUNCH("frame: trace");
-    if (timed) {
+    if (c->volume_timed) {
         VCT_CUDA(cudaEventRecord(c->ev[4], st));
         c->timers_recorded = true;
     }

@@ -30,6 +30,7 @@ struct vct_ctx {
     bool tex_ready = false;
     bool timers_on = false;
     bool timers_recorded = false;
+    bool volume_timed = false;  // the last volume pass recorded ev[0..3]: a trace after it records ev[4]
     cudaEvent_t ev[5] = {};
     void* vox_scratch = nullptr;  // voxeliser work-distribution arrays
     long long vox_scratch_bytes = 0;
