@@ -58,9 +58,9 @@ def parse():
     ap.add_argument("--learned-scenes", type=int, default=8, help="learned: held-out scenes timed")
     ap.add_argument("--frames", type=int, default=120, help="dynamic: frames of the actor animation")
     ap.add_argument("--no-autotune", action="store_true", help="batched: keep the default launch shapes")
-    ap.add_argument("--filter", default="software", choices=["software", "levels", "hardware"],
-                    help="cone sampler: fp32 trilinear (exact), texture units per level + fp32 level blend, "
-                         "or texture units' trilinear-mip")
+    ap.add_argument("--filter", default="software", choices=["software", "hybrid", "levels", "hardware"],
+                    help="cone sampler: fp32 trilinear (exact), exact finer level + texture-unit coarser level, "
+                         "texture units per level + fp32 level blend, or texture units' trilinear-mip")
     ap.add_argument("--voxelizer", default="raster", choices=["raster", "tess"],
                     help="rasterising voxeliser (voxelize.geom/.frag, the benchmark frame's) or the "
                          "tessellation voxeliser (testTesselation.tesc/.tese)")
@@ -227,7 +227,7 @@ def run_ours(args, rank, world):
     out = api.trace_out(color=color)
     ctx = api.Context(api.config_for(sc, device=local))
     params = api.scene_params(sc)
-    params.trace_filter = {"software": L.VCT_FILTER_SOFTWARE, "levels": L.VCT_FILTER_HARDWARE_LEVELS,
+    params.trace_filter = {"software": L.VCT_FILTER_SOFTWARE, "hybrid": L.VCT_FILTER_HYBRID, "levels": L.VCT_FILTER_HARDWARE_LEVELS,
                            "hardware": L.VCT_FILTER_HARDWARE}[args.filter]
     params.voxelize_tesselation = int(args.voxelizer == "tess")
     params.warp_mode = L.VCT_WARP_PERSPECTIVE if args.warp == "perspective" else L.VCT_WARP_NONE
@@ -433,7 +433,7 @@ def run_batch(args, rank, world):
     t0 = time.perf_counter()
     scs = [scenes.batch_scene(seed=args.seed + 1000 * rank, index=i) for i in range(args.batch_scenes)]
     gen_s = time.perf_counter() - t0
-    filt = {"software": L.VCT_FILTER_SOFTWARE, "levels": L.VCT_FILTER_HARDWARE_LEVELS,
+    filt = {"software": L.VCT_FILTER_SOFTWARE, "hybrid": L.VCT_FILTER_HYBRID, "levels": L.VCT_FILTER_HARDWARE_LEVELS,
             "hardware": L.VCT_FILTER_HARDWARE}[args.filter]
     inputs, descs, colors = [], [], []
     for sc in scs:

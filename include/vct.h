@@ -110,6 +110,8 @@ typedef struct vct_cone_settings {
 #define VCT_FILTER_SOFTWARE 0 /* fp32 trilinear (exact GL semantics) from a bordered fp32 copy of the chain */
 #define VCT_FILTER_HARDWARE 1 /* texture units' trilinear-mip filtering */
 #define VCT_FILTER_HARDWARE_LEVELS 2 /* texture units' trilinear filtering per level, levels blended in fp32 */
+#define VCT_FILTER_HYBRID 3 /* the finer level of each trilinear-mip sample in exact fp32 (as SOFTWARE), the
+                               coarser one by the texture units, blended in fp32 */
 
 /* Voxel warping: positions in [0,1]^3 volume coordinates are remapped before
  * they index or sample the grid, in the voxeliser (voxelize.frag:100-106),

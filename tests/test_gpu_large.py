@@ -70,7 +70,8 @@ def test_large_accumulators_bitexact(large):
         assert np.array_equal(occ, ref["count"] > 0)
 
 
-@pytest.mark.parametrize("filt", [L.VCT_FILTER_SOFTWARE, L.VCT_FILTER_HARDWARE_LEVELS, L.VCT_FILTER_HARDWARE])
+@pytest.mark.parametrize("filt", [L.VCT_FILTER_SOFTWARE, L.VCT_FILTER_HYBRID, L.VCT_FILTER_HARDWARE_LEVELS,
+                                  L.VCT_FILTER_HARDWARE])
 def test_large_frame(large, filt):
     import torch
 
@@ -93,8 +94,9 @@ def test_large_frame(large, filt):
     e32 = rel_l2(got, rgb(_rows(ref["irr32"], W)))
     print(f"\nfilter {filt}: irradiance rel-L2 vs fp64 {e64:.3e}, vs fp32 oracle {e32:.3e}")
     # The texture units filter with 8-bit fixed-point weights: measured 1.2e-3
-    # (per-level) and 1.9e-3 (trilinear-mip) on this frame, so only the
-    # software sampler is held to the 1e-3 target; the others to 1e-2.
-    assert e64 <= (1e-3 if filt == L.VCT_FILTER_SOFTWARE else 1e-2)
+    # (per-level) and 1.9e-3 (trilinear-mip) on this frame, so they are held to
+    # 1e-2.  The software sampler and the hybrid (texture units only on the
+    # coarser level of each sample) are held to the 1e-3 target.
+    assert e64 <= (1e-3 if filt in (L.VCT_FILTER_SOFTWARE, L.VCT_FILTER_HYBRID) else 1e-2)
     if filt == L.VCT_FILTER_SOFTWARE:
         assert e32 <= 1e-5

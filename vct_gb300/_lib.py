@@ -27,6 +27,7 @@ VCT_CONFIG_COLOR_MIPS = 1
 VCT_FILTER_SOFTWARE = 0
 VCT_FILTER_HARDWARE = 1
 VCT_FILTER_HARDWARE_LEVELS = 2
+VCT_FILTER_HYBRID = 3
 VCT_WARP_NONE = 0
 VCT_WARP_ANALYTIC = 1
 VCT_WARP_TEXTURE = 2

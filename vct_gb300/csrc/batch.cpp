@@ -63,6 +63,8 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         if (s == VCT_OK) s = validate_gbuffer(&d.gbuffer);
         if (s != VCT_OK) return s;
         if (c->params.trace_filter != filter) return fail(VCT_ERR_INVALID_ARGUMENT, "all scenes of a batch must use the same trace_filter");
+        if (filter == VCT_FILTER_HYBRID)
+            return fail(VCT_ERR_UNSUPPORTED, "batches use VCT_FILTER_SOFTWARE or the texture-unit samplers");
         if (filter != VCT_FILTER_SOFTWARE && (s = ensure_texture(c)) != VCT_OK) return s;
         const bool hw = filter != VCT_FILTER_SOFTWARE;
         if (c->params.warp_mode == VCT_WARP_TEXTURE || c->params.warp_mode == VCT_WARP_PERSPECTIVE)

@@ -140,7 +140,7 @@ vct_status validate_params(const vct_params* p) {
             return fail(VCT_ERR_INVALID_ARGUMENT, "cone bias/lod offset must be finite, initial height > 0");
     }
     if (p->trace_filter != VCT_FILTER_SOFTWARE && p->trace_filter != VCT_FILTER_HARDWARE &&
-        p->trace_filter != VCT_FILTER_HARDWARE_LEVELS)
+        p->trace_filter != VCT_FILTER_HARDWARE_LEVELS && p->trace_filter != VCT_FILTER_HYBRID)
         return fail(VCT_ERR_INVALID_ARGUMENT, "trace_filter must be one of VCT_FILTER_*");
     if (p->axis_override < -1 || p->axis_override > 2) return fail(VCT_ERR_INVALID_ARGUMENT, "axis_override in [-1, 2]");
     if (!std::isfinite(p->voxel_set_opacity) || !std::isfinite(p->temporal_decay))
@@ -442,6 +442,11 @@ MipLevels mip_levels(vct_ctx* ctx, uint2* chain, int levels) {
     for (int l = 0; l < levels; ++l) M.level[l] = level_ptr(chain, ctx, l);
     return M;
 }
+
+// The samplers' copies of the radiance chain: the texture array (texture-unit
+// filtering) and the bordered fp32 chain (software filtering).
+bool filter_uses_texture(int filter) { return filter != VCT_FILTER_SOFTWARE; }
+bool filter_uses_bordered(int filter) { return filter == VCT_FILTER_SOFTWARE || filter == VCT_FILTER_HYBRID; }
 
 vct_status ensure_texture(vct_ctx* ctx) {
     if (ctx->tex_array) return VCT_OK;
@@ -877,10 +882,11 @@ vct_status vct_build_mips(vct_ctx* c, int32_t volume, void* stream) {
     if (volume == VCT_VOLUME_RADIANCE) {
         launch_mips(mip_levels(c, c->radiance, c->levels), 0, st);
         VCT_CHECK_LAUNCH("build mips");
-        if (c->params.trace_filter != VCT_FILTER_SOFTWARE) {
+        if (filter_uses_texture(c->params.trace_filter)) {
             vct_status s = refresh_texture(c, st);
             if (s != VCT_OK) return s;
-        } else {
+        }
+        if (filter_uses_bordered(c->params.trace_filter)) {
             launch_pad_copy(c->radiance, c->pchain, c->dim, c->levels, st);
             VCT_CHECK_LAUNCH("bordered chain copy");
             c->pad_ready = true;
@@ -904,10 +910,10 @@ vct_status vct_trace(vct_ctx* c, const vct_gbuffer* g, const float eye[3], const
     DeviceScope ds(c->device);
     VCT_CUDA(ds.err);
     cudaStream_t st = as_stream(stream);
-    if (c->params.trace_filter != VCT_FILTER_SOFTWARE && !c->tex_ready) {
+    if (filter_uses_texture(c->params.trace_filter) && !c->tex_ready) {
         if ((s = refresh_texture(c, st)) != VCT_OK) return s;
     }
-    if (c->params.trace_filter == VCT_FILTER_SOFTWARE && (s = ensure_padded_chain(c, st)) != VCT_OK) return s;
+    if (filter_uses_bordered(c->params.trace_filter) && (s = ensure_padded_chain(c, st)) != VCT_OK) return s;
     TraceParams P;
     if ((s = fill_trace(c, g, eye, out, P)) != VCT_OK) return s;
     launch_trace(P, st);
@@ -942,7 +948,8 @@ vct_status frame_volume(vct_ctx* c, const vct_triangles* tris, const vct_light* 
     launch_inject_mark(I, st);
     VCT_CHECK_LAUNCH("frame: inject mark");
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[2], st));
-    const bool hw = c->params.trace_filter != VCT_FILTER_SOFTWARE;
+    const bool hw = filter_uses_texture(c->params.trace_filter);
+    const bool pad = filter_uses_bordered(c->params.trace_filter);
     if (hw && (s = ensure_texture(c)) != VCT_OK) return s;
     ResolveParams R;
     std::memset(&R, 0, sizeof R);
@@ -962,7 +969,7 @@ vct_status frame_volume(vct_ctx* c, const vct_triangles* tris, const vct_light* 
     for (int l = 0; l <= R.mip_levels; ++l) {
         R.radiance_levels[l] = level_ptr(c->radiance, c, l);
         R.surf[l] = hw ? c->surf[l] : 0;
-        R.pad_levels[l] = hw ? nullptr : c->pchain + padded_level_offset(c->dim, l);
+        R.pad_levels[l] = pad ? c->pchain + padded_level_offset(c->dim, l) : nullptr;
     }
     launch_resolve(R, st);
     VCT_CHECK_LAUNCH("frame: resolve");
@@ -971,13 +978,13 @@ vct_status frame_volume(vct_ctx* c, const vct_triangles* tris, const vct_light* 
         MipLevels M = mip_levels(c, c->radiance, c->levels);
         for (int l = 0; l < c->levels; ++l) {
             M.surf[l] = hw ? c->surf[l] : 0;
-            M.pad[l] = hw ? nullptr : c->pchain + padded_level_offset(c->dim, l);
+            M.pad[l] = pad ? c->pchain + padded_level_offset(c->dim, l) : nullptr;
         }
         launch_mips(M, 4, st);
         VCT_CHECK_LAUNCH("frame: coarse mips");
     }
     c->tex_ready = hw;
-    c->pad_ready = !hw;
+    c->pad_ready = pad;
     c->stats_reset_pending = true;
     c->radiance_ready = true;
     c->mips_ready = true;

@@ -93,6 +93,16 @@ __device__ __forceinline__ float4 sample_lod(const TraceParams& P, const int* of
         return lerp4(tex3DLod<float4>(P.tex, p.x, p.y, p.z, fl), tex3DLod<float4>(P.tex, p.x, p.y, p.z, fl + 1.0f),
                      lambda - fl);
     }
+    if (MODE == VCT_FILTER_HYBRID && lambda > 0.0f && lambda < (float)q) {
+        // The finer level exactly, the coarser one (weight lambda - floor(lambda))
+        // by the texture units at its integral level.
+        const float fl = floorf(lambda);
+        const int d1 = (int)fl;
+        const rgba2 fine = trilinear2(P, off, d1, p, warp_leaves_volume(P.warp.mode));
+        const float4 c = tex3DLod<float4>(P.tex, p.x, p.y, p.z, fl + 1.0f);
+        const rgba2 coarse = {make_float2(c.x, c.y), make_float2(c.z, c.w)};
+        return to_float4(lerp2(fine, coarse, lambda - fl));
+    }
     if (lambda <= 0.0f) {  // magnification: GL_NEAREST on level 0 (index S = border)
         const int S = P.dim;
         return texel(P.chain, S, (int)floorf(p.x * S), (int)floorf(p.y * S), (int)floorf(p.z * S));

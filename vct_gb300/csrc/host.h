@@ -103,6 +103,8 @@ void fill_inject(vct_ctx* ctx, const vct_shadow_desc* s, const float* eye, Injec
 WarpDev warp_dev(const vct_ctx* ctx, const float* eye);
 // VCT_WARP_TEXTURE: the 32^3 occupancy voxelisation of `A`'s triangles and
 // the warp map built from it (A: the main pass's parameters, scratch bound).
+bool filter_uses_texture(int filter);
+bool filter_uses_bordered(int filter);
 vct_status build_warpmap(vct_ctx* ctx, const AccumParams& A, cudaStream_t s);
 MipLevels mip_levels(vct_ctx* ctx, uint2* chain, int levels);
 vct_status ensure_texture(vct_ctx* ctx);

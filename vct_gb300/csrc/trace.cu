@@ -127,6 +127,8 @@ void launch_trace_set(const Scenes& S, int filter, long long tiles, cudaStream_t
         trace_kernel<VCT_FILTER_HARDWARE><<<(unsigned)tiles, 256, 0, s>>>(S);
     else if (filter == VCT_FILTER_HARDWARE_LEVELS)
         trace_kernel<VCT_FILTER_HARDWARE_LEVELS><<<(unsigned)tiles, 256, 0, s>>>(S);
+    else if (filter == VCT_FILTER_HYBRID)
+        trace_kernel<VCT_FILTER_HYBRID><<<(unsigned)tiles, 256, 0, s>>>(S);
     else
         trace_kernel<VCT_FILTER_SOFTWARE><<<(unsigned)tiles, 256, 0, s>>>(S);
     note_launches(1);
