@@ -378,6 +378,10 @@ def run_ours(args, rank, world):
                             "mapped and summed into its voxel), not by HBM")
     if dom == "trace":
         roofline["samples_per_s"] = round(n_samples / (kernel_ms[dom] * 1e-3), 1)
+        # the tracer's own ceiling: the sampler's peak rate with L1-resident texels (vct_sampler_rate)
+        peak_rate = ctx.sampler_rate(params.trace_filter, 1 << 31, stream)
+        roofline["sampler_peak_samples_per_s"] = round(peak_rate, 1)
+        roofline["sampler_frac"] = round(n_samples / (kernel_ms[dom] * 1e-3) / peak_rate, 4)
         if headline:
             roofline["issue"] = dict(NCU_TRACE_ISSUE, source="ncu capture of this workload")
         roofline["note"] = ("cone tracing is gather-bound (L1/L2 trilinear samples), not HBM-bound: its HBM "

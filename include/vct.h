@@ -334,6 +334,15 @@ vct_status vct_frame(vct_ctx* ctx, const vct_triangles* tris, const vct_light* l
 vct_status vct_frame_volume(vct_ctx* ctx, const vct_triangles* tris, const vct_light* lights,
                             int32_t n_lights, const vct_shadow_desc* shadow, const float eye[3],
                             void* stream);
+/* Peak rate of the cone tracer's textureLod samples on this GPU, the
+ * denominator of its roofline (the tracer is bound by sample filtering, not
+ * HBM): `samples` samples spread over the GPU, each through the sampler of
+ * `filter` (VCT_FILTER_*), at positions inside one small region of the
+ * current radiance chain (so its texels stay in L1) and at the levels and
+ * fractions cone steps use.  Needs a built chain (vct_frame, or
+ * vct_build_mips).  Synchronises `stream`. */
+vct_status vct_sampler_rate(vct_ctx* ctx, int32_t filter, int64_t samples, double* samples_per_second,
+                            void* stream);
 /* Synchronises `stream` and returns the VoxelizeInfo counters of the last
  * vct_normalize / vct_frame. */
 vct_status vct_get_stats(vct_ctx* ctx, vct_stats* out, void* stream);

@@ -170,6 +170,7 @@ SIGNATURES = {
     "vct_frame": (st, [vp, P(vct_triangles), P(vct_light), C.c_int32, P(vct_shadow_desc), P(C.c_float),
                        P(vct_gbuffer), P(vct_trace_out), vp]),
     "vct_frame_volume": (st, [vp, P(vct_triangles), P(vct_light), C.c_int32, P(vct_shadow_desc), P(C.c_float), vp]),
+    "vct_sampler_rate": (st, [vp, C.c_int32, C.c_int64, P(C.c_double), vp]),
     "vct_get_stats": (st, [vp, P(vct_stats), vp]),
     "vct_enable_timers": (st, [vp, C.c_int32]),
     "vct_get_timers": (st, [vp, P(vct_timers)]),

@@ -202,6 +202,12 @@ class Context:
         L.check(self._lib.vct_frame_volume(self.handle, C.byref(tris), arr, n, C.byref(shadow), f3(eye),
                                            _stream(stream)), "vct_frame_volume")
 
+    def sampler_rate(self, filt: int, samples: int = 1 << 31, stream=None) -> float:
+        r = C.c_double()
+        L.check(self._lib.vct_sampler_rate(self.handle, int(filt), int(samples), C.byref(r), _stream(stream)),
+                "vct_sampler_rate")
+        return r.value
+
     def enable_timers(self, on: bool = True):
         L.check(self._lib.vct_enable_timers(self.handle, int(on)), "vct_enable_timers")
 

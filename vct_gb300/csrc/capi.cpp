@@ -1036,6 +1036,54 @@ vct_status vct_frame(vct_ctx* c, const vct_triangles* tris, const vct_light* lig
     return VCT_OK;
 }
 
+vct_status vct_sampler_rate(vct_ctx* c, int32_t filter, int64_t samples, double* rate, void* stream) {
+    if (!c || !rate) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (filter < VCT_FILTER_SOFTWARE || filter > VCT_FILTER_HYBRID)
+        return fail(VCT_ERR_INVALID_ARGUMENT, "filter must be one of VCT_FILTER_*");
+    if (samples < 1 || samples > (1LL << 40)) return fail(VCT_ERR_INVALID_ARGUMENT, "samples out of range");
+    if (!c->mips_ready) return fail(VCT_ERR_STATE, "no radiance chain: run vct_frame or vct_build_mips first");
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    cudaStream_t st = as_stream(stream);
+    vct_status s = VCT_OK;
+    if (filter_uses_texture(filter) && !c->tex_ready && (s = refresh_texture(c, st)) != VCT_OK) return s;
+    if (filter_uses_bordered(filter) && (s = ensure_padded_chain(c, st)) != VCT_OK) return s;
+    vct_gbuffer g;
+    std::memset(&g, 0, sizeof g);
+    g.width = g.height = 1;
+    vct_trace_out o;
+    std::memset(&o, 0, sizeof o);
+    TraceParams P;
+    const float eye[3] = {0.f, 0.f, 0.f};
+    if ((s = fill_trace(c, &g, eye, &o, P)) != VCT_OK) return s;
+    P.filter = filter;
+    const int blocks = c->num_sms * 4;
+    const long long threads = (long long)blocks * 256;
+    const int iters = (int)std::max<long long>(1, std::min<long long>(1 << 20, samples / threads));
+    float* sink = nullptr;
+    VCT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&sink), (size_t)threads * sizeof(float), st));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    if (err == cudaSuccess) {
+        launch_sampler_rate(P, filter, blocks, std::max(1, iters / 8), sink, st);  // warm-up
+        err = cudaEventRecord(e0, st);
+    }
+    if (err == cudaSuccess) {
+        launch_sampler_rate(P, filter, blocks, iters, sink, st);
+        err = cudaEventRecord(e1, st);
+    }
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFreeAsync(sink, st);
+    if (err != cudaSuccess) return fail(VCT_ERR_CUDA, std::string("sampler rate: ") + cudaGetErrorString(err));
+    *rate = ms > 0.0f ? (double)threads * (double)iters / (ms * 1e-3) : 0.0;
+    return VCT_OK;
+}
+
 vct_status vct_enable_timers(vct_ctx* c, int32_t enable) {
     if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
     DeviceScope ds(c->device);

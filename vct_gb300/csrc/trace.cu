@@ -118,7 +118,49 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const Scenes S) {
     }
 }
 
+// Peak rate of textureLod samples (the denominator of the cone tracer's
+// roofline): every thread takes `iters` samples with the tracer's sampler at
+// positions inside one 8-voxel-wide region near the volume's centre, at the
+// levels and fractions cone steps use, so the texels stay in L1 and nothing
+// but sampling is timed.  The sum goes to `sink` so the work is kept.
+template <int MODE>
+__global__ void __launch_bounds__(256, 4) sampler_rate_kernel(const TraceParams P, int iters, float* sink) {
+    __shared__ int s_off[VCT_MAX_LEVELS];
+    if (threadIdx.x < VCT_MAX_LEVELS)
+        s_off[threadIdx.x] = threadIdx.x < P.levels ? (int)padded_level_offset(P.dim, threadIdx.x) : 0;
+    __syncthreads();
+    const float span = 8.0f / (float)P.dim;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    f3 p = mk(0.5f + span * (float)(t & 7) * 0.125f, 0.5f + span * (float)((t >> 3) & 7) * 0.125f,
+              0.5f + span * (float)((t >> 6) & 7) * 0.125f);
+    const f3 step = mk(span * 0.031f, span * 0.017f, span * 0.023f);
+    const float top = (float)(P.levels - 1);
+    float acc = 0.0f;
+    for (int i = 0; i < iters; ++i) {
+        const float lambda = fminf(0.1f + 0.37f * (float)(i & 7), top - 0.05f);
+        const float4 v = sample_lod<MODE>(P, s_off, p, lambda);
+        acc += v.x + v.y + v.z + v.w;
+        p = add(p, step);
+        if (p.x > 0.5f + span) p.x -= span;
+        if (p.y > 0.5f + span) p.y -= span;
+        if (p.z > 0.5f + span) p.z -= span;
+    }
+    sink[t] = acc;
+}
+
 }  // namespace
+
+void launch_sampler_rate(const TraceParams& P, int filter, int blocks, int iters, float* sink, cudaStream_t s) {
+    if (filter == VCT_FILTER_HARDWARE)
+        sampler_rate_kernel<VCT_FILTER_HARDWARE><<<blocks, 256, 0, s>>>(P, iters, sink);
+    else if (filter == VCT_FILTER_HARDWARE_LEVELS)
+        sampler_rate_kernel<VCT_FILTER_HARDWARE_LEVELS><<<blocks, 256, 0, s>>>(P, iters, sink);
+    else if (filter == VCT_FILTER_HYBRID)
+        sampler_rate_kernel<VCT_FILTER_HYBRID><<<blocks, 256, 0, s>>>(P, iters, sink);
+    else
+        sampler_rate_kernel<VCT_FILTER_SOFTWARE><<<blocks, 256, 0, s>>>(P, iters, sink);
+    note_launches(1);
+}
 
 template <class Scenes>
 void launch_trace_set(const Scenes& S, int filter, long long tiles, cudaStream_t s) {

@@ -266,6 +266,8 @@ void launch_resolve(const ResolveParams& P, cudaStream_t s);
 // Builds levels [first+1, levels) from level `first`.
 void launch_mips(const MipLevels& M, int first, cudaStream_t s);
 void launch_trace(const TraceParams& P, cudaStream_t s);
+// Sampler throughput microbenchmark (vct_sampler_rate): blocks x 256 threads x iters samples.
+void launch_sampler_rate(const TraceParams& P, int filter, int blocks, int iters, float* sink, cudaStream_t s);
 void launch_shadow_raster(const ShadowRasterParams& P, cudaStream_t s);
 void launch_gbuffer_raster(const GbufferRasterParams& P, cudaStream_t s);
 void launch_fill_u32(uint32_t* p, uint32_t v, long long n, cudaStream_t s);
