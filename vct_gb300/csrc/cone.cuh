@@ -116,14 +116,14 @@ __device__ __forceinline__ float4 sample_lod(const TraceParams& P, const int* of
     return to_float4(lerp2(trilinear2(P, off, d1, p), trilinear2(P, off, d1 + 1, p), f));
 }
 
+// `tanh` is tanf(c.cone_angle * 0.5f), which callers with many cones of one
+// setting compute once.
 template <int MODE>
 __device__ __forceinline__ float4 trace_cone(const TraceParams& P, const int* off, f3 pos, f3 n, f3 dir,
-                                             const vct_cone_settings c,
-                             float maxd, unsigned& ns) {
+                                             const vct_cone_settings c, float maxd, unsigned& ns, float tanh) {
     dir = fnormalize(dir);
     const float scale = 1.0f / (float)P.dim;
     const f3 start = add(pos, mul(mul(n, c.bias), scale));
-    const float tanh = tanf(c.cone_angle * 0.5f);
     float h = c.cone_initial_height;
     float alpha = 0.0f;
     f3 col = mk(0.f, 0.f, 0.f);
@@ -143,6 +143,12 @@ __device__ __forceinline__ float4 trace_cone(const TraceParams& P, const int* of
         h += r;
     }
     return make_float4(col.x, col.y, col.z, alpha);
+}
+
+template <int MODE>
+__device__ __forceinline__ float4 trace_cone(const TraceParams& P, const int* off, f3 pos, f3 n, f3 dir,
+                                             const vct_cone_settings c, float maxd, unsigned& ns) {
+    return trace_cone<MODE>(P, off, pos, n, dir, c, maxd, ns, tanf(c.cone_angle * 0.5f));
 }
 
 }  // namespace cone

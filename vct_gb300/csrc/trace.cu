@@ -51,8 +51,11 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const Scenes S) {
     const int y = (ty << thl) + ((wid >> wxl) << (5 - wwl)) + (lane >> wwl);
     // Offsets of the bordered levels (32-bit: the chain holds < 2^31 voxels).
     __shared__ int s_off[VCT_MAX_LEVELS];
+    __shared__ float s_tan[2];  // tanf of the diffuse and specular half-apertures
     if (threadIdx.x < VCT_MAX_LEVELS)
         s_off[threadIdx.x] = threadIdx.x < P.levels ? (int)padded_level_offset(P.dim, threadIdx.x) : 0;
+    if (threadIdx.x == 32) s_tan[0] = tanf(P.diffuse.cone_angle * 0.5f);
+    if (threadIdx.x == 64) s_tan[1] = tanf(P.specular_cone.cone_angle * 0.5f);
     __syncthreads();
     unsigned ns = 0;
     if (x < P.width && y < P.height) {
@@ -81,7 +84,7 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const Scenes S) {
                     const float dx = kConeDir[c][0], dy = kConeDir[c][1], dz = kConeDir[c][2];
                     f3 d = P.ref_tbn_quirk ? add(add(mul(T, dx), mul(B, dy)), mul(N, dz))
                                            : sub(add(mul(T, dx), mul(N, dy)), mul(B, dz));
-                    float4 cr = trace_cone<MODE>(P, s_off, vp, N, d, P.diffuse, P.max_distance, ns);
+                    float4 cr = trace_cone<MODE>(P, s_off, vp, N, d, P.diffuse, P.max_distance, ns, s_tan[0]);
                     const float w = kConeWeight[c];
                     ind = make_float4(fmaf(w, cr.x, ind.x), fmaf(w, cr.y, ind.y), fmaf(w, cr.z, ind.z),
                                       fmaf(w, cr.w, ind.w));
@@ -92,7 +95,7 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const Scenes S) {
                 if (P.enable_reflections) {
                     const f3 I = sub(mk(gp.x, gp.y, gp.z), P.eye);
                     const f3 R = sub(I, mul(N, 2.0f * dot(N, I)));
-                    spc = trace_cone<MODE>(P, s_off, vp, N, R, P.specular_cone, P.max_distance, ns);
+                    spc = trace_cone<MODE>(P, s_off, vp, N, R, P.specular_cone, P.max_distance, ns, s_tan[1]);
                     rgb = add(rgb, mul(mk(spc.x, spc.y, spc.z), P.reflect_scale));
                 }
                 const float as = P.ambient_scale;
