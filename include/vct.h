@@ -245,8 +245,9 @@ typedef struct vct_stats {
 
 /* Device time of the last vct_frame's stages, the reference's GLBufferedTimer
  * regions (src/Application.h:192): voxelize = rasterise + accumulate,
- * radiance = injection marking, mipmap = normalise + inject resolve + mip
- * chain, render = cone tracing, total = all of them. */
+ * radiance = what remains of injection marking after the voxeliser (the
+ * marking runs concurrently with it, so usually about 0), mipmap = normalise
+ * + inject resolve + mip chain, render = cone tracing, total = all of them. */
 typedef struct vct_timers {
     float voxelize_ms;
     float radiance_ms;

@@ -714,6 +714,15 @@ vct_status vct_create(const vct_config* cfg, vct_ctx** out) {
             return fail(e == cudaErrorMemoryAllocation ? VCT_ERR_OUT_OF_MEMORY : VCT_ERR_CUDA, msg);
         }
     }
+    cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        std::string msg = std::string("stream/event creation failed: ") + cudaGetErrorString(e);
+        vct_destroy(c);
+        return fail(VCT_ERR_CUDA, msg);
+    }
     *out = c;
     return VCT_OK;
 }
@@ -723,6 +732,9 @@ vct_status vct_destroy(vct_ctx* c) {
     DeviceScope ds(c->device);
     for (auto e : c->ev)
         if (e) cudaEventDestroy(e);
+    if (c->fork) cudaEventDestroy(c->fork);
+    if (c->join) cudaEventDestroy(c->join);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->tex) cudaDestroyTextureObject(c->tex);
     if (c->tex_array) cudaFreeMipmappedArray(c->tex_array);
     for (auto sf : c->surf)
@@ -936,17 +948,25 @@ vct_status frame_volume(vct_ctx* c, const vct_triangles* tris, const vct_light* 
     c->volume_timed = false;
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[0], st));
     VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
-    VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, st));
     AccumParams A;
     if ((s = fill_accum(c, tris, lights, n, shadow, eye, A)) != VCT_OK) return s;
     if (c->params.warp_mode == VCT_WARP_TEXTURE && (s = build_warpmap(c, A, st)) != VCT_OK) return s;
+    // The shadow-map half of injection (the lit mask) needs neither the
+    // voxeliser's output nor its SMs' full attention: it runs on the side
+    // stream, forked after everything the caller enqueued so far (the last
+    // frame's resolve read the mask) and joined before the resolve.
+    VCT_CUDA(cudaEventRecord(c->fork, st));
+    VCT_CUDA(cudaStreamWaitEvent(c->side, c->fork, 0));
+    VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, c->side));
+    InjectParams I;
+    fill_inject(c, shadow, eye, I);
+    launch_inject_mark(I, c->side);
+    VCT_CHECK_LAUNCH("frame: inject mark");
+    VCT_CUDA(cudaEventRecord(c->join, c->side));
     launch_voxelizer(c, A, st);
     VCT_CHECK_LAUNCH("frame: accumulate");
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[1], st));
-    InjectParams I;
-    fill_inject(c, shadow, eye, I);
-    launch_inject_mark(I, st);
-    VCT_CHECK_LAUNCH("frame: inject mark");
+    VCT_CUDA(cudaStreamWaitEvent(st, c->join, 0));
     if (timed) VCT_CUDA(cudaEventRecord(c->ev[2], st));
     const bool hw = filter_uses_texture(c->params.trace_filter);
     const bool pad = filter_uses_bordered(c->params.trace_filter);

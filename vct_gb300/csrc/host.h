@@ -32,6 +32,10 @@ struct vct_ctx {
     bool timers_recorded = false;
     bool volume_timed = false;  // the last volume pass recorded ev[0..3]: a trace after it records ev[4]
     cudaEvent_t ev[5] = {};
+    // vct_frame runs the shadow-map half of injection on `side`, concurrently
+    // with the voxeliser: `fork` / `join` order it against the caller's stream.
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     void* vox_scratch = nullptr;  // voxeliser work-distribution arrays
     long long vox_scratch_bytes = 0;
     float4* pchain = nullptr;  // bordered fp32 radiance chain read by the software sampler
