@@ -144,13 +144,37 @@ def test_perspective_frame_trace(persp_frame):
     assert np.array_equal(stage["irr"].view(np.uint32), fused["irr"].view(np.uint32))
 
 
-def test_batch_refuses_tesselation_and_perspective():
+def test_batch_refuses_tesselation():
     sc = scenes.batch_scene(seed=1, index=0)
     g = GpuScene(sc)
     b = api.Batch([api.config_for(sc)])
-    for over in (dict(voxelize_tesselation=1), dict(warp_mode=L.VCT_WARP_PERSPECTIVE)):
-        b.set_params(api.scene_params(sc, **over), 0)
+    b.set_params(api.scene_params(sc, voxelize_tesselation=1), 0)
+    o = g.new_outputs()
+    with pytest.raises(L.VctError) as e:
+        b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))])
+    assert e.value.status == L.VCT_ERR_UNSUPPORTED
+
+
+def test_batch_with_perspective_warp_equals_single_frames():
+    import torch
+
+    scs = [scenes.batch_scene(seed=7, index=i) for i in range(3)]
+    gs = [GpuScene(sc) for sc in scs]
+    ref = []
+    for sc, g in zip(scs, gs):
+        ctx = api.Context(api.config_for(sc))
+        ctx.set_params(api.scene_params(sc, warp_mode=L.VCT_WARP_PERSPECTIVE))
         o = g.new_outputs()
-        with pytest.raises(L.VctError) as e:
-            b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))])
-        assert e.value.status == L.VCT_ERR_UNSUPPORTED
+        ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
+        torch.cuda.synchronize()
+        ref.append((read_chain(ctx), o[0].cpu().numpy()))
+    b = api.Batch([api.config_for(sc) for sc in scs])
+    for i, sc in enumerate(scs):
+        b.set_params(api.scene_params(sc, warp_mode=L.VCT_WARP_PERSPECTIVE), i)
+    outs = [g.new_outputs() for g in gs]
+    b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
+             for sc, g, o in zip(scs, gs, outs)])
+    torch.cuda.synchronize()
+    for (chain, irr), ctx, o in zip(ref, b.scenes, outs):
+        assert np.array_equal(read_chain(ctx), chain)
+        assert np.array_equal(o[0].cpu().numpy().view(np.uint32), irr.view(np.uint32))

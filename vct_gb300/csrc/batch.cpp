@@ -67,8 +67,8 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
             return fail(VCT_ERR_UNSUPPORTED, "batches use VCT_FILTER_SOFTWARE or the texture-unit samplers");
         if (filter != VCT_FILTER_SOFTWARE && (s = ensure_texture(c)) != VCT_OK) return s;
         const bool hw = filter != VCT_FILTER_SOFTWARE;
-        if (c->params.warp_mode == VCT_WARP_TEXTURE || c->params.warp_mode == VCT_WARP_PERSPECTIVE)
-            return fail(VCT_ERR_UNSUPPORTED, "batches support VCT_WARP_NONE and VCT_WARP_ANALYTIC only");
+        if (c->params.warp_mode == VCT_WARP_TEXTURE)
+            return fail(VCT_ERR_UNSUPPORTED, "batches do not build warp maps: use another VCT_WARP_* mode");
         if (c->params.voxelize_tesselation)
             return fail(VCT_ERR_UNSUPPORTED, "batches use the rasterising voxeliser (voxelize_tesselation = 0)");
         AccumParams A;
