@@ -15,7 +15,7 @@ G-buffer to the device, runs the frame and copies the composite image back.
 
 Reference arm (--impl reference): the reference's path is OpenGL/GLSL, which
 cannot run here (no graphics stack), so its CPU restatement (oracle/, the
-same code that judges parity) is timed on all host threads; each step
+same code that checks parity) is timed on all host threads; each step
 voxelises, normalises, injects and filters the full grid and traces a row
 sample of the frame, extrapolated to the full frame.
 

@@ -1,6 +1,6 @@
 """numpy binding of the CPU oracle (liboracle.so, built from vct_oracle.cpp).
 
-TEST INFRASTRUCTURE ONLY.  The oracle is the correctness judge of the CUDA
+TEST INFRASTRUCTURE ONLY.  The oracle is the correctness reference of the CUDA
 library and the timed CPU baseline.  Only tests/, the smoke check and the
 benchmark's CPU-baseline leg use it; the product never imports it.
 

@@ -6,7 +6,7 @@ packed parameters W1[64][42] b1[64] W2[64][64] b2[64] W3[64][64] b3[64]
 W4[3][64] b4[3]; loss = mean squared error over the n x 3 outputs.
 
 Two evaluations:
-  - float64 throughout (the judge of the gradients' mathematics);
+  - float64 throughout (the reference for the gradients' mathematics);
   - BF16-emulating: weights, inputs, hidden activations, dY and dZ rounded to
     BF16 (round to nearest even) where the kernels round them, products
     summed in float64 (the kernels sum in fp32); this one matches the kernels

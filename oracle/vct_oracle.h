@@ -1,6 +1,6 @@
 /*
  * CPU oracle of the VCT hot path.  TEST INFRASTRUCTURE ONLY: it is the
- * correctness judge of the CUDA library and the timed CPU baseline; nothing
+ * correctness reference of the CUDA library and the timed CPU baseline; nothing
  * in the product links or calls it.
  *
  * It restates, in plain single-threaded C++17, the GLSL of sfreed141/vct:
@@ -144,7 +144,7 @@ void orc_build_mips(int32_t dim, int32_t levels, uint16_t* chain, int32_t nthrea
 
 /* Rows [row0, row1) of the G-buffer are traced; outputs are full-size float4
  * images (rows outside the range untouched).  Any output may be NULL.
- * precision: 32 = the fp32 transcription, 64 = the fp64 judge. */
+ * precision: 32 = the fp32 transcription, 64 = the fp64 reference. */
 void orc_trace(const orc_volume* vol, int32_t levels, const uint16_t* chain,
                const orc_trace_params* tp, const float* gpos, const float* gnrm,
                const float* galb, int32_t width, int32_t height, int32_t row0, int32_t row1,

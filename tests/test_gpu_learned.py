@@ -1,5 +1,5 @@
 """The learned path against the oracle: cheap quarter-resolution features,
-the 16-cone reference trace (FP64 judge), feature rows, the fused learned
+the 16-cone reference trace (against FP64), feature rows, the fused learned
 trace against the network run on those rows, the per-tile fallback, and
 what a trained network gains over the cheap trace without it."""
 
