@@ -921,7 +921,7 @@ def run_reference(args, rank, world):
                    "seed": args.seed, "triangles": sc.ntri, "grid": sc.dim},
         "cpu_baseline": {"value": round(value, 2), "unit": "ms/frame", "cores": nthreads, "kind": "port",
                          "sample": sample, "cpu": cpu_model(),
-                         "why_port": "the reference's own path is OpenGL/GLSL: no graphics stack here or on the GPU box"},
+                         "why_port": "the reference's own path is OpenGL/GLSL, and this machine has no graphics stack"},
         "e2e": {"value": round(value, 2), "unit": "ms/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "stage_ms_last": {k: round(v, 2) for k, v in detail.items()},
     }
