@@ -144,15 +144,44 @@ def test_perspective_frame_trace(persp_frame):
     assert np.array_equal(stage["irr"].view(np.uint32), fused["irr"].view(np.uint32))
 
 
-def test_batch_refuses_tesselation():
-    sc = scenes.batch_scene(seed=1, index=0)
-    g = GpuScene(sc)
-    b = api.Batch([api.config_for(sc)])
-    b.set_params(api.scene_params(sc, voxelize_tesselation=1), 0)
-    o = g.new_outputs()
+@pytest.mark.parametrize("mode", [L.VCT_WARP_NONE, L.VCT_WARP_PERSPECTIVE], ids=["linear", "persp"])
+def test_batch_tesselation_equals_single_frames(mode):
+    import torch
+
+    scs = [scenes.batch_scene(seed=11, index=i) for i in range(3)]
+    gs = [GpuScene(sc) for sc in scs]
+    ref = []
+    for sc, g in zip(scs, gs):
+        ctx = api.Context(api.config_for(sc))
+        ctx.set_params(api.scene_params(sc, voxelize_tesselation=1, warp_mode=mode))
+        o = g.new_outputs()
+        ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
+        torch.cuda.synchronize()
+        ref.append((read_chain(ctx), o[0].cpu().numpy(), ctx.stats()))
+    b = api.Batch([api.config_for(sc) for sc in scs])
+    for i, sc in enumerate(scs):
+        b.set_params(api.scene_params(sc, voxelize_tesselation=1, warp_mode=mode), i)
+    outs = [g.new_outputs() for g in gs]
+    b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
+             for sc, g, o in zip(scs, gs, outs)])
+    torch.cuda.synchronize()
+    for (chain, irr, st), ctx, o in zip(ref, b.scenes, outs):
+        assert np.array_equal(read_chain(ctx), chain)
+        assert np.array_equal(o[0].cpu().numpy().view(np.uint32), irr.view(np.uint32))
+        assert ctx.stats()["total_voxel_fragments"] == st["total_voxel_fragments"] > 0
+
+
+def test_batch_refuses_mixed_voxelisers():
+    scs = [scenes.batch_scene(seed=1, index=i) for i in range(2)]
+    gs = [GpuScene(sc) for sc in scs]
+    b = api.Batch([api.config_for(sc) for sc in scs])
+    b.set_params(api.scene_params(scs[0], voxelize_tesselation=1), 0)
+    b.set_params(api.scene_params(scs[1]), 1)
+    outs = [g.new_outputs() for g in gs]
     with pytest.raises(L.VctError) as e:
-        b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))])
-    assert e.value.status == L.VCT_ERR_UNSUPPORTED
+        b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
+                 for sc, g, o in zip(scs, gs, outs)])
+    assert e.value.status == L.VCT_ERR_INVALID_ARGUMENT
 
 
 def test_batch_with_perspective_warp_equals_single_frames():

@@ -69,8 +69,10 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         const bool hw = filter != VCT_FILTER_SOFTWARE;
         if (c->params.warp_mode == VCT_WARP_TEXTURE)
             return fail(VCT_ERR_UNSUPPORTED, "batches do not build warp maps: use another VCT_WARP_* mode");
-        if (c->params.voxelize_tesselation)
-            return fail(VCT_ERR_UNSUPPORTED, "batches use the rasterising voxeliser (voxelize_tesselation = 0)");
+        if (c->params.voxelize_tesselation != b->ctx[0]->params.voxelize_tesselation)
+            return fail(VCT_ERR_INVALID_ARGUMENT, "all scenes of a batch must use the same voxeliser");
+        if (c->params.voxelize_tesselation && d.triangles.count > (1LL << 24))
+            return fail(VCT_ERR_UNSUPPORTED, "the tessellation voxeliser takes at most 2^24 triangles per scene");
         AccumParams A;
         fill_accum_inputs(c->cfg, c->params, c->mvp, &d.triangles, d.lights, d.n_lights, &d.shadow, A);
         A.warp = warp_dev(c, d.eye);
@@ -128,6 +130,8 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
     brick_off[n] = tot.bricks;
     tile_off[n] = tot.tiles;
     if (tot.tris > 0x7fffffffLL) return fail(VCT_ERR_INVALID_ARGUMENT, "a batch holds at most 2^31-1 triangles");
+    if (b->ctx[0]->params.voxelize_tesselation && tot.tris > (1LL << 24))
+        return fail(VCT_ERR_UNSUPPORTED, "the tessellation voxeliser takes at most 2^24 triangles per batch");
     const long long need = accumulate_scratch_bytes(std::max(tot.tris, 1LL));
     if (need > b->work_bytes) {
         if (!allow_alloc) return fail(VCT_ERR_STATE, "batch work arrays too small for the captured scenes");
@@ -165,9 +169,11 @@ vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cu
                        ilog2(b->tuning.voxel_unit_pixels)};
     if (timed) VCT_CUDA(cudaEventRecord(b->ev[0], st));
     if (tot.tris > 0) {
-        launch_accumulate_batch(
-            SceneBatch<AccumParams>{reinterpret_cast<const AccumParams*>(b->d_blob + b->off_accum), d_tables, n}, W,
-            b->num_sms, b->tuning.voxel_blocks_per_sm, st);
+        const SceneBatch<AccumParams> SB{reinterpret_cast<const AccumParams*>(b->d_blob + b->off_accum), d_tables, n};
+        if (b->ctx[0]->params.voxelize_tesselation)
+            launch_tesselate_batch(SB, W, b->num_sms, st);
+        else
+            launch_accumulate_batch(SB, W, b->num_sms, b->tuning.voxel_blocks_per_sm, st);
         VCT_CHECK_LAUNCH("batch: accumulate");
     }
     if (timed) VCT_CUDA(cudaEventRecord(b->ev[1], st));

@@ -276,6 +276,7 @@ void launch_fill_u32(uint32_t* p, uint32_t v, long long n, cudaStream_t s);
 int accumulate_batch_max_scenes();
 void launch_accumulate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, int num_sms, int blocks_per_sm,
                              cudaStream_t s);
+void launch_tesselate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, int num_sms, cudaStream_t s);
 void launch_inject_mark_batch(const SceneBatch<InjectParams>& B, long long ntexels, cudaStream_t s);
 void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks, cudaStream_t s);
 void launch_mip_tail_batch(const SceneBatch<MipLevels>& B, cudaStream_t s);
