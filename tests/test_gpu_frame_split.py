@@ -43,3 +43,31 @@ def test_split_frame_equals_frame():
         assert torch.equal(a.view(torch.int32), b.cpu().view(torch.int32))
     t = ctx2.timers()
     assert t["render_ms"] > 0 and t["total_ms"] >= t["render_ms"]
+
+
+def test_frame_captured_in_a_cuda_graph():
+    """vct_frame inside a caller's stream capture (its side-stream fork and
+    join are events, which capture records): replays equal direct frames."""
+    import torch
+
+    sc = scenes.cornell(seed=10, gbuffer=(160, 90))
+    g = GpuScene(sc)
+    ctx = api.Context(api.config_for(sc))
+    ctx.set_params(api.scene_params(sc))
+    irr, spec, col, samples = g.new_outputs()
+    out = api.trace_out(irr, spec, col)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, out, s)  # sizes the work arrays before capture
+    s.synchronize()
+    ref = irr.clone()
+    chain_ref = read_chain(ctx)
+    irr.zero_()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, out, s)
+    for _ in range(3):
+        graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(irr.view(torch.int32), ref.view(torch.int32))
+    assert np.array_equal(read_chain(ctx), chain_ref)
