@@ -57,12 +57,14 @@ def test_frame_captured_in_a_cuda_graph():
     irr, spec, col, samples = g.new_outputs()
     out = api.trace_out(irr, spec, col)
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())  # the inputs were rendered on the default stream
     with torch.cuda.stream(s):
         ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, out, s)  # sizes the work arrays before capture
     s.synchronize()
     ref = irr.clone()
     chain_ref = read_chain(ctx)
     irr.zero_()
+    s.wait_stream(torch.cuda.current_stream())
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.graph(graph, stream=s):
         ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, out, s)

@@ -107,6 +107,7 @@ def test_autotune_batch():
     b.capture(descs, stream)
     for o in outs:
         o[0].zero_()
+    stream.wait_stream(torch.cuda.current_stream())  # the zeroing runs on the default stream
     b.replay(stream)
     stream.synchronize()
     for o, r in zip(outs, ref):

@@ -10,13 +10,13 @@
 //     units of 2^unit_log2 pixels (a tuning setting), with a block-local
 //     exclusive scan;
 //  2. voxelize_scan_kernel, one CTA: exclusive scan of the per-block totals;
-//  3. voxelize_raster_kernel, persistent: every warp takes an equal
-//     contiguous range of work units, tests 32 pixel centres at a time for
-//     coverage, compacts covered fragments (clipped to the depth range) with
-//     a ballot into a per-warp queue in shared memory, and whenever 32 are
-//     queued each lane lights one fragment (all enabled lights, 5-tap PCF for
-//     shadow casters) and adds it into the voxel's 32-byte accumulator record
-//     with fire-and-forget 64-bit reductions.
+//  3. voxelize_raster_kernel, persistent: warps take work units from a
+//     shared counter, test 32 pixel centres at a time for coverage, compact
+//     covered fragments (clipped to the depth range) with a ballot into a
+//     per-warp ring queue in shared memory, and whenever 32 are queued each
+//     lane lights one fragment (all enabled lights, 5-tap PCF for shadow
+//     casters) and adds it into the voxel's 32-byte accumulator record with
+//     fire-and-forget 64-bit reductions.
 //
 // Integer sums make the result independent of fragment order: it is
 // bit-exact against the CPU oracle.  Compiled with --fmad=false (see
@@ -246,7 +246,9 @@ __device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQ
     unsigned long long* rec = reinterpret_cast<unsigned long long*>(P.acc + (long long)kAccWords * v);
     const unsigned long long qr = quant16(color.x), qg = quant16(color.y), qb = quant16(color.z);
     const unsigned long long qx = quant16(n01.x), qy = quant16(n01.y), qz = quant16(n01.z);
-    // Fire-and-forget reductions: no result is waited for.
+    // Fire-and-forget reductions: no result is waited for.  (Setting the
+    // occupancy bit only for the fragment that finds the count at 0 waits
+    // for the first add's result and is slower.)
     atomicAdd(rec + 0, 1ull | (qr << 32));
     atomicAdd(rec + 1, qg | (qb << 32));
     atomicAdd(rec + 2, qx | (qy << 32));
@@ -280,20 +282,23 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
     // The queue is a ring of kQueue entries: fragments [head, head + qn).
     int qn = 0, head = 0;  // warp-uniform
 
-    // Shades the 32 oldest queued fragments (or `nact`), one per lane, and
-    // counts them per scene (one shared-memory atomic per distinct scene in
-    // the warp).
+    // Shades the 32 oldest queued fragments (or `nact`), one per lane.
     auto shade32 = [&](int nact) {
         __syncwarp();
         if (lane < nact) {
             const int e = (head + lane) & (kQueue - 1);
-            const int s = (int)(q.pix[e] >> 24);
-            const AccumParams& P = S.get(s);
-            shade_fragment(P, q, e);
-            const unsigned same = __match_any_sync(__activemask(), s);
-            if (lane == __ffs(same) - 1 && !P.occupancy_only) atomicAdd(&frag_count[s], (unsigned)__popc(same));
+            shade_fragment(S.get((int)(q.pix[e] >> 24)), q, e);
         }
         __syncwarp();
+    };
+    // VoxelizeInfo.totalVoxelFragments: covered fragments are counted where
+    // they are queued, for the unit's scene, and added to the CTA's
+    // per-scene counter when the scene changes.
+    int cur_scene = 0;
+    unsigned pending = 0;
+    auto flush_count = [&]() {
+        if (lane == 0 && pending && !S.get(cur_scene).occupancy_only) atomicAdd(&frag_count[cur_scene], pending);
+        pending = 0;
     };
 
     // Warps take kGrabUnits work units at a time from a shared counter until
@@ -339,6 +344,10 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
             }
             long long tl;
             const int scene = S.find(g, tl);
+            if (scene != cur_scene) {
+                flush_count();
+                cur_scene = scene;
+            }
             const uint4* rp = W.tri_rec + 3 * g;
             const uint4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
             const int X[3] = {(int)r0.x, (int)r0.z, (int)r1.x};
@@ -404,6 +413,7 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
                     q.z[slot] = zf;
                 }
                 qn += __popc(m);
+                pending += (unsigned)__popc(m);
                 if (qn >= 32) {
                     shade32(32);
                     head = (head + 32) & (kQueue - 1);
@@ -413,6 +423,7 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
         }
     }
     shade32(qn);
+    flush_count();
     __syncthreads();
     for (int i = threadIdx.x; i < nscenes; i += blockDim.x)
         if (frag_count[i]) atomicAdd(&S.get(i).stats->total_voxel_fragments, frag_count[i]);
