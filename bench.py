@@ -388,6 +388,16 @@ def run_ours(args, rank, world):
                             "reads and the image write. The texel loads (16 bytes per lane, 16 per sample) keep "
                             "the L1 data pipe at l1_data_pipe_frac of its 128 bytes per clock per SM")
 
+    # every stage against the same HBM roofline (stage times from the context's timers; the
+    # voxelise stage includes the inject marking that overlaps it on the side stream)
+    stages = {}
+    for k, b in (("accumulate", alg["accumulate"]), ("resolve+mips", alg["resolve"] + alg["mip_tail"]),
+                 ("trace", alg["trace"])):
+        gbs = b / (kernel_ms[k] * 1e-3) / 1e9
+        stages[k] = {"ms": round(kernel_ms[k], 4), "algorithmic_bytes": int(b), "achieved_gbs": round(gbs, 1),
+                     "frac": round(gbs / peaks["hbm_gbs"], 4), "traffic": NCU_TRAFFIC.get(k) if headline else None}
+    roofline["stages"] = stages
+
     result = {
         "metric": METRIC, "value": round(ms_per_frame, 4), "unit": "ms/frame", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_frame * world, 4),
