@@ -297,51 +297,73 @@ def run_ours(args, rank, world):
     h2d = sum(t.numel() * t.element_size() for t in (h_pos, h_nrm, h_alb, h_sm, h_gpos, h_gnrm, h_galb))
     d2h = h_color.numel() * 4
 
-    # The step through the public API with the copies overlapped: triangles and shadow map go up on the
-    # frame stream, the G-buffer on a copy stream while vct_frame_volume runs, and the trace runs in two
-    # row halves whose images come back as each half finishes.
-    copy_stream = torch.cuda.Stream(device=dev)
-    ev_gb, ev_top = torch.cuda.Event(), torch.cuda.Event()
+    # Steps through the public API with frames in flight, as a renderer streams them: every step
+    # uploads its triangles, shadow map and G-buffer from pinned host memory and reads its image
+    # back, and those copies run on two copy streams beside the frames.  Step k+1's triangles and
+    # shadow map go up once step k's volume pass has consumed them (during step k's trace), its
+    # G-buffer into the other of two device buffers, and step k's image comes back in two row
+    # halves while step k+1's volume pass runs.  The K steps are timed as one region; each step
+    # moves 138 MB in and 33 MB out and touches over 1 GB of HBM (more than L2), so no flush runs
+    # between them.
+    up = torch.cuda.Stream(device=dev)
+    down = torch.cuda.Stream(device=dev)
+    d_gb = [(d_gpos, d_gnrm, d_galb)] + [tuple(torch.empty_like(t) for t in (d_gpos, d_gnrm, d_galb))]
+    d_col = [color, torch.empty_like(color)]
     half = H // 2
     rows = lambda t, r0, r1: t[r0 * W * 4:r1 * W * 4]  # noqa: E731
-    halves = []
-    for r0, r1 in ((0, half), (half, H)):
-        halves.append((api.gbuffer(rows(d_gpos, r0, r1), rows(d_gnrm, r0, r1), rows(d_galb, r0, r1), W, r1 - r0),
-                       api.trace_out(color=rows(color, r0, r1)), rows(color, r0, r1), rows(h_color, r0, r1)))
+    plans = []  # per buffer parity: the two halves' (gbuffer, trace_out, device rows, host rows)
+    for par in range(2):
+        gp, gn, ga = d_gb[par]
+        plans.append([(api.gbuffer(rows(gp, r0, r1), rows(gn, r0, r1), rows(ga, r0, r1), W, r1 - r0),
+                       api.trace_out(color=rows(d_col[par], r0, r1)), rows(d_col[par], r0, r1), rows(h_color, r0, r1))
+                      for r0, r1 in ((0, half), (half, H))])
+    ev_tri, ev_vol = torch.cuda.Event(), torch.cuda.Event()
+    ev_gb = [torch.cuda.Event(), torch.cuda.Event()]
+    ev_top = [torch.cuda.Event(), torch.cuda.Event()]
+    ev_done = [torch.cuda.Event(), torch.cuda.Event()]
+    ev_d2h = [torch.cuda.Event(), torch.cuda.Event()]
 
-    def e2e_step():
-        for d, h in ((d_pos, h_pos), (d_nrm, h_nrm), (d_alb, h_alb), (d_sm, h_sm)):
-            d.copy_(h, non_blocking=True)
-        copy_stream.wait_stream(stream)  # the previous step's trace is done with the G-buffer
-        with torch.cuda.stream(copy_stream):
-            for d, h in ((d_gpos, h_gpos), (d_gnrm, h_gnrm), (d_galb, h_galb)):
+    def e2e_step(k):
+        par = k & 1
+        up.wait_event(ev_vol)  # the previous step's volume pass has read the triangles and shadow map
+        with torch.cuda.stream(up):
+            for d, h in ((d_pos, h_pos), (d_nrm, h_nrm), (d_alb, h_alb), (d_sm, h_sm)):
                 d.copy_(h, non_blocking=True)
-            ev_gb.record(copy_stream)
+            ev_tri.record(up)
+            up.wait_event(ev_done[par])  # the trace of two steps ago is done with this G-buffer
+            for d, h in zip(d_gb[par], (h_gpos, h_gnrm, h_galb)):
+                d.copy_(h, non_blocking=True)
+            ev_gb[par].record(up)
+        stream.wait_event(ev_tri)
         ctx.frame_volume(e_tris, lights, e_shadow, sc.eye, stream)
-        stream.wait_event(ev_gb)
-        (g0, o0, c0, hc0), (g1, o1, c1, hc1) = halves
+        ev_vol.record(stream)
+        stream.wait_event(ev_gb[par])
+        stream.wait_event(ev_d2h[par])  # the image of two steps ago has been read back
+        (g0, o0, c0, hc0), (g1, o1, c1, hc1) = plans[par]
         ctx.trace(g0, sc.eye, o0, stream)
-        ev_top.record(stream)
-        copy_stream.wait_event(ev_top)
-        with torch.cuda.stream(copy_stream):
-            hc0.copy_(c0, non_blocking=True)
+        ev_top[par].record(stream)
         ctx.trace(g1, sc.eye, o1, stream)
-        hc1.copy_(c1, non_blocking=True)
-        stream.wait_stream(copy_stream)
+        ev_done[par].record(stream)
+        down.wait_event(ev_top[par])
+        with torch.cuda.stream(down):
+            hc0.copy_(c0, non_blocking=True)
+            down.wait_event(ev_done[par])
+            hc1.copy_(c1, non_blocking=True)
+            ev_d2h[par].record(down)
 
-    for _ in range(max(3, args.warmup)):
-        e2e_step()
+    for k in range(max(3, args.warmup)):
+        e2e_step(k)
     torch.cuda.synchronize()
     barrier(world)
-    e_starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    e_ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    for i in range(args.steps):
-        flush.fill_(float(i))
-        e_starts[i].record(stream)
-        e2e_step()
-        e_ends[i].record(stream)
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_start.record(stream)
+    for k in range(args.steps):
+        e2e_step(k)
+    stream.wait_stream(up)
+    stream.wait_stream(down)
+    e_end.record(stream)
     torch.cuda.synchronize()
-    e2e_total = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(e_starts, e_ends)), world)
+    e2e_total = max_over_ranks(e_start.elapsed_time(e_end), world)
     e2e_ms = e2e_total / (args.steps * world)
     assert torch.isfinite(h_color).all(), "non-finite output"
     # the split, overlapped path gives the image of one vct_frame, bit for bit
@@ -415,8 +437,10 @@ def run_ours(args, rank, world):
         "wall_s": round(wall_s, 3),
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/frame", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
-                "path": "vct_frame_volume + two half-frame vct_trace calls; G-buffer upload overlapped with the "
-                        "volume pass on a second stream, the first half's image read back during the second half"},
+                "path": "vct_frame_volume + two half-frame vct_trace calls per step, frames in flight: the next "
+                        "step's uploads run during this step's trace (G-buffer double-buffered), this step's image "
+                        "comes back during the next volume pass; K steps timed as one region",
+                "l2": "no flush: steps overlap, each moves 138 MB in and 33 MB out and touches over 1 GB of HBM"},
         "gpu_launches": int(launches),
         "roofline": roofline,
         "clocks": clk.summary(),
