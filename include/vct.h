@@ -562,7 +562,7 @@ vct_status vct_learned_trace(vct_ctx* ctx, vct_mlp* mlp, const vct_gbuffer* gbuf
  *  - cfg->voxel_dim <= VCT_STATIC_MAX_DIM and tris->count <=
  *    VCT_STATIC_MAX_TRIANGLES, otherwise VCT_ERR_INVALID_ARGUMENT.
  *  - color_dev, normal_dev, radiance_dev: dim^3 RGBA16F voxels each
- *    (8 bytes per voxel, x fastest), 16-byte aligned; radiance_dev receives
+ *    (8 bytes per voxel, x fastest), 32-byte aligned; radiance_dev receives
  *    level 0 as transferVoxels.comp seeds it (and is read first when the
  *    temporal filter is on).
  *  - Runs on the current CUDA device, which must be cfg->device (checked;

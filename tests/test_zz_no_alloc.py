@@ -97,3 +97,10 @@ def test_static_scratch_rejects_oversize():
                                  api._stream(None))
     assert rc == L.VCT_ERR_INVALID_ARGUMENT
     assert b"VCT_STATIC_MAX_TRIANGLES" in lib.vct_last_error()
+    # Output volumes must be 32-byte aligned (checked before any device work).
+    vol = torch.zeros(sc.dim ** 3 * 4 + 16, dtype=torch.int16, device="cuda:0")
+    rc = lib.vct_voxelize_static(C.byref(api.config_for(sc)), C.byref(params), C.byref(tris), lights, n,
+                                 C.byref(shadow), vol.data_ptr() + 16, vol.data_ptr(), vol.data_ptr(), None,
+                                 api._stream(None))
+    assert rc == L.VCT_ERR_INVALID_ARGUMENT
+    assert b"32-byte aligned" in lib.vct_last_error()

@@ -81,8 +81,8 @@ extern "C" vct_status vct_voxelize_static(const vct_config* cfg, const vct_param
     if (!color_dev || !normal_dev || !radiance_dev)
         return set_error(VCT_ERR_INVALID_ARGUMENT, "vct_voxelize_static: output volumes must be non-NULL");
     for (const void* p : {(const void*)color_dev, (const void*)normal_dev, (const void*)radiance_dev})
-        if (reinterpret_cast<uintptr_t>(p) % 16 != 0)
-            return set_error(VCT_ERR_INVALID_ARGUMENT, "vct_voxelize_static: output volumes must be 16-byte aligned");
+        if (reinterpret_cast<uintptr_t>(p) % 32 != 0)  // the resolve writes 4 voxels per 32-byte store
+            return set_error(VCT_ERR_INVALID_ARGUMENT, "vct_voxelize_static: output volumes must be 32-byte aligned");
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {

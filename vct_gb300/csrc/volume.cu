@@ -42,10 +42,14 @@ __device__ __forceinline__ void block_stats(StatsDev* stats, uint32_t uniq, uint
     }
 }
 
+// Four consecutive binary16 RGBA voxels (32 bytes, 32-byte aligned: the
+// first voxel's index is a multiple of 4) in one 256-bit store, so that every
+// lane writes a whole sector.  Two 16-byte stores per lane left each warp
+// instruction writing half of 32 sectors.
 __device__ __forceinline__ void store4(uint2* dst, const uint2 v[4]) {
-    uint4* d = reinterpret_cast<uint4*>(dst);
-    d[0] = make_uint4(v[0].x, v[0].y, v[1].x, v[1].y);
-    d[1] = make_uint4(v[2].x, v[2].y, v[3].x, v[3].y);
+    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(dst), "r"(v[0].x), "r"(v[0].y),
+                 "r"(v[1].x), "r"(v[1].y), "r"(v[2].x), "r"(v[2].y), "r"(v[3].x), "r"(v[3].y)
+                 : "memory");
 }
 
 __device__ __forceinline__ bool in_grid(int x, int y, int z, int N) {
@@ -252,11 +256,17 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
             for (int j = 0; j < 4; ++j) {
                 s0[(lz * kBrick + ly) * kBrick + lx + j] = rad[j];
                 if (R.surf[0]) surf3Dwrite(rad[j], R.surf[0], (x + j) * (int)sizeof(uint2), y, z);
-                if (R.pad_levels[0]) R.pad_levels[0][pad_index(x + j, y, z, N)] = unpack_h4(rad[j]);
             }
         }
     }
     if (FUSED) __syncthreads();
+    if (FUSED && R.pad_levels[0]) {
+        // The sampler's bordered copy of level 0 from the brick in shared
+        // memory: each half-warp writes one row of 16 texels (256 bytes).
+        for (int t = threadIdx.x; t < kBrickVox; t += kThreads)
+            R.pad_levels[0][pad_index(bx * kBrick + (t & 15), by * kBrick + ((t >> 4) & 15), bz * kBrick + (t >> 8), N)] =
+                unpack_h4(s0[t]);
+    }
     block_stats(P.stats, uniq, mx, flags);
     if (FUSED) {
         brick_mips(s0, s1, R.mip_levels, R.radiance_levels, R.surf, R.pad_levels, N, bx, by, bz);
