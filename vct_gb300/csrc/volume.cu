@@ -196,9 +196,11 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
         uint4* recp = reinterpret_cast<uint4*>(P.acc + (long long)kAccWords * v0);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            if ((ob >> j) & 1u) {
-                rec[j][0] = __ldcs(recp + 2 * j);
-                rec[j][1] = __ldcs(recp + 2 * j + 1);
+            if ((ob >> j) & 1u) {  // the whole 32-byte record in one streaming load
+                asm volatile("ld.global.cs.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                             : "=r"(rec[j][0].x), "=r"(rec[j][0].y), "=r"(rec[j][0].z), "=r"(rec[j][0].w),
+                               "=r"(rec[j][1].x), "=r"(rec[j][1].y), "=r"(rec[j][1].z), "=r"(rec[j][1].w)
+                             : "l"(recp + 2 * j));
             } else {
                 rec[j][0] = rec[j][1] = make_uint4(0u, 0u, 0u, 0u);
             }
@@ -217,8 +219,9 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
             col[j] = make_uint2(0u, 0u);
             nrm[j] = make_uint2(0u, 0u);
             if ((ob >> j) & 1u) {
-                __stcs(recp + 2 * j, make_uint4(0u, 0u, 0u, 0u));
-                __stcs(recp + 2 * j + 1, make_uint4(0u, 0u, 0u, 0u));
+                // zeroed for the next frame's accumulation, in one streaming store
+                asm volatile("st.global.cs.v8.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1};" ::"l"(recp + 2 * j), "r"(0u)
+                             : "memory");
                 ++uniq;
                 mx = max(mx, c);
                 if (c >= VCT_MAX_EXACT_FRAGMENTS) flags |= VCT_STATS_COUNT_OVERFLOW;
