@@ -33,8 +33,9 @@ __constant__ float kConeDir[6][3] = {{0.f, 1.f, 0.f},
                                      {-0.823639f, 0.5f, 0.267617f}};
 __constant__ float kConeWeight[6] = {0.25f, 0.15f, 0.15f, 0.15f, 0.15f, 0.15f};
 
-// Four resident CTAs per SM (64 registers): the cone march is issue-bound
-// and its texel loads hit L1, so the extra warps hide the load latency.
+// Four resident CTAs per SM (64 registers): the cone march keeps the L1
+// data pipe busy with its 16-byte texel loads (which mostly hit L1) and
+// issues at about 60% of peak, and the extra warps hide the load latency.
 template <int MODE, class Scenes>
 __global__ void __launch_bounds__(256, 4) trace_kernel(const Scenes S) {
     // One CTA per tile of 2^tile_w_log2 x 2^tile_h_log2 = 256 pixels (a
