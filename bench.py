@@ -900,8 +900,8 @@ def run_dynamic(args, rank, world):
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each frame
 # stage, from one ncu capture of the large frame (profiles/kernels_large_frame.md):
 # accumulate = setup + raster, resolve+mips = resolve + tail; only for --config large.
-NCU_TRAFFIC = {"accumulate": 18.9e6 + 501.3e6, "resolve+mips": 1163.2e6 + 0.05e6, "inject_mark": 18.2e6,
-               "trace": 98.1e6}
+NCU_TRAFFIC = {"accumulate": 18.9e6 + 498.1e6, "resolve+mips": 1154.2e6 + 0.05e6, "inject_mark": 18.2e6,
+               "trace": 98.2e6}
 # Issue-side figures of the cone tracer from its ncu capture (the same workload): it is bound by
 # instruction issue and L1 texel traffic, not HBM.
 NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.626, "fma_pipe_frac": 0.522, "l1_hit_rate": 0.942,
