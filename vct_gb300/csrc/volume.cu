@@ -347,7 +347,14 @@ __global__ void __launch_bounds__(kThreads) inject_mark_kernel(const Scenes S, l
         int a = ix + kDilate[k][0], b = iy + kDilate[k][1], c = iz + kDilate[k][2];
         if (!in_grid(a, b, c, N)) continue;
         long long v = ((long long)c * N + b) * N + a;
-        atomicOr(P.lit + (v >> 5), 1u << (v & 31));
+        // Many texels land in one voxel (with a warp map, distant surfaces
+        // compress into few voxels), and their ORs on one word serialise in
+        // L2.  The mask only gains bits during the pass, so a texel that
+        // already sees its bit set skips the atomic; a stale read only costs
+        // a redundant OR.
+        uint32_t* w = P.lit + (v >> 5);
+        const uint32_t bit = 1u << (v & 31);
+        if (!(__ldcg(w) & bit)) atomicOr(w, bit);
     }
 }
 
