@@ -915,7 +915,8 @@ def run_dynamic(args, rank, world):
 NCU_TRAFFIC = {"accumulate": 18.9e6 + 498.1e6, "resolve+mips": 1154.2e6 + 0.05e6, "inject_mark": 18.2e6,
                "trace": 98.2e6}
 # Issue-side figures of the cone tracer from its ncu capture (the same workload): it is bound by
-# instruction issue and L1 texel traffic, not HBM.
+# the L1 data pipe (its 16-byte texel loads) and instruction issue, not HBM.  Both dictionaries
+# come from captures of `bench.py --profile-frames 3`, which runs the default launch shapes.
 NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.626, "fma_pipe_frac": 0.522, "l1_hit_rate": 0.942,
                    "l1_data_pipe_frac": 0.776}
 
