@@ -1,0 +1,69 @@
+"""Host-side pieces of the benchmark's JSON line, without a GPU: the
+throttle-reason and clock summary of the nvidia-smi samples (a run that saw
+hw_slowdown, hw_thermal_slowdown or sw_thermal_slowdown is rejected, so the
+parsing must find them), the algorithmic bytes behind `roofline`, and the
+peak denominators."""
+
+from __future__ import annotations
+
+import os
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+from vct_gb300 import scenes  # noqa: E402
+
+# index, clocks.sm, clocks.max.sm, power.draw, reasons.active, hw_slowdown, hw_thermal_slowdown,
+# sw_thermal_slowdown, sw_power_cap (nvidia-smi --format=csv,noheader,nounits)
+_IDLE = "0, 2070, 2070, 412.3, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active"
+_CAPPED = "0, 1980, 2070, 1390.0, 0x0000000000000004, Not Active, Not Active, Not Active, Active"
+_THERMAL = "0, 1500, 2070, 1200.0, 0x0000000000000040, Not Active, Active, Not Active, Not Active"
+
+
+def _summary(lines):
+    c = bench.ClockSampler(0)
+    c.lines = list(lines)
+    return c.summary()
+
+
+def test_clock_summary_median_and_reasons():
+    s = _summary([_IDLE, _IDLE, _CAPPED])
+    assert s["samples"] == 3 and s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    s = _summary([_IDLE, _THERMAL, _THERMAL])
+    assert s["sm_mhz"] == 1500.0
+    assert s["reasons"] == ["hw_thermal_slowdown"]
+
+
+def test_clock_summary_ignores_malformed_lines():
+    s = _summary(["", "[N/A]", "0, [N/A], 2070, 0, 0x0, Not Active, Not Active, Not Active, Not Active", _IDLE])
+    assert s["samples"] == 1 and s["sm_mhz"] == 2070.0 and s["reasons"] == []
+    assert _summary([])["sm_mhz"] is None
+
+
+def test_algorithmic_bytes_of_the_large_frame():
+    sc = scenes.large(seed=0)
+    # the voxeliser's counters of this scene (seed 0), as the frame reports them
+    stats = {"total_voxel_fragments": 6666268, "unique_voxels": 5181082}
+    a = bench.algorithmic_bytes(sc, stats, None)
+    N, T = 256, 262144
+    nv = N ** 3
+    assert a["accumulate"] == T * 84 + 6666268 * 56
+    assert a["trace"] == 1920 * 1080 * 64
+    assert a["inject_mark"] == 2048 * 2048 * 4 + nv // 8
+    lv = lambda lo, hi: sum((N >> l) ** 3 for l in range(lo, hi))  # noqa: E731
+    assert a["resolve"] == nv // 4 + 5181082 * 64 + nv * 24 + lv(1, 5) * 8 + lv(0, 5) * 16
+    assert a["mip_tail"] == (N >> 4) ** 3 * 8 + lv(5, 9) * 24
+    # 1.06 GB for resolve + tail: 170 MB read (masks, occupied records), 895 MB written
+    assert 1.0e9 < a["resolve"] + a["mip_tail"] < 1.1e9
+
+
+def test_peaks_come_from_the_measured_file():
+    p = bench.load_peaks()
+    if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+        assert p["source"] == "measured" and p["hbm_gbs"] > 1000 and p["bf16_tflops"] > 100
+    else:
+        assert p["source"] == "fallback" and p["hbm_gbs"] == 6800.0
