@@ -195,6 +195,27 @@ def algorithmic_bytes(sc, stats, launches_per_frame):
     }
 
 
+def stage_rooflines(alg: dict, kernel_ms: dict, hbm_gbs: float, traffic: dict, fragments: int,
+                    voxelizer: str) -> dict:
+    """Every frame stage against the same HBM roofline (stage times from the
+    context's timers; the voxelise stage includes the inject marking that
+    overlaps it on the side stream), with the voxeliser's fragment (or point)
+    rate and its rate of record reductions: four 64-bit adds and one occupancy
+    OR per rasterised fragment; four adds per tessellated point, whose
+    occupancy bit is set once per voxel."""
+    stages = {}
+    for k, b in (("accumulate", alg["accumulate"]), ("resolve+mips", alg["resolve"] + alg["mip_tail"]),
+                 ("trace", alg["trace"])):
+        gbs = b / (kernel_ms[k] * 1e-3) / 1e9
+        stages[k] = {"ms": round(kernel_ms[k], 4), "algorithmic_bytes": int(b), "achieved_gbs": round(gbs, 1),
+                     "frac": round(gbs / hbm_gbs, 4), "traffic": traffic.get(k)}
+    t = kernel_ms["accumulate"] * 1e-3
+    per = 4 if voxelizer == "tess" else 5
+    stages["accumulate"]["fragments_per_s"] = round(fragments / t, 1)
+    stages["accumulate"]["reductions_per_s"] = round(per * fragments / t, 1)
+    return stages
+
+
 def run_ours(args, rank, world):
     import ctypes as C
 
@@ -421,15 +442,8 @@ def run_ours(args, rank, world):
                             "reads and the image write. The texel loads (16 bytes per lane, 16 per sample) keep "
                             "the L1 data pipe at l1_data_pipe_frac of its 128 bytes per clock per SM")
 
-    # every stage against the same HBM roofline (stage times from the context's timers; the
-    # voxelise stage includes the inject marking that overlaps it on the side stream)
-    stages = {}
-    for k, b in (("accumulate", alg["accumulate"]), ("resolve+mips", alg["resolve"] + alg["mip_tail"]),
-                 ("trace", alg["trace"])):
-        gbs = b / (kernel_ms[k] * 1e-3) / 1e9
-        stages[k] = {"ms": round(kernel_ms[k], 4), "algorithmic_bytes": int(b), "achieved_gbs": round(gbs, 1),
-                     "frac": round(gbs / peaks["hbm_gbs"], 4), "traffic": NCU_TRAFFIC.get(k) if headline else None}
-    roofline["stages"] = stages
+    roofline["stages"] = stage_rooflines(alg, kernel_ms, peaks["hbm_gbs"], NCU_TRAFFIC if headline else {},
+                                         stats["total_voxel_fragments"], args.voxelizer)
 
     result = {
         "metric": METRIC, "value": round(ms_per_frame, 4), "unit": "ms/frame", "n_gpus": world,

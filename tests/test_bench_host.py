@@ -67,3 +67,18 @@ def test_peaks_come_from_the_measured_file():
         assert p["source"] == "measured" and p["hbm_gbs"] > 1000 and p["bf16_tflops"] > 100
     else:
         assert p["source"] == "fallback" and p["hbm_gbs"] == 6800.0
+
+
+def test_stage_rooflines():
+    alg = {"accumulate": 400e6, "resolve": 1000e6, "mip_tail": 60e6, "trace": 130e6, "inject_mark": 20e6}
+    ms = {"accumulate": 0.4, "resolve+mips": 0.25, "trace": 0.6, "inject_mark": 0.002}
+    s = bench.stage_rooflines(alg, ms, 6800.0, {"trace": 98e6}, 6_000_000, "raster")
+    assert set(s) == {"accumulate", "resolve+mips", "trace"}
+    r = s["resolve+mips"]
+    assert r["algorithmic_bytes"] == 1060000000 and r["achieved_gbs"] == 4240.0
+    assert r["frac"] == round(4240.0 / 6800.0, 4) and r["traffic"] is None
+    assert s["trace"]["traffic"] == 98e6
+    a = s["accumulate"]
+    assert a["fragments_per_s"] == 1.5e10 and a["reductions_per_s"] == 7.5e10
+    t = bench.stage_rooflines(alg, ms, 6800.0, {}, 6_000_000, "tess")["accumulate"]
+    assert t["reductions_per_s"] == 6.0e10
