@@ -2,7 +2,7 @@
 resources/*.obj with tinyobjloader, src/Graphics/Mesh.cpp:41-190): faces of
 every index form, fan triangulation of polygons, negative indices, zero
 normals where the file has none, objects; and the reference's own meshes
-where the reference tree is present."""
+when VCT_REFERENCE_RESOURCES names the reference's resources/ folder."""
 
 from __future__ import annotations
 
@@ -13,7 +13,7 @@ import pytest
 
 from vct_gb300 import scenes
 
-REF_RESOURCES = "/root/reference/resources"
+REF_RESOURCES = os.environ.get("VCT_REFERENCE_RESOURCES", "")
 
 
 def test_faces_of_every_index_form():

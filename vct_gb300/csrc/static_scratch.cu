@@ -39,7 +39,10 @@ std::mutex g_mutex;
 void* g_scratch_addr[kMaxDevices] = {};
 
 // Device address of g_static_scratch on the current device `dev`, looked up
-// on the first call made on that device.
+// on the first call made on that device (with lazy module loading, that
+// lookup is also when the driver loads this file's module and allocates the
+// array).  The cached address is not invalidated: it does not survive a
+// cudaDeviceReset of that device.
 vct_status scratch_address(int dev, char** out) {
     if (dev < 0 || dev >= kMaxDevices) return set_error(VCT_ERR_UNSUPPORTED, "device ordinal too large");
     std::lock_guard<std::mutex> lock(g_mutex);
@@ -91,9 +94,19 @@ extern "C" vct_status vct_voxelize_static(const vct_config* cfg, const vct_param
     }
     if (dev != cfg->device)
         return set_error(VCT_ERR_INVALID_ARGUMENT, "vct_voxelize_static: cfg->device must be the current device");
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (stats) {  // the counters' read-back synchronises the stream, which a capture forbids
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(VCT_ERR_CUDA, "vct_voxelize_static: cudaStreamIsCapturing failed");
+        }
+        if (cs != cudaStreamCaptureStatusNone)
+            return set_error(VCT_ERR_INVALID_ARGUMENT,
+                             "vct_voxelize_static: stats must be NULL while the stream is being captured");
+    }
     char* base = nullptr;
     if ((s = scratch_address(dev, &base)) != VCT_OK) return s;
-    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const long long nv = (long long)cfg->voxel_dim * cfg->voxel_dim * cfg->voxel_dim;
     uint32_t* acc = reinterpret_cast<uint32_t*>(base);
     uint32_t* occ = reinterpret_cast<uint32_t*>(base + kRecordBytes);
