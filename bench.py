@@ -1,10 +1,13 @@
 """Benchmark: ms per voxel-cone-tracing frame (voxelize + inject + mip +
 trace) on the large plain frame: 262,144 triangles, 256^3 RGBA16F grid with
 9 levels, 2048^2 shadow map, 1920x1080 G-buffer, 6 diffuse cones (60 deg) +
-1 specular cone (10 deg).
+1 specular cone (10 deg); the cone sampler is the hybrid one (the level of
+each trilinear-mip sample with the larger weight in exact fp32, the other
+by the texture units), within 1e-3 of the fp64 cone-trace oracle.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--config large|cornell] [--filter software|hardware]
+                  [--config large|cornell|batch|learned|dynamic]
+                  [--filter software|hybrid|levels|hardware]
 
 Our arm: inputs (triangles, shadow map, G-buffer) are resident in HBM; every
 timed step is one vct_frame call through the C ABI, timed with CUDA events on
@@ -13,11 +16,18 @@ the 129 MB L2.  `e2e` repeats the measurement through the same C ABI with the
 inputs in pinned host memory: each step copies the triangles, shadow map and
 G-buffer to the device, runs the frame and copies the composite image back.
 
+Outside the timed regions the default line also carries: the other cone
+sampler's frame time (`samplers`); the oracle's single-threaded frame with
+the whole frame traced (`cpu_baseline`); the frame's irradiance per sampler
+against the fp64 and fp32 cone-trace oracle over every covered pixel, and
+the radiance chain against the oracle's bit for bit (`accuracy`); and compact
+runs of the batched family (`batch`) and of the learned path (`learned`).
+
 Reference arm (--impl reference): the reference's path is OpenGL/GLSL, which
 cannot run here (no graphics stack), so its CPU restatement (oracle/, the
 same code that checks parity) is timed on all host threads; each step
-voxelises, normalises, injects and filters the full grid and traces a row
-sample of the frame, extrapolated to the full frame.
+voxelises, normalises, injects and filters the full grid and traces the
+whole frame.
 
 With --gpus N (launched by torchrun) every rank runs an independent replica
 (the path does not shard a single frame); `value` is the job's effective
@@ -55,12 +65,14 @@ def parse():
                     help="large plain frame (default), the small Cornell box, or the batched family: "
                          "--batch-scenes seeded scenes in one captured graph")
     ap.add_argument("--batch-scenes", type=int, default=32)
-    ap.add_argument("--learned-scenes", type=int, default=8, help="learned: held-out scenes timed")
+    ap.add_argument("--learned-scenes", type=int, default=None,
+                    help="learned: held-out scenes timed (8; 2 in the default line's learned block)")
     ap.add_argument("--frames", type=int, default=120, help="dynamic: frames of the actor animation")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
-    ap.add_argument("--filter", default="software", choices=["software", "hybrid", "levels", "hardware"],
-                    help="cone sampler: fp32 trilinear (exact), exact finer level + texture-unit coarser level, "
-                         "texture units per level + fp32 level blend, or texture units' trilinear-mip")
+    ap.add_argument("--filter", default="hybrid", choices=["software", "hybrid", "levels", "hardware"],
+                    help="cone sampler: fp32 trilinear (exact); the heavier-weighted level of each sample exact and "
+                         "the other by the texture units (the default: within 1e-3 of the fp64 trace); texture "
+                         "units per level + fp32 level blend; or texture units' trilinear-mip")
     ap.add_argument("--voxelizer", default="raster", choices=["raster", "tess"],
                     help="rasterising voxeliser (voxelize.geom/.frag, the benchmark frame's) or the "
                          "tessellation voxeliser (testTesselation.tesc/.tese)")
@@ -68,7 +80,10 @@ def parse():
                     help="perspective: the voxelizeTesselationWarp froxel grid over the camera frustum")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-rows", type=int, default=24, help="rows of the frame traced by the CPU baseline")
+    ap.add_argument("--no-extra-configs", action="store_true",
+                    help="large: skip the compact batched and learned blocks after the frame's line")
+    ap.add_argument("--cpu-sample-rows", type=int, default=0,
+                    help="rows of the frame the CPU oracle traces (0: every row; the batched family: 24)")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only run this many frames (no timing, no JSON): the command profiled with ncu")
     return ap.parse_args()
@@ -176,12 +191,13 @@ def algorithmic_bytes(sc, stats, launches_per_frame):
     W, H = sc.gbuffer_size
     P = W * H
     SW, SH = sc.shadow_size
-    F = stats["total_voxel_fragments"]
     U = stats["unique_voxels"]
+    C = stats.get("covered_pixels", P)
     lv = lambda a, b: sum((N >> l) ** 3 for l in range(a, min(b, sc.levels)))  # noqa: E731
     return {
-        # triangles in (positions, normals, albedo); 7 accumulator words read-modify-written per fragment
-        "accumulate": T * (36 + 36 + 12) + F * 7 * 4 * 2,
+        # triangles in (positions, normals, albedo); the 32-byte record of every occupied voxel read and
+        # written once (fragments of one voxel meet in L2); the occupancy mask written once
+        "accumulate": T * (36 + 36 + 12) + U * 32 * 2 + nv // 8,
         # shadow map read, lit bit set per texel (bit mask written once)
         "inject_mark": SW * SH * 4 + nv // 8,
         # occupancy and lit masks read; records of occupied voxels read and zeroed; colour, normal,
@@ -190,8 +206,9 @@ def algorithmic_bytes(sc, stats, launches_per_frame):
         "resolve": nv // 8 * 2 + U * 32 * 2 + nv * 8 * 3 + lv(1, 5) * 8 + lv(0, 5) * 16,
         # level 4 read, levels 5.. written (RGBA16F and the bordered fp32 copy)
         "mip_tail": (N >> 4) ** 3 * 8 + lv(5, 99) * (8 + 16),
-        # G-buffer (3 float4) read, composite float4 written
-        "trace": P * (48 + 16),
+        # G-buffer positions read for every pixel, normals and albedo only for covered ones (gp.w != 0),
+        # composite float4 written for every pixel
+        "trace": P * (16 + 16) + C * 32,
     }
 
 
@@ -216,12 +233,29 @@ def stage_rooflines(alg: dict, kernel_ms: dict, hbm_gbs: float, traffic: dict, f
     return stages
 
 
-def run_ours(args, rank, world):
-    import ctypes as C
+SAMPLER_NAMES = ("software", "hybrid", "levels", "hardware")
 
+
+def sampler_id(name: str) -> int:
+    from vct_gb300 import _lib as L
+
+    return {"software": L.VCT_FILTER_SOFTWARE, "hybrid": L.VCT_FILTER_HYBRID, "levels": L.VCT_FILTER_HARDWARE_LEVELS,
+            "hardware": L.VCT_FILTER_HARDWARE}[name]
+
+
+def frame_config(args, sc, world: int) -> dict:
+    """The workload of a single-frame line, with the same keys in both arms."""
+    headline = args.config == "large" and args.voxelizer == "raster" and args.warp == "none"
+    return {"workload": WORKLOAD if headline else f"{args.config} scene, {args.voxelizer} voxeliser, {args.warp} warp",
+            "scene": args.config, "voxelizer": args.voxelizer, "warp": args.warp, "seed": args.seed,
+            "triangles": sc.ntri, "grid": sc.dim, "levels": sc.levels, "shadow_map": list(sc.shadow_size),
+            "gbuffer": list(sc.gbuffer_size), "cones": "6x60deg + 1x10deg", "parallelism": f"replicas x{world}",
+            "l2": "256 MiB buffer written between timed frames (outside the events)"}
+
+
+def run_ours(args, rank, world):
     import torch
 
-    import oracle as O
     from vct_gb300 import _lib as L
     from vct_gb300 import api
 
@@ -241,6 +275,7 @@ def run_ours(args, rank, world):
     gpos, gnrm, galb = (torch.empty(W * H * 4, dtype=torch.float32, device=dev) for _ in range(3))
     api.render_gbuffer(tris, sc, keys, gpos, gnrm, galb)
     del keys
+    covered = int((gpos.view(-1, 4)[:, 3] != 0).sum())
     color = torch.empty(W * H * 4, dtype=torch.float32, device=dev)
     lights = api.light_array(sc.lights)
     shadow = api.shadow_desc(sc, sm)
@@ -248,8 +283,7 @@ def run_ours(args, rank, world):
     out = api.trace_out(color=color)
     ctx = api.Context(api.config_for(sc, device=local))
     params = api.scene_params(sc)
-    params.trace_filter = {"software": L.VCT_FILTER_SOFTWARE, "hybrid": L.VCT_FILTER_HYBRID, "levels": L.VCT_FILTER_HARDWARE_LEVELS,
-                           "hardware": L.VCT_FILTER_HARDWARE}[args.filter]
+    params.trace_filter = sampler_id(args.filter)
     params.voxelize_tesselation = int(args.voxelizer == "tess")
     params.warp_mode = L.VCT_WARP_PERSPECTIVE if args.warp == "perspective" else L.VCT_WARP_NONE
     ctx.set_params(params)
@@ -265,7 +299,7 @@ def run_ours(args, rank, world):
             frame()
         torch.cuda.synchronize()
         ctx.close()
-        return None, sc
+        return None, sc, None
 
     for _ in range(max(3, args.warmup)):
         frame()
@@ -282,23 +316,21 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
     tuning = api.tuning_dict(ctx.tuning())
     stats = ctx.stats()
+    stats["covered_pixels"] = covered
     # samples per frame (counted once, outside the timed region)
     samples = torch.zeros(1, dtype=torch.int64, device=dev)
     ctx.frame(tris, lights, shadow, sc.eye, gb, api.trace_out(color=color, samples=samples), stream)
     torch.cuda.synchronize()
     n_samples = int(samples.item())
 
-    # ---- timed region: K frames, per-frame events, L2 flushed between frames
-    ctx.enable_timers(True)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    stage = {k: 0.0 for k in ("voxelize_ms", "radiance_ms", "mipmap_ms", "render_ms", "total_ms")}
-    barrier(world)
-    torch.cuda.synchronize()
-    launches0 = lib.vct_launch_count()
-    t_wall = time.perf_counter()
-    with ClockSampler(local) as clk:
-        for i in range(args.steps):
+    def timed_frames(steps, clk_sampler=None):
+        """`steps` frames, each between CUDA events on the launching stream,
+        the L2 flushed before each (outside the events); per-stage timers."""
+        ctx.enable_timers(True)
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        stage = {k: 0.0 for k in ("voxelize_ms", "radiance_ms", "mipmap_ms", "render_ms", "total_ms")}
+        for i in range(steps):
             flush.fill_(float(i))
             starts[i].record(stream)
             frame()
@@ -306,15 +338,22 @@ def run_ours(args, rank, world):
             for k, v in ctx.timers().items():  # waits for this frame's end event
                 stage[k] += v
         torch.cuda.synchronize()
+        ctx.enable_timers(False)
+        return [s.elapsed_time(e) for s, e in zip(starts, ends)], {k: v / steps for k, v in stage.items()}
+
+    # ---- timed region: K frames, per-frame events, L2 flushed between frames
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = lib.vct_launch_count()
+    t_wall = time.perf_counter()
+    with ClockSampler(local) as clk:
+        frame_ms, stage = timed_frames(args.steps)
     barrier(world)
     wall_s = time.perf_counter() - t_wall
     launches = lib.vct_launch_count() - launches0
-    ctx.enable_timers(False)
-    frame_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = sum(frame_ms)
     total_ms_max = max_over_ranks(total_ms, world)
     ms_per_frame = total_ms_max / (args.steps * world)
-    stage = {k: v / args.steps for k, v in stage.items()}
 
     # ---- e2e through the C ABI with host buffers (pinned), copies timed
     h_pos, h_nrm, h_alb = (t.cpu().pin_memory() for t in (pos, nrm, alb))
@@ -325,7 +364,6 @@ def run_ours(args, rank, world):
     d_gpos, d_gnrm, d_galb = (torch.empty_like(t, device=dev) for t in (h_gpos, h_gnrm, h_galb))
     e_tris = api.triangles(d_pos, d_nrm, d_alb)
     e_shadow = api.shadow_desc(sc, d_sm)
-    e_gb = api.gbuffer(d_gpos, d_gnrm, d_galb, W, H)
     h2d = sum(t.numel() * t.element_size() for t in (h_pos, h_nrm, h_alb, h_sm, h_gpos, h_gnrm, h_galb))
     d2h = h_color.numel() * 4
 
@@ -403,13 +441,39 @@ def run_ours(args, rank, world):
     ctx.frame(tris, lights, shadow, sc.eye, gb, api.trace_out(color=check), stream)
     torch.cuda.synchronize()
     assert torch.equal(check.cpu().view(torch.int32), h_color.view(torch.int32)), "e2e image differs from vct_frame"
+    del d_gb, d_col, plans, check
+
+    # ---- outside the timed regions: the other samplers' frame times (same launch shapes), and
+    # this frame's irradiance per sampler and radiance chain for the oracle's checks on rank 0
+    others = [n for n in ("software", "hybrid") if n != args.filter]
+    samplers = {args.filter: {"frame_ms": round(statistics.median(frame_ms), 4),
+                              "trace_ms": round(stage["render_ms"], 4), "resolve_mips_ms": round(stage["mipmap_ms"], 4)}}
+    irr_dev = torch.empty(W * H * 4, dtype=torch.float32, device=dev)
+    art = {"irr": {}} if rank == 0 else None
+    for name in [args.filter] + others:
+        params.trace_filter = sampler_id(name)
+        ctx.set_params(params)
+        if name != args.filter:
+            for _ in range(3):
+                frame()
+            fm, st = timed_frames(args.steps)
+            samplers[name] = {"frame_ms": round(statistics.median(fm), 4), "trace_ms": round(st["render_ms"], 4),
+                              "resolve_mips_ms": round(st["mipmap_ms"], 4)}
+        if art is not None:
+            ctx.frame(tris, lights, shadow, sc.eye, gb, api.trace_out(irradiance=irr_dev, color=color), stream)
+            torch.cuda.synchronize()
+            art["irr"][name] = irr_dev.cpu().numpy()
+    params.trace_filter = sampler_id(args.filter)
+    ctx.set_params(params)
+    if art is not None:
+        art["chain"] = np.concatenate([ctx.read_volume(L.VCT_VOLUME_RADIANCE, lv).cpu().numpy().view(np.uint16)
+                                       for lv in range(sc.levels)])
+        art["sm"] = sm.cpu().numpy()
+        art["gbuf"] = tuple(t.cpu().numpy() for t in (gpos, gnrm, galb))
+        art["stats"] = dict(stats)
 
     # ---- roofline of the dominant kernel
     alg = algorithmic_bytes(sc, stats, None)
-    if args.voxelizer == "tess":
-        # triangles read once; the record of every occupied voxel read and written once (points that
-        # land in one voxel are summed before they reach memory)
-        alg["accumulate"] = sc.ntri * (36 + 36 + 12) + stats["unique_voxels"] * 32 * 2
     kernel_ms = {"accumulate": stage["voxelize_ms"], "inject_mark": stage["radiance_ms"],
                  "resolve+mips": stage["mipmap_ms"], "trace": stage["render_ms"]}
     dom = max(kernel_ms, key=kernel_ms.get)
@@ -419,12 +483,12 @@ def run_ours(args, rank, world):
     else:
         bytes_dom = alg[dom]
     achieved = bytes_dom / (kernel_ms[dom] * 1e-3) / 1e9
-    headline = args.config == "large" and args.voxelizer == "raster" and args.warp == "none"
-    traffic = NCU_TRAFFIC.get(dom) if headline else None
+    headline = args.config == "large" and args.voxelizer == "raster" and args.warp == "none" and \
+        args.filter == NCU_CAPTURE_SAMPLER
+    traffic, traffic_note = ncu_traffic(headline)
     roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
-                "traffic_source": "ncu dram read+write per launch, one capture of this workload",
-                "peak_source": peaks["source"], "algorithmic_bytes": int(bytes_dom),
+                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic.get(dom),
+                **traffic_note, "peak_source": peaks["source"], "algorithmic_bytes": int(bytes_dom),
                 "kernel_ms": round(kernel_ms[dom], 4)}
     if dom == "accumulate" and args.voxelizer == "tess":
         roofline["points_per_s"] = round(stats["total_voxel_fragments"] / (kernel_ms[dom] * 1e-3), 1)
@@ -436,31 +500,28 @@ def run_ours(args, rank, world):
         peak_rate = ctx.sampler_rate(params.trace_filter, 1 << 31, stream)
         roofline["sampler_peak_samples_per_s"] = round(peak_rate, 1)
         roofline["sampler_frac"] = round(n_samples / (kernel_ms[dom] * 1e-3) / peak_rate, 4)
-        if headline:
+        if traffic:
             roofline["issue"] = dict(NCU_TRACE_ISSUE, source="ncu capture of this workload")
         roofline["note"] = ("cone tracing is gather-bound, not HBM-bound: its HBM fraction counts only G-buffer "
-                            "reads and the image write. The texel loads (16 bytes per lane, 16 per sample) keep "
-                            "the L1 data pipe at l1_data_pipe_frac of its 128 bytes per clock per SM")
+                            "reads and the image write; its ceiling is the sampler's own peak rate "
+                            "(sampler_peak_samples_per_s, vct_sampler_rate)")
 
-    roofline["stages"] = stage_rooflines(alg, kernel_ms, peaks["hbm_gbs"], NCU_TRAFFIC if headline else {},
+    roofline["stages"] = stage_rooflines(alg, kernel_ms, peaks["hbm_gbs"], traffic,
                                          stats["total_voxel_fragments"], args.voxelizer)
 
+    config = frame_config(args, sc, world)
     result = {
         "metric": METRIC, "value": round(ms_per_frame, 4), "unit": "ms/frame", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_frame * world, 4),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32 math, f16 volumes, u32 accumulators",
         "data": "synthetic seeded scene (no dataset); inputs resident in HBM",
-        "config": {"workload": WORKLOAD if headline else f"{args.config} scene, {args.voxelizer} voxeliser, "
-                                                             f"{args.warp} warp",
-                   "scene": args.config, "voxelizer": args.voxelizer, "warp": args.warp,
-                   "seed": args.seed, "triangles": sc.ntri, "grid": sc.dim, "levels": sc.levels,
-                   "shadow_map": list(sc.shadow_size), "gbuffer": list(sc.gbuffer_size), "cones": "6x60deg + 1x10deg",
-                   "sampler": args.filter, "parallelism": f"replicas x{world}",
-                   "l2": "256 MiB buffer written between timed frames (outside the events)",
-                   "tuning": tuning, "autotuned": not args.no_autotune, "autotune_s": round(tune_s, 2)},
+        "config": config,
+        "sampler": args.filter,
+        "tuning": tuning, "autotuned": not args.no_autotune, "autotune_s": round(tune_s, 2),
         "stage_ms": {k: round(v, 4) for k, v in stage.items()},
         "frame_ms_min": round(min(frame_ms), 4), "frame_ms_median": round(statistics.median(frame_ms), 4),
         "wall_s": round(wall_s, 3),
+        "samplers": samplers,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/frame", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "path": "vct_frame_volume + two half-frame vct_trace calls per step, frames in flight: the next "
@@ -474,19 +535,21 @@ def run_ours(args, rank, world):
         "samples_per_frame": n_samples,
     }
     ctx.close()
-    return result, sc
+    return result, sc, art
 
 
 # ------------------------------------------------------------- batched
 BATCH_METRIC = "ms per batch of 32 scenes voxelize+inject+mip+trace (one captured graph)"
 
 
-def run_batch(args, rank, world):
+def run_batch(args, rank, world, compact=False):
     """Batched family: --batch-scenes seeded scenes (triangles log-uniform in
     1k-200k, grids from {64,128,256}^3, G-buffers 320x180..1920x1080, 1-4
     lights) run as one vct_batch frame per step, replayed from a captured
     CUDA graph, with the launch shapes picked by the library's autotuner.
-    Compared with the same scenes run as sequential vct_frame calls."""
+    Compared with the same scenes run as sequential vct_frame calls.  With
+    `compact`, only the graph replays and the sequential frames are timed
+    and a short summary is returned."""
     import torch
 
     from vct_gb300 import _lib as L
@@ -579,6 +642,18 @@ def run_batch(args, rank, world):
     for ctx in b.scenes:
         ctx.set_tuning(tuning)
     seq_tuned_ms = timed(sequential, args.steps)
+    if compact:
+        b.close()
+        return {"workload": f"{args.batch_scenes} seeded scenes of the batched family (seed {args.seed}): "
+                            f"{sum(sc.ntri for sc in scs)} tris, grids {{64,128,256}}^3, "
+                            f"{sum(sc.gbuffer_size[0] * sc.gbuffer_size[1] for sc in scs)} pixels",
+                "graph_replay_ms": round(value, 4), "sequential_ms": round(statistics.median(seq_default_ms), 4),
+                "sequential_tuned_ms": round(statistics.median(seq_tuned_ms), 4),
+                "speedup_vs_sequential": round(statistics.median(seq_default_ms) / value, 3),
+                "scenes_per_s": round(args.batch_scenes * 1e3 / value, 1), "launches_per_replay":
+                    int(launches // max(1, args.steps)), "stage_ms": {k: round(v, 4) for k, v in stage.items()},
+                "tuning": api.tuning_dict(tuning), "steps": args.steps,
+                "l2": "256 MiB buffer written between timed steps (outside the events)"}, scs
 
     # e2e with batches in flight: every step copies all scenes' inputs from pinned host memory,
     # replays a captured batch graph and copies the images back.  Two batch objects (each with its
@@ -710,16 +785,33 @@ def run_batch(args, rank, world):
 
 # ------------------------------------------------------------- learned
 LEARNED_METRIC = "ms per 1080p irradiance image: learned 2-cone+MLP vs plain 16-cone trace at matched RMSE"
-LEARNED_THRESHOLDS = (0.02, 0.03, 0.04, 0.06, 0.1, float("inf"))
+# per-tile bounds (relative error of the network at 4 probe pixels of a 16x16 tile) and per-pixel bounds
+# (the network's error estimate over the frame's RMS irradiance)
+LEARNED_TILE_THRESHOLDS = (0.02, 0.03, 0.04, 0.06, 0.1)
+LEARNED_PIXEL_THRESHOLDS = (0.015, 0.02, 0.03, 0.05, 0.1, 0.2, 0.5)
 
 
-def run_learned(args, rank, world):
+def pareto_front(points: list[dict]) -> list[dict]:
+    """The operating points no other point beats on both time and error,
+    fastest first."""
+    front = []
+    for p in sorted(points, key=lambda r: (r["ms"], r["rel_l2"])):
+        if not front or p["rel_l2"] < front[-1]["rel_l2"]:
+            front.append(p)
+    return front
+
+
+def run_learned(args, rank, world, compact=False):
     """Learned configuration on held-out scenes of the large frame's family
     (256^3, 1920x1080): the plain 16-cone irradiance trace against the
     learned trace (cheap quarter-resolution features + the trained network
-    on every pixel + per-tile probes and 16-cone fallback), for a sweep of
-    per-tile error bounds; the headline is the learned time at the largest
-    bound whose mean relative L2 error stays <= 2% ("matched RMSE")."""
+    on every pixel) with no fallback, with the per-tile fallback (16-cone
+    probes at 4 pixels per 16x16 tile, the tiles above a bound re-traced) and
+    with the per-pixel fallback (the pixels whose error estimate, the
+    network's fourth output, exceeds a bound re-traced), over a sweep of
+    bounds.  The headline is the fastest operating point whose mean relative
+    L2 error stays <= 2% ("matched RMSE"); the Pareto front of time against
+    error is reported beside it."""
     import torch
 
     from vct_gb300 import _lib as L
@@ -729,6 +821,8 @@ def run_learned(args, rank, world):
     torch.cuda.set_device(local)
     params = learned.load_params()
     if params is None:
+        if compact:
+            return {"unavailable": "no trained weights of this network in vct_gb300/weights"}
         raise SystemExit("no trained weights: run python -m vct_gb300.learned train first")
     W, H, dim = 1920, 1080, 256
     kw = dict(dim=dim, shadow=2048, gbuffer=(W, H))
@@ -738,7 +832,8 @@ def run_learned(args, rank, world):
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=state.dev)
     lib = L.load()
-    seeds = [10_000_000 + 1000 * rank + i for i in range(args.learned_scenes)]
+    n_scenes = args.learned_scenes or (2 if compact else 8)
+    seeds = [10_000_000 + 1000 * rank + i for i in range(n_scenes)]
     reps = max(1, args.steps)
 
     def timed(fn):
@@ -755,8 +850,21 @@ def run_learned(args, rank, world):
             ts.append(a.elapsed_time(b))
         return statistics.median(ts)
 
-    plain_ms, feat_ms, err, t_ms, fb = [], [], {t: [] for t in LEARNED_THRESHOLDS}, {t: [] for t in LEARNED_THRESHOLDS}, \
-        {t: [] for t in LEARNED_THRESHOLDS}
+    modes = [("network", None)] + [("tile", t) for t in LEARNED_TILE_THRESHOLDS] + \
+        [("pixel", t) for t in LEARNED_PIXEL_THRESHOLDS]
+
+    def run(mode, t, want=False):
+        if mode == "network":
+            api.learned_trace(state.ctx, mlp, state.gb, state.sc.eye, state.out, float("inf"))
+            return 0.0
+        if mode == "tile":
+            st = api.learned_trace(state.ctx, mlp, state.gb, state.sc.eye, state.out, t, want_stats=want)
+            return st["fallback_tiles"] / st["tiles"] if want else None
+        n = api.learned_trace_pixels(state.ctx, mlp, state.gb, state.sc.eye, state.out, t, want_count=want)
+        return n / ncov if want else None
+
+    plain_ms, feat_ms = [], []
+    rec = {m: {"ms": [], "err": [], "fb": []} for m in modes}
     launches0 = lib.vct_launch_count()
     with ClockSampler(local) as clk:
         for seed in seeds:
@@ -765,48 +873,61 @@ def run_learned(args, rank, world):
             plain_ms.append(timed(lambda: state.reference()))
             truth = state.ref.view(-1, 4)[:, :3].clone()
             mask = state.covered()
+            ncov = max(1, int(mask.sum()))
             feat_ms.append(timed(lambda: state.features()))
-            for t in LEARNED_THRESHOLDS:
-                t_ms[t].append(timed(lambda: api.learned_trace(state.ctx, mlp, state.gb, sc.eye, state.out, t)))
-                st = api.learned_trace(state.ctx, mlp, state.gb, sc.eye, state.out, t, want_stats=True)
-                err[t].append(learned.rel_l2(state.out.view(-1, 4)[:, :3], truth, mask))
-                fb[t].append(st["fallback_tiles"] / st["tiles"])
+            for m in modes:
+                rec[m]["ms"].append(timed(lambda: run(*m)))
+                rec[m]["fb"].append(run(*m, want=True))
+                rec[m]["err"].append(learned.rel_l2(state.out.view(-1, 4)[:, :3], truth, mask))
     launches = lib.vct_launch_count() - launches0
     mean = lambda v: float(np.mean(v))  # noqa: E731
-    sweep = [{"threshold": (t if t != float("inf") else None), "ms": round(mean(t_ms[t]), 4),
-              "rel_l2": round(mean(err[t]), 5), "rel_l2_max": round(float(np.max(err[t])), 5),
-              "fallback_fraction": round(mean(fb[t]), 4)} for t in LEARNED_THRESHOLDS]
-    ok = [r for r in sweep if r["rel_l2"] <= 0.02]
-    matched = max(ok, key=lambda r: r["threshold"] or 0.0) if ok else sweep[0]
+    sweep = [{"mode": m[0], "threshold": m[1], "ms": round(mean(rec[m]["ms"]), 4),
+              "rel_l2": round(mean(rec[m]["err"]), 5), "rel_l2_max": round(float(np.max(rec[m]["err"])), 5),
+              "fallback_fraction": round(mean(rec[m]["fb"]), 4),
+              "fallback_of": {"network": "-", "tile": "tiles", "pixel": "covered pixels"}[m[0]]} for m in modes]
     plain = mean(plain_ms)
-    # e2e: G-buffer planes from pinned host memory, learned trace, irradiance back
+    for r in sweep:
+        r["speedup_vs_plain16"] = round(plain / r["ms"], 3)
+    ok = [r for r in sweep if r["rel_l2"] <= 0.02]
+    matched = min(ok, key=lambda r: r["ms"]) if ok else None
+    net_only = sweep[0]
+    front = [{k: r[k] for k in ("mode", "threshold", "ms", "rel_l2", "speedup_vs_plain16")} for r in pareto_front(sweep)]
+    summary = {"plain16_ms": round(plain, 4), "network_only_ms": net_only["ms"],
+               "network_only_rel_l2": net_only["rel_l2"], "features_ms": round(mean(feat_ms), 4),
+               "matched": ({k: matched[k] for k in ("mode", "threshold", "ms", "rel_l2", "fallback_fraction",
+                                                     "speedup_vs_plain16")} if matched else None),
+               "bar": "mean rel-L2 <= 0.02 against the 16-cone trace, fastest point meeting it",
+               "target": "learned >= 3x faster than plain 16-cone at <= 2% (not met: see pareto)",
+               "pareto": front}
+    if compact:
+        return dict({"workload": f"{len(seeds)} held-out scenes of the large frame's family, 256^3, {W}x{H}",
+                     "steps": reps}, **summary)
+    # e2e: G-buffer planes from pinned host memory, learned trace at the matched point, irradiance back
     h = [t.cpu().pin_memory() for t in (state.gpos, state.gnrm, state.galb)]
     h_out = torch.empty_like(state.out, device="cpu").pin_memory()
-    thr = matched["threshold"] if matched["threshold"] is not None else float("inf")
+    head = matched or net_only
 
     def e2e():
         for d, src in zip((state.gpos, state.gnrm, state.galb), h):
             d.copy_(src, non_blocking=True)
-        api.learned_trace(state.ctx, mlp, state.gb, state.sc.eye, state.out, thr)
+        run(head["mode"], head["threshold"])
         h_out.copy_(state.out, non_blocking=True)
 
     e2e_ms = timed(e2e)
-    net_ms = mean(t_ms[float("inf")]) - mean(feat_ms)
+    net_ms = net_only["ms"] - mean(feat_ms)
     flops = 2.0 * (48 * 64 + 64 * 64 * 2 + 64 * 16) * W * H  # tensor-core work of the network (padded shapes)
     peaks = load_peaks()
     tflops = flops / (net_ms * 1e-3) / 1e12 if net_ms > 0 else None
-    return {
-        "metric": LEARNED_METRIC, "value": round(matched["ms"], 4), "unit": "ms/frame", "n_gpus": world,
-        "steps": reps, "warmup": max(3, args.warmup), "ms_per_step": round(matched["ms"], 4),
+    return dict({
+        "metric": LEARNED_METRIC, "value": round(head["ms"], 4), "unit": "ms/frame", "n_gpus": world,
+        "steps": reps, "warmup": max(3, args.warmup), "ms_per_step": round(head["ms"], 4),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16 network (fp32 accumulate), f32 cone math, f16 volumes",
         "data": "synthetic seeded held-out scenes of the large frame's family (no dataset)",
-        "config": {"workload": "learned: 256^3, 1920x1080, quarter-res 2x90deg cones + MLP 42-64-64-64-3 vs 16 cones",
+        "config": {"workload": "learned: 256^3, 1920x1080, quarter-res 2x90deg cones + MLP 42-64-64-64-4 vs 16 cones",
                    "scenes": len(seeds), "l2": "256 MiB buffer written between timed runs (outside the events)",
                    "weights": "vct_gb300/weights/learned_mlp.f32 (trained by python -m vct_gb300.learned train)"},
-        "plain16_ms": round(plain, 4), "speedup_vs_plain16": round(plain / matched["ms"], 3),
-        "matched_threshold": matched["threshold"], "matched_rel_l2": matched["rel_l2"], "sweep": sweep,
-        "features_ms": round(mean(feat_ms), 4), "network_ms": round(net_ms, 4),
+        "sweep": sweep,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/frame", "h2d_bytes_per_step": int(sum(t.numel() * 4 for t in h)),
                 "d2h_bytes_per_step": int(h_out.numel() * 4)},
         "gpu_launches": int(launches),
@@ -816,7 +937,7 @@ def run_learned(args, rank, world):
                      "traffic": None, "peak_source": peaks["source"], "flops_per_frame": flops,
                      "kernel_ms": round(net_ms, 4), "note": "network time = learned (no fallback) - features"},
         "clocks": clk.summary(),
-    }
+    }, **summary)
 
 
 # ------------------------------------------------------------- dynamic
@@ -831,7 +952,8 @@ def run_dynamic(args, rank, world):
     temporal radiance filter, and traces 8 viewpoints at 1280x720 with the
     plain 6+1 cones and with the learned form (network only).  Timed per
     frame with CUDA events: actor transform + vct_frame of viewpoint 0 +
-    vct_trace of viewpoints 1-7 (plain); the 8 learned traces (learned).
+    viewpoints 1-7 in one vct_trace_views launch (plain); the 8 learned
+    traces (learned).
     The shadow map and the 8 G-buffers of each frame are set-up passes,
     rendered outside the timed regions."""
     import torch
@@ -857,6 +979,7 @@ def run_dynamic(args, rank, world):
         g = [torch.empty(W * H * 4, dtype=torch.float32, device=dev) for _ in range(3)]
         gbs.append((g, api.gbuffer(g[0], g[1], g[2], W, H)))
     color = torch.empty(W * H * 4, dtype=torch.float32, device=dev)
+    view_colors = [torch.empty(W * H * 4, dtype=torch.float32, device=dev) for _ in views[1:]]
     irr = torch.empty(W * H * 4, dtype=torch.float32, device=dev)
     ctx = api.Context(api.config_for(sc, device=local))
     params = api.scene_params(sc, temporal_filter=1, temporal_decay=0.8, warp_mode=L.VCT_WARP_TEXTURE)
@@ -887,8 +1010,8 @@ def run_dynamic(args, rank, world):
             ev[0].record(stream)
             api.transform_actors(local_tris, models, pos, nrm, stream)
             ctx.frame(tris, lights, shadow, views[0].eye, gbs[0][1], api.trace_out(color=color), stream)
-            for v, (_, gb) in zip(views[1:], gbs[1:]):
-                ctx.trace(gb, v.eye, api.trace_out(color=color), stream)
+            ctx.trace_views([gb for _, gb in gbs[1:]], [v.eye for v in views[1:]],
+                            [api.trace_out(color=c) for c in view_colors], stream)
             ev[1].record(stream)
             for v, (_, gb) in zip(views, gbs):
                 api.learned_trace(ctx, mlp, gb, v.eye, irr, float("inf"), stream=stream)
@@ -912,8 +1035,8 @@ def run_dynamic(args, rank, world):
         "config": {"workload": "dynamic warped frames: 64 rigid actors (2k-8k tris) + 199k static tris = "
                                f"{sc.ntri} tris, 256^3 + 32^3 warp map + temporal filter, 8 views 1280x720",
                    "frames": n_frames, "actors": len(actors.first), "triangles": sc.ntri,
-                   "timed": "actor transform + vct_frame (view 0) + vct_trace (views 1-7); shadow map and "
-                            "G-buffers rendered outside the events"},
+                   "timed": "actor transform + vct_frame (view 0) + one vct_trace_views launch (views 1-7); shadow "
+                            "map and G-buffers rendered outside the events"},
         "plain_ms_median": round(med(plain), 4), "learned_traces_ms_median": round(med(learned_ms), 4),
         "stage_ms_median_view0": {k: round(med(v), 4) for k, v in stages.items()},
         "fragments_per_frame_median": int(statistics.median(frags)),
@@ -924,13 +1047,15 @@ def run_dynamic(args, rank, world):
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each frame
-# stage, from one ncu capture of the large frame (profiles/kernels_large_frame.md):
-# accumulate = setup + raster, resolve+mips = resolve + tail; only for --config large.
+# stage, from one ncu capture of the large frame (`bench.py --profile-frames 3`, default
+# launch shapes): accumulate = setup + raster, resolve+mips = resolve + tail; only for the
+# default workload, and only while the frame kernels' sources hash to NCU_CAPTURE_DIGEST.
+NCU_CAPTURE_DIGEST = ""
+NCU_CAPTURE_SAMPLER = "hybrid"
 NCU_TRAFFIC = {"accumulate": 18.9e6 + 498.1e6, "resolve+mips": 1154.2e6 + 0.05e6, "inject_mark": 18.2e6,
                "trace": 98.2e6}
-# Issue-side figures of the cone tracer from its ncu capture (the same workload): it is bound by
-# the L1 data pipe (its 16-byte texel loads) and instruction issue, not HBM.  Both dictionaries
-# come from captures of `bench.py --profile-frames 3`, which runs the default launch shapes.
+# Issue-side figures of the cone tracer from the same capture: it is bound by the L1 data pipe
+# (its 16-byte texel loads) and instruction issue, not HBM.
 NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.626, "fma_pipe_frac": 0.522, "l1_hit_rate": 0.942,
                    "l1_data_pipe_frac": 0.776}
 
@@ -944,17 +1069,19 @@ def load_peaks() -> dict:
 
 
 # ----------------------------------------------------------- CPU side
-def cpu_frame_ms(sc, nthreads: int, sample_rows: int, shadowmap=None, gbuf=None, tesselation=False,
-                 warp_mode=0) -> tuple[float, dict]:
-    """One CPU-oracle frame: full voxelize/normalize/inject/mips, trace of
-    `sample_rows` evenly spaced rows, extrapolated to the full frame."""
+def cpu_frame(sc, nthreads: int, sample_rows: int = 0, shadowmap=None, gbuf=None, tesselation=False,
+              warp_mode=0, want=("color",)) -> tuple[float, dict, np.ndarray, tuple]:
+    """One CPU-oracle frame: voxelize/normalize/inject/mips of the full grid
+    and the trace of the whole frame (sample_rows = 0) or of `sample_rows`
+    evenly spaced rows, extrapolated to the full frame.  Returns the frame's
+    ms, per-stage ms, the radiance chain and the trace's outputs (irradiance,
+    specular, colour, samples)."""
     import oracle as O
 
     W, H = sc.gbuffer_size
     sm = O.render_shadowmap(sc, nthreads) if shadowmap is None else shadowmap
     gp, gn, ga = O.render_gbuffer(sc) if gbuf is None else gbuf
     w = O.warp(sc, warp_mode) if warp_mode else None
-    t = {}
     t0 = time.perf_counter()
     if tesselation:
         count, sums, total = O.voxelize_tess(sc, nthreads=nthreads, warp=w)
@@ -968,25 +1095,136 @@ def cpu_frame_ms(sc, nthreads: int, sample_rows: int, shadowmap=None, gbuf=None,
     t3 = time.perf_counter()
     O.build_mips(sc.dim, sc.levels, chain, nthreads)
     t4 = time.perf_counter()
-    step = max(1, H // max(1, sample_rows))
-    O.trace(sc, chain, gp, gn, ga, precision=32, rows=(0, H), row_step=step, nthreads=nthreads, want=("color",),
-            warp=w)
+    step = max(1, H // sample_rows) if sample_rows > 0 else 1
+    traced = O.trace(sc, chain, gp, gn, ga, precision=32, rows=(0, H), row_step=step, nthreads=nthreads, want=want,
+                     warp=w)
     t5 = time.perf_counter()
     rows_traced = len(range(0, H, step))
     t = {"voxelize_ms": (t1 - t0) * 1e3, "normalize_ms": (t2 - t1) * 1e3, "inject_ms": (t3 - t2) * 1e3,
-         "mips_ms": (t4 - t3) * 1e3, "trace_ms_full_frame": (t5 - t4) * 1e3 * H / rows_traced,
-         "rows_traced": rows_traced}
-    return (t4 - t0) * 1e3 + t["trace_ms_full_frame"], t
+         "mips_ms": (t4 - t3) * 1e3, "trace_ms": (t5 - t4) * 1e3 * H / rows_traced, "rows_traced": rows_traced}
+    return (t4 - t0) * 1e3 + t["trace_ms"], t, chain, traced
 
 
-def cpu_model() -> str:
-    try:
-        for line in open("/proc/cpuinfo"):
-            if line.lower().startswith(("model name", "cpu part")):
-                return line.split(":", 1)[1].strip()
-    except OSError:
-        pass
+def cpu_sample_text(detail: dict, H: int, nthreads: int) -> str:
+    what = "the whole frame traced" if detail["rows_traced"] == H else (
+        f"trace of {detail['rows_traced']} evenly spaced rows of {H}, scaled to the full frame")
+    return f"one frame: full voxelize/normalize/inject/mips + {what}, {nthreads} thread(s)"
+
+
+def accuracy_block(sc, art: dict, chain32: np.ndarray, irr32: np.ndarray, headline: str, nthreads: int,
+                   warp_mode: int = 0) -> dict:
+    """The frame's irradiance per sampler against the fp64 cone-trace oracle
+    (the 1e-3 bar) and the fp32 oracle, over every covered pixel of the
+    frame; and whether the GPU radiance chain equals the oracle's, bit for
+    bit.  Inputs: the GPU's shadow map and G-buffer (bit-exact against the
+    oracle's own) and the oracle's chain."""
+    import oracle as O
+
+    gp, gn, ga = art["gbuf"]
+    w = O.warp(sc, warp_mode) if warp_mode else None
+    t0 = time.perf_counter()
+    irr64, _, _, _ = O.trace(sc, chain32, gp, gn, ga, precision=64, nthreads=nthreads, want=("irr",), warp=w)
+    fp64_s = time.perf_counter() - t0
+    cov = gp.reshape(-1, 4)[:, 3] != 0
+    out = {"judge": "fp64 cone-trace oracle (exact trilinear) over every covered pixel of the frame",
+           "bar": "irradiance rel-L2 <= 1e-3 vs fp64", "chain_bitexact": bool(np.array_equal(art["chain"], chain32)),
+           "oracle_fp32_vs_fp64_rel_l2": irradiance_accuracy(irr32, irr64, cov)["rel_l2"],
+           "fp64_trace_s": round(fp64_s, 2), "threads": nthreads, "samplers": {}}
+    for name, g in art["irr"].items():
+        a64 = irradiance_accuracy(g, irr64, cov)
+        a32 = irradiance_accuracy(g, irr32, cov)
+        out["samplers"][name] = {"vs_fp64": {k: (round(v, 9) if isinstance(v, float) else v) for k, v in a64.items()},
+                                 "vs_fp32_oracle_rel_l2": a32["rel_l2"], "vs_fp32_oracle_max_rel": a32["max_rel"]}
+    h = out["samplers"].get(headline)
+    if h is not None:
+        out["headline_sampler"] = headline
+        out["headline_rel_l2_vs_fp64"] = h["vs_fp64"]["rel_l2"]
+        out["meets_bar"] = bool(h["vs_fp64"]["rel_l2"] <= 1e-3)
+    return out
+
+
+# Arm Ltd. (implementer 0x41) part numbers of server cores, as /proc/cpuinfo prints them
+ARM_PARTS = {"0xd0c": "Neoverse-N1", "0xd40": "Neoverse-V1", "0xd49": "Neoverse-N2", "0xd4f": "Neoverse-V2",
+             "0xd8e": "Neoverse-N3", "0xd84": "Neoverse-V3"}
+
+
+def cpu_model(cpuinfo: str | None = None) -> str:
+    """The host CPU's model name: x86 /proc/cpuinfo's "model name", or an
+    Arm core's part number mapped to its name (Grace is Neoverse-V2)."""
+    if cpuinfo is None:
+        try:
+            cpuinfo = open("/proc/cpuinfo").read()
+        except OSError:
+            cpuinfo = ""
+    part = impl = None
+    for line in cpuinfo.splitlines():
+        key, _, val = line.partition(":")
+        key, val = key.strip().lower(), val.strip()
+        if key == "model name" and val:
+            return val
+        if key == "cpu part" and part is None:
+            part = val.lower()
+        if key == "cpu implementer" and impl is None:
+            impl = val.lower()
+    if part is not None:
+        name = ARM_PARTS.get(part) if impl in (None, "0x41") else None
+        return f"{name} (Arm part {part})" if name else f"Arm part {part}, implementer {impl}"
     return platform.processor() or platform.machine()
+
+
+def irradiance_accuracy(gpu: np.ndarray, ref: np.ndarray, covered: np.ndarray, floor_frac: float = 1e-3) -> dict:
+    """Error of a GPU irradiance image against an oracle image (RGBA float
+    arrays of the frame; alpha ignored) over the covered pixels: the relative
+    L2 error over all covered pixels' RGB, and the per-pixel relative error
+    |g - r| / |r| (Euclidean over RGB) of the pixels whose reference
+    irradiance exceeds floor_frac times its root mean square (darker pixels'
+    relative errors divide by almost nothing): maximum, 99.9th and 99th
+    percentiles, and the fraction within 1e-3."""
+    g = np.asarray(gpu, dtype=np.float64).reshape(-1, 4)[covered, :3]
+    r = np.asarray(ref, dtype=np.float64).reshape(-1, 4)[covered, :3]
+    d = np.linalg.norm(g - r, axis=1)
+    n = np.linalg.norm(r, axis=1)
+    tot = float(np.sqrt(np.sum(n * n)))
+    out = {"rel_l2": float(np.sqrt(np.sum(d * d)) / tot) if tot > 0 else float(np.sqrt(np.sum(d * d))),
+           "pixels": int(g.shape[0])}
+    floor = floor_frac * float(np.sqrt(np.mean(n * n))) if n.size else 0.0
+    sel = n > floor
+    e = d[sel] / n[sel]
+    out.update({"pixels_judged": int(sel.sum()), "judged_floor": floor,
+                "max_rel": float(e.max()) if e.size else 0.0,
+                "p999_rel": float(np.quantile(e, 0.999)) if e.size else 0.0,
+                "p99_rel": float(np.quantile(e, 0.99)) if e.size else 0.0,
+                "frac_within_1e-3": float(np.mean(e <= 1e-3)) if e.size else 1.0})
+    return out
+
+
+KERNEL_SOURCES = ("cone.cuh", "vct_device.cuh", "warp.cuh", "voxelize.cu", "volume.cu", "trace.cu")
+
+
+def kernel_sources_digest() -> str:
+    """sha256 (first 16 hex digits) of the frame kernels' sources: the ncu
+    traffic figures below hold only for the sources they were captured from."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, "vct_gb300", "csrc", name), "rb") as f:
+            h.update(name.encode() + b"\0" + f.read())
+    return h.hexdigest()[:16]
+
+
+def ncu_traffic(headline: bool) -> tuple[dict, dict]:
+    """The ncu DRAM traffic per frame stage (and the tracer's issue figures)
+    when this workload's kernels are the ones they were captured from; else
+    empty, with the reason."""
+    if not headline:
+        return {}, {"traffic_source": "no ncu capture of this workload"}
+    digest = kernel_sources_digest()
+    if digest != NCU_CAPTURE_DIGEST:
+        return {}, {"traffic_stale": f"the frame kernels' sources (digest {digest}) changed since the ncu capture "
+                                     f"(digest {NCU_CAPTURE_DIGEST}): traffic withheld"}
+    return dict(NCU_TRAFFIC), {"traffic_source": "ncu dram read+write per launch, one capture of this workload",
+                               "traffic_digest": digest}
 
 
 def run_reference_batch(args, world):
@@ -996,15 +1234,16 @@ def run_reference_batch(args, world):
     from vct_gb300 import scenes
 
     nthreads = os.cpu_count() or 1
+    rows = args.cpu_sample_rows or 24
     scs = [scenes.batch_scene(seed=args.seed, index=i) for i in range(args.batch_scenes)]
     times = []
     for i in range(args.warmup + args.steps):
-        ms = sum(cpu_frame_ms(sc, nthreads, args.cpu_sample_rows)[0] for sc in scs)
+        ms = sum(cpu_frame(sc, nthreads, rows)[0] for sc in scs)
         if i >= args.warmup:
             times.append(ms)
     value = sum(times) / len(times)
     sample = (f"each step: all {len(scs)} scenes, full voxelize/normalize/inject/mips + trace of "
-              f"{args.cpu_sample_rows} evenly spaced rows per scene scaled to the full frame")
+              f"{rows} evenly spaced rows per scene scaled to the full frame")
     return {
         "impl": "reference", "metric": BATCH_METRIC.replace("32", str(args.batch_scenes)), "value": round(value, 2),
         "unit": "ms/batch", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -1018,6 +1257,9 @@ def run_reference_batch(args, world):
 
 
 def run_reference(args, rank, world):
+    """The reference's path on the host cores: its GLSL cannot run here (no
+    graphics stack), so the oracle, which restates it, runs every stage of the
+    same workload on all host threads, the whole frame traced every step."""
     if args.config == "batch":
         return run_reference_batch(args, world)
     sc = make_scene(args)
@@ -1026,23 +1268,23 @@ def run_reference(args, rank, world):
 
     sm = O.render_shadowmap(sc, nthreads)
     gbuf = O.render_gbuffer(sc)
+    tess, warp_mode = args.voxelizer == "tess", 3 if args.warp == "perspective" else 0
     times = []
     for i in range(args.warmup + args.steps):
-        ms, detail = cpu_frame_ms(sc, nthreads, args.cpu_sample_rows, sm, gbuf)
+        ms, detail, _, _ = cpu_frame(sc, nthreads, args.cpu_sample_rows, sm, gbuf, tesselation=tess,
+                                     warp_mode=warp_mode)
         if i >= args.warmup:
             times.append(ms)
     value = sum(times) / len(times)
-    sample = (f"each step: full voxelize/normalize/inject/mips of the workload + trace of {detail['rows_traced']} "
-              f"evenly spaced rows of {sc.gbuffer_size[1]}, trace time scaled to the full frame")
+    H = sc.gbuffer_size[1]
     return {
         "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": "ms/frame", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 2), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 math, f16 volumes, u32 accumulators",
         "data": "synthetic seeded scene (no dataset)",
-        "config": {"workload": WORKLOAD if args.config == "large" else f"{args.config} scene", "scene": args.config,
-                   "seed": args.seed, "triangles": sc.ntri, "grid": sc.dim},
+        "config": dict(frame_config(args, sc, world), l2="not applicable: host cores"),
         "cpu_baseline": {"value": round(value, 2), "unit": "ms/frame", "cores": nthreads, "kind": "port",
-                         "sample": sample, "cpu": cpu_model(),
+                         "sample": "each step " + cpu_sample_text(detail, H, nthreads), "cpu": cpu_model(),
                          "why_port": "the reference's own path is OpenGL/GLSL, and this machine has no graphics stack"},
         "e2e": {"value": round(value, 2), "unit": "ms/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "stage_ms_last": {k: round(v, 2) for k, v in detail.items()},
@@ -1072,7 +1314,7 @@ def main():
             # one single-threaded oracle frame of the smallest scene of the batch, row-sampled trace,
             # scaled by the batch's voxel + pixel work relative to that scene
             small = min(scs, key=lambda s: s.dim ** 3 + s.gbuffer_size[0] * s.gbuffer_size[1])
-            ms, detail = cpu_frame_ms(small, 1, args.cpu_sample_rows)
+            ms, detail, _, _ = cpu_frame(small, 1, args.cpu_sample_rows or 24)
             result["cpu_baseline"] = {"value": round(ms, 2), "unit": "ms/frame of the smallest scene", "cores": 1,
                                       "kind": "port", "sample": f"scene {small.name}: {small.ntri} tris, "
                                       f"{small.dim}^3, {small.gbuffer_size[0]}x{small.gbuffer_size[1]}, trace of "
@@ -1080,19 +1322,32 @@ def main():
         if rank == 0:
             print(json.dumps(result), flush=True)
         return
-    result, sc = run_ours(args, rank, world)
+    result, sc, art = run_ours(args, rank, world)
     if result is None:  # --profile-frames
         return
     if rank == 0 and not args.no_cpu_baseline:
-        # the tessellation voxeliser's hundreds of millions of points take minutes on one core: all cores
+        # the oracle on the GPU's own shadow map and G-buffer (both bit-exact against the oracle's): the
+        # single-threaded baseline frame, whole frame traced (the tessellation voxeliser's hundreds of
+        # millions of points take minutes on one core: all cores there)
         cores = 1 if args.voxelizer == "raster" else (os.cpu_count() or 1)
-        ms, detail = cpu_frame_ms(sc, cores, args.cpu_sample_rows, tesselation=args.voxelizer == "tess",
-                                  warp_mode=3 if args.warp == "perspective" else 0)
+        warp_mode = 3 if args.warp == "perspective" else 0
+        ms, detail, chain32, (irr32, _, _, _) = cpu_frame(
+            sc, cores, args.cpu_sample_rows, art["sm"], art["gbuf"], tesselation=args.voxelizer == "tess",
+            warp_mode=warp_mode, want=("irr", "color"))
         result["cpu_baseline"] = {"value": round(ms, 2), "unit": "ms/frame", "cores": cores, "kind": "port",
-                                  "sample": f"one frame: full voxelize/normalize/inject/mips + trace of "
-                                            f"{detail['rows_traced']} evenly spaced rows scaled to the full frame, "
-                                            f"{cores} thread(s)", "cpu": cpu_model(), "nproc": os.cpu_count(),
-                                  "stage_ms": {k: round(v, 1) for k, v in detail.items()}}
+                                  "sample": cpu_sample_text(detail, sc.gbuffer_size[1], cores), "cpu": cpu_model(),
+                                  "nproc": os.cpu_count(), "stage_ms": {k: round(v, 1) for k, v in detail.items()}}
+        if detail["rows_traced"] == sc.gbuffer_size[1]:
+            result["accuracy"] = accuracy_block(sc, art, chain32, irr32, args.filter, os.cpu_count() or 1,
+                                                warp_mode)
+    if rank == 0 and args.config == "large" and not args.no_extra_configs:
+        # the benchmark's other configurations, compact and outside the timed region (rank 0 alone)
+        import torch
+
+        torch.cuda.empty_cache()
+        result["batch"], _ = run_batch(args, 0, 1, compact=True)
+        torch.cuda.empty_cache()
+        result["learned"] = run_learned(args, 0, 1, compact=True)
     if rank == 0:
         print(json.dumps(result), flush=True)
     if world > 1:

@@ -110,8 +110,8 @@ typedef struct vct_cone_settings {
 #define VCT_FILTER_SOFTWARE 0 /* fp32 trilinear (exact GL semantics) from a bordered fp32 copy of the chain */
 #define VCT_FILTER_HARDWARE 1 /* texture units' trilinear-mip filtering */
 #define VCT_FILTER_HARDWARE_LEVELS 2 /* texture units' trilinear filtering per level, levels blended in fp32 */
-#define VCT_FILTER_HYBRID 3 /* the finer level of each trilinear-mip sample in exact fp32 (as SOFTWARE), the
-                               coarser one by the texture units, blended in fp32 */
+#define VCT_FILTER_HYBRID 3 /* of the two levels of each trilinear-mip sample, the one with the larger weight in
+                               exact fp32 (as SOFTWARE), the other by the texture units, blended in fp32 */
 
 /* Voxel warping: positions in [0,1]^3 volume coordinates are remapped before
  * they index or sample the grid, in the voxeliser (voxelize.frag:100-106),
@@ -240,7 +240,12 @@ typedef struct vct_stats {
     uint32_t error_flags; /* VCT_STATS_* */
 } vct_stats;
 
-#define VCT_STATS_COUNT_OVERFLOW 1u /* some voxel exceeded VCT_MAX_EXACT_FRAGMENTS */
+/* Some voxel's colour and normal sums are not exact: the rasterising
+ * voxeliser put VCT_MAX_EXACT_FRAGMENTS or more fragments into it (its
+ * packed 32-bit sums carry), or the tessellation voxeliser, whose sums stay
+ * exact past that bound, found no free slot in its table of voxels whose
+ * sums passed 2^32 (65,536 slots). */
+#define VCT_STATS_COUNT_OVERFLOW 1u
 #define VCT_MAX_EXACT_FRAGMENTS 65537u
 
 /* Device time of the last vct_frame's stages, the reference's GLBufferedTimer
@@ -321,6 +326,12 @@ vct_status vct_build_mips(vct_ctx* ctx, int32_t volume, void* stream);
 /* phong.frag indirect term: six diffuse cones + one specular cone per pixel. */
 vct_status vct_trace(vct_ctx* ctx, const vct_gbuffer* gbuffer, const float eye[3],
                      const vct_trace_out* out, void* stream);
+/* No counterpart in the reference, which draws one camera per frame.  The
+ * phong.frag trace of n viewpoints of the same volumes (gbuffers[i], eye
+ * eyes[3*i..3*i+2], outputs outs[i]) in one launch per 8 viewpoints:
+ * equal, bit for bit, to n vct_trace calls. */
+vct_status vct_trace_views(vct_ctx* ctx, int32_t n, const vct_gbuffer* gbuffers, const float* eyes,
+                           const vct_trace_out* outs, void* stream);
 /* All four stages; normalisation, injection and the first mip levels are
  * fused.  Results equal vct_voxelize + vct_inject + vct_build_mips +
  * vct_trace on the same inputs. */
@@ -473,17 +484,22 @@ vct_status vct_batch_autotune(vct_batch* batch, const vct_scene_desc* scenes, in
 vct_status vct_tensor_core_check(const uint16_t* a_dev, const uint16_t* b_dev, int32_t k, int32_t n,
                                  int32_t variant, float* d_dev, void* stream);
 
-/* The network: 42 inputs, three hidden layers of 64 with ReLU, 3 linear
- * outputs (irradiance RGB); BF16 weights and activations, FP32 accumulation
- * on the tensor cores, FP32 master parameters and Adam state.  Parameters
- * are packed fp32: W1[64][42] b1[64] W2[64][64] b2[64] W3[64][64] b3[64]
- * W4[3][64] b4[3] (W[out][in]).  Training minimises the mean squared error
- * over the n x 3 outputs.  Feature rows: n x 42 fp32, row-major, 8-byte
- * aligned. */
+/* The network: 42 inputs, three hidden layers of 64 with ReLU, 4 linear
+ * outputs: irradiance RGB and the network's estimate of its own error there
+ * (|irradiance - target|, Euclidean over RGB); BF16 weights and activations,
+ * FP32 accumulation on the tensor cores, FP32 master parameters and Adam
+ * state.  Parameters are packed fp32: W1[64][42] b1[64] W2[64][64] b2[64]
+ * W3[64][64] b3[64] W4[4][64] b4[4] (W[out][in]).  Training minimises the
+ * mean squared error over the n x 3 irradiance outputs plus
+ * VCT_MLP_CONFIDENCE_WEIGHT times the mean over the n rows of
+ * (estimate - |irradiance - target|)^2, the second term's |irradiance -
+ * target| held constant.  Feature rows: n x 42 fp32, row-major, 8-byte
+ * aligned; targets: n x 3 fp32. */
 #define VCT_MLP_INPUTS 42
 #define VCT_MLP_HIDDEN 64
-#define VCT_MLP_OUTPUTS 3
-#define VCT_MLP_PARAMS 11267
+#define VCT_MLP_OUTPUTS 4
+#define VCT_MLP_PARAMS 11332
+#define VCT_MLP_CONFIDENCE_WEIGHT 0.5f
 typedef struct vct_mlp vct_mlp;
 typedef struct vct_adam {
     float lr, beta1, beta2, eps;
@@ -497,7 +513,7 @@ vct_status vct_mlp_destroy(vct_mlp* mlp);
  * training or inference launch gave up waiting for the tensor core. */
 vct_status vct_mlp_set_params(vct_mlp* mlp, const float* params, int64_t count);
 vct_status vct_mlp_get_params(vct_mlp* mlp, float* params, int64_t count, void* stream);
-/* out_dev (n x 3) = network(rows_dev). */
+/* out_dev (n x 4, 16-byte aligned) = network(rows_dev). */
 vct_status vct_mlp_forward(vct_mlp* mlp, const float* rows_dev, int64_t n, float* out_dev, void* stream);
 /* grad_dev (VCT_MLP_PARAMS fp32) = d loss / d params and loss_dev (1 fp32,
  * may be NULL) for rows_dev and targets_dev (n x 3); parameters unchanged.
@@ -548,6 +564,16 @@ typedef struct vct_learned_stats {
  * NULL) synchronises `stream`. */
 vct_status vct_learned_trace(vct_ctx* ctx, vct_mlp* mlp, const vct_gbuffer* gbuffer, const float eye[3],
                              float threshold, float* irradiance_dev, vct_learned_stats* stats, void* stream);
+/* Learned irradiance with a per-pixel fallback: cheap features and the
+ * network on every pixel as in vct_learned_trace; then every covered pixel
+ * whose error estimate (the network's fourth output) exceeds `threshold`
+ * times the root-mean-square of the network's irradiance over the frame's
+ * covered pixels is listed and re-traced with the 16-cone reference
+ * (INFINITY: no fallback).  fallback_pixels (host, may be NULL) receives the
+ * number of re-traced pixels and synchronises `stream`. */
+vct_status vct_learned_trace_pixels(vct_ctx* ctx, vct_mlp* mlp, const vct_gbuffer* gbuffer, const float eye[3],
+                                    float threshold, float* irradiance_dev, int64_t* fallback_pixels,
+                                    void* stream);
 
 /* ---- voxelisation without allocation ---------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc
@@ -569,11 +595,22 @@ vct_status vct_learned_trace(vct_ctx* ctx, vct_mlp* mlp, const vct_gbuffer* gbuf
  *    this call never changes the current device).  The first call on a device looks up
  *    the array's device address (cudaGetSymbolAddress) for that device; make
  *    that first call before any stream capture.
+ *  - With CUDA's lazy module loading (the default since CUDA 12.2) the array
+ *    comes into being at that first call on each device: the driver then
+ *    allocates its ~9 MiB.  Make the first call before reserving the rest of
+ *    the device's memory, or run with CUDA_MODULE_LOADING=EAGER so that the
+ *    array is allocated when the context is created.  Later calls allocate
+ *    nothing.
+ *  - The address looked up at the first call is kept for the life of the
+ *    process: do not use this entry point across a cudaDeviceReset (or any
+ *    other tear-down of the device's primary context).
  *  - All calls share the one array: calls whose work overlaps on the GPU
  *    (different streams, or different host threads) race.  Each call clears
  *    the parts of the array that must start at zero.
  *  - stats (host pointer) may be NULL; when given, the call synchronises
- *    `stream` and returns the VoxelizeInfo counters of this call. */
+ *    `stream` and returns the VoxelizeInfo counters of this call.  While
+ *    `stream` is being captured, stats must be NULL (VCT_ERR_INVALID_ARGUMENT
+ *    otherwise, before any work is enqueued). */
 #define VCT_STATIC_MAX_DIM 64
 #define VCT_STATIC_MAX_TRIANGLES 16384
 vct_status vct_voxelize_static(const vct_config* cfg, const vct_params* params,

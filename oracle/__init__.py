@@ -183,13 +183,13 @@ def warp_occupancy(scene, shadowmap: np.ndarray, nthreads: int = 1) -> np.ndarra
 
 def voxelize(scene, shadowmap: np.ndarray, lighting: int = 1, axis_override: int = -1, nthreads: int = 1,
              positions=None, normals=None, albedo=None, dim: int | None = None, warp=None):
-    """Returns (count[N^3] u32, sums[6*N^3] u32, total_fragments)."""
+    """Returns (count[N^3] u32, sums[6*N^3] u64, total_fragments)."""
     N = int(dim or scene.dim)
     pos = np.ascontiguousarray(scene.positions if positions is None else positions, dtype=np.float32)
     nrm = np.ascontiguousarray(scene.normals if normals is None else normals, dtype=np.float32)
     alb = np.ascontiguousarray(scene.albedo if albedo is None else albedo, dtype=np.float32)
     count = np.zeros(N ** 3, dtype=np.uint32)
-    sums = np.zeros(6 * N ** 3, dtype=np.uint32)
+    sums = np.zeros(6 * N ** 3, dtype=np.uint64)
     total = C.c_uint32(0)
     arr, n = lights(scene)
     v = volume(scene, N)
@@ -230,7 +230,7 @@ def voxelize_tess(scene, max_level: float = 64.0, nthreads: int = 1, positions=N
     nrm = np.ascontiguousarray(scene.normals if normals is None else normals, dtype=np.float32)
     alb = np.ascontiguousarray(scene.albedo if albedo is None else albedo, dtype=np.float32)
     count = np.zeros(N ** 3, dtype=np.uint32)
-    sums = np.zeros(6 * N ** 3, dtype=np.uint32)
+    sums = np.zeros(6 * N ** 3, dtype=np.uint64)
     total = C.c_uint64(0)
     v = volume(scene, N)
     load().orc_voxelize_tess(C.byref(v), _p(pos), _p(nrm), _p(alb), C.c_int64(pos.shape[0]), C.c_float(max_level),
@@ -245,6 +245,8 @@ def normalize(scene, count, sums, opacity=0.5, temporal=0, decay=0.8, radiance=N
     given array, updated in place, when the temporal filter reads it)."""
     N = int(dim or scene.dim)
     nv = N ** 3
+    count = np.ascontiguousarray(count, dtype=np.uint32)
+    sums = np.ascontiguousarray(sums, dtype=np.uint64)
     color = np.zeros(4 * nv, dtype=np.uint16)
     normal = np.zeros(4 * nv, dtype=np.uint16)
     rad = radiance if radiance is not None else np.zeros(4 * (chain_voxels or nv), dtype=np.uint16)

@@ -1,9 +1,12 @@
 """CPU restatement of the learned path's network for checking the tensor-core
 kernels.  TEST INFRASTRUCTURE ONLY (tests/ and the benchmark's checks).
 
-The network: 42 inputs, hidden layers of 64 with ReLU, 3 linear outputs;
+The network: 42 inputs, hidden layers of 64 with ReLU, 4 linear outputs
+(irradiance RGB and an estimate e of the network's own error there);
 packed parameters W1[64][42] b1[64] W2[64][64] b2[64] W3[64][64] b3[64]
-W4[3][64] b4[3]; loss = mean squared error over the n x 3 outputs.
+W4[4][64] b4[4]; loss = mean squared error over the n x 3 irradiance
+outputs + CONF_WEIGHT * mean over the n rows of (e - |y - t|)^2, with
+|y - t| (the Euclidean error of the row's irradiance) held constant.
 
 Two evaluations:
   - float64 throughout (the reference for the gradients' mathematics);
@@ -17,7 +20,8 @@ from __future__ import annotations
 
 import numpy as np
 
-IN, HID, OUT = 42, 64, 3
+IN, HID, OUT = 42, 64, 4
+CONF_WEIGHT = 0.5
 SHAPES = [("W1", (HID, IN)), ("b1", (HID,)), ("W2", (HID, HID)), ("b2", (HID,)), ("W3", (HID, HID)), ("b3", (HID,)),
           ("W4", (OUT, HID)), ("b4", (OUT,))]
 NPARAMS = sum(int(np.prod(s)) for _, s in SHAPES)
@@ -45,8 +49,8 @@ def bf16(x) -> np.ndarray:
 
 
 def forward_backward(p: np.ndarray, x: np.ndarray, y: np.ndarray | None = None, emulate_bf16: bool = False):
-    """Returns (predictions (n, 3), loss, gradient (NPARAMS,)); loss and
-    gradient are None without targets."""
+    """Returns (predictions (n, 4), loss, gradient (NPARAMS,)); loss and
+    gradient are None without targets (n, 3)."""
     r = bf16 if emulate_bf16 else (lambda a: np.asarray(a, dtype=np.float64))
     w = unpack(p)
     W = {k: (r(v) if k.startswith("W") else v) for k, v in w.items()}
@@ -61,13 +65,19 @@ def forward_backward(p: np.ndarray, x: np.ndarray, y: np.ndarray | None = None, 
     out = h3 @ W["W4"].T + W["b4"]
     if y is None:
         return out, None, None
-    diff = out - np.asarray(y, dtype=np.float64)
-    loss = float((diff ** 2).sum() / (3 * n))
+    diff = out[:, :3] - np.asarray(y, dtype=np.float64)
+    err = np.sqrt((diff ** 2).sum(1))  # held constant: no gradient through it
+    dc = out[:, 3] - err
+    loss = float((diff ** 2).sum() / (3 * n) + CONF_WEIGHT * (dc ** 2).sum() / n)
     if emulate_bf16:
-        # the kernels round (2 / 3n) * diff, computed in fp32, to BF16
-        dy = r(np.float32(2.0 / (3.0 * n)) * diff.astype(np.float32))
+        # the kernels compute (2 / 3n) * diff and (2 w / n) * dc in fp32 and round them to BF16
+        d32 = diff.astype(np.float32)
+        e32 = np.sqrt((d32 * d32).sum(1, dtype=np.float32))
+        dc32 = out[:, 3].astype(np.float32) - e32
+        dy = np.concatenate([r(np.float32(2.0 / (3.0 * n)) * d32),
+                             r(np.float32(2.0 * CONF_WEIGHT / n) * dc32)[:, None]], 1)
     else:
-        dy = 2.0 * diff / (3 * n)
+        dy = np.concatenate([2.0 * diff / (3 * n), (2.0 * CONF_WEIGHT / n) * dc[:, None]], 1)
     g = {"W4": dy.T @ h3, "b4": dy.sum(0)}
     dz3 = r((dy @ W["W4"]) * (z3 > 0))
     g["W3"], g["b3"] = dz3.T @ h2, dz3.sum(0)

@@ -422,7 +422,7 @@ void orc_mat4_mul(const float a[16], const float b[16], float out[16]) { matmul(
 void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, const float* albedo,
                   int64_t ntri, const orc_light* lights, int32_t nlights, int32_t lighting,
                   int32_t axis_override, const float* sm, int32_t sw, int32_t sh, const float ls[16],
-                  uint32_t* count, uint32_t* sums, uint32_t* total_fragments, int32_t nthreads,
+                  uint32_t* count, uint64_t* sums, uint32_t* total_fragments, int32_t nthreads,
                   const orc_warp* warp) {
     // voxelize.frag reads warpVoxels and warpTexture; voxelizeTesselationWarp
     // (mode 3) leaves the rasterised grid linear.
@@ -433,7 +433,7 @@ void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, con
     voxel_mvp(vol, mvp);
     std::atomic<uint64_t> total{0};
     const bool atomic = nthreads > 1;
-    auto addu = [atomic](uint32_t* p, uint32_t v) {
+    auto addu = [atomic](auto* p, uint32_t v) {
         if (atomic)
             __atomic_fetch_add(p, v, __ATOMIC_RELAXED);
         else
@@ -687,7 +687,7 @@ void orc_tess_coords(const int32_t lv[4], float* out) {
 }
 
 void orc_voxelize_tess(const orc_volume* vol, const float* pos, const float* nrm, const float* albedo,
-                       int64_t ntri, float max_level, const orc_warp* warp, uint32_t* count, uint32_t* sums,
+                       int64_t ntri, float max_level, const orc_warp* warp, uint32_t* count, uint64_t* sums,
                        uint64_t* total_points, int32_t nthreads) {
     const int N = vol->dim;
     const int64_t NV = (int64_t)N * N * N;
@@ -696,7 +696,7 @@ void orc_voxelize_tess(const orc_volume* vol, const float* pos, const float* nrm
     const bool persp = warp && warp->mode == 3;  // the other warps are off in the evaluation shader
     std::atomic<uint64_t> total{0};
     const bool atomic = nthreads > 1;
-    auto addu = [atomic](uint32_t* p, uint32_t v) {
+    auto addu = [atomic](auto* p, uint32_t v) {
         if (atomic)
             __atomic_fetch_add(p, v, __ATOMIC_RELAXED);
         else
@@ -754,7 +754,7 @@ void orc_voxelize_tess(const orc_volume* vol, const float* pos, const float* nrm
 
 // --------------------------------------------------------------- normalize
 void orc_normalize(const orc_volume* vol, float opacity, int32_t temporal, float decay,
-                   const uint32_t* count, const uint32_t* sums, uint16_t* color, uint16_t* normal,
+                   const uint32_t* count, const uint64_t* sums, uint16_t* color, uint16_t* normal,
                    uint16_t* radiance, orc_stats* stats, int32_t nthreads) {
     const int64_t NV = (int64_t)vol->dim * vol->dim * vol->dim;
     std::atomic<uint32_t> uniq{0}, mx{0}, flags{0};
@@ -768,7 +768,7 @@ void orc_normalize(const orc_volume* vol, float opacity, int32_t temporal, float
             if (c > 0) {
                 ++lu;
                 lm = std::max(lm, c);
-                if (c >= 65537u) lf |= 1u;
+                // the sums are 64-bit: exact for any number of fragments
                 float denom = 65535.0f * (float)c;
                 alpha = opacity > 0.0f ? opacity : 1.0f;
                 for (int k = 0; k < 3; ++k) C[k] = f2h((float)sums[k * NV + v] / denom);

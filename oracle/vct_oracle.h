@@ -87,11 +87,12 @@ void orc_ortho(float l, float r, float b, float t, float n, float f, float out[1
 void orc_perspective(float fovy, float aspect, float znear, float zfar, float out[16]);
 void orc_mat4_mul(const float a[16], const float b[16], float out[16]);
 
-/* count[dim^3], sums[6*dim^3] (SoA r,g,b,nx,ny,nz) are ADDED to. */
+/* count[dim^3] (uint32), sums[6*dim^3] (uint64, SoA r,g,b,nx,ny,nz) are ADDED
+ * to; the sums are exact for any number of fragments per voxel. */
 void orc_voxelize(const orc_volume* vol, const float* pos, const float* nrm, const float* albedo,
                   int64_t ntri, const orc_light* lights, int32_t nlights, int32_t lighting,
                   int32_t axis_override, const float* shadowmap, int32_t sw, int32_t sh,
-                  const float ls[16], uint32_t* count, uint32_t* sums, uint32_t* total_fragments,
+                  const float ls[16], uint32_t* count, uint64_t* sums, uint32_t* total_fragments,
                   int32_t nthreads, const orc_warp* warp);
 
 /* Tessellation voxeliser (testTesselation.tesc/.tese): levels of one
@@ -107,12 +108,12 @@ void orc_tess_coords(const int32_t levels[4], float* out);
  * the voxel holding it (linear mapping, or warp mode 3).  count/sums as for
  * orc_voxelize; total_points counts the generated points. */
 void orc_voxelize_tess(const orc_volume* vol, const float* pos, const float* nrm, const float* albedo,
-                       int64_t ntri, float max_level, const orc_warp* warp, uint32_t* count, uint32_t* sums,
+                       int64_t ntri, float max_level, const orc_warp* warp, uint32_t* count, uint64_t* sums,
                        uint64_t* total_points, int32_t nthreads);
 
 /* transferVoxels.comp; radiance/colour/normal are dim^3 RGBA16F (uint16 x4). */
 void orc_normalize(const orc_volume* vol, float voxel_set_opacity, int32_t temporal_filter,
-                   float temporal_decay, const uint32_t* count, const uint32_t* sums,
+                   float temporal_decay, const uint32_t* count, const uint64_t* sums,
                    uint16_t* color, uint16_t* normal, uint16_t* radiance, orc_stats* stats,
                    int32_t nthreads);
 

@@ -51,8 +51,10 @@ def test_algorithmic_bytes_of_the_large_frame():
     a = bench.algorithmic_bytes(sc, stats, None)
     N, T = 256, 262144
     nv = N ** 3
-    assert a["accumulate"] == T * 84 + 6666268 * 56
-    assert a["trace"] == 1920 * 1080 * 64
+    assert a["accumulate"] == T * 84 + 5181082 * 64 + nv // 8
+    assert a["trace"] == 1920 * 1080 * 64  # every pixel covered unless the counters say otherwise
+    a = bench.algorithmic_bytes(sc, dict(stats, covered_pixels=1000), None)
+    assert a["trace"] == 1920 * 1080 * 32 + 1000 * 32
     assert a["inject_mark"] == 2048 * 2048 * 4 + nv // 8
     lv = lambda lo, hi: sum((N >> l) ** 3 for l in range(lo, hi))  # noqa: E731
     assert a["resolve"] == nv // 4 + 5181082 * 64 + nv * 24 + lv(1, 5) * 8 + lv(0, 5) * 16
@@ -82,3 +84,85 @@ def test_stage_rooflines():
     assert a["fragments_per_s"] == 1.5e10 and a["reductions_per_s"] == 7.5e10
     t = bench.stage_rooflines(alg, ms, 6800.0, {}, 6_000_000, "tess")["accumulate"]
     assert t["reductions_per_s"] == 6.0e10
+
+
+def test_irradiance_accuracy():
+    import numpy as np
+
+    rng = np.random.default_rng(0)
+    ref = rng.uniform(0.1, 1.0, size=(1000, 4)).astype(np.float32)
+    cov = np.ones(1000, dtype=bool)
+    cov[:100] = False
+    gpu = ref.copy()
+    gpu[100:, :3] *= 1.0005  # every judged pixel off by 5e-4 of its value
+    gpu[:100] = 7.0  # uncovered pixels are not judged
+    a = bench.irradiance_accuracy(gpu, ref, cov)
+    assert a["pixels"] == 900 and a["pixels_judged"] == 900
+    assert abs(a["rel_l2"] - 5e-4) < 1e-6 and abs(a["max_rel"] - 5e-4) < 1e-6
+    assert a["frac_within_1e-3"] == 1.0
+    # a dark pixel below the floor counts in rel_l2 but not in the per-pixel figures
+    ref2 = ref.copy()
+    ref2[500, :3] = 1e-9
+    gpu2 = ref2.copy()
+    gpu2[500, :3] = 1e-3
+    b = bench.irradiance_accuracy(gpu2, ref2, cov)
+    assert b["pixels_judged"] == 899 and b["max_rel"] == 0.0 and b["rel_l2"] > 0.0
+
+
+def test_cpu_model_names():
+    assert bench.cpu_model("processor : 0\nmodel name : Intel(R) Xeon(R) CPU @ 2.70GHz\n") == \
+        "Intel(R) Xeon(R) CPU @ 2.70GHz"
+    grace = "processor : 0\nCPU implementer : 0x41\nCPU architecture: 8\nCPU part : 0xd4f\n"
+    assert bench.cpu_model(grace) == "Neoverse-V2 (Arm part 0xd4f)"
+    assert "0x123" in bench.cpu_model("CPU implementer : 0x51\nCPU part : 0x123\n")
+
+
+def test_ncu_traffic_only_for_the_captured_sources():
+    digest = bench.kernel_sources_digest()
+    assert len(digest) == 16
+    traffic, note = bench.ncu_traffic(False)
+    assert traffic == {} and "no ncu capture" in note["traffic_source"]
+    saved = bench.NCU_CAPTURE_DIGEST
+    try:
+        bench.NCU_CAPTURE_DIGEST = digest
+        traffic, note = bench.ncu_traffic(True)
+        assert traffic == bench.NCU_TRAFFIC and note["traffic_digest"] == digest
+        bench.NCU_CAPTURE_DIGEST = "0" * 16
+        traffic, note = bench.ncu_traffic(True)
+        assert traffic == {} and "traffic_stale" in note
+    finally:
+        bench.NCU_CAPTURE_DIGEST = saved
+
+
+def test_both_arms_share_the_config_keys():
+    import argparse
+
+    sc = scenes.cornell(seed=0)
+    args = argparse.Namespace(config="cornell", voxelizer="raster", warp="none", seed=0)
+    ours = bench.frame_config(args, sc, 1)
+    assert {"workload", "triangles", "grid", "levels", "shadow_map", "gbuffer", "cones", "voxelizer", "warp",
+            "l2"} <= set(ours)
+
+
+def test_accuracy_block_on_the_oracles_own_frame():
+    """The bench's accuracy block judged on the oracle's own fp32 frame: the
+    chain matches itself, the fp32 trace is 0 from itself and within the
+    1e-3 bar of the fp64 trace."""
+    import oracle as O
+
+    sc = scenes.cornell(seed=0)
+    sm, gb = O.render_shadowmap(sc), O.render_gbuffer(sc)
+    ms, detail, chain, (irr, _, _, _) = bench.cpu_frame(sc, 4, 0, sm, gb, want=("irr", "color"))
+    assert ms > 0 and detail["rows_traced"] == sc.gbuffer_size[1]
+    art = {"irr": {"software": irr}, "chain": chain, "gbuf": gb, "sm": sm}
+    a = bench.accuracy_block(sc, art, chain, irr, "software", 4)
+    assert a["chain_bitexact"] and a["meets_bar"]
+    s = a["samplers"]["software"]
+    assert s["vs_fp32_oracle_rel_l2"] == 0.0 and 0.0 < s["vs_fp64"]["rel_l2"] < 1e-5
+
+
+def test_pareto_front():
+    pts = [{"ms": 1.0, "rel_l2": 0.05}, {"ms": 0.5, "rel_l2": 0.2}, {"ms": 1.2, "rel_l2": 0.06},
+           {"ms": 2.0, "rel_l2": 0.01}, {"ms": 0.5, "rel_l2": 0.3}]
+    f = bench.pareto_front(pts)
+    assert [(p["ms"], p["rel_l2"]) for p in f] == [(0.5, 0.2), (1.0, 0.05), (2.0, 0.01)]

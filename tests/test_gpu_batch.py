@@ -77,7 +77,7 @@ def _same(a, b, what):
         assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), f"{what}: {k}"
 
 
-@pytest.mark.parametrize("filt", [L.VCT_FILTER_SOFTWARE, L.VCT_FILTER_HARDWARE])
+@pytest.mark.parametrize("filt", [L.VCT_FILTER_SOFTWARE, L.VCT_FILTER_HARDWARE, L.VCT_FILTER_HYBRID])
 def test_batch_frame_equals_single_frames(setup, filt):
     import torch
 

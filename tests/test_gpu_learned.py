@@ -129,8 +129,9 @@ def test_learned_trace_is_the_network_on_the_rows_and_falls_back_per_tile(frame)
     pix = torch.arange(W * H, dtype=torch.int32, device="cuda")
     rows = torch.empty(W * H, 42, device="cuda")
     api.learned_rows(ctx, g.gb, sc.eye, q, pix, rows)
-    net = torch.empty(W * H, 3, device="cuda")
-    mlp.forward(rows, net)
+    net4 = torch.empty(W * H, 4, device="cuda")
+    mlp.forward(rows, net4)
+    net = net4[:, :3]
     out = torch.zeros(W * H * 4, device="cuda")
     api.learned_trace(ctx, mlp, g.gb, sc.eye, out, float("inf"))
     torch.cuda.synchronize()
@@ -158,6 +159,50 @@ def test_learned_trace_is_the_network_on_the_rows_and_falls_back_per_tile(frame)
                 assert np.array_equal(o[sl][..., :3], nn[sl]), (tx, ty)
                 n_net += 1
     assert n_ref >= st["fallback_tiles"]
+
+
+def test_pixel_fallback_retraces_exactly_the_flagged_pixels(frame):
+    """vct_learned_trace_pixels: the covered pixels whose error estimate (the
+    network's fourth output, as vct_mlp_forward gives it on the same rows)
+    exceeds threshold x the RMS of the network's irradiance over covered
+    pixels hold the 16-cone trace bit for bit; every other pixel holds the
+    network's irradiance; the reported count is their number.  (The RMS is
+    summed on the device in an arbitrary order, so estimates within 1e-4 of
+    the bound may go either way.)"""
+    import torch
+
+    sc, g, ctx, chain, q, host = frame
+    W, H = sc.gbuffer_size
+    mlp = api.Mlp(seed=2)
+    w = mlp.params()
+    w[api.Mlp.NPARAMS - 1] += 4.0  # the error estimate's bias: every estimate positive
+    mlp.set_params(w)
+    pix = torch.arange(W * H, dtype=torch.int32, device="cuda")
+    rows = torch.empty(W * H, 42, device="cuda")
+    api.learned_rows(ctx, g.gb, sc.eye, q, pix, rows)
+    net = torch.empty(W * H, 4, device="cuda")
+    mlp.forward(rows, net)
+    ref = torch.zeros(W * H * 4, device="cuda")
+    api.trace_reference16(ctx, g.gb, sc.eye, ref)
+    cov = torch.from_numpy(host["gpos"].reshape(-1, 4)[:, 3] != 0).cuda()
+    rms = float(net[cov, :3].double().pow(2).sum(1).mean().sqrt())
+    thr = float(net[cov, 3].double().median()) / rms
+    out = torch.full((W * H * 4,), -1.0, device="cuda")
+    n = api.learned_trace_pixels(ctx, mlp, g.gb, sc.eye, out, thr, want_count=True)
+    est, bound = net[:, 3].double(), thr * rms
+    flagged = cov & (est > bound * (1 + 1e-4))
+    kept = cov & (est < bound * (1 - 1e-4))
+    assert 0 < int(flagged.sum()) <= n <= int(flagged.sum()) + int((cov & ~flagged & ~kept).sum())
+    assert int(kept.sum()) > 0
+    o, r = out.view(-1, 4), ref.view(-1, 4)
+    assert torch.equal(o[flagged], r[flagged])
+    assert torch.equal(o[kept, :3], net[kept, :3]) and torch.all(o[kept, 3] == 0)
+    assert torch.all(o[~cov] == 0)
+    # no bound: the network alone, the same image as vct_learned_trace without fallback
+    plain = torch.zeros(W * H * 4, device="cuda")
+    api.learned_trace(ctx, mlp, g.gb, sc.eye, plain, float("inf"))
+    assert api.learned_trace_pixels(ctx, mlp, g.gb, sc.eye, out, float("inf"), want_count=True) == 0
+    assert torch.equal(out, plain)
 
 
 def test_trained_network_beats_the_cheap_trace():

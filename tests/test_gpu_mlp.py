@@ -62,7 +62,7 @@ def _net(seed=3):
     p = m.params().astype(np.float64)
     rng = np.random.default_rng(seed)
     # non-zero biases exercise the bias paths
-    for name, (o, n) in {"b1": (2688, 64), "b2": (6848, 64), "b3": (11008, 64), "b4": (11264, 3)}.items():
+    for name, (o, n) in {"b1": (2688, 64), "b2": (6848, 64), "b3": (11008, 64), "b4": (11328, 4)}.items():
         p[o:o + n] = rng.uniform(-0.2, 0.2, n)
     m.set_params(p.astype(np.float32))
     return m, m.params().astype(np.float64)
@@ -99,7 +99,7 @@ def test_mlp_forward_matches_oracle(n):
 
     m, p = _net()
     x, _, dx, _ = _rows(n)
-    out = torch.empty(n, 3, device="cuda")
+    out = torch.empty(n, 4, device="cuda")
     m.forward(dx, out)
     got = out.cpu().numpy()
     emu = OM.forward_backward(p, x, emulate_bf16=True)[0]
@@ -126,7 +126,8 @@ def test_mlp_gradients_match_oracle(n):
     cos = float(g @ g64 / (np.linalg.norm(g) * np.linalg.norm(g64)))
     assert cos > 0.998, cos
     # every parameter block carries gradient
-    for name, (o, k) in {"W1": (0, 2688), "b1": (2688, 64), "W4": (11072, 192), "b4": (11264, 3)}.items():
+    for name, (o, k) in {"W1": (0, 2688), "b1": (2688, 64), "W4": (11072, 256), "b4": (11328, 4),
+                         "W4 error row": (11072 + 192, 64), "b4 error": (11331, 1)}.items():
         assert _rel(g[o:o + k], g_emu[o:o + k]) < 2e-2, name
 
 
@@ -149,8 +150,9 @@ def test_training_fits_a_teacher_network():
 
     teacher, tp = _net(11)
     x, _, dx, _ = _rows(65536, seed=4)
-    dy = torch.empty(65536, 3, device="cuda")
-    teacher.forward(dx, dy)
+    out = torch.empty(65536, 4, device="cuda")
+    teacher.forward(dx, out)
+    dy = out[:, :3].contiguous()
     m = api.Mlp(seed=12)
     loss = torch.zeros(1, device="cuda")
     first = None

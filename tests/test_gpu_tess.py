@@ -1,8 +1,9 @@
 """The tessellation voxeliser (testTesselation.tesc/.tese) and the
 perspective warp (voxelizeTesselationWarp) against the oracle: accumulators
-bit-exact with and without the warp, the whole frame with either voxeliser
-under the perspective warp (volumes bit-exact, irradiance within the trace
-tolerances), and the batch's refusal."""
+bit-exact with and without the warp, sums past 2^32 (more than 65,536 points
+in one voxel) exact through the carry table, the whole frame with either
+voxeliser under the perspective warp (volumes bit-exact, irradiance within
+the trace tolerances), and the batch's refusal."""
 
 from __future__ import annotations
 
@@ -84,6 +85,58 @@ def test_slivers_exercise_the_aggregated_stores():
     torch.cuda.synchronize()
     gc, gs, _, _ = split_records(*ctx.read_accumulators())
     assert np.array_equal(gc, count) and np.array_equal(gs, sums)
+
+
+def _tess_volumes(sc, mode=L.VCT_WARP_NONE):
+    """GPU tessellation voxelisation + normalisation: (records, colour, normal, stats)."""
+    import torch
+
+    g = GpuScene(sc)
+    ctx = api.Context(api.config_for(sc))
+    ctx.set_params(api.scene_params(sc, voxelize_tesselation=1, warp_mode=mode))
+    ctx.voxelize_accumulate(g.tris, g.lights, g.shadow, sc.eye)
+    torch.cuda.synchronize()
+    rec = split_records(*ctx.read_accumulators())
+    ctx.normalize()
+    torch.cuda.synchronize()
+    vols = [ctx.read_volume(v, 0).cpu().numpy().view(np.uint16) for v in (L.VCT_VOLUME_COLOR, L.VCT_VOLUME_NORMAL)]
+    return rec, vols[0], vols[1], ctx.stats()
+
+
+def _check_exact_past_the_packed_bound(sc, ref, got):
+    count, sums, total = ref
+    (gc, gs, gocc, _), color, normal, stats = got
+    assert count.max() > 65537 and sums.max() >= 2 ** 32  # the case the packed record cannot sum alone
+    # records the carry pass rewrote have bit 31 of the count set and their sums' float values
+    rewritten = (gc >> 31) != 0
+    assert rewritten.any() and np.all(count[rewritten] >= 65537)
+    assert np.array_equal(gc & 0x7FFFFFFF, count) and np.array_equal(gocc, count > 0)
+    small = np.tile(~rewritten, 6)  # elsewhere the record's halves are the sums themselves
+    assert np.array_equal(gs[small], sums[small])
+    big = np.tile(rewritten, 6)
+    assert np.array_equal(gs[big].view(np.float32), sums[big].astype(np.float32))
+    rcol, rnrm, _, rst = O.normalize(sc, count, sums, nthreads=8)
+    assert np.array_equal(color, rcol) and np.array_equal(normal, rnrm)
+    assert stats["error_flags"] == 0
+    assert stats["total_voxel_fragments"] == total and stats["max_fragments_per_voxel"] == int(count.max())
+
+
+def test_tess_sums_exact_past_65536_points_per_voxel():
+    """1,600 coincident slivers put up to 185,600 points into one voxel and
+    sums past 2^32 into its fields: the carry table keeps colour and normal
+    bit-exact against the oracle's 64-bit sums, with no overflow flag."""
+    sc = scenes.stacked_slivers(1600)
+    _check_exact_past_the_packed_bound(sc, O.voxelize_tess(sc, nthreads=8), _tess_volumes(sc))
+
+
+def test_large_frame_perspective_tess_exact():
+    """The large frame through the tessellation voxeliser with the
+    perspective warp (the reference's default voxeliser): up to ~91,000
+    points fall into one froxel; colour and normal stay bit-exact."""
+    sc = scenes.large(seed=0)
+    w = O.warp(sc, L.VCT_WARP_PERSPECTIVE)
+    _check_exact_past_the_packed_bound(sc, O.voxelize_tess(sc, nthreads=16, warp=w),
+                                       _tess_volumes(sc, L.VCT_WARP_PERSPECTIVE))
 
 
 @pytest.fixture(scope="module", params=[True, False], ids=["tess", "raster"])

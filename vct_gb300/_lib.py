@@ -167,6 +167,7 @@ SIGNATURES = {
     "vct_inject": (st, [vp, P(vct_shadow_desc), P(C.c_float), vp]),
     "vct_build_mips": (st, [vp, C.c_int32, vp]),
     "vct_trace": (st, [vp, P(vct_gbuffer), P(C.c_float), P(vct_trace_out), vp]),
+    "vct_trace_views": (st, [vp, C.c_int32, P(vct_gbuffer), P(C.c_float), P(vct_trace_out), vp]),
     "vct_frame": (st, [vp, P(vct_triangles), P(vct_light), C.c_int32, P(vct_shadow_desc), P(C.c_float),
                        P(vct_gbuffer), P(vct_trace_out), vp]),
     "vct_frame_volume": (st, [vp, P(vct_triangles), P(vct_light), C.c_int32, P(vct_shadow_desc), P(C.c_float), vp]),
@@ -206,6 +207,7 @@ SIGNATURES = {
     "vct_learned_rows": (st, [vp, P(vct_gbuffer), P(C.c_float), vp, vp, C.c_int64, vp, vp]),
     "vct_trace_reference16": (st, [vp, P(vct_gbuffer), P(C.c_float), vp, vp]),
     "vct_learned_trace": (st, [vp, vp, P(vct_gbuffer), P(C.c_float), C.c_float, vp, P(vct_learned_stats), vp]),
+    "vct_learned_trace_pixels": (st, [vp, vp, P(vct_gbuffer), P(C.c_float), C.c_float, vp, P(C.c_int64), vp]),
     "vct_default_tuning": (None, [P(vct_tuning)]),
     "vct_get_tuning": (st, [vp, P(vct_tuning)]),
     "vct_set_tuning": (st, [vp, P(vct_tuning)]),

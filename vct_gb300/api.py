@@ -192,6 +192,14 @@ class Context:
     def trace(self, gb, eye, out, stream=None):
         L.check(self._lib.vct_trace(self.handle, C.byref(gb), f3(eye), C.byref(out), _stream(stream)), "vct_trace")
 
+    def trace_views(self, gbs, eyes, outs, stream=None):
+        """vct_trace_views: the trace of several viewpoints in one launch."""
+        n = len(gbs)
+        g = (L.vct_gbuffer * max(1, n))(*gbs)
+        e = (C.c_float * max(3, 3 * n))(*[float(v) for eye in eyes for v in eye])
+        o = (L.vct_trace_out * max(1, n))(*outs)
+        L.check(self._lib.vct_trace_views(self.handle, n, g, e, o, _stream(stream)), "vct_trace_views")
+
     def frame(self, tris, lights, shadow, eye, gb, out, stream=None):
         arr, n = lights
         L.check(self._lib.vct_frame(self.handle, C.byref(tris), arr, n, C.byref(shadow), f3(eye), C.byref(gb),
@@ -360,7 +368,8 @@ class Batch:
 class Mlp:
     """Owns a vct_mlp: the learned path's network (see include/vct.h)."""
 
-    NPARAMS = 11267
+    NPARAMS = 11332
+    OUTPUTS = 4
 
     def __init__(self, device: int = 0, seed: int = 0):
         self._lib = L.load()
@@ -429,6 +438,17 @@ def learned_trace(ctx: Context, mlp: Mlp, gb, eye, irradiance, threshold: float 
     if st is not None:
         return {k: getattr(st, k) for k, _ in L.vct_learned_stats._fields_}
     return None
+
+
+def learned_trace_pixels(ctx: Context, mlp: Mlp, gb, eye, irradiance, threshold: float, want_count: bool = False,
+                         stream=None):
+    """vct_learned_trace_pixels; with want_count, returns the number of
+    re-traced pixels (and synchronises the stream)."""
+    n = C.c_int64(0)
+    L.check(L.load().vct_learned_trace_pixels(ctx.handle, mlp.handle, C.byref(gb), f3(eye), C.c_float(threshold),
+                                              _ptr(irradiance), C.byref(n) if want_count else None,
+                                              _stream(stream)), "vct_learned_trace_pixels")
+    return int(n.value) if want_count else None
 
 
 def actor_array(actors) -> tuple:

@@ -63,10 +63,10 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         if (s == VCT_OK) s = validate_gbuffer(&d.gbuffer);
         if (s != VCT_OK) return s;
         if (c->params.trace_filter != filter) return fail(VCT_ERR_INVALID_ARGUMENT, "all scenes of a batch must use the same trace_filter");
-        if (filter == VCT_FILTER_HYBRID)
-            return fail(VCT_ERR_UNSUPPORTED, "batches use VCT_FILTER_SOFTWARE or the texture-unit samplers");
-        if (filter != VCT_FILTER_SOFTWARE && (s = ensure_texture(c)) != VCT_OK) return s;
-        const bool hw = filter != VCT_FILTER_SOFTWARE;
+        // The resolve and mip kernels write the chain copies the sampler reads:
+        // the texture-unit surfaces, the bordered fp32 chain, or both (hybrid).
+        const bool hw = filter_uses_texture(filter), pad = filter_uses_bordered(filter);
+        if (hw && (s = ensure_texture(c)) != VCT_OK) return s;
         if (c->params.warp_mode == VCT_WARP_TEXTURE)
             return fail(VCT_ERR_UNSUPPORTED, "batches do not build warp maps: use another VCT_WARP_* mode");
         if (c->params.voxelize_tesselation != b->ctx[0]->params.voxelize_tesselation)
@@ -79,6 +79,8 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         apply_tuning(b->tuning, A);
         A.acc = c->acc;
         A.occ = c->occ;
+        A.carry = c->params.voxelize_tesselation ? c->carry : nullptr;
+        A.brick_exact = c->params.voxelize_tesselation ? c->brick_exact : nullptr;
         A.stats = c->stats;
         A.num_sms = c->num_sms;
         InjectParams I;
@@ -99,12 +101,12 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         for (int l = 0; l <= R.mip_levels; ++l) {
             R.radiance_levels[l] = level_ptr(c->radiance, c, l);
             R.surf[l] = hw ? c->surf[l] : 0;
-            R.pad_levels[l] = hw ? nullptr : c->pchain + padded_level_offset(c->dim, l);
+            R.pad_levels[l] = pad ? c->pchain + padded_level_offset(c->dim, l) : nullptr;
         }
         MipLevels M = mip_levels(c, c->radiance, c->levels);
         for (int l = 0; l < c->levels; ++l) {
             M.surf[l] = hw ? c->surf[l] : 0;
-            M.pad[l] = hw ? nullptr : c->pchain + padded_level_offset(c->dim, l);
+            M.pad[l] = pad ? c->pchain + padded_level_offset(c->dim, l) : nullptr;
         }
         M.first = std::min(4, c->levels - 1);
         TraceParams T;
@@ -160,6 +162,10 @@ vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cu
     for (vct_ctx* c : b->ctx) {
         VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
         VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, st));
+        if (c->params.voxelize_tesselation) {
+            VCT_CUDA(cudaMemsetAsync(c->carry, 0, (size_t)kCarryBytes, st));
+            VCT_CUDA(cudaMemsetAsync(c->brick_exact, 0, (size_t)(c->nv / 4096 + 1) * 4, st));
+        }
     }
     const long long* d_tables = reinterpret_cast<const long long*>(b->d_blob + b->off_tables);
     AccumParams W0;
@@ -183,7 +189,7 @@ vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cu
     VCT_CHECK_LAUNCH("batch: inject mark");
     launch_resolve_batch(SceneBatch<ResolveParams>{reinterpret_cast<const ResolveParams*>(b->d_blob + b->off_resolve),
                                                   d_tables + 2 * (n + 1), n},
-                         tot.bricks, st);
+                         tot.bricks, b->ctx[0]->params.voxelize_tesselation != 0, st);
     VCT_CHECK_LAUNCH("batch: resolve");
     for (vct_ctx* c : b->ctx) VCT_CUDA(cudaMemsetAsync(c->occ, 0, (size_t)((c->nv + 31) / 32) * 4, st));
     launch_mip_tail_batch(SceneBatch<MipLevels>{reinterpret_cast<const MipLevels*>(b->d_blob + b->off_mips), nullptr, n},
@@ -195,12 +201,12 @@ vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cu
                        b->ctx[0]->params.trace_filter, tot.tiles, st);
     VCT_CHECK_LAUNCH("batch: trace");
     if (timed) VCT_CUDA(cudaEventRecord(b->ev[3], st));
-    const bool hw = b->ctx[0]->params.trace_filter != VCT_FILTER_SOFTWARE;
+    const int filter = b->ctx[0]->params.trace_filter;
     for (vct_ctx* c : b->ctx) {
         c->stats_reset_pending = true;
         c->radiance_ready = c->mips_ready = true;
-        c->tex_ready = hw;
-        c->pad_ready = !hw;
+        c->tex_ready = filter_uses_texture(filter);
+        c->pad_ready = filter_uses_bordered(filter);
     }
     return VCT_OK;
 }

@@ -344,10 +344,14 @@ vct_status build_warpmap(vct_ctx* ctx, const AccumParams& A, cudaStream_t st) {
 // The voxeliser the parameters select: rasterising (voxelize.geom/.frag) or
 // tessellating (testTesselation.tesc/.tese).
 void launch_voxelizer(const vct_ctx* ctx, const AccumParams& P, cudaStream_t st) {
-    if (ctx->params.voxelize_tesselation)
+    if (ctx->params.voxelize_tesselation) {
+        // (errors of these clears surface at the launch check)
+        cudaMemsetAsync(P.carry, 0, (size_t)kCarryBytes, st);
+        cudaMemsetAsync(P.brick_exact, 0, (size_t)(ctx->nv / 4096 + 1) * 4, st);
         launch_tesselate(P, st);
-    else
+    } else {
         launch_accumulate(P, st);
+    }
 }
 
 vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lights, int n,
@@ -359,6 +363,8 @@ vct_status fill_accum(vct_ctx* ctx, const vct_triangles* t, const vct_light* lig
     apply_tuning(ctx->tuning, P);
     P.acc = ctx->acc;
     P.occ = ctx->occ;
+    P.carry = ctx->params.voxelize_tesselation ? ctx->carry : nullptr;
+    P.brick_exact = ctx->params.voxelize_tesselation ? ctx->brick_exact : nullptr;
     P.stats = ctx->stats;
     P.num_sms = ctx->num_sms;
     const long long need = accumulate_scratch_bytes(t->count);
@@ -384,6 +390,7 @@ void fill_norm(vct_ctx* ctx, NormalizeParams& P) {
     P.decay = ctx->params.temporal_decay;
     P.acc = ctx->acc;
     P.occ = ctx->occ;
+    P.brick_exact = ctx->params.voxelize_tesselation ? ctx->brick_exact : nullptr;
     P.color = ctx->color;
     P.normal = ctx->normal;
     P.radiance = ctx->radiance;
@@ -703,6 +710,8 @@ vct_status vct_create(const vct_config* cfg, vct_ctx** out) {
         {(void**)&c->occ32, (size_t)(VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM / 32) * 4},
         {(void**)&c->warpmap, (size_t)VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM * 8},
         {(void**)&c->warpmap_f, (size_t)VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM * 16},
+        {(void**)&c->carry, (size_t)kCarryBytes},
+        {(void**)&c->brick_exact, (size_t)(c->nv / 4096 + 1) * 4},
     };
     for (auto& a : allocs) {
         cudaError_t e = cudaMalloc(a.p, a.bytes);
@@ -739,8 +748,9 @@ vct_status vct_destroy(vct_ctx* c) {
     if (c->tex_array) cudaFreeMipmappedArray(c->tex_array);
     for (auto sf : c->surf)
         if (sf) cudaDestroySurfaceObject(sf);
-    void* ptrs[] = {c->acc,    c->occ,   c->lit,         c->color,  c->normal,  c->radiance,
-                    c->stats,  c->vox_scratch, c->pchain, c->learned, c->occ32, c->warpmap, c->warpmap_f};
+    void* ptrs[] = {c->acc,    c->occ,   c->lit,         c->color,  c->normal,  c->radiance, c->stats,
+                    c->vox_scratch, c->pchain, c->learned, c->occ32, c->warpmap, c->warpmap_f, c->carry,
+                    c->brick_exact};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -933,6 +943,38 @@ vct_status vct_trace(vct_ctx* c, const vct_gbuffer* g, const float eye[3], const
     if (c->timers_on && c->volume_timed) {  // render stage of a timed vct_frame_volume
         VCT_CUDA(cudaEventRecord(c->ev[4], st));
         c->timers_recorded = true;
+    }
+    return VCT_OK;
+}
+
+vct_status vct_trace_views(vct_ctx* c, int32_t n, const vct_gbuffer* gbuffers, const float* eyes,
+                           const vct_trace_out* outs, void* stream) {
+    if (!c || (n > 0 && (!gbuffers || !eyes || !outs))) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n < 0) return fail(VCT_ERR_INVALID_ARGUMENT, "n must be >= 0");
+    vct_status s = VCT_OK;
+    for (int i = 0; i < n; ++i)
+        if ((s = validate_gbuffer(&gbuffers[i])) != VCT_OK) return s;
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    cudaStream_t st = as_stream(stream);
+    if (n == 0) return VCT_OK;
+    if (filter_uses_texture(c->params.trace_filter) && !c->tex_ready) {
+        if ((s = refresh_texture(c, st)) != VCT_OK) return s;
+    }
+    if (filter_uses_bordered(c->params.trace_filter) && (s = ensure_padded_chain(c, st)) != VCT_OK) return s;
+    // kMaxViews viewpoints per launch, their parameters in kernel-parameter space
+    for (int first = 0; first < n; first += kMaxViews) {
+        ViewSet V;
+        std::memset(&V, 0, sizeof V);
+        V.n = std::min(kMaxViews, n - first);
+        for (int k = 0; k < V.n; ++k) {
+            TraceParams& P = V.p[k];
+            if ((s = fill_trace(c, &gbuffers[first + k], eyes + 3 * (first + k), &outs[first + k], P)) != VCT_OK)
+                return s;
+            V.off[k + 1] = V.off[k] + trace_tiles(P.width, P.height, P.tile_w_log2, P.tile_h_log2);
+        }
+        launch_trace_views(V, c->params.trace_filter, st);
+        VCT_CHECK_LAUNCH("trace views");
     }
     return VCT_OK;
 }

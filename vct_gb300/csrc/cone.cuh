@@ -94,14 +94,22 @@ __device__ __forceinline__ float4 sample_lod(const TraceParams& P, const int* of
                      lambda - fl);
     }
     if (MODE == VCT_FILTER_HYBRID && lambda > 0.0f && lambda < (float)q) {
-        // The finer level exactly, the coarser one (weight lambda - floor(lambda))
-        // by the texture units at its integral level.
+        // The level with the larger weight exactly, the other one by the
+        // texture units at its integral level: the texture units' fixed-point
+        // filter weights then enter the sample scaled by at most 1/2.  (The
+        // step's level is the same in every lane, so the branch is uniform.)
         const float fl = floorf(lambda);
         const int d1 = (int)fl;
-        const rgba2 fine = trilinear2(P, off, d1, p, warp_leaves_volume(P.warp.mode));
-        const float4 c = tex3DLod<float4>(P.tex, p.x, p.y, p.z, fl + 1.0f);
-        const rgba2 coarse = {make_float2(c.x, c.y), make_float2(c.z, c.w)};
-        return to_float4(lerp2(fine, coarse, lambda - fl));
+        const float f = lambda - fl;
+        const bool guard = warp_leaves_volume(P.warp.mode);
+        if (f <= 0.5f) {
+            const rgba2 fine = trilinear2(P, off, d1, p, guard);
+            const float4 c = tex3DLod<float4>(P.tex, p.x, p.y, p.z, fl + 1.0f);
+            return to_float4(lerp2(fine, {make_float2(c.x, c.y), make_float2(c.z, c.w)}, f));
+        }
+        const float4 c = tex3DLod<float4>(P.tex, p.x, p.y, p.z, fl);
+        const rgba2 coarse = trilinear2(P, off, d1 + 1, p, guard);
+        return to_float4(lerp2({make_float2(c.x, c.y), make_float2(c.z, c.w)}, coarse, f));
     }
     if (lambda <= 0.0f) {  // magnification: GL_NEAREST on level 0 (index S = border)
         const int S = P.dim;

@@ -46,6 +46,8 @@ struct vct_ctx {
     uint32_t* occ32 = nullptr;   // VCT_WARP_TEXTURE: 32^3 occupancy bit mask
     uint16_t* warpmap = nullptr; // VCT_WARP_TEXTURE: 32^3 RGBA16 unorm warp map
     float4* warpmap_f = nullptr; // its fp32 copy read by the lookups
+    uint32_t* carry = nullptr;   // the tessellation voxeliser's carry table (kCarrySlots entries)
+    uint32_t* brick_exact = nullptr;  // per 16^3 brick: flagged by the carry pass for the exact resolve
 };
 
 namespace vct {

@@ -1,7 +1,7 @@
 // Learned indirect light (the "learned" configuration): a cheap two-cone
 // quarter-resolution trace plus G-buffer features feed a small BF16 MLP
-// (42-64-64-64-3, FP32 accumulation) that predicts the 16-cone full-resolution
-// irradiance.  Inference and training run on the fifth-generation tensor
+// (42-64-64-64-4, FP32 accumulation) that predicts the 16-cone full-resolution
+// irradiance and an estimate of its own error there.  Inference and training run on the fifth-generation tensor
 // cores (tcgen05.mma, accumulators in TMEM; umma.cuh).
 //
 // Compiled with --fmad=false: the cone marching (cone.cuh) writes its fused
@@ -302,6 +302,48 @@ __global__ void __launch_bounds__(256) trace16_kernel(const LearnedParams P, int
     }
 }
 
+// The per-pixel fallback's list: every covered pixel whose error estimate
+// exceeds threshold x the frame's root-mean-square network irradiance over
+// covered pixels.  A warp scans an 8 x 4 pixel tile and appends its flagged
+// pixels with one atomic, so the list holds them in small 2D clusters whose
+// cones march through neighbouring voxels when the fallback traces them.
+__global__ void __launch_bounds__(256) learned_flag_kernel(const LearnedParams P) {
+    const int W = P.T.width, H = P.T.height, tiles_x = (W + 7) / 8;
+    const long long tile = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int x = (int)(tile % tiles_x) * 8 + (lane & 7), y = (int)(tile / tiles_x) * 4 + (lane >> 3);
+    const long long i = (long long)y * W + x;
+    const float n = P.frame_sums[1];
+    const float bound = P.threshold * sqrtf(n > 0.0f ? P.frame_sums[0] / n : 0.0f);
+    const bool fb = x < W && y < H && P.est[i] >= 0.0f && P.est[i] > bound;
+    const unsigned m = __ballot_sync(0xffffffffu, fb);
+    if (m) {
+        const int first = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == first) base = atomicAdd(P.count, (uint32_t)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, first);
+        if (fb) P.list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+    }
+}
+
+// 16-cone irradiance of the listed pixels (the per-pixel fallback), one
+// thread per list entry; the grid covers the longest possible list and
+// threads past the list's length return at once.
+__global__ void __launch_bounds__(256) trace16_pixels_kernel(const LearnedParams P) {
+    __shared__ int s_off[VCT_MAX_LEVELS];
+    __shared__ float s_dirs[16][4];
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((long long)blockIdx.x * blockDim.x >= (long long)*P.count) return;  // the whole CTA is past the list
+    level_offsets(P.T, s_off);
+    load_dirs(P, s_dirs);
+    __syncthreads();
+    if (i >= (long long)*P.count) return;
+    const long long pix = (long long)P.list[i];
+    unsigned ns = 0;
+    const float4 r = irradiance16(P, s_off, s_dirs, __ldg(P.T.gpos + pix), __ldg(P.T.gnrm + pix), ns);
+    P.out[pix] = make_float4(r.x, r.y, r.z, 0.0f);
+}
+
 // Per-tile error estimate of the network's output: the 16-cone irradiance at
 // four probe pixels of each 16x16 tile (offsets 4 and 12 on each axis) against
 // the network, relative L2 over the covered probes.  Tiles above the bound
@@ -447,6 +489,7 @@ __global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const Learn
     long long t = (long long)blockIdx.x * kInferGroups + grp;
     uint32_t f[24];
     bool covered = gather_features<ROWS>(P, t * 128 + row, f);
+    float sum_sq = 0.0f, n_cov = 0.0f;
     for (; t < ntiles && ok; t += stride) {
         const long long idx = t * 128 + row;
         const bool valid = idx < P.n, cov = covered;
@@ -456,7 +499,7 @@ __global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const Learn
                 make_uint4(f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3]);
         fence_async_smem();
         group_sync();
-        float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+        float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
 #pragma unroll 1
         for (int layer = 0; layer < 4; ++layer) {
             const int K = layer == 0 ? kMlpInPad : kMlpHidden;
@@ -497,17 +540,34 @@ __global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const Learn
                 o0 = v[0] + s_bias[3 * kMlpHidden];
                 o1 = v[1] + s_bias[3 * kMlpHidden + 1];
                 o2 = v[2] + s_bias[3 * kMlpHidden + 2];
+                o3 = v[3] + s_bias[3 * kMlpHidden + 3];
             }
         }
         if (!ok) break;
-        if (valid) {
-            if (ROWS) {
-                P.out_rows[idx * 3] = o0;
-                P.out_rows[idx * 3 + 1] = o1;
-                P.out_rows[idx * 3 + 2] = o2;
-            } else {
-                P.out[idx] = cov ? make_float4(o0, o1, o2, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (ROWS) {
+            if (valid) *reinterpret_cast<float4*>(P.out_rows + idx * 4) = make_float4(o0, o1, o2, o3);
+        } else {
+            if (valid) P.out[idx] = cov ? make_float4(o0, o1, o2, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (P.est && valid) {
+                // the per-pixel fallback's inputs: the error estimate (-1 for
+                // background) and the frame's sum of squared irradiance
+                P.est[idx] = cov ? o3 : -1.0f;
+                if (cov) {
+                    sum_sq += o0 * o0 + o1 * o1 + o2 * o2;
+                    n_cov += 1.0f;
+                }
             }
+        }
+    }
+    if (P.est) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sum_sq += __shfl_xor_sync(0xffffffffu, sum_sq, o);
+            n_cov += __shfl_xor_sync(0xffffffffu, n_cov, o);
+        }
+        if ((tid & 31) == 0 && n_cov > 0.0f) {
+            atomicAdd(P.frame_sums, sum_sq);
+            atomicAdd(P.frame_sums + 1, n_cov);
         }
     }
     if (!ok && leader) atomicOr(P.status, 1u);
@@ -526,7 +586,10 @@ __global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const Learn
 // row of ones below the features, so the same MMA also accumulates the bias
 // gradient.  At the end each CTA adds its TMEM gradients to the global fp32
 // gradient with fire-and-forget atomics.  Loss: mean squared error over the
-// n x 3 outputs.
+// n x 3 irradiance outputs, plus kMlpConfidenceWeight times the mean over the
+// n samples of (e - |y - t|)^2, where e is the fourth output (the error
+// estimate) and |y - t| the Euclidean error of the sample's irradiance, held
+// constant (no gradient flows from this term into the irradiance outputs).
 constexpr int kTrW = 0;
 constexpr int kTrA = kImgAll;                      // 128 x 64 A operand
 constexpr int kTrT = kTrA + 128 * 64 * 2;          // 4 transposed activation tiles, 128 x 128 each
@@ -550,7 +613,7 @@ __global__ void __launch_bounds__(128, 1) mlp_train_kernel(const TrainParams P) 
     __shared__ float s_bias[kBiasPad];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t s_tmem;
-    __shared__ float s_loss[4];
+    __shared__ float s_loss[4], s_closs[4];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     for (int i = tid; i < kImgAll / 16; i += 128)
         reinterpret_cast<uint4*>(smem + kTrW)[i] = __ldg(reinterpret_cast<const uint4*>(P.mlp.img) + i);
@@ -585,7 +648,7 @@ __global__ void __launch_bounds__(128, 1) mlp_train_kernel(const TrainParams P) 
     uint32_t phase = 0;
     int ok = 1;
     bool first = true;
-    float loss = 0.0f;
+    float loss = 0.0f, closs = 0.0f;
 
     // Issues nothing itself: waits for the MMAs committed by thread 0.
     auto wait_mma = [&]() -> int {
@@ -664,20 +727,27 @@ __global__ void __launch_bounds__(128, 1) mlp_train_kernel(const TrainParams P) 
         {
             float v[16];
             tmem_ld16(tmem_addr(tm + kColFb, warp, 0), v);
-            float d[3] = {0.f, 0.f, 0.f};
+            float d[4] = {0.f, 0.f, 0.f, 0.f};
             if (valid) {
+                float e2 = 0.0f;
 #pragma unroll
                 for (int o = 0; o < 3; ++o) {
                     const float diff = (v[o] + s_bias[3 * kMlpHidden + o]) - __ldg(P.targets + row * 3 + o);
                     loss += diff * diff;
+                    e2 += diff * diff;
                     d[o] = P.scale * diff;
                 }
+                // the error estimate's target |output - target| is a constant of the step
+                const float dc = (v[3] + s_bias[3 * kMlpHidden + 3]) - sqrtf(e2);
+                closs += dc * dc;
+                d[3] = P.conf_scale * dc;
             }
-            const uint32_t p01 = bf16x2(d[0], d[1]), p2 = bf16x2(d[2], 0.0f);
-            *reinterpret_cast<uint4*>(dy + tile_offset(tid, 0, 128)) = make_uint4(p01, p2, 0u, 0u);
+            const uint32_t p01 = bf16x2(d[0], d[1]), p23 = bf16x2(d[2], d[3]);
+            *reinterpret_cast<uint4*>(dy + tile_offset(tid, 0, 128)) = make_uint4(p01, p23, 0u, 0u);
             st_t(dyt, 0, tid, (uint16_t)(p01 & 0xFFFFu), 16);
             st_t(dyt, 1, tid, (uint16_t)(p01 >> 16), 16);
-            st_t(dyt, 2, tid, (uint16_t)(p2 & 0xFFFFu), 16);
+            st_t(dyt, 2, tid, (uint16_t)(p23 & 0xFFFFu), 16);
+            st_t(dyt, 3, tid, (uint16_t)(p23 >> 16), 16);
         }
         fence_async_smem();
         tc_sync();
@@ -757,11 +827,19 @@ __global__ void __launch_bounds__(128, 1) mlp_train_kernel(const TrainParams P) 
         }
     }
     // ---- loss
-    for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
-    if (lane == 0) s_loss[warp] = loss;
+    for (int o = 16; o > 0; o >>= 1) {
+        loss += __shfl_xor_sync(0xffffffffu, loss, o);
+        closs += __shfl_xor_sync(0xffffffffu, closs, o);
+    }
+    if (lane == 0) {
+        s_loss[warp] = loss;
+        s_closs[warp] = closs;
+    }
     if (!ok && tid == 0) atomicOr(P.status, 1u);
     tc_sync();
-    if (tid == 0) atomicAdd(P.mlp.loss, (s_loss[0] + s_loss[1] + s_loss[2] + s_loss[3]) * (0.5f * P.scale));
+    if (tid == 0)
+        atomicAdd(P.mlp.loss, (s_loss[0] + s_loss[1] + s_loss[2] + s_loss[3]) * (0.5f * P.scale) +
+                                  (s_closs[0] + s_closs[1] + s_closs[2] + s_closs[3]) * (0.5f * P.conf_scale));
     if (warp == 0) tmem_dealloc(tm, 512);
 }
 
@@ -862,6 +940,14 @@ void launch_trace16(const LearnedParams& P, bool listed, int num_sms, cudaStream
     const long long grid = listed ? cap : (tiles < cap * 4 ? tiles : cap * 4);
     trace16_kernel<<<(unsigned)(grid > 0 ? grid : 1), 256, 0, s>>>(P, listed ? 1 : 0);
     note_launches(1);
+}
+
+void launch_trace16_pixels(const LearnedParams& P, cudaStream_t s) {
+    const long long n = (long long)P.T.width * P.T.height;
+    const long long tiles = (long long)((P.T.width + 7) / 8) * ((P.T.height + 3) / 4);  // one warp each
+    learned_flag_kernel<<<(unsigned)((tiles + 7) / 8), 256, 0, s>>>(P);
+    trace16_pixels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P);
+    note_launches(2);
 }
 
 void launch_mlp_train(const TrainParams& P, int num_sms, cudaStream_t s) {

@@ -1,7 +1,7 @@
 // C ABI of the learned path (include/vct.h): the tensor-core GEMM check, the
 // MLP object (inference, gradients, Adam training steps) and the traces of
 // the learned configuration (cheap quarter-resolution features, the 16-cone
-// reference, the learned trace with its per-tile fallback).
+// reference, the learned trace with its per-tile or per-pixel fallback).
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -114,6 +114,51 @@ vct_status learned_setup(vct_ctx* c, const vct_gbuffer* g, const float eye[3], c
     return VCT_OK;
 }
 
+
+// The learned traces' scratch in the context: quarter-resolution features,
+// the per-tile error estimates, the fallback list (tiles, or pixels: one
+// entry per pixel of the frame), the per-pixel error estimates, the frame's
+// two sums and the list's length.
+vct_status learned_scratch(vct_ctx* c, long long W, long long H, LearnedParams& L) {
+    const long long tiles = ((W + kLearnTile - 1) / kLearnTile) * ((H + kLearnTile - 1) / kLearnTile);
+    const long long entries = tiles > W * H ? tiles : W * H;
+    auto a256 = [](long long b) { return (size_t)((b + 255) & ~255LL); };
+    const size_t qbytes = (size_t)L.wq * L.hq * kCheapFeatures * 2;
+    const size_t need = a256((long long)qbytes) + a256(tiles * 4) + a256(entries * 4) + a256(W * H * 4) + 256 + 256;
+    if (need > c->learned_bytes) {
+        if (c->learned) cudaFree(c->learned);
+        c->learned = nullptr;
+        c->learned_bytes = 0;
+        cudaError_t e = cudaMalloc(&c->learned, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(VCT_ERR_OUT_OF_MEMORY, std::string("learned scratch: ") + cudaGetErrorString(e));
+        }
+        c->learned_bytes = need;
+    }
+    char* p = static_cast<char*>(c->learned);
+    L.qfeat = reinterpret_cast<uint16_t*>(p);
+    p += a256((long long)qbytes);
+    L.tile_err = reinterpret_cast<float*>(p);
+    p += a256(tiles * 4);
+    L.list = reinterpret_cast<uint32_t*>(p);
+    p += a256(entries * 4);
+    L.est = reinterpret_cast<float*>(p);
+    p += a256(W * H * 4);
+    L.frame_sums = reinterpret_cast<float*>(p);
+    p += 256;
+    L.count = reinterpret_cast<uint32_t*>(p);
+    return VCT_OK;
+}
+
+vct_status learned_check(vct_ctx* c, vct_mlp* m, float* irradiance, float threshold) {
+    if (!c || !m || !irradiance) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (reinterpret_cast<uintptr_t>(irradiance) % 16 != 0) return fail(VCT_ERR_INVALID_ARGUMENT, "irradiance must be 16-byte aligned");
+    if (m->device != c->device) return fail(VCT_ERR_INVALID_ARGUMENT, "context and MLP live on different devices");
+    if (!(threshold >= 0.0f)) return fail(VCT_ERR_INVALID_ARGUMENT, "threshold must be >= 0 (infinity: no fallback)");
+    return VCT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -212,6 +257,7 @@ vct_status vct_mlp_get_params(vct_mlp* m, float* host, int64_t count, void* stre
 
 vct_status vct_mlp_forward(vct_mlp* m, const float* rows, int64_t n, float* out, void* stream) {
     if (!m || (n > 0 && !out)) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (reinterpret_cast<uintptr_t>(out) % 16 != 0) return fail(VCT_ERR_INVALID_ARGUMENT, "out must be 16-byte aligned");
     vct_status s = validate_rows(rows, n);
     if (s != VCT_OK) return s;
     DeviceScope ds(m->device);
@@ -245,6 +291,7 @@ static vct_status train_launch(vct_mlp* m, const float* rows, const float* targe
     P.index = index;
     P.n = n;
     P.scale = (float)(2.0 / (3.0 * (double)n));
+    P.conf_scale = (float)(2.0 * (double)kMlpConfidenceWeight / (double)n);
     P.status = m->status;
     launch_mlp_train(P, m->num_sms, st);
     VCT_CHECK_LAUNCH("mlp training kernel");
@@ -334,41 +381,57 @@ vct_status vct_trace_reference16(vct_ctx* c, const vct_gbuffer* g, const float e
     return VCT_OK;
 }
 
-vct_status vct_learned_trace(vct_ctx* c, vct_mlp* m, const vct_gbuffer* g, const float eye[3], float threshold,
-                             float* irradiance, vct_learned_stats* stats, void* stream) {
-    if (!c || !m || !irradiance) return fail(VCT_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (reinterpret_cast<uintptr_t>(irradiance) % 16 != 0) return fail(VCT_ERR_INVALID_ARGUMENT, "irradiance must be 16-byte aligned");
-    if (m->device != c->device) return fail(VCT_ERR_INVALID_ARGUMENT, "context and MLP live on different devices");
-    if (!(threshold >= 0.0f)) return fail(VCT_ERR_INVALID_ARGUMENT, "threshold must be >= 0 (infinity: no fallback)");
+
+vct_status vct_learned_trace_pixels(vct_ctx* c, vct_mlp* m, const vct_gbuffer* g, const float eye[3], float threshold,
+                                    float* irradiance, int64_t* fallback_pixels, void* stream) {
+    vct_status s = learned_check(c, m, irradiance, threshold);
+    if (s != VCT_OK) return s;
     DeviceScope ds(c->device);
     VCT_CUDA(ds.err);
     cudaStream_t st = as_stream(stream);
     LearnedParams L;
-    vct_status s = learned_setup(c, g, eye, st, L);
+    if ((s = learned_setup(c, g, eye, st, L)) != VCT_OK) return s;
+    if ((s = learned_scratch(c, g->width, g->height, L)) != VCT_OK) return s;
+    const bool fallback = !std::isinf(threshold);
+    L.img = m->dev.img;
+    L.bias = m->dev.bias;
+    L.n = (long long)g->width * g->height;
+    L.out = reinterpret_cast<float4*>(irradiance);
+    L.threshold = threshold;
+    L.status = m->status;
+    if (!fallback) L.est = nullptr;
+    VCT_CUDA(cudaMemsetAsync(L.count, 0, sizeof(uint32_t), st));
+    if (fallback) VCT_CUDA(cudaMemsetAsync(L.frame_sums, 0, 2 * sizeof(float), st));
+    launch_learned_features(L, st);
+    VCT_CHECK_LAUNCH("learned features");
+    launch_mlp_infer(L, m->num_sms, st);
+    VCT_CHECK_LAUNCH("mlp inference");
+    if (fallback) {
+        launch_trace16_pixels(L, st);
+        VCT_CHECK_LAUNCH("16-cone pixel fallback");
+    }
+    if (fallback_pixels) {
+        uint32_t count = 0;
+        VCT_CUDA(cudaMemcpyAsync(&count, L.count, sizeof count, cudaMemcpyDeviceToHost, st));
+        if ((s = check_status(m, st)) != VCT_OK) return s;
+        *fallback_pixels = fallback ? (int64_t)count : 0;
+    }
+    return VCT_OK;
+}
+
+vct_status vct_learned_trace(vct_ctx* c, vct_mlp* m, const vct_gbuffer* g, const float eye[3], float threshold,
+                             float* irradiance, vct_learned_stats* stats, void* stream) {
+    vct_status s = learned_check(c, m, irradiance, threshold);
     if (s != VCT_OK) return s;
+    DeviceScope ds(c->device);
+    VCT_CUDA(ds.err);
+    cudaStream_t st = as_stream(stream);
+    LearnedParams L;
+    if ((s = learned_setup(c, g, eye, st, L)) != VCT_OK) return s;
     const long long W = g->width, H = g->height;
     const long long tiles = ((W + kLearnTile - 1) / kLearnTile) * ((H + kLearnTile - 1) / kLearnTile);
-    const size_t qbytes = (size_t)L.wq * L.hq * kCheapFeatures * 2;
-    const size_t need = ((qbytes + 255) & ~(size_t)255) + ((tiles * 4 + 255) & ~255LL) * 2 + 256;
-    if (need > c->learned_bytes) {
-        if (c->learned) cudaFree(c->learned);
-        c->learned = nullptr;
-        c->learned_bytes = 0;
-        cudaError_t e = cudaMalloc(&c->learned, need);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return fail(VCT_ERR_OUT_OF_MEMORY, std::string("learned scratch: ") + cudaGetErrorString(e));
-        }
-        c->learned_bytes = need;
-    }
-    char* p = static_cast<char*>(c->learned);
-    L.qfeat = reinterpret_cast<uint16_t*>(p);
-    p += (qbytes + 255) & ~(size_t)255;
-    L.tile_err = reinterpret_cast<float*>(p);
-    p += (tiles * 4 + 255) & ~255LL;
-    L.list = reinterpret_cast<uint32_t*>(p);
-    p += (tiles * 4 + 255) & ~255LL;
-    L.count = reinterpret_cast<uint32_t*>(p);
+    if ((s = learned_scratch(c, W, H, L)) != VCT_OK) return s;
+    L.est = nullptr;
     L.img = m->dev.img;
     L.bias = m->dev.bias;
     L.n = W * H;

@@ -143,6 +143,7 @@ extern "C" vct_status vct_voxelize_static(const vct_config* cfg, const vct_param
     N.decay = params->temporal_decay;
     N.acc = acc;
     N.occ = occ;
+    N.brick_exact = nullptr;  // the rasterising voxeliser only: no carry pass
     N.color = reinterpret_cast<uint2*>(color_dev);
     N.normal = reinterpret_cast<uint2*>(normal_dev);
     N.radiance = reinterpret_cast<uint2*>(radiance_dev);

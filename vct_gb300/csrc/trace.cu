@@ -194,4 +194,8 @@ void launch_trace_batch(const SceneBatch<TraceParams>& B, int filter, long long 
     launch_trace_set(ManyScenes<TraceParams>{B}, filter, tiles, s);
 }
 
+void launch_trace_views(const ViewSet& V, int filter, cudaStream_t s) {
+    launch_trace_set(FewScenes{V}, filter, V.off[V.n], s);
+}
+
 }  // namespace vct

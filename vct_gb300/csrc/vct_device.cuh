@@ -16,6 +16,35 @@
 
 namespace vct {
 
+// ---- the carry table of exact accumulation (vct_internal.h, kCarrySlots)
+__device__ __forceinline__ uint32_t carry_slot(uint32_t v, int probe) {
+    return (((v * 2654435761u) >> (32 - kCarrySlotsLog2)) + (uint32_t)probe) & (uint32_t)(kCarrySlots - 1);
+}
+// Adds the crossings ev[] of voxel v to its entry (claimed on first use).
+__device__ __forceinline__ void carry_add(uint32_t* table, uint32_t v, const uint32_t (&ev)[kCarryEvents],
+                                          StatsDev* stats) {
+    const uint32_t key = v + 1u;
+    for (int i = 0; i < kCarryProbes; ++i) {
+        uint32_t* e = table + 8 * carry_slot(v, i);
+        const uint32_t k = atomicCAS(e, 0u, key);
+        if (k == 0u || k == key) {
+#pragma unroll
+            for (int f = 0; f < kCarryEvents; ++f)
+                if (ev[f]) atomicAdd(e + 1 + f, ev[f]);
+            return;
+        }
+    }
+    atomicOr(&stats->error_flags, VCT_STATS_COUNT_OVERFLOW);
+}
+// Whether adding `a` to the 64-bit word whose value was `o` carried out of
+// the low 32-bit field, and whether the high field (with that carry) wrapped.
+__device__ __forceinline__ uint32_t carry_lo(unsigned long long o, unsigned long long a) {
+    return (uint32_t)(((o & 0xffffffffull) + (a & 0xffffffffull)) >> 32);
+}
+__device__ __forceinline__ uint32_t wrap_hi(unsigned long long o, unsigned long long a) {
+    return (uint32_t)(((o >> 32) + (a >> 32) + carry_lo(o, a)) >> 32);
+}
+
 __device__ __forceinline__ f3 mk(float x, float y, float z) { return {x, y, z}; }
 __device__ __forceinline__ f3 add(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
 __device__ __forceinline__ f3 sub(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
@@ -236,6 +265,19 @@ struct ManyScenes {
         }
         local = w - __ldg(b.off + lo);
         return lo;
+    }
+};
+
+// The viewpoints of a ViewSet (at most kMaxViews): found by a linear scan.
+struct FewScenes {
+    ViewSet v;
+    __device__ __forceinline__ int count() const { return v.n; }
+    __device__ __forceinline__ const TraceParams& get(int s) const { return v.p[s]; }
+    __device__ __forceinline__ int find(long long w, long long& local) const {
+        int s = 0;
+        while (s + 1 < v.n && v.off[s + 1] <= w) ++s;
+        local = w - v.off[s];
+        return s;
     }
 };
 

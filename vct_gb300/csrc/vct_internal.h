@@ -77,6 +77,8 @@ struct AccumParams {
     int sw, sh;
     uint32_t* acc;  // accumulator records, kAccWords uint32 per voxel
     uint32_t* occ;  // occupancy bit mask, one bit per voxel
+    uint32_t* carry;  // tessellation voxeliser: crossings of 2^32 per record field (kCarrySlots entries), or nullptr
+    uint32_t* brick_exact;  // with `carry`: per 16^3 brick, set by the carry pass for the bricks it rewrote
     StatsDev* stats;
     int num_sms;
     int unit_log2;      // log2 of the bounding-box pixels per work unit
@@ -131,8 +133,28 @@ void accumulate_bind_scratch(AccumParams& P, void* scratch);
 // Sums are of 16-bit fixed point (round(x * 65535)); they are updated as
 // four 64-bit atomics whose low halves (count, g, nx, nz) never carry into
 // the high halves while a voxel receives fewer than VCT_MAX_EXACT_FRAGMENTS
-// fragments, so the record then equals seven independent 32-bit sums.
+// fragments, so the record then equals seven independent 32-bit sums.  The
+// last word's high half only ever receives nz's carries, so {nz, pad} is
+// nz's exact 64-bit sum.
 constexpr int kAccWords = 8;
+
+// Exact sums past VCT_MAX_EXACT_FRAGMENTS (the tessellation voxeliser, whose
+// slivers put up to ~10^5 points into one voxel): every 64-bit add returns
+// the word's old value, from which the adder sees whether its low field
+// crossed 2^32 (a carry into the high field) and whether the high field
+// wrapped.  Such crossings (rare: only voxels past 65,536 points have them)
+// are counted per voxel in an open-addressing table of kCarrySlots entries
+// {voxel + 1, r wraps, g carries, b wraps, nx carries, ny wraps, nz carries,
+// 0}.  After the voxeliser, a carry pass rebuilds each listed voxel's six
+// 64-bit sums and rewrites its record: the sums' float values (the value
+// the resolve divides) in the six sum fields and bit 31 set in the count;
+// it flags the voxel's 16^3 brick, which a second instantiation of the
+// resolve handles (the common one skips it).
+// A table with no free slot within kCarryProbes probes raises
+// VCT_STATS_COUNT_OVERFLOW.
+constexpr int kCarrySlotsLog2 = 16, kCarrySlots = 1 << kCarrySlotsLog2, kCarryProbes = 64;
+constexpr long long kCarryBytes = (long long)kCarrySlots * 8 * 4;
+constexpr int kCarryEvents = 6;
 
 struct NormalizeParams {
     int dim;
@@ -141,6 +163,7 @@ struct NormalizeParams {
     float decay;
     uint32_t* acc;
     const uint32_t* occ;
+    const uint32_t* brick_exact;  // per 16^3 brick: the carry pass rewrote one of its records; nullptr: no carry pass
     uint2* color;     // level 0 of the colour volume
     uint2* normal;
     uint2* radiance;  // level 0 of the radiance chain
@@ -219,6 +242,16 @@ struct TraceParams {
     WarpDev warp;
 };
 
+// Several viewpoints of one volume traced by one launch (vct_trace_views):
+// the views' parameters travel in kernel-parameter space, `off` is the
+// exclusive prefix sum of their pixel tiles.
+constexpr int kMaxViews = 8;
+struct ViewSet {
+    TraceParams p[kMaxViews];
+    long long off[kMaxViews + 1];
+    int n;
+};
+
 struct ShadowRasterParams {
     const float* pos;
     long long ntri;
@@ -278,16 +311,21 @@ void launch_accumulate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W,
                              cudaStream_t s);
 void launch_tesselate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, int num_sms, cudaStream_t s);
 void launch_inject_mark_batch(const SceneBatch<InjectParams>& B, long long ntexels, cudaStream_t s);
-void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks, cudaStream_t s);
+void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks, bool exact, cudaStream_t s);
 void launch_mip_tail_batch(const SceneBatch<MipLevels>& B, cudaStream_t s);
 long long trace_tiles(int width, int height, int tile_w_log2, int tile_h_log2);
 void launch_trace_batch(const SceneBatch<TraceParams>& B, int filter, long long tiles, cudaStream_t s);
+void launch_trace_views(const ViewSet& V, int filter, cudaStream_t s);
 // ------------------------------------------------------------- learned path
-// MLP 42-64-64-64-3.  Packed fp32 parameters: W1[64][42] b1[64] W2[64][64]
-// b2[64] W3[64][64] b3[64] W4[3][64] b4[3].
-constexpr int kMlpIn = 42, kMlpInPad = 48, kMlpHidden = 64, kMlpOut = 3, kMlpOutPad = 16;
+// MLP 42-64-64-64-4: irradiance RGB and the network's estimate of its own
+// error.  Packed fp32 parameters: W1[64][42] b1[64] W2[64][64] b2[64]
+// W3[64][64] b3[64] W4[4][64] b4[4].
+constexpr int kMlpIn = 42, kMlpInPad = 48, kMlpHidden = 64, kMlpOut = 4, kMlpOutPad = 16;
 constexpr int kOffW1 = 0, kOffB1 = 2688, kOffW2 = 2752, kOffB2 = 6848, kOffW3 = 6912, kOffB3 = 11008,
-              kOffW4 = 11072, kOffB4 = 11264, kMlpParams = 11267;
+              kOffW4 = 11072, kOffB4 = 11328, kMlpParams = 11332;
+// Weight of the error-estimate term in the training loss (relative to the
+// mean squared error of the irradiance).
+constexpr float kMlpConfidenceWeight = 0.5f;
 // BF16 operand images in the tensor core's shared-memory tile layout:
 // forward B operands W1 (64 x 48), W2, W3 (64 x 64), W4 (16 x 64), then the
 // transposes used by the backward pass W4^T (64 x 16), W3^T, W2^T (64 x 64).
@@ -325,10 +363,12 @@ struct LearnedParams {
     float4* out;               // irradiance per pixel
     const int* pixels;         // rows kernel: pixel indices
     float* rows_out;           // rows kernel: n x 42
-    float threshold;           // per-tile relative error bound
+    float threshold;           // per-tile relative error bound, or the per-pixel bound relative to the frame's RMS
     float* tile_err;           // per 16x16 tile
-    uint32_t* list;            // fallback tiles; list[-1] is not used: count at `count`
+    uint32_t* list;            // fallback tiles or pixels; their count at `count`
     uint32_t* count;
+    float* est;                // per pixel: the network's error estimate (-1: background), or nullptr
+    float* frame_sums;         // sum of squared network irradiance over covered pixels, covered pixels
     uint32_t* status;
 };
 
@@ -338,7 +378,8 @@ struct TrainParams {
     const float* targets;  // n x 3
     const int* index;      // optional permutation of rows
     long long n;
-    float scale;           // 2 / (3 n)
+    float scale;           // 2 / (3 n): d loss / d irradiance output = scale * (output - target)
+    float conf_scale;      // 2 w / n: d loss / d error estimate = conf_scale * (estimate - |output - target|)
     uint32_t* status;
 };
 
@@ -347,6 +388,9 @@ void launch_learned_rows(const LearnedParams& P, cudaStream_t s);
 void launch_mlp_infer(const LearnedParams& P, int num_sms, cudaStream_t s);
 void launch_learned_probe(const LearnedParams& P, cudaStream_t s);
 void launch_trace16(const LearnedParams& P, bool listed, int num_sms, cudaStream_t s);
+// The per-pixel fallback after inference with `est` set: the list of flagged
+// pixels, then their 16-cone trace.
+void launch_trace16_pixels(const LearnedParams& P, cudaStream_t s);
 void launch_mlp_train(const TrainParams& P, int num_sms, cudaStream_t s);
 void launch_mlp_update(const MlpDev& M, int step, float lr, float beta1, float beta2, float eps, int update,
                        cudaStream_t s);

@@ -171,13 +171,19 @@ __device__ __forceinline__ void brick_mips(uint2* s0, uint2* s1, int nlev, uint2
 //                result equals normalise; inject; filter because the value
 //                injectRadiance stores into a voxel depends only on that
 //                voxel (its stores are idempotent).
-template <bool FUSED, class Scenes>
+//
+// EXACT = false: every brick the carry pass did not flag (all of them for
+// the rasterising voxeliser).  EXACT = true: only the flagged bricks, whose
+// rewritten records hold their sums' float values (bit 31 of the count);
+// a separate instantiation so that the common path keeps its registers.
+template <bool FUSED, bool EXACT, class Scenes>
 __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
     __shared__ uint2 s0[FUSED ? kBrickVox : 1];
     __shared__ uint2 s1[FUSED ? kBrickVox / 8 : 1];
     long long brick;
     const ResolveParams& R = S.get(S.find(blockIdx.x, brick));
     const NormalizeParams& P = R.norm;
+    if ((P.brick_exact ? P.brick_exact[brick] != 0u : false) != EXACT) return;  // the other pass's brick
     const int N = P.dim;
     const int bpa = N / kBrick;
     const int bx = (int)(brick % bpa), by = (int)((brick / bpa) % bpa), bz = (int)(brick / (bpa * bpa));
@@ -214,7 +220,10 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
         uint2 col[4], nrm[4], rad[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const uint32_t c = rec[j][0].x;
+            // EXACT: bit 31 of the count says the six sums hold the float values
+            // of their 64-bit sums (records the carry pass rewrote)
+            const bool fbits = EXACT && (rec[j][0].x >> 31) != 0u;
+            const uint32_t c = EXACT ? rec[j][0].x & 0x7fffffffu : rec[j][0].x;
             float alpha = 0.0f;
             col[j] = make_uint2(0u, 0u);
             nrm[j] = make_uint2(0u, 0u);
@@ -224,16 +233,24 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
                              : "memory");
                 ++uniq;
                 mx = max(mx, c);
-                if (c >= VCT_MAX_EXACT_FRAGMENTS) flags |= VCT_STATS_COUNT_OVERFLOW;
                 // transferVoxels.comp:37-51: colour / count, opacity override.
                 const float denom = 65535.0f * __uint2float_rn(c);
                 alpha = P.opacity > 0.0f ? P.opacity : 1.0f;
-                col[j] = pack_h4(__fdiv_rn(__uint2float_rn(rec[j][0].y), denom),
-                                 __fdiv_rn(__uint2float_rn(rec[j][0].z), denom),
-                                 __fdiv_rn(__uint2float_rn(rec[j][0].w), denom), alpha);
-                nrm[j] = pack_h4(__fdiv_rn(__uint2float_rn(rec[j][1].x), denom),
-                                 __fdiv_rn(__uint2float_rn(rec[j][1].y), denom),
-                                 __fdiv_rn(__uint2float_rn(rec[j][1].z), denom), 1.0f);
+                if (c >= VCT_MAX_EXACT_FRAGMENTS && !P.brick_exact) flags |= VCT_STATS_COUNT_OVERFLOW;
+                if (EXACT) {
+                    auto sum = [fbits](uint32_t f) { return fbits ? __uint_as_float(f) : __uint2float_rn(f); };
+                    col[j] = pack_h4(__fdiv_rn(sum(rec[j][0].y), denom), __fdiv_rn(sum(rec[j][0].z), denom),
+                                     __fdiv_rn(sum(rec[j][0].w), denom), alpha);
+                    nrm[j] = pack_h4(__fdiv_rn(sum(rec[j][1].x), denom), __fdiv_rn(sum(rec[j][1].y), denom),
+                                     __fdiv_rn(sum(rec[j][1].z), denom), 1.0f);
+                } else {
+                    col[j] = pack_h4(__fdiv_rn(__uint2float_rn(rec[j][0].y), denom),
+                                     __fdiv_rn(__uint2float_rn(rec[j][0].z), denom),
+                                     __fdiv_rn(__uint2float_rn(rec[j][0].w), denom), alpha);
+                    nrm[j] = pack_h4(__fdiv_rn(__uint2float_rn(rec[j][1].x), denom),
+                                     __fdiv_rn(__uint2float_rn(rec[j][1].y), denom),
+                                     __fdiv_rn(__uint2float_rn(rec[j][1].z), denom), 1.0f);
+                }
             }
             // transferVoxels.comp:53-62: radiance seed.
             if (P.temporal) {
@@ -565,7 +582,11 @@ void launch_normalize(const NormalizeParams& P, cudaStream_t s) {
     memset(&R, 0, sizeof R);
     R.norm = P;
     const int bpa = P.dim / kBrick;
-    resolve_kernel<false><<<bpa * bpa * bpa, kThreads, 0, s>>>(OneScene<ResolveParams>{R});
+    resolve_kernel<false, false><<<bpa * bpa * bpa, kThreads, 0, s>>>(OneScene<ResolveParams>{R});
+    if (P.brick_exact) {
+        resolve_kernel<false, true><<<bpa * bpa * bpa, kThreads, 0, s>>>(OneScene<ResolveParams>{R});
+        note_launches(1);
+    }
     note_launches(1);
 }
 
@@ -608,7 +629,11 @@ void launch_inject_mark(const InjectParams& P, cudaStream_t s) {
 
 void launch_resolve(const ResolveParams& R, cudaStream_t s) {
     const int bpa = R.norm.dim / kBrick;
-    resolve_kernel<true><<<bpa * bpa * bpa, kThreads, 0, s>>>(OneScene<ResolveParams>{R});
+    resolve_kernel<true, false><<<bpa * bpa * bpa, kThreads, 0, s>>>(OneScene<ResolveParams>{R});
+    if (R.norm.brick_exact) {
+        resolve_kernel<true, true><<<bpa * bpa * bpa, kThreads, 0, s>>>(OneScene<ResolveParams>{R});
+        note_launches(1);
+    }
     note_launches(1);
 }
 
@@ -640,8 +665,12 @@ void launch_inject_mark_batch(const SceneBatch<InjectParams>& B, long long ntexe
     note_launches(1);
 }
 
-void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks, cudaStream_t s) {
-    resolve_kernel<true><<<(unsigned)nbricks, kThreads, 0, s>>>(ManyScenes<ResolveParams>{B});
+void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks, bool exact, cudaStream_t s) {
+    resolve_kernel<true, false><<<(unsigned)nbricks, kThreads, 0, s>>>(ManyScenes<ResolveParams>{B});
+    if (exact) {
+        resolve_kernel<true, true><<<(unsigned)nbricks, kThreads, 0, s>>>(ManyScenes<ResolveParams>{B});
+        note_launches(1);
+    }
     note_launches(1);
 }
 

@@ -646,12 +646,54 @@ __device__ __forceinline__ void tess_store32(const Scenes& S, const TessQueue& q
         qz += pz;
     }
     unsigned long long* rec = reinterpret_cast<unsigned long long*>(P.acc + (long long)kAccWords * v);
-    const unsigned long long was = atomicAdd(rec + 0, cnt | ((unsigned long long)qr << 32));
-    atomicAdd(rec + 1, (unsigned long long)qg | ((unsigned long long)qb << 32));
-    atomicAdd(rec + 2, (unsigned long long)qx | ((unsigned long long)qy << 32));
-    atomicAdd(rec + 3, (unsigned long long)qz);
+    const unsigned long long a0 = cnt | ((unsigned long long)qr << 32);
+    const unsigned long long a1 = (unsigned long long)qg | ((unsigned long long)qb << 32);
+    const unsigned long long a2 = (unsigned long long)qx | ((unsigned long long)qy << 32);
+    const unsigned long long was = atomicAdd(rec + 0, a0);
+    if (P.carry) {
+        // Exact past 65,536 points: the old values show every crossing of
+        // 2^32 by a field (the count itself never gets near one).
+        const unsigned long long w1 = atomicAdd(rec + 1, a1), w2 = atomicAdd(rec + 2, a2),
+                                 w3 = atomicAdd(rec + 3, (unsigned long long)qz);
+        const uint32_t ev[kCarryEvents] = {wrap_hi(was, a0), carry_lo(w1, a1), wrap_hi(w1, a1),
+                                           carry_lo(w2, a2), wrap_hi(w2, a2), carry_lo(w3, qz)};
+        if (ev[0] | ev[1] | ev[2] | ev[3] | ev[4] | ev[5]) carry_add(P.carry, v, ev, P.stats);
+    } else {
+        atomicAdd(rec + 1, a1);
+        atomicAdd(rec + 2, a2);
+        atomicAdd(rec + 3, (unsigned long long)qz);
+    }
     // The voxel's occupancy bit, once: by the store that found its count at 0.
     if ((was & 0xffffffffull) == 0ull) atomicOr(P.occ + (v >> 5), 1u << (v & 31));
+}
+
+// The carry pass: every voxel listed in a scene's carry table gets its six
+// 64-bit sums rebuilt from its record and its crossings of 2^32, its record
+// rewritten with their float values (the resolve's dividend) and bit 31 of
+// the count set, and its brick flagged for the resolve's exact pass.  One
+// thread per table slot, blockIdx.y the scene.
+template <class Scenes>
+__global__ void __launch_bounds__(256) carry_fixup_kernel(const Scenes S) {
+    const AccumParams& P = S.get(blockIdx.y);
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!P.carry || slot >= kCarrySlots) return;
+    const uint32_t* e = P.carry + 8 * slot;
+    if (e[0] == 0u) return;
+    const long long v = (long long)e[0] - 1;
+    uint4* r = reinterpret_cast<uint4*>(P.acc + (long long)kAccWords * v);
+    const uint4 r0 = r[0], r1 = r[1];
+    const unsigned long long t = 1ull << 32;
+    // {count | r}, {g | b}, {nx | ny}, {nz | nz's carries}: a high field holds
+    // its own sum plus the low field's carries, modulo 2^32
+    const unsigned long long sr = r0.y + t * e[1], sg = r0.z + t * e[2], sb = r0.w + t * e[3] - e[2],
+                             sx = r1.x + t * e[4], sy = r1.y + t * e[5] - e[4], sz = r1.z + t * r1.w;
+    r[0] = make_uint4(r0.x | 0x80000000u, __float_as_uint(__ull2float_rn(sr)), __float_as_uint(__ull2float_rn(sg)),
+                      __float_as_uint(__ull2float_rn(sb)));
+    r[1] = make_uint4(__float_as_uint(__ull2float_rn(sx)), __float_as_uint(__ull2float_rn(sy)),
+                      __float_as_uint(__ull2float_rn(sz)), 0u);
+    const long long N = P.dim, bpa = N / 16;  // the voxel's 16^3 brick, in the resolve's brick order
+    const long long x = v % N, y = (v / N) % N, z = v / (N * N);
+    P.brick_exact[((z / 16) * bpa + y / 16) * bpa + x / 16] = 1u;
 }
 
 template <class Scenes>
@@ -750,10 +792,16 @@ void launch_tess(const Scenes& S, const VoxWork& W, int num_sms, cudaStream_t s)
 void launch_tesselate(const AccumParams& P, cudaStream_t s) {
     const VoxWork W = {P.tri_rec, P.tri_units, P.tri_scan, P.block_off, P.ntri, 0};
     launch_tess(OneScene<AccumParams>{P}, W, P.num_sms, s);
+    if (P.carry) {
+        carry_fixup_kernel<<<dim3(kCarrySlots / 256, 1), 256, 0, s>>>(OneScene<AccumParams>{P});
+        note_launches(1);
+    }
 }
 
 void launch_tesselate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, int num_sms, cudaStream_t s) {
     launch_tess(ManyScenes<AccumParams>{B}, W, num_sms, s);
+    carry_fixup_kernel<<<dim3(kCarrySlots / 256, B.n), 256, 0, s>>>(ManyScenes<AccumParams>{B});
+    note_launches(1);
 }
 
 void accumulate_bind_scratch(AccumParams& P, void* scratch) {

@@ -5,7 +5,9 @@ features into the 16-cone full-resolution irradiance.
 Everything runs on the GPU through the C ABI (include/vct.h): scenes are
 voxelised, injected and filtered by the frame kernels, the 16-cone targets
 come from vct_trace_reference16, feature rows from vct_learned_rows, and the
-network trains with the tensor-core kernels behind vct_mlp_train_step.
+network (irradiance and an estimate of its own error, which drives the
+per-pixel fallback) trains with the tensor-core kernels behind
+vct_mlp_train_step.
 torch only allocates device memory and draws random permutations.
 
     python -m vct_gb300.learned train --scenes 2000 --holdout 200 --out vct_gb300/weights/learned_mlp
@@ -179,19 +181,27 @@ def train(mlp: api.Mlp, rows, targets, epochs: int = 20, batch: int = 16384, lr:
     return hist
 
 
-def evaluate(mlp: api.Mlp, state: FrameState, seeds, kw: dict, threshold: float = 0.02, workers: int = 0,
-             log=None) -> dict:
-    """Per held-out scene: relative L2 irradiance error of the network alone,
-    of the network with the per-tile fallback, and of the cheap two-cone
-    estimate, all against the 16-cone trace; plus the fallback fraction."""
-    import torch
+# Per-pixel fallback bounds (error estimate / the frame's RMS irradiance) evaluated on held-out scenes.
+PIXEL_THRESHOLDS = (0.02, 0.03, 0.05, 0.1, 0.2, 0.5)
 
+
+def evaluate(mlp: api.Mlp, state: FrameState, seeds, kw: dict, threshold: float = 0.02, workers: int = 0,
+             log=None, pixel_thresholds=PIXEL_THRESHOLDS) -> dict:
+    """Per held-out scene: relative L2 irradiance error of the network alone,
+    of the network with the per-tile fallback, of the network with the
+    per-pixel fallback at each bound, and of the cheap two-cone estimate, all
+    against the 16-cone trace; plus the fallback fractions (of tiles, and of
+    covered pixels)."""
     res = {"network": [], "with_fallback": [], "cheap": [], "fallback_fraction": [], "est_tile_error": []}
+    for t in pixel_thresholds:
+        res[f"pixel_{t}"] = []
+        res[f"pixel_{t}_fraction"] = []
     for i, sc in enumerate(scene_stream(seeds, kw, workers)):
         state.load(sc)
         state.reference()
         state.features()
         mask = state.covered()
+        ncov = max(1, int(mask.sum()))
         truth = state.ref.view(-1, 4)[:, :3]
         api.learned_trace(state.ctx, mlp, state.gb, sc.eye, state.out, float("inf"))
         res["network"].append(rel_l2(state.out.view(-1, 4)[:, :3], truth, mask))
@@ -199,6 +209,10 @@ def evaluate(mlp: api.Mlp, state: FrameState, seeds, kw: dict, threshold: float 
         res["with_fallback"].append(rel_l2(state.out.view(-1, 4)[:, :3], truth, mask))
         res["fallback_fraction"].append(st["fallback_tiles"] / st["tiles"])
         res["est_tile_error"].append(st["mean_tile_error"])
+        for t in pixel_thresholds:
+            n = api.learned_trace_pixels(state.ctx, mlp, state.gb, sc.eye, state.out, t, want_count=True)
+            res[f"pixel_{t}"].append(rel_l2(state.out.view(-1, 4)[:, :3], truth, mask))
+            res[f"pixel_{t}_fraction"].append(n / ncov)
         res["cheap"].append(rel_l2(state.cheap_irradiance(), truth, mask))
         if log and (i + 1) % 50 == 0:
             log(f"eval: {i + 1}/{len(seeds)}: network {np.mean(res['network']):.4f} fallback "

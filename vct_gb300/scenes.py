@@ -308,6 +308,26 @@ def tiny(seed: int = 0, dim: int = 16, shadow: int = 64, gbuffer=(48, 32), n_box
                    tuple(gbuffer), BASELINE_CONES)
 
 
+def stacked_slivers(copies: int = 1600, seed: int = 0, dim: int = 64, shadow: int = 64,
+                    gbuffer=(64, 36)) -> Scene:
+    """`copies` coincident long thin triangles (a sliver along x inside one
+    row of voxels, each copy with its own albedo): the tessellation
+    voxeliser puts ~48 points per copy into each voxel of the row, so with
+    more than ~1,400 copies a voxel receives more than 65,536 points and its
+    sums pass 2^32."""
+    rng = np.random.default_rng(seed)
+    tri = np.array([[-0.9, 0.010, 0.013], [0.9, 0.010, 0.013], [0.9, 0.012, 0.0135]], dtype=np.float64)
+    n = np.cross(tri[1] - tri[0], tri[2] - tri[0])
+    n /= np.linalg.norm(n)
+    tris = np.repeat(tri[None], copies, 0)
+    nrms = np.repeat(np.repeat(n[None, None], 3, 1), copies, 0)
+    alb = rng.uniform(0, 1, size=(copies, 3))
+    light, ls = _directional_light(rng, 1.0)
+    levels = int(np.log2(dim)) + 1
+    return _finish("slivers", tris, nrms, alb, [light], ls, dim, levels, 1.0, (shadow, shadow),
+                   np.array([0.0, 0.5, 2.5]), np.zeros(3), 50 * DEG, tuple(gbuffer), BASELINE_CONES)
+
+
 # Batched scene family: per scene a triangle count log-uniform in [1k, 200k]
 # (rotated boxes of log-uniform size), a grid from {64, 128, 256}^3, a 16:9
 # G-buffer from 320x180 to 1920x1080 and 1-4 lights (one directional shadow
