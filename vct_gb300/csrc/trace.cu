@@ -65,7 +65,6 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const Scenes S) {
         const float4 gp = __ldg(P.gpos + pix);
         if (gp.w != 0.0f) {
             const float4 gn = __ldg(P.gnrm + pix);
-            const float4 ga = __ldg(P.galb + pix);
             const f3 N = fnormalize(mk(gn.x, gn.y, gn.z));
             f3 rgb;
             if (P.enable_indirect) {
@@ -94,15 +93,20 @@ __global__ void __launch_bounds__(256, 4) trace_kernel(const Scenes S) {
                 const float occ = 1.0f - clampf(ind.w, 0.0f, 1.0f);
                 rgb = mk(ind.x, ind.y, ind.z);
                 if (P.enable_reflections) {
-                    const f3 I = sub(mk(gp.x, gp.y, gp.z), P.eye);
+                    // the position is read again rather than kept live across the diffuse cones
+                    const float4 gq = __ldg(P.gpos + pix);
+                    const f3 I = sub(mk(gq.x, gq.y, gq.z), P.eye);
                     const f3 R = sub(I, mul(N, 2.0f * dot(N, I)));
                     spc = trace_cone<MODE>(P, s_off, vp, N, R, P.specular_cone, P.max_distance, ns, s_tan[1]);
                     rgb = add(rgb, mul(mk(spc.x, spc.y, spc.z), P.reflect_scale));
                 }
+                // the albedo is loaded after the cones: it is not live across them
+                const float4 ga = __ldg(P.galb + pix);
                 const float as = P.ambient_scale;
                 rgb = mk(rgb.x * (as * ga.x), rgb.y * (as * ga.y), rgb.z * (as * ga.z));
                 if (P.draw_occlusion) rgb = mul(rgb, occ);
             } else {
+                const float4 ga = __ldg(P.galb + pix);
                 rgb = mk(P.ambient_scale * ga.x, P.ambient_scale * ga.y, P.ambient_scale * ga.z);
             }
             if (P.enable_postprocess) {
