@@ -144,8 +144,9 @@ constexpr int kAccWords = 8;
 // crossed 2^32 (a carry into the high field) and whether the high field
 // wrapped.  Such crossings (rare: only voxels past 65,536 points have them)
 // are counted per voxel in an open-addressing table of kCarrySlots entries
-// {voxel + 1, r wraps, g carries, b wraps, nx carries, ny wraps, nz carries,
-// 0}.  After the voxeliser, a carry pass rebuilds each listed voxel's six
+// {voxel + 1, r wraps, g carries, b wraps, nx carries, ny wraps, 0, 0}; nz's
+// carries need no count (they accumulate in the last word's high half), and
+// every voxel past 65,536 points is listed, crossing or not.  After the voxeliser, a carry pass rebuilds each listed voxel's six
 // 64-bit sums and rewrites its record: the sums' float values (the value
 // the resolve divides) in the six sum fields and bit 31 set in the count;
 // it flags the voxel's 16^3 brick, which a second instantiation of the
@@ -154,7 +155,7 @@ constexpr int kAccWords = 8;
 // VCT_STATS_COUNT_OVERFLOW.
 constexpr int kCarrySlotsLog2 = 16, kCarrySlots = 1 << kCarrySlotsLog2, kCarryProbes = 64;
 constexpr long long kCarryBytes = (long long)kCarrySlots * 8 * 4;
-constexpr int kCarryEvents = 6;
+constexpr int kCarryEvents = 5;
 
 struct NormalizeParams {
     int dim;

@@ -652,12 +652,18 @@ __device__ __forceinline__ void tess_store32(const Scenes& S, const TessQueue& q
     const unsigned long long was = atomicAdd(rec + 0, a0);
     if (P.carry) {
         // Exact past 65,536 points: the old values show every crossing of
-        // 2^32 by a field (the count itself never gets near one).
-        const unsigned long long w1 = atomicAdd(rec + 1, a1), w2 = atomicAdd(rec + 2, a2),
-                                 w3 = atomicAdd(rec + 3, (unsigned long long)qz);
+        // 2^32 by r, g, b, nx and ny (the count itself never gets near one;
+        // nz's carries land in the last word's unused high half).  The store
+        // that takes the count past 65,536 lists the voxel even without a
+        // crossing, so that the carry pass rewrites every voxel whose nz may
+        // have carried.
+        const unsigned long long w1 = atomicAdd(rec + 1, a1), w2 = atomicAdd(rec + 2, a2);
+        atomicAdd(rec + 3, (unsigned long long)qz);
         const uint32_t ev[kCarryEvents] = {wrap_hi(was, a0), carry_lo(w1, a1), wrap_hi(w1, a1),
-                                           carry_lo(w2, a2), wrap_hi(w2, a2), carry_lo(w3, qz)};
-        if (ev[0] | ev[1] | ev[2] | ev[3] | ev[4] | ev[5]) carry_add(P.carry, v, ev, P.stats);
+                                           carry_lo(w2, a2), wrap_hi(w2, a2)};
+        const unsigned long long c0 = was & 0xffffffffull;
+        if ((ev[0] | ev[1] | ev[2] | ev[3] | ev[4]) || (c0 <= 65536ull && c0 + cnt > 65536ull))
+            carry_add(P.carry, v, ev, P.stats);
     } else {
         atomicAdd(rec + 1, a1);
         atomicAdd(rec + 2, a2);
