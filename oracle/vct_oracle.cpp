@@ -56,11 +56,18 @@ static void parallel_for(int64_t n, int nthreads, F&& fn) {
         return;
     }
     int nt = (int)std::min<int64_t>(nthreads, n);
+    // Items differ in cost by orders of magnitude (a column sliver rasterises thousands of
+    // fragments, a small box triangle a few; a covered pixel traces cones, a background one
+    // nothing), so the threads take chunks from a shared counter. Every caller's result is
+    // independent of which thread handles an item.
+    const int64_t chunk = std::max<int64_t>(1, n / ((int64_t)nt * 64));
+    std::atomic<int64_t> next{0};
     std::vector<std::thread> th;
     th.reserve(nt);
     for (int t = 0; t < nt; ++t) {
-        int64_t a = n * t / nt, b = n * (t + 1) / nt;
-        th.emplace_back([&fn, a, b] { fn(a, b); });
+        th.emplace_back([&fn, &next, n, chunk] {
+            for (int64_t a = next.fetch_add(chunk); a < n; a = next.fetch_add(chunk)) fn(a, std::min(n, a + chunk));
+        });
     }
     for (auto& t : th) t.join();
 }
