@@ -304,32 +304,40 @@ __global__ void __launch_bounds__(256) trace16_kernel(const LearnedParams P, int
 
 // The per-pixel fallback's list: every covered pixel whose error estimate
 // exceeds threshold x the frame's root-mean-square network irradiance over
-// covered pixels.  A warp scans an 8 x 4 pixel tile and appends its flagged
-// pixels with one atomic, so the list holds them in small 2D clusters whose
-// cones march through neighbouring voxels when the fallback traces them.
+// covered pixels.  A CTA scans a 16 x 16 pixel tile, each warp an 8 x 4
+// part of it, and appends the tile's flagged pixels with one atomic, in
+// warp order: the list holds them in 2D clusters whose cones march through
+// neighbouring voxels when the fallback traces them.
 __global__ void __launch_bounds__(256) learned_flag_kernel(const LearnedParams P) {
-    const int W = P.T.width, H = P.T.height, tiles_x = (W + 7) / 8;
-    const long long tile = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const int x = (int)(tile % tiles_x) * 8 + (lane & 7), y = (int)(tile / tiles_x) * 4 + (lane >> 3);
+    const int W = P.T.width, H = P.T.height, tiles_x = (W + 15) / 16;
+    const int tile = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int x = (tile % tiles_x) * 16 + (warp & 1) * 8 + (lane & 7);
+    const int y = (tile / tiles_x) * 16 + (warp >> 1) * 4 + (lane >> 3);
     const long long i = (long long)y * W + x;
     const float n = P.frame_sums[1];
     const float bound = P.threshold * sqrtf(n > 0.0f ? P.frame_sums[0] / n : 0.0f);
     const bool fb = x < W && y < H && P.est[i] >= 0.0f && P.est[i] > bound;
     const unsigned m = __ballot_sync(0xffffffffu, fb);
-    if (m) {
-        const int first = __ffs(m) - 1;
-        uint32_t base = 0;
-        if (lane == first) base = atomicAdd(P.count, (uint32_t)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, first);
-        if (fb) P.list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+    __shared__ uint32_t s_off[8], s_base;
+    if (lane == 0) s_off[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (int w = 0; w < 8; ++w) {
+            const uint32_t c = s_off[w];
+            s_off[w] = tot;
+            tot += c;
+        }
+        s_base = tot ? atomicAdd(P.count, tot) : 0u;
     }
+    __syncthreads();
+    if (fb) P.list[s_base + s_off[warp] + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
 }
 
 // 16-cone irradiance of the listed pixels (the per-pixel fallback), one
 // thread per list entry; the grid covers the longest possible list and
 // threads past the list's length return at once.
-__global__ void __launch_bounds__(256) trace16_pixels_kernel(const LearnedParams P) {
+__global__ void __launch_bounds__(256, 4) trace16_pixels_kernel(const LearnedParams P) {
     __shared__ int s_off[VCT_MAX_LEVELS];
     __shared__ float s_dirs[16][4];
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -944,8 +952,8 @@ void launch_trace16(const LearnedParams& P, bool listed, int num_sms, cudaStream
 
 void launch_trace16_pixels(const LearnedParams& P, cudaStream_t s) {
     const long long n = (long long)P.T.width * P.T.height;
-    const long long tiles = (long long)((P.T.width + 7) / 8) * ((P.T.height + 3) / 4);  // one warp each
-    learned_flag_kernel<<<(unsigned)((tiles + 7) / 8), 256, 0, s>>>(P);
+    const long long tiles = (long long)((P.T.width + 15) / 16) * ((P.T.height + 15) / 16);  // one CTA each
+    learned_flag_kernel<<<(unsigned)tiles, 256, 0, s>>>(P);
     trace16_pixels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P);
     note_launches(2);
 }
