@@ -70,6 +70,41 @@ def test_warpmap_bitexact(warped):
     assert not np.array_equal(st["wmap"].reshape(D, D, D, 4)[..., 0], np.broadcast_to(ident, (D, D, D)))
 
 
+def test_warpmap_bitexact_turned_slivers():
+    """The map's occupancy pass on thin cylinder slivers turned off the grid axes
+    (the dynamic scene's actors moved to t = 1.3), boxes and columns, plus a
+    floor quad whose triangles span the whole 32^2 viewport: small bounding
+    boxes are walked by their own thread, the large ones by the warp."""
+    import copy
+
+    import torch
+
+    sc, actors = scenes.dynamic_scene(seed=2, n_actors=8, dim=64, shadow=512, gbuffer=(160, 90), static_boxes=200,
+                                      static_cyl=6)
+    pos = sc.positions.reshape(-1, 3, 3).astype(np.float64)
+    nrm = sc.normals.reshape(-1, 3, 3).astype(np.float64)
+    for first, count, M in actors.models(1.3):
+        pos[first:first + count] = pos[first:first + count] @ M[:3, :3].T + M[:3, 3]
+        nrm[first:first + count] = nrm[first:first + count] @ M[:3, :3].T
+    f = 0.97
+    floor = np.array([[[-f, -f, -f], [-f, -f, f], [f, -f, f]], [[-f, -f, -f], [f, -f, f], [f, -f, -f]]])
+    sc2 = copy.copy(sc)
+    sc2.positions = np.ascontiguousarray(np.concatenate([pos, floor]).reshape(-1, 9), dtype=np.float32)
+    sc2.normals = np.ascontiguousarray(
+        np.concatenate([nrm, np.broadcast_to([0.0, 1.0, 0.0], (2, 3, 3))]).reshape(-1, 9), dtype=np.float32)
+    sc2.albedo = np.ascontiguousarray(np.concatenate([sc.albedo, np.full((2, 3), 0.5)]), dtype=np.float32)
+    g = GpuScene(sc2)
+    sm, _ = g.host_inputs()
+    occ = O.warp_occupancy(sc2, sm, nthreads=8)
+    assert 0 < occ.sum() < occ.size
+    ctx = api.Context(api.config_for(sc2))
+    ctx.set_params(api.scene_params(sc2, warp_mode=L.VCT_WARP_TEXTURE))
+    ctx.voxelize_accumulate(g.tris, g.lights, g.shadow, sc2.eye)
+    torch.cuda.synchronize()
+    wmap = ctx.read_warpmap().cpu().numpy().view(np.uint16)
+    assert np.array_equal(wmap, O.warpmap(occ))
+
+
 def test_warped_accumulators_bitexact(warped):
     mode, sc, ref, _, st, _ = warped
     assert ref["count"].sum() > 100

@@ -19,7 +19,7 @@ using namespace vct::host;
 struct vct_batch {
     int n = 0, device = 0, num_sms = 0;
     std::vector<vct_ctx*> ctx;
-    size_t off_accum = 0, off_inject = 0, off_resolve = 0, off_mips = 0, off_trace = 0, off_tables = 0;
+    size_t off_accum = 0, off_inject = 0, off_resolve = 0, off_mips = 0, off_trace = 0, off_tables = 0, off_clear = 0;
     size_t blob_bytes = 0;
     char* d_blob = nullptr;
     char* h_blob = nullptr;        // staging of vct_batch_frame
@@ -40,7 +40,15 @@ size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct BatchTotals {
     long long tris = 0, texels = 0, bricks = 0, tiles = 0;
+    // The frame's clears, zeroed by one launch each: before the voxeliser
+    // (statistics, lit masks; carry tables and brick flags of the tessellation
+    // voxeliser) at [0, n_pre) of the blob's clear list, and after the resolve
+    // (occupancy masks, for the next frame's accumulation) at [kClearPre n, +n).
+    int n_pre = 0;
+    long long max_pre = 0, max_post = 0;
 };
+
+constexpr int kClearPre = 4;  // clear-list entries per scene before the voxeliser (one more after the resolve)
 
 // Validates the scene descriptors and fills the staging blob `h` (parameter
 // structs and prefix tables).  Allocates the voxeliser work arrays when the
@@ -127,6 +135,23 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         tot.bricks += bpa * bpa * bpa;
         tot.tiles += trace_tiles(d.gbuffer.width, d.gbuffer.height, T.tile_w_log2, T.tile_h_log2);
     }
+    ClearRange* clr = reinterpret_cast<ClearRange*>(h + b->off_clear);
+    auto pre = [&](void* p, long long words) {
+        clr[tot.n_pre++] = ClearRange{static_cast<uint32_t*>(p), words};
+        tot.max_pre = std::max(tot.max_pre, words);
+    };
+    for (int i = 0; i < n; ++i) {
+        vct_ctx* c = b->ctx[i];
+        const long long mask_words = (c->nv + 31) / 32;
+        pre(c->stats, (long long)(sizeof(StatsDev) / 4));
+        pre(c->lit, mask_words);
+        if (c->params.voxelize_tesselation) {
+            pre(c->carry, (long long)(kCarryBytes / 4));
+            pre(c->brick_exact, c->nv / 4096 + 1);
+        }
+        clr[kClearPre * n + i] = ClearRange{c->occ, mask_words};
+        tot.max_post = std::max(tot.max_post, mask_words);
+    }
     tri_off[n] = tot.tris;
     tex_off[n] = tot.texels;
     brick_off[n] = tot.bricks;
@@ -159,14 +184,9 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
 vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cudaStream_t st, bool timed = false) {
     const int n = b->n;
     VCT_CUDA(cudaMemcpyAsync(b->d_blob, h, b->blob_bytes, cudaMemcpyHostToDevice, st));
-    for (vct_ctx* c : b->ctx) {
-        VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
-        VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, st));
-        if (c->params.voxelize_tesselation) {
-            VCT_CUDA(cudaMemsetAsync(c->carry, 0, (size_t)kCarryBytes, st));
-            VCT_CUDA(cudaMemsetAsync(c->brick_exact, 0, (size_t)(c->nv / 4096 + 1) * 4, st));
-        }
-    }
+    const ClearRange* d_clear = reinterpret_cast<const ClearRange*>(b->d_blob + b->off_clear);
+    launch_clear_ranges(d_clear, tot.n_pre, tot.max_pre, st);
+    VCT_CHECK_LAUNCH("batch: clear");
     const long long* d_tables = reinterpret_cast<const long long*>(b->d_blob + b->off_tables);
     AccumParams W0;
     W0.ntri = tot.tris;
@@ -191,7 +211,8 @@ vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cu
                                                   d_tables + 2 * (n + 1), n},
                          tot.bricks, b->ctx[0]->params.voxelize_tesselation != 0, st);
     VCT_CHECK_LAUNCH("batch: resolve");
-    for (vct_ctx* c : b->ctx) VCT_CUDA(cudaMemsetAsync(c->occ, 0, (size_t)((c->nv + 31) / 32) * 4, st));
+    launch_clear_ranges(d_clear + kClearPre * n, n, tot.max_post, st);
+    VCT_CHECK_LAUNCH("batch: clear occupancy");
     launch_mip_tail_batch(SceneBatch<MipLevels>{reinterpret_cast<const MipLevels*>(b->d_blob + b->off_mips), nullptr, n},
                           st);
     VCT_CHECK_LAUNCH("batch: coarse mips");
@@ -255,6 +276,8 @@ vct_status vct_batch_create(const vct_config* configs, int32_t n, vct_batch** ou
     off = up256(off + sizeof(TraceParams) * n);
     b->off_tables = off;
     off = up256(off + sizeof(long long) * 4 * (n + 1));
+    b->off_clear = off;
+    off = up256(off + sizeof(ClearRange) * (kClearPre + 1) * n);
     b->blob_bytes = off;
     DeviceScope ds(b->device);
     cudaError_t e = cudaMalloc(&b->d_blob, off);

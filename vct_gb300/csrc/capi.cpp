@@ -324,16 +324,15 @@ WarpDev warp_dev(const vct_ctx* ctx, const float* eye) {
 
 vct_status build_warpmap(vct_ctx* ctx, const AccumParams& A, cudaStream_t st) {
     // voxelize.frag:187-192 into the 32^3 occupancy grid (Application.cpp:
-    // 235-285): the same rasteriser at a 32^2 viewport, unwarped.
+    // 235-285): the rasteriser's rule at a 32^2 viewport, unwarped.
     AccumParams O = A;
     O.dim = VCT_WARP_DIM;
     O.occ = ctx->occ32;
     O.acc = nullptr;
     O.stats = nullptr;
-    O.occupancy_only = 1;
     O.warp.mode = VCT_WARP_NONE;
     VCT_CUDA(cudaMemsetAsync(ctx->occ32, 0, (VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM / 32) * 4, st));
-    launch_accumulate(O, st);
+    launch_occupancy(O, st);
     VCT_CHECK_LAUNCH("warp occupancy");
     launch_warpmap(ctx->occ32, ctx->params.warp_high_resolution, ctx->params.warp_low_resolution, ctx->warpmap,
                    ctx->warpmap_f, st);
@@ -709,7 +708,7 @@ vct_status vct_create(const vct_config* cfg, vct_ctx** out) {
         {(void**)&c->pchain, (size_t)padded_level_offset(c->dim, c->levels) * 16},
         {(void**)&c->occ32, (size_t)(VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM / 32) * 4},
         {(void**)&c->warpmap, (size_t)VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM * 8},
-        {(void**)&c->warpmap_f, (size_t)VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM * 16},
+        {(void**)&c->warpmap_f, (size_t)(VCT_WARP_DIM + 2) * (VCT_WARP_DIM + 2) * (VCT_WARP_DIM + 2) * 16},
         {(void**)&c->carry, (size_t)kCarryBytes},
         {(void**)&c->brick_exact, (size_t)(c->nv / 4096 + 1) * 4},
     };

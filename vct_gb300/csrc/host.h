@@ -45,7 +45,7 @@ struct vct_ctx {
     size_t learned_bytes = 0;
     uint32_t* occ32 = nullptr;   // VCT_WARP_TEXTURE: 32^3 occupancy bit mask
     uint16_t* warpmap = nullptr; // VCT_WARP_TEXTURE: 32^3 RGBA16 unorm warp map
-    float4* warpmap_f = nullptr; // its fp32 copy read by the lookups
+    float4* warpmap_f = nullptr; // its bordered fp32 copy read by the lookups ((32+2)^3)
     uint32_t* carry = nullptr;   // the tessellation voxeliser's carry table (kCarrySlots entries)
     uint32_t* brick_exact = nullptr;  // per 16^3 brick: flagged by the carry pass for the exact resolve
 };

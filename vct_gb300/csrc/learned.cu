@@ -87,6 +87,13 @@ __device__ __forceinline__ uint32_t bf16x2(float a, float b) {
     const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<const uint32_t*>(&v);
 }
+// max(a, 0) and max(b, 0) rounded to BF16 and packed (a low): one
+// conversion with ReLU, which commutes with round-to-nearest.
+__device__ __forceinline__ uint32_t bf16x2_relu(float a, float b) {
+    uint32_t r;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+    return r;
+}
 __device__ __forceinline__ uint16_t bf16(float a) { return __bfloat16_as_ushort(__float2bfloat16_rn(a)); }
 __device__ __forceinline__ float bf16f(uint32_t bits16) { return __uint_as_float(bits16 << 16); }
 
@@ -465,7 +472,7 @@ __device__ __forceinline__ bool gather_features(const LearnedParams& P, long lon
 template <bool ROWS>
 __global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const LearnedParams P) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ float s_bias[kBiasPad];
+    __shared__ __align__(16) float s_bias[kBiasPad];
     __shared__ __align__(8) uint64_t mbar[kInferGroups];
     __shared__ uint32_t s_tmem;
     __shared__ int s_done[kInferGroups];
@@ -526,15 +533,18 @@ __global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const Learn
             ok = s_done[grp];
             if (!ok) break;
             if (layer < 3) {
-                const float* bb = s_bias + kMlpHidden * layer;
+                const float2* bb = reinterpret_cast<const float2*>(s_bias + kMlpHidden * layer);
 #pragma unroll
                 for (int c = 0; c < kMlpHidden; c += 32) {
                     float v[32];
                     tmem_ld32(tmem_addr(tm, warp, c), v);
                     uint32_t pk[16];
+                    // bias in packed FP32 pairs, then ReLU and rounding in one conversion
 #pragma unroll
-                    for (int i = 0; i < 16; ++i)
-                        pk[i] = bf16x2(fmaxf(v[2 * i] + bb[c + 2 * i], 0.0f), fmaxf(v[2 * i + 1] + bb[c + 2 * i + 1], 0.0f));
+                    for (int i = 0; i < 16; ++i) {
+                        const float2 z = __fadd2_rn(make_float2(v[2 * i], v[2 * i + 1]), bb[c / 2 + i]);
+                        pk[i] = bf16x2_relu(z.x, z.y);
+                    }
 #pragma unroll
                     for (int q = 0; q < 4; ++q)
                         *reinterpret_cast<uint4*>(sa + tile_offset(row, c + 8 * q, 128)) =

@@ -84,7 +84,6 @@ struct AccumParams {
     int unit_log2;      // log2 of the bounding-box pixels per work unit
     int blocks_per_sm;  // raster CTAs per SM (1..3)
     WarpDev warp;
-    int occupancy_only;  // only set occupancy bits (the warp map's occupancy voxelisation)
     f3 vmin, vcenter, ext;  // voxelLinearPosition of the tessellation voxeliser
     float max_tess_level;   // GL_MAX_TESS_GEN_LEVEL
     // Work distribution scratch (sized for ntri; see voxelize.cu).
@@ -291,6 +290,9 @@ void fill_accum_inputs(const vct_config& cfg, const vct_params& prm, const float
                        const vct_light* lights, int n, const vct_shadow_desc* sh, AccumParams& P);
 
 void launch_accumulate(const AccumParams& P, cudaStream_t s);
+// The warp map's 32^3 occupancy voxelisation into P.occ (P.dim = 32, unwarped):
+// one thread per triangle, no scratch.
+void launch_occupancy(const AccumParams& P, cudaStream_t s);
 // The tessellation voxeliser into the same accumulators (testTesselation.tesc/.tese).
 void launch_tesselate(const AccumParams& P, cudaStream_t s);
 void launch_normalize(const NormalizeParams& P, cudaStream_t s);
@@ -314,6 +316,13 @@ void launch_tesselate_batch(const SceneBatch<AccumParams>& B, const VoxWork& W, 
 void launch_inject_mark_batch(const SceneBatch<InjectParams>& B, long long ntexels, cudaStream_t s);
 void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks, bool exact, cudaStream_t s);
 void launch_mip_tail_batch(const SceneBatch<MipLevels>& B, cudaStream_t s);
+// A device range of 32-bit words to zero (p 16-byte aligned, as cudaMalloc returns).
+struct ClearRange {
+    uint32_t* p;
+    long long words;
+};
+// Zeroes n ranges (a device array) in one launch; max_words sizes the grid.
+void launch_clear_ranges(const ClearRange* ranges, int n, long long max_words, cudaStream_t s);
 long long trace_tiles(int width, int height, int tile_w_log2, int tile_h_log2);
 void launch_trace_batch(const SceneBatch<TraceParams>& B, int filter, long long tiles, cudaStream_t s);
 void launch_trace_views(const ViewSet& V, int filter, cudaStream_t s);

@@ -502,7 +502,7 @@ struct WarpmapArgs {
     const uint32_t* occ;  // 32^3 bit mask
     float high, low;
     uint16_t* map;
-    float4* mapf;  // fp32 copy read by the lookups
+    float4* mapf;  // bordered fp32 copy read by the lookups ((D+2)^3)
 };
 
 __global__ void __launch_bounds__(1024) warpmap_kernel(const WarpmapArgs A) {
@@ -565,8 +565,18 @@ __global__ void __launch_bounds__(1024) warpmap_kernel(const WarpmapArgs A) {
         out[3] = (uint16_t)((tot[0] & 0x1F) | ((tot[1] & 0x1F) << 5) | ((tot[2] & 0x1F) << 10) | ((o ? 1 : 0) << 15));
         reinterpret_cast<uint2*>(A.map)[i] =
             make_uint2((uint32_t)out[0] | ((uint32_t)out[1] << 16), (uint32_t)out[2] | ((uint32_t)out[3] << 16));
-        A.mapf[i] = make_float4(__fdiv_rn((float)out[0], 65535.0f), __fdiv_rn((float)out[1], 65535.0f),
-                                __fdiv_rn((float)out[2], 65535.0f), __fdiv_rn((float)out[3], 65535.0f));
+        A.mapf[((z + 1) * kWarpPad + y + 1) * kWarpPad + x + 1] =
+            make_float4(__fdiv_rn((float)out[0], 65535.0f), __fdiv_rn((float)out[1], 65535.0f),
+                        __fdiv_rn((float)out[2], 65535.0f), __fdiv_rn((float)out[3], 65535.0f));
+    }
+    // the border of the fp32 copy: the nearest edge texel (clamp-to-edge)
+    __syncthreads();
+    constexpr int P = kWarpPad;
+    for (int i = t; i < P * P * P; i += blockDim.x) {
+        const int x = i % P, y = (i / P) % P, z = i / (P * P);
+        if (x > 0 && x < P - 1 && y > 0 && y < P - 1 && z > 0 && z < P - 1) continue;
+        const int sx = min(max(x, 1), P - 2), sy = min(max(y, 1), P - 2), sz = min(max(z, 1), P - 2);
+        A.mapf[i] = A.mapf[(sz * P + sy) * P + sx];
     }
 }
 
@@ -676,6 +686,30 @@ void launch_resolve_batch(const SceneBatch<ResolveParams>& B, long long nbricks,
 
 void launch_mip_tail_batch(const SceneBatch<MipLevels>& B, cudaStream_t s) {
     mip_tail_kernel<<<B.n, kThreads, 0, s>>>(ManyScenes<MipLevels>{B});
+    note_launches(1);
+}
+
+namespace {
+// The per-scene clears of a batched frame (statistics, masks, carry tables)
+// in one launch instead of a memset per buffer: range blockIdx.y, 16-byte
+// stores and word stores for a ragged end.
+__global__ void __launch_bounds__(kThreads) clear_ranges_kernel(const ClearRange* __restrict__ R) {
+    const ClearRange r = R[blockIdx.y];
+    const long long stride = (long long)gridDim.x * kThreads * 4;
+    for (long long i = ((long long)blockIdx.x * kThreads + threadIdx.x) * 4; i < r.words; i += stride) {
+        if (i + 4 <= r.words)
+            *reinterpret_cast<uint4*>(r.p + i) = make_uint4(0u, 0u, 0u, 0u);
+        else
+            for (long long k = i; k < r.words; ++k) r.p[k] = 0u;
+    }
+}
+}  // namespace
+
+void launch_clear_ranges(const ClearRange* ranges, int n, long long max_words, cudaStream_t s) {
+    if (n <= 0 || max_words <= 0) return;
+    const long long per_cta = (long long)kThreads * 4 * 4;  // four 16-byte stores per thread
+    const unsigned gx = (unsigned)std::min<long long>((max_words + per_cta - 1) / per_cta, 1024);
+    clear_ranges_kernel<<<dim3(gx, (unsigned)n), kThreads, 0, s>>>(ranges);
     note_launches(1);
 }
 

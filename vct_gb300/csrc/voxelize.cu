@@ -74,6 +74,39 @@ __device__ __forceinline__ void block_scan_units(const VoxWork& W, long long g, 
 }
 
 // ------------------------------------------------------------- 1. setup
+// voxelize.geom:25-73 for triangle t of P: the dominant axis of the summed
+// normals (strict >, ties to z, or the override), the projection through
+// that axis' orthographic matrix into the N x N viewport, and the snapped
+// raster set-up.  False when the triangle covers no pixel centre's bounding
+// box (zero snapped area, or outside the viewport).
+__device__ __forceinline__ bool project_triangle(const AccumParams& P, long long t, RasterTri& rt, float z[3],
+                                                 int& axis) {
+    const float* Pp = P.pos + t * 9;
+    const float* Pn = P.nrm + t * 9;
+    f3 n0 = ld3(Pn), n1 = ld3(Pn + 3), n2 = ld3(Pn + 6);
+    f3 fn = normalize(add(add(n0, n1), n2));
+    float ax = fabsf(fn.x), ay = fabsf(fn.y), az = fabsf(fn.z);
+    axis = 2;
+    if (ax > ay && ax > az)
+        axis = 0;
+    else if (ay > ax && ay > az)
+        axis = 1;
+    if (P.axis_override >= 0 && P.axis_override <= 2) axis = P.axis_override;
+    const float* M = P.mvp + 16 * axis;
+    const int N = P.dim;
+    float wx[3], wy[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float c[4];
+        mat_vec(M, Pp[3 * k], Pp[3 * k + 1], Pp[3 * k + 2], 1.0f, c);
+        float nx = __fdiv_rn(c[0], c[3]), ny = __fdiv_rn(c[1], c[3]);
+        z[k] = __fdiv_rn(c[2], c[3]);
+        wx[k] = (nx + 1.0f) * 0.5f * (float)N;
+        wy[k] = (ny + 1.0f) * 0.5f * (float)N;
+    }
+    return raster_setup(wx, wy, N, N, rt);
+}
+
 template <class Scenes>
 __global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Scenes S, const VoxWork W) {
     const long long g = (long long)blockIdx.x * kSetupThreads + threadIdx.x;
@@ -81,31 +114,10 @@ __global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Sce
     if (g < W.ntri) {
         long long t;
         const AccumParams& P = S.get(S.find(g, t));
-        const float* Pp = P.pos + t * 9;
-        const float* Pn = P.nrm + t * 9;
-        f3 n0 = ld3(Pn), n1 = ld3(Pn + 3), n2 = ld3(Pn + 6);
-        f3 fn = normalize(add(add(n0, n1), n2));
-        float ax = fabsf(fn.x), ay = fabsf(fn.y), az = fabsf(fn.z);
-        int axis = 2;
-        if (ax > ay && ax > az)
-            axis = 0;
-        else if (ay > ax && ay > az)
-            axis = 1;
-        if (P.axis_override >= 0 && P.axis_override <= 2) axis = P.axis_override;
-        const float* M = P.mvp + 16 * axis;
-        const int N = P.dim;
-        float wx[3], wy[3], z[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            float c[4];
-            mat_vec(M, Pp[3 * k], Pp[3 * k + 1], Pp[3 * k + 2], 1.0f, c);
-            float nx = __fdiv_rn(c[0], c[3]), ny = __fdiv_rn(c[1], c[3]);
-            z[k] = __fdiv_rn(c[2], c[3]);
-            wx[k] = (nx + 1.0f) * 0.5f * (float)N;
-            wy[k] = (ny + 1.0f) * 0.5f * (float)N;
-        }
         RasterTri rt;
-        if (raster_setup(wx, wy, N, N, rt)) {
+        float z[3];
+        int axis;
+        if (project_triangle(P, t, rt, z, axis)) {
             const uint32_t bw = rt.px1 - rt.px0 + 1, bh = rt.py1 - rt.py0 + 1;
             const uint32_t bias = (rt.bias[0] ? 1u : 0u) | (rt.bias[1] ? 2u : 0u) | (rt.bias[2] ? 4u : 0u);
             const float inv = __fdiv_rn(1.0f, __ll2float_rn(rt.area));
@@ -204,10 +216,6 @@ __device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQ
     if (!fragment_voxel(P, px, py, axis, q.z[e], vx, vy, vz)) return;
     const int N = P.dim;
     const long long v = ((long long)vz * N + vy) * N + vx;
-    if (P.occupancy_only) {  // voxelize.frag:187-192
-        atomicOr(P.occ + (v >> 5), 1u << (v & 31));
-        return;
-    }
     const float l[3] = {q.l0[e], q.l1[e], q.l2[e]};
     const float* Pp = P.pos + t * 9;
     const float* Pn = P.nrm + t * 9;
@@ -256,6 +264,33 @@ __device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQ
     atomicOr(P.occ + (v >> 5), 1u << (v & 31));
 }
 
+// Coverage of pixel (px, py) by a set-up triangle (snapped vertices X, Y; edge
+// k runs from vertex a = k+1 to b = k+2 with deltas dX, dY; bit k of `bias`
+// set for an edge that is not top-left) and the fragment's barycentrics and
+// depth.  The edge function at the pixel centre is dX (sy - Ya) - dY (sx - Xa),
+// every factor within 32 bits (|snapped coordinates| <= 2^28), each product
+// exact in 64.  False outside the triangle or outside GL's depth clip.
+__device__ __forceinline__ bool pixel_fragment(const int X[3], const int Y[3], const int dX[3], const int dY[3],
+                                               int bias, int perm1, float inv, const float z[3], int px, int py,
+                                               float l[3], float& zf) {
+    const int sx = px * (int)kSub + (int)kSub / 2, sy = py * (int)kSub + (int)kSub / 2;
+    long long e[3];
+    bool cov = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int a = (k + 1) % 3;
+        e[k] = (long long)dX[k] * (long long)(sy - Y[a]) - (long long)dY[k] * (long long)(sx - X[a]);
+        cov = cov && (e[k] - ((bias >> k) & 1) >= 0);
+    }
+    if (!cov) return false;
+    const float w0 = __ll2float_rn(e[0]) * inv, w1 = __ll2float_rn(e[1]) * inv, w2 = __ll2float_rn(e[2]) * inv;
+    l[0] = w0;
+    l[1] = perm1 ? w2 : w1;
+    l[2] = perm1 ? w1 : w2;
+    zf = interp(l, z[0], z[1], z[2]);
+    return zf >= -1.0f && zf <= 1.0f;  // GL clipping
+}
+
 template <class Scenes>
 __device__ __forceinline__ long long unit_start(const VoxWork& W, long long g) {
     return (long long)W.block_off[g / kSetupThreads] + W.tri_scan[g];
@@ -297,7 +332,7 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
     int cur_scene = 0;
     unsigned pending = 0;
     auto flush_count = [&]() {
-        if (lane == 0 && pending && !S.get(cur_scene).occupancy_only) atomicAdd(&frag_count[cur_scene], pending);
+        if (lane == 0 && pending) atomicAdd(&frag_count[cur_scene], pending);
         pending = 0;
     };
 
@@ -359,10 +394,7 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
             const int bw = (int)(r2.w & 0x7ffu), bh = (int)(r2.w >> 11);
             const int p_begin = (int)(u - start) << W.unit_log2;
             const int p_end = min(p_begin + (1 << W.unit_log2), bw * bh);
-            // Edge k runs from vertex a = k+1 to b = k+2; its function at a pixel
-            // centre is dX (sy - Ya) - dY (sx - Xa), every factor within 32 bits
-            // (|snapped coordinates| <= 2^28), each product exact in 64.
-            int dX[3], dY[3];
+            int dX[3], dY[3];  // edge k: vertex k+2 minus vertex k+1
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 dX[k] = X[(k + 2) % 3] - X[(k + 1) % 3];
@@ -382,24 +414,7 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
                         ++row;
                     py = py0 + row;
                     px = px0 + (idx - row * bw);
-                    const int sx = px * (int)kSub + (int)kSub / 2, sy = py * (int)kSub + (int)kSub / 2;
-                    long long e[3];
-                    cov = true;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        const int a = (k + 1) % 3;
-                        e[k] = (long long)dX[k] * (long long)(sy - Y[a]) - (long long)dY[k] * (long long)(sx - X[a]);
-                        cov = cov && (e[k] - ((bias >> k) & 1) >= 0);
-                    }
-                    if (cov) {
-                        const float w0 = __ll2float_rn(e[0]) * inv, w1 = __ll2float_rn(e[1]) * inv,
-                                    w2 = __ll2float_rn(e[2]) * inv;
-                        l[0] = w0;
-                        l[1] = perm1 ? w2 : w1;
-                        l[2] = perm1 ? w1 : w2;
-                        zf = interp(l, z[0], z[1], z[2]);
-                        cov = zf >= -1.0f && zf <= 1.0f;  // GL clipping
-                    }
+                    cov = pixel_fragment(X, Y, dX, dY, bias, perm1, inv, z, px, py, l, zf);
                 }
                 const unsigned m = __ballot_sync(FULL, cov);
                 if (cov) {
@@ -438,6 +453,97 @@ void launch_voxelize(const Scenes& S, const VoxWork& W, int num_sms, int blocks_
     const int bps = blocks_per_sm < 1 ? 1 : (blocks_per_sm > kRasterBlocksPerSM ? kRasterBlocksPerSM : blocks_per_sm);
     voxelize_raster_kernel<Scenes><<<num_sms * bps, kWarps * 32, 0, s>>>(S, W, nblocks);
     note_launches(3);
+}
+
+// ================================================ warp-map occupancy pass
+// voxelize.frag:187-192: the occupancy voxelisation that the warp map is
+// built from (Application.cpp:235-285), the same rasterisation rule as above
+// at a 32^2 viewport, unwarped and unshaded.  Nearly every triangle of a
+// scene covers a handful of pixels at that size, so the persistent raster's
+// work units (one shared-counter grab, a search and three dependent loads
+// each) would cost far more than the pixels: one thread takes one triangle,
+// sets it up and walks a bounding box of up to kOccLanePixels pixels itself;
+// the warp walks the larger ones together, 32 pixels at a time.  The result
+// is an OR of bits, so the order of the walks does not matter.
+constexpr int kOccThreads = 256;
+constexpr int kOccLanePixels = 32;
+
+__device__ __forceinline__ void occupancy_fragment(const AccumParams& P, int axis, int px, int py, float zf) {
+    int vx, vy, vz;
+    if (!fragment_voxel(P, px, py, axis, zf, vx, vy, vz)) return;
+    const long long v = ((long long)vz * P.dim + vy) * P.dim + vx;
+    atomicOr(P.occ + (v >> 5), 1u << (v & 31));
+}
+
+__global__ void __launch_bounds__(kOccThreads) occupancy_kernel(const AccumParams P) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const long long g = (long long)blockIdx.x * kOccThreads + threadIdx.x;
+    RasterTri rt;
+    float z[3] = {0.f, 0.f, 0.f};
+    int axis = 0;
+    const bool ok = g < P.ntri && project_triangle(P, g, rt, z, axis);
+    int X[3] = {0, 0, 0}, Y[3] = {0, 0, 0}, dX[3], dY[3];
+    int bias = 0, perm1 = 0, px0 = 0, py0 = 0, bw = 0, bh = 0;
+    float inv = 0.f;
+    if (ok) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            X[k] = (int)rt.X[k];
+            Y[k] = (int)rt.Y[k];
+        }
+        bias = (rt.bias[0] ? 1 : 0) | (rt.bias[1] ? 2 : 0) | (rt.bias[2] ? 4 : 0);
+        perm1 = rt.perm1;
+        inv = __fdiv_rn(1.0f, __ll2float_rn(rt.area));
+        px0 = rt.px0;
+        py0 = rt.py0;
+        bw = rt.px1 - rt.px0 + 1;
+        bh = rt.py1 - rt.py0 + 1;
+    }
+    const int npix = bw * bh;
+    if (npix <= kOccLanePixels) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            dX[k] = X[(k + 2) % 3] - X[(k + 1) % 3];
+            dY[k] = Y[(k + 2) % 3] - Y[(k + 1) % 3];
+        }
+        for (int py = py0; py < py0 + bh; ++py)
+            for (int px = px0; px < px0 + bw; ++px) {
+                float l[3], zf;
+                if (pixel_fragment(X, Y, dX, dY, bias, perm1, inv, z, px, py, l, zf))
+                    occupancy_fragment(P, axis, px, py, zf);
+            }
+    }
+    unsigned big = __ballot_sync(FULL, npix > kOccLanePixels);
+    while (big) {
+        const int src = __ffs(big) - 1;
+        big &= big - 1;
+        int sX[3], sY[3], sdX[3], sdY[3];
+        float sz[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            sX[k] = __shfl_sync(FULL, X[k], src);
+            sY[k] = __shfl_sync(FULL, Y[k], src);
+            sz[k] = __shfl_sync(FULL, z[k], src);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            sdX[k] = sX[(k + 2) % 3] - sX[(k + 1) % 3];
+            sdY[k] = sY[(k + 2) % 3] - sY[(k + 1) % 3];
+        }
+        const int sbias = __shfl_sync(FULL, bias, src), sperm1 = __shfl_sync(FULL, perm1, src);
+        const float sinv = __shfl_sync(FULL, inv, src);
+        const int saxis = __shfl_sync(FULL, axis, src);
+        const int spx0 = __shfl_sync(FULL, px0, src), spy0 = __shfl_sync(FULL, py0, src);
+        const int sbw = __shfl_sync(FULL, bw, src), sn = __shfl_sync(FULL, npix, src);
+        for (int idx = lane; idx < sn; idx += 32) {
+            const int row = idx / sbw;
+            const int px = spx0 + (idx - row * sbw), py = spy0 + row;
+            float l[3], zf;
+            if (pixel_fragment(sX, sY, sdX, sdY, sbias, sperm1, sinv, sz, px, py, l, zf))
+                occupancy_fragment(P, saxis, px, py, zf);
+        }
+    }
 }
 
 // ====================================================== tessellation voxeliser
@@ -820,6 +926,12 @@ void accumulate_bind_scratch(AccumParams& P, void* scratch) {
     P.tri_scan = reinterpret_cast<uint32_t*>(p);
     p += align256(ntri * 4);
     P.block_off = reinterpret_cast<uint32_t*>(p);
+}
+
+void launch_occupancy(const AccumParams& P, cudaStream_t s) {
+    if (P.ntri <= 0) return;
+    occupancy_kernel<<<(unsigned)((P.ntri + kOccThreads - 1) / kOccThreads), kOccThreads, 0, s>>>(P);
+    note_launches(1);
 }
 
 void launch_accumulate(const AccumParams& P, cudaStream_t s) {

@@ -37,40 +37,42 @@ __device__ __forceinline__ f3 voxel_warp(f3 p, f3 c) {
     return r;
 }
 
+// The fp32 copy of the map read by the lookups is bordered: (D+2)^3 texels,
+// texel (i, j, k) at (i+1, j+1, k+1) and the border repeating the edge
+// texels, which is what clamp-to-edge reads there.
+constexpr int kWarpPad = kWarpDim + 2;
+
 // texture(warpmap, p).xyz: GL_LINEAR with clamp-to-edge over the 32^3 RGBA16
-// unorm map, read through its fp32 copy (texel value c / 65535), lerped
-// along x, then y, then z.
+// unorm map, read through its bordered fp32 copy (texel value c / 65535),
+// lerped along x, then y, then z.  The footprint's lower corner is clamped to
+// the border, so the eight loads are constant offsets from one address and
+// read the texels the clamped indices would; x and y are interpolated as
+// packed fp32 pairs (each element rounds as the scalar product and sum do).
 __device__ __forceinline__ f3 warp_lookup(const float4* __restrict__ mapf, f3 p) {
     const float u = p.x * (float)kWarpDim - 0.5f, v = p.y * (float)kWarpDim - 0.5f, w = p.z * (float)kWarpDim - 0.5f;
     const float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     const float a = u - fu, b = v - fv, c = w - fw;
-    const int i0 = (int)fu, j0 = (int)fv, k0 = (int)fw;
-    const int ix[2] = {min(max(i0, 0), kWarpDim - 1), min(max(i0 + 1, 0), kWarpDim - 1)};
-    const int iy[2] = {min(max(j0, 0), kWarpDim - 1), min(max(j0 + 1, 0), kWarpDim - 1)};
-    const int iz[2] = {min(max(k0, 0), kWarpDim - 1), min(max(k0 + 1, 0), kWarpDim - 1)};
-    float t[8][3];
-#pragma unroll
-    for (int n = 0; n < 8; ++n) {
-        const float4 q = __ldg(mapf + ((iz[n >> 2] * kWarpDim + iy[(n >> 1) & 1]) * kWarpDim + ix[n & 1]));
-        t[n][0] = q.x;
-        t[n][1] = q.y;
-        t[n][2] = q.z;
-    }
-    float o[3];
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-        const float x00 = t[0][ch] * (1.0f - a) + t[1][ch] * a;
-        const float x10 = t[2][ch] * (1.0f - a) + t[3][ch] * a;
-        const float x01 = t[4][ch] * (1.0f - a) + t[5][ch] * a;
-        const float x11 = t[6][ch] * (1.0f - a) + t[7][ch] * a;
-        const float y0 = x00 * (1.0f - b) + x10 * b;
-        const float y1 = x01 * (1.0f - b) + x11 * b;
-        o[ch] = y0 * (1.0f - c) + y1 * c;
-    }
+    const int i = min(max((int)fu + 1, 0), kWarpDim), j = min(max((int)fv + 1, 0), kWarpDim),
+              k = min(max((int)fw + 1, 0), kWarpDim);
+    const float4* q = mapf + ((k * kWarpPad + j) * kWarpPad + i);
+    constexpr int sy = kWarpPad, sz = kWarpPad * kWarpPad;
+    const float4 t0 = __ldg(q), t1 = __ldg(q + 1), t2 = __ldg(q + sy), t3 = __ldg(q + sy + 1);
+    const float4 t4 = __ldg(q + sz), t5 = __ldg(q + sz + 1), t6 = __ldg(q + sz + sy), t7 = __ldg(q + sz + sy + 1);
+    // p * (1 - s) + q * s on the (x, y) pair and on z
+    auto lerp_xy = [](float2 p, float2 q, float s) {
+        return __fadd2_rn(__fmul2_rn(p, make_float2(1.0f - s, 1.0f - s)), __fmul2_rn(q, make_float2(s, s)));
+    };
+    auto lerp_z = [](float p, float q, float s) { return p * (1.0f - s) + q * s; };
+    auto xy = [](float4 t) { return make_float2(t.x, t.y); };
+    const float2 x00 = lerp_xy(xy(t0), xy(t1), a), x10 = lerp_xy(xy(t2), xy(t3), a);
+    const float2 x01 = lerp_xy(xy(t4), xy(t5), a), x11 = lerp_xy(xy(t6), xy(t7), a);
+    const float2 o = lerp_xy(lerp_xy(x00, x10, b), lerp_xy(x01, x11, b), c);
+    const float z00 = lerp_z(t0.z, t1.z, a), z10 = lerp_z(t2.z, t3.z, a);
+    const float z01 = lerp_z(t4.z, t5.z, a), z11 = lerp_z(t6.z, t7.z, a);
     f3 r;
-    r.x = o[0];
-    r.y = o[1];
-    r.z = o[2];
+    r.x = o.x;
+    r.y = o.y;
+    r.z = lerp_z(lerp_z(z00, z10, b), lerp_z(z01, z11, b), c);
     return r;
 }
 
