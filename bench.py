@@ -1050,14 +1050,14 @@ def run_dynamic(args, rank, world):
 # stage, from one ncu capture of the large frame (`bench.py --profile-frames 3`, default
 # launch shapes): accumulate = setup + raster, resolve+mips = resolve + tail; only for the
 # default workload, and only while the frame kernels' sources hash to NCU_CAPTURE_DIGEST.
-NCU_CAPTURE_DIGEST = "566978f8a7acd1be"
+NCU_CAPTURE_DIGEST = "31ab859802622a6c"
 NCU_CAPTURE_SAMPLER = "hybrid"
-NCU_TRAFFIC = {"accumulate": 18.890e6 + 317.546e6 + 180.410e6, "resolve+mips": 316.401e6 + 991.915e6 + 0.047e6,
-               "inject_mark": 18.282e6, "trace": 89.188e6 + 12.720e6}
+NCU_TRAFFIC = {"accumulate": 18.894e6 + 317.959e6 + 180.398e6, "resolve+mips": 316.371e6 + 991.991e6 + 0.046e6,
+               "inject_mark": 18.284e6, "trace": 89.188e6 + 12.647e6}
 # Issue-side figures of the cone tracer (hybrid sampler) from its full capture of the same
 # command: it is bound by issue and load latency at its occupancy, not HBM.
-NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.629, "fma_pipe_frac": 0.439, "l1_hit_rate": 0.971,
-                   "l1_lsu_data_pipe_frac": 0.658, "l1_tex_data_pipe_frac": 0.239}
+NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.635, "fma_pipe_frac": 0.440, "l1_hit_rate": 0.971,
+                   "l1_lsu_data_pipe_frac": 0.664, "l1_tex_data_pipe_frac": 0.241}
 
 
 def load_peaks() -> dict:

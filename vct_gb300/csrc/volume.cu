@@ -565,18 +565,18 @@ __global__ void __launch_bounds__(1024) warpmap_kernel(const WarpmapArgs A) {
         out[3] = (uint16_t)((tot[0] & 0x1F) | ((tot[1] & 0x1F) << 5) | ((tot[2] & 0x1F) << 10) | ((o ? 1 : 0) << 15));
         reinterpret_cast<uint2*>(A.map)[i] =
             make_uint2((uint32_t)out[0] | ((uint32_t)out[1] << 16), (uint32_t)out[2] | ((uint32_t)out[3] << 16));
-        A.mapf[((z + 1) * kWarpPad + y + 1) * kWarpPad + x + 1] =
-            make_float4(__fdiv_rn((float)out[0], 65535.0f), __fdiv_rn((float)out[1], 65535.0f),
-                        __fdiv_rn((float)out[2], 65535.0f), __fdiv_rn((float)out[3], 65535.0f));
-    }
-    // the border of the fp32 copy: the nearest edge texel (clamp-to-edge)
-    __syncthreads();
-    constexpr int P = kWarpPad;
-    for (int i = t; i < P * P * P; i += blockDim.x) {
-        const int x = i % P, y = (i / P) % P, z = i / (P * P);
-        if (x > 0 && x < P - 1 && y > 0 && y < P - 1 && z > 0 && z < P - 1) continue;
-        const int sx = min(max(x, 1), P - 2), sy = min(max(y, 1), P - 2), sz = min(max(z, 1), P - 2);
-        A.mapf[i] = A.mapf[(sz * P + sy) * P + sx];
+        const float4 f = make_float4(__fdiv_rn((float)out[0], 65535.0f), __fdiv_rn((float)out[1], 65535.0f),
+                                     __fdiv_rn((float)out[2], 65535.0f), __fdiv_rn((float)out[3], 65535.0f));
+        // the fp32 copy at (x+1, y+1, z+1), and on the border beside an edge
+        // texel (clamp-to-edge): up to 8 places for a corner texel
+        const int xs[2] = {x + 1, x == 0 ? 0 : x == D - 1 ? D + 1 : -1};
+        const int ys[2] = {y + 1, y == 0 ? 0 : y == D - 1 ? D + 1 : -1};
+        const int zs[2] = {z + 1, z == 0 ? 0 : z == D - 1 ? D + 1 : -1};
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+            const int bx = xs[n & 1], by = ys[(n >> 1) & 1], bz = zs[n >> 2];
+            if (bx >= 0 && by >= 0 && bz >= 0) A.mapf[(bz * kWarpPad + by) * kWarpPad + bx] = f;
+        }
     }
 }
 
