@@ -435,19 +435,25 @@ __global__ void __launch_bounds__(kProbeThreads) learned_probe_kernel(const Lear
 
 // ------------------------------------------------------- MLP inference
 // A CTA holds the forward weights once in shared memory and runs kInferGroups
-// independent groups of four warps; a group owns a 128-pixel tile (one pixel
-// per thread and per TMEM lane) and its own 64 TMEM columns, A-operand tile
-// and mbarrier, and synchronises on its own named barrier, so the groups'
-// MMA chains and epilogues interleave on the SM.  Per layer the group's
-// elected thread issues the K/16 MMAs (A = the tile's BF16 activations,
-// B = the layer's weights) into the FP32 accumulator and commits to the
-// group's mbarrier; every thread then loads its row, adds the bias, applies
-// ReLU and writes the BF16 row back as the next layer's A operand.  The
-// features of the group's next tile are gathered while its first MMA runs.
+// independent groups of four warps; a group owns kInferTiles 128-pixel tiles
+// at a time (one pixel of each per thread and per TMEM lane), 64 TMEM columns
+// and an A-operand tile per tile, an mbarrier, and its own named barrier, so
+// the groups' MMA chains and epilogues interleave on the SM.  Per layer the
+// group's elected thread issues the K/16 MMAs of every tile (A = the tile's
+// BF16 activations, B = the layer's weights) into the tiles' FP32
+// accumulators and commits once to the group's mbarrier; every thread then
+// loads its rows, adds the bias, applies ReLU and writes the BF16 rows back as
+// the next layer's A operands.  Each wait and barrier thus serves kInferTiles
+// tiles: the chain of MMA, commit, wait, barrier, TMEM load and epilogue is
+// mostly latency, and one group's tiles share it.  The features of the
+// group's next tiles are gathered while its first MMAs run.
 constexpr int kInferGroups = 2;
+constexpr int kInferTiles = 2;
 constexpr int kInferThreads = 128 * kInferGroups;
 constexpr int kInferTile = 128 * kMlpHidden * 2;
-constexpr int kInferSmem = kImgFwd + kInferGroups * kInferTile;
+constexpr int kInferSmem = kImgFwd + kInferGroups * kInferTiles * kInferTile;
+constexpr int kInferCols = 64 * kInferTiles * kInferGroups;  // TMEM columns per CTA
+constexpr int kInferBlocksPerSM = 2;                        // 2 x 88 KB of shared memory, 2 x 256 TMEM columns
 
 template <bool ROWS>
 __device__ __forceinline__ bool gather_features(const LearnedParams& P, long long idx, uint32_t (&f)[24]) {
@@ -470,7 +476,7 @@ __device__ __forceinline__ bool gather_features(const LearnedParams& P, long lon
 }
 
 template <bool ROWS>
-__global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const LearnedParams P) {
+__global__ void __launch_bounds__(kInferThreads, kInferBlocksPerSM) mlp_infer_kernel(const LearnedParams P) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(16) float s_bias[kBiasPad];
     __shared__ __align__(8) uint64_t mbar[kInferGroups];
@@ -483,13 +489,21 @@ __global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const Learn
     if (tid < kInferGroups) mbar_init(smem_u32(&mbar[tid]), 1);
     if (tid == 0) fence_mbar_init();
     if (warp == 0) {
-        tmem_alloc(smem_u32(&s_tmem), 64 * kInferGroups);
+        tmem_alloc(smem_u32(&s_tmem), kInferCols);
         tmem_relinquish();  // lets the SM's other CTAs allocate
     }
     fence_async_smem();
     tc_sync();
-    uint8_t* sa = smem + kImgFwd + grp * kInferTile;
-    const uint32_t tm = s_tmem + 64u * grp, a0 = smem_u32(sa), w0 = smem_u32(smem), mb = smem_u32(&mbar[grp]);
+    // tile k of the group: A operand at sa[k], accumulator at TMEM columns tm[k]
+    uint8_t* sa[kInferTiles];
+    uint32_t tm[kInferTiles], a0[kInferTiles];
+#pragma unroll
+    for (int k = 0; k < kInferTiles; ++k) {
+        sa[k] = smem + kImgFwd + (grp * kInferTiles + k) * kInferTile;
+        a0[k] = smem_u32(sa[k]);
+        tm[k] = s_tmem + 64u * (uint32_t)(grp * kInferTiles + k);
+    }
+    const uint32_t w0 = smem_u32(smem), mb = smem_u32(&mbar[grp]);
     const int bar = 1 + grp;
     const bool leader = row == 0;
     auto group_sync = [&]() {
@@ -498,23 +512,29 @@ __global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const Learn
         fence_after_sync();
     };
     const long long ntiles = (P.n + 127) / 128;
-    const long long stride = (long long)gridDim.x * kInferGroups;
+    // the group's tiles: kInferTiles consecutive ones per step
+    const long long stride = (long long)gridDim.x * kInferGroups * kInferTiles;
     uint32_t phase = 0;
     int ok = 1;
-    long long t = (long long)blockIdx.x * kInferGroups + grp;
-    uint32_t f[24];
-    bool covered = gather_features<ROWS>(P, t * 128 + row, f);
+    long long t = ((long long)blockIdx.x * kInferGroups + grp) * kInferTiles;
+    uint32_t f[kInferTiles][24];
+    bool covered[kInferTiles];
+#pragma unroll
+    for (int k = 0; k < kInferTiles; ++k) covered[k] = gather_features<ROWS>(P, (t + k) * 128 + row, f[k]);
     float sum_sq = 0.0f, n_cov = 0.0f;
     for (; t < ntiles && ok; t += stride) {
-        const long long idx = t * 128 + row;
-        const bool valid = idx < P.n, cov = covered;
+        bool cov[kInferTiles];
 #pragma unroll
-        for (int c = 0; c < 6; ++c)
-            *reinterpret_cast<uint4*>(sa + tile_offset(row, 8 * c, 128)) =
-                make_uint4(f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3]);
+        for (int k = 0; k < kInferTiles; ++k) {
+            cov[k] = covered[k];
+#pragma unroll
+            for (int c = 0; c < 6; ++c)
+                *reinterpret_cast<uint4*>(sa[k] + tile_offset(row, 8 * c, 128)) =
+                    make_uint4(f[k][4 * c], f[k][4 * c + 1], f[k][4 * c + 2], f[k][4 * c + 3]);
+        }
         fence_async_smem();
         group_sync();
-        float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
+        float o[kInferTiles][4];
 #pragma unroll 1
         for (int layer = 0; layer < 4; ++layer) {
             const int K = layer == 0 ? kMlpInPad : kMlpHidden;
@@ -522,57 +542,76 @@ __global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const Learn
             const uint32_t b = w0 + (layer == 0 ? kImgW1 : layer == 1 ? kImgW2 : layer == 2 ? kImgW3 : kImgW4);
             if (leader) {
                 const uint32_t id = idesc_bf16_f32(128, N);
-                for (int j = 0; j < K / 16; ++j) mma_bf16(tm, tile_desc(a0, 128, j), tile_desc(b, N, j), id, j > 0);
+#pragma unroll
+                for (int k = 0; k < kInferTiles; ++k)
+                    for (int j = 0; j < K / 16; ++j)
+                        mma_bf16(tm[k], tile_desc(a0[k], 128, j), tile_desc(b, N, j), id, j > 0);
                 commit(mb);
             }
-            // the next tile's features load while the first layer runs
-            if (layer == 0) covered = gather_features<ROWS>(P, (t + stride) * 128 + row, f);
+            // the next tiles' features load while the first layer runs
+            if (layer == 0) {
+#pragma unroll
+                for (int k = 0; k < kInferTiles; ++k)
+                    covered[k] = gather_features<ROWS>(P, (t + stride + k) * 128 + row, f[k]);
+            }
             if (leader) s_done[grp] = mbar_wait(mb, phase) ? 1 : 0;
             phase ^= 1u;
             group_sync();
             ok = s_done[grp];
             if (!ok) break;
             if (layer < 3) {
-                const float2* bb = reinterpret_cast<const float2*>(s_bias + kMlpHidden * layer);
+                const float4* bb = reinterpret_cast<const float4*>(s_bias + kMlpHidden * layer);
 #pragma unroll
-                for (int c = 0; c < kMlpHidden; c += 32) {
-                    float v[32];
-                    tmem_ld32(tmem_addr(tm, warp, c), v);
-                    uint32_t pk[16];
-                    // bias in packed FP32 pairs, then ReLU and rounding in one conversion
+                for (int k = 0; k < kInferTiles; ++k) {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const float2 z = __fadd2_rn(make_float2(v[2 * i], v[2 * i + 1]), bb[c / 2 + i]);
-                        pk[i] = bf16x2_relu(z.x, z.y);
+                    for (int c = 0; c < kMlpHidden; c += 32) {
+                        float v[32];
+                        tmem_ld32(tmem_addr(tm[k], warp, c), v);
+                        uint32_t pk[16];
+                        // bias in packed FP32 pairs, then ReLU and rounding in one conversion
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            const float4 b4 = bb[c / 4 + i];
+                            const float2 z0 = __fadd2_rn(make_float2(v[4 * i], v[4 * i + 1]), make_float2(b4.x, b4.y));
+                            const float2 z1 = __fadd2_rn(make_float2(v[4 * i + 2], v[4 * i + 3]), make_float2(b4.z, b4.w));
+                            pk[2 * i] = bf16x2_relu(z0.x, z0.y);
+                            pk[2 * i + 1] = bf16x2_relu(z1.x, z1.y);
+                        }
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            *reinterpret_cast<uint4*>(sa[k] + tile_offset(row, c + 8 * q, 128)) =
+                                make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
                     }
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        *reinterpret_cast<uint4*>(sa + tile_offset(row, c + 8 * q, 128)) =
-                            make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
                 }
                 fence_async_smem();
                 group_sync();
             } else {
-                float v[16];
-                tmem_ld16(tmem_addr(tm, warp, 0), v);
-                o0 = v[0] + s_bias[3 * kMlpHidden];
-                o1 = v[1] + s_bias[3 * kMlpHidden + 1];
-                o2 = v[2] + s_bias[3 * kMlpHidden + 2];
-                o3 = v[3] + s_bias[3 * kMlpHidden + 3];
+#pragma unroll
+                for (int k = 0; k < kInferTiles; ++k) {
+                    float v[16];
+                    tmem_ld16(tmem_addr(tm[k], warp, 0), v);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) o[k][q] = v[q] + s_bias[3 * kMlpHidden + q];
+                }
             }
         }
         if (!ok) break;
-        if (ROWS) {
-            if (valid) *reinterpret_cast<float4*>(P.out_rows + idx * 4) = make_float4(o0, o1, o2, o3);
-        } else {
-            if (valid) P.out[idx] = cov ? make_float4(o0, o1, o2, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
-            if (P.est && valid) {
-                // the per-pixel fallback's inputs: the error estimate (-1 for
-                // background) and the frame's sum of squared irradiance
-                P.est[idx] = cov ? o3 : -1.0f;
-                if (cov) {
-                    sum_sq += o0 * o0 + o1 * o1 + o2 * o2;
-                    n_cov += 1.0f;
+#pragma unroll
+        for (int k = 0; k < kInferTiles; ++k) {
+            const long long idx = (t + k) * 128 + row;
+            if (idx >= P.n) continue;
+            if (ROWS) {
+                *reinterpret_cast<float4*>(P.out_rows + idx * 4) = make_float4(o[k][0], o[k][1], o[k][2], o[k][3]);
+            } else {
+                P.out[idx] = cov[k] ? make_float4(o[k][0], o[k][1], o[k][2], 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+                if (P.est) {
+                    // the per-pixel fallback's inputs: the error estimate (-1 for
+                    // background) and the frame's sum of squared irradiance
+                    P.est[idx] = cov[k] ? o[k][3] : -1.0f;
+                    if (cov[k]) {
+                        sum_sq += o[k][0] * o[k][0] + o[k][1] * o[k][1] + o[k][2] * o[k][2];
+                        n_cov += 1.0f;
+                    }
                 }
             }
         }
@@ -590,7 +629,7 @@ __global__ void __launch_bounds__(kInferThreads, 3) mlp_infer_kernel(const Learn
     }
     if (!ok && leader) atomicOr(P.status, 1u);
     tc_sync();
-    if (warp == 0) tmem_dealloc(s_tmem, 64 * kInferGroups);
+    if (warp == 0) tmem_dealloc(s_tmem, kInferCols);
 }
 
 // ------------------------------------------------------- MLP training
@@ -930,9 +969,10 @@ void launch_learned_rows(const LearnedParams& P, cudaStream_t s) {
 void launch_mlp_infer(const LearnedParams& P, int num_sms, cudaStream_t s) {
     if (P.n <= 0) return;
     const long long tiles = (P.n + 127) / 128;
-    // Three CTAs per SM (3 x 57 KB of shared memory, 3 x 128 TMEM columns).
-    const long long groups = (long long)num_sms * 3 * kInferGroups;
-    const long long grid = (tiles < groups ? tiles + kInferGroups - 1 : groups) / kInferGroups;
+    // kInferBlocksPerSM resident CTAs per SM, each taking kInferGroups x kInferTiles tiles a step.
+    const long long per_cta = (long long)kInferGroups * kInferTiles;
+    const long long slots = (long long)num_sms * kInferBlocksPerSM * per_cta;
+    const long long grid = (tiles < slots ? tiles + per_cta - 1 : slots) / per_cta;
     if (P.rows) {
         cudaFuncSetAttribute(mlp_infer_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem);
         mlp_infer_kernel<true><<<(unsigned)grid, kInferThreads, kInferSmem, s>>>(P);
