@@ -182,9 +182,14 @@ def make_scene(args):
     return scenes.make(args.config, seed=args.seed)
 
 
-def algorithmic_bytes(sc, stats, launches_per_frame):
+def algorithmic_bytes(sc, stats, launches_per_frame, sampler="software", fused_single=False):
     """Per-launch algorithmic HBM bytes of each frame kernel (the minimum a
-    kernel must move: inputs read once, outputs written once)."""
+    kernel must move: inputs read once, outputs written once).  The radiance
+    chain is written in the layouts the sampler reads: the bordered fp32 copy
+    (software, hybrid), the texture array's binary16 copy (hybrid, levels,
+    hardware) and the linear binary16 chain.  A single-scene fused frame
+    whose sampler reads both copies writes the linear chain only from level
+    4 (the mip tail's source) on."""
     N = sc.dim
     nv = N ** 3
     T = sc.ntri
@@ -194,18 +199,22 @@ def algorithmic_bytes(sc, stats, launches_per_frame):
     U = stats["unique_voxels"]
     C = stats.get("covered_pixels", P)
     lv = lambda a, b: sum((N >> l) ** 3 for l in range(a, min(b, sc.levels)))  # noqa: E731
+    tex = sampler in ("hybrid", "levels", "hardware")
+    pad = sampler in ("hybrid", "software")
+    linear_from = 4 if (fused_single and tex and pad) else 0
+    per_texel = (8 if tex else 0) + (16 if pad else 0)
     return {
         # triangles in (positions, normals, albedo); the 32-byte record of every occupied voxel read and
         # written once (fragments of one voxel meet in L2); the occupancy mask written once
         "accumulate": T * (36 + 36 + 12) + U * 32 * 2 + nv // 8,
         # shadow map read, lit bit set per texel (bit mask written once)
         "inject_mark": SW * SH * 4 + nv // 8,
-        # occupancy and lit masks read; records of occupied voxels read and zeroed; colour, normal,
-        # radiance level 0 written (RGBA16F); radiance levels 1-4 written; the software sampler's
-        # bordered fp32 copy of levels 0-4 written (interiors)
-        "resolve": nv // 8 * 2 + U * 32 * 2 + nv * 8 * 3 + lv(1, 5) * 8 + lv(0, 5) * 16,
-        # level 4 read, levels 5.. written (RGBA16F and the bordered fp32 copy)
-        "mip_tail": (N >> 4) ** 3 * 8 + lv(5, 99) * (8 + 16),
+        # occupancy and lit masks read; records of occupied voxels read and zeroed; colour and normal
+        # level 0 written (RGBA16F); radiance levels 0-4 written in the sampler's copies (interiors of
+        # the bordered one) and in the linear chain
+        "resolve": nv // 8 * 2 + U * 32 * 2 + nv * 8 * 2 + lv(linear_from, 5) * 8 + lv(0, 5) * per_texel,
+        # level 4 read, levels 5.. written (the linear chain and the sampler's copies)
+        "mip_tail": (N >> 4) ** 3 * 8 + lv(5, 99) * (8 + per_texel),
         # G-buffer positions read for every pixel, normals and albedo only for covered ones (gp.w != 0),
         # composite float4 written for every pixel
         "trace": P * (16 + 16) + C * 32,
@@ -473,7 +482,7 @@ def run_ours(args, rank, world):
         art["stats"] = dict(stats)
 
     # ---- roofline of the dominant kernel
-    alg = algorithmic_bytes(sc, stats, None)
+    alg = algorithmic_bytes(sc, stats, None, sampler=args.filter, fused_single=params.temporal_filter == 0)
     kernel_ms = {"accumulate": stage["voxelize_ms"], "inject_mark": stage["radiance_ms"],
                  "resolve+mips": stage["mipmap_ms"], "trace": stage["render_ms"]}
     dom = max(kernel_ms, key=kernel_ms.get)
@@ -735,7 +744,7 @@ def run_batch(args, rank, world, compact=False):
 
     # roofline of the dominant stage: algorithmic bytes summed over scenes
     stats = [ctx.stats(stream) for ctx in b.scenes]
-    alg = [algorithmic_bytes(sc, st, None) for sc, st in zip(scs, stats)]
+    alg = [algorithmic_bytes(sc, st, None, sampler=args.filter) for sc, st in zip(scs, stats)]
     sums = {k: sum(a[k] for a in alg) for k in alg[0]}
     stage_bytes = {"voxelize_ms": sums["accumulate"],
                    "mipmap_ms": sums["inject_mark"] + sums["resolve"] + sums["mip_tail"],
@@ -1050,14 +1059,14 @@ def run_dynamic(args, rank, world):
 # stage, from one ncu capture of the large frame (`bench.py --profile-frames 3`, default
 # launch shapes): accumulate = setup + raster, resolve+mips = resolve + tail; only for the
 # default workload, and only while the frame kernels' sources hash to NCU_CAPTURE_DIGEST.
-NCU_CAPTURE_DIGEST = "31ab859802622a6c"
+NCU_CAPTURE_DIGEST = "3f49e0ad1e33aba5"
 NCU_CAPTURE_SAMPLER = "hybrid"
-NCU_TRAFFIC = {"accumulate": 18.894e6 + 317.959e6 + 180.398e6, "resolve+mips": 316.371e6 + 991.991e6 + 0.046e6,
-               "inject_mark": 18.284e6, "trace": 89.188e6 + 12.647e6}
+NCU_TRAFFIC = {"accumulate": 18.890e6 + 317.639e6 + 180.502e6, "resolve+mips": 315.985e6 + 839.123e6 + 0.047e6,
+               "inject_mark": 18.286e6, "trace": 89.188e6 + 13.100e6}
 # Issue-side figures of the cone tracer (hybrid sampler) from its full capture of the same
 # command: it is bound by issue and load latency at its occupancy, not HBM.
-NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.635, "fma_pipe_frac": 0.440, "l1_hit_rate": 0.971,
-                   "l1_lsu_data_pipe_frac": 0.664, "l1_tex_data_pipe_frac": 0.241}
+NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.632, "fma_pipe_frac": 0.440, "l1_hit_rate": 0.971,
+                   "l1_lsu_data_pipe_frac": 0.661, "l1_tex_data_pipe_frac": 0.240}
 
 
 def load_peaks() -> dict:

@@ -288,7 +288,13 @@ vct_status vct_destroy(vct_ctx* ctx);
 vct_status vct_set_params(vct_ctx* ctx, const vct_params* params);
 vct_status vct_get_params(const vct_ctx* ctx, vct_params* out);
 vct_status vct_get_config(const vct_ctx* ctx, vct_config* out);
-/* Device pointer of one level of a volume (read-only view for callers). */
+/* Device pointer of one level of a volume (read-only view for callers).
+ * With VCT_FILTER_HYBRID and no temporal filter, vct_frame / vct_frame_volume
+ * leave the linear copy of radiance levels 0-3 to the sampler's texture array
+ * (the same binary16 texels); the first call for such a level synchronises
+ * the device and copies them back.  The stage entry points that read the
+ * radiance chain (vct_normalize, vct_inject, vct_build_mips,
+ * vct_decay_radiance) do the same copy on their stream. */
 vct_status vct_volume_level(const vct_ctx* ctx, int32_t volume, int32_t level,
                             const uint16_t** data_dev, int32_t* dim);
 /* Device pointers of the integer accumulators: one 8 x uint32 record per

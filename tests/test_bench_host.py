@@ -61,6 +61,13 @@ def test_algorithmic_bytes_of_the_large_frame():
     assert a["mip_tail"] == (N >> 4) ** 3 * 8 + lv(5, 9) * 24
     # 1.06 GB for resolve + tail: 170 MB read (masks, occupied records), 895 MB written
     assert 1.0e9 < a["resolve"] + a["mip_tail"] < 1.1e9
+    # the hybrid sampler's fused frame: both sampler copies, the linear chain from level 4 on
+    h = bench.algorithmic_bytes(sc, stats, None, sampler="hybrid", fused_single=True)
+    assert h["resolve"] == nv // 4 + 5181082 * 64 + nv * 16 + lv(4, 5) * 8 + lv(0, 5) * 24
+    assert h["mip_tail"] == (N >> 4) ** 3 * 8 + lv(5, 9) * 32
+    # a batch writes the whole linear chain as well
+    b = bench.algorithmic_bytes(sc, stats, None, sampler="hybrid")
+    assert b["resolve"] - h["resolve"] == lv(0, 4) * 8
 
 
 def test_peaks_come_from_the_measured_file():

@@ -282,3 +282,34 @@ def test_hybrid_sampler_staged_and_fused(cornell):
         torch.cuda.synchronize()
         assert np.array_equal(irr.cpu().numpy(), staged["irr"])
         assert np.array_equal(spec.cpu().numpy(), staged["spec"])
+        # levels 0-3 of the linear chain come back from the texture array
+        assert np.array_equal(read_chain(ctx), ref["chain"])
+
+
+def test_hybrid_frame_then_stage_paths(cornell):
+    """A fused hybrid frame without the temporal filter leaves the linear copy
+    of radiance levels 0-3 to the texture array.  The entry points that read
+    the linear chain copy it back first: build_mips, a temporal frame (which
+    reads last frame's level 0) and the radiance decay give the chain a
+    software-sampler context, which writes every linear level, holds."""
+    import torch
+
+    sc, g, ref, _ = cornell
+    chains = {}
+    for filt in (L.VCT_FILTER_SOFTWARE, L.VCT_FILTER_HYBRID):
+        with api.Context(api.config_for(sc)) as ctx:
+            ctx.set_params(api.scene_params(sc, trace_filter=filt))
+            irr, spec, col, samples = g.new_outputs()
+            ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(irr, spec, col, samples))
+            ctx.build_mips()
+            torch.cuda.synchronize()
+            assert np.array_equal(read_chain(ctx), ref["chain"])
+            ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(irr, spec, col, samples))
+            ctx.set_params(api.scene_params(sc, trace_filter=filt, temporal_filter=1, temporal_decay=0.8))
+            ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(irr, spec, col, samples))
+            ctx.decay_radiance()
+            ctx.build_mips()
+            torch.cuda.synchronize()
+            chains[filt] = read_chain(ctx)
+    assert np.array_equal(chains[L.VCT_FILTER_SOFTWARE], chains[L.VCT_FILTER_HYBRID])
+    assert not np.array_equal(chains[L.VCT_FILTER_HYBRID], ref["chain"])

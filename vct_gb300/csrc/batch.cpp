@@ -184,6 +184,15 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
 vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cudaStream_t st, bool timed = false) {
     const int n = b->n;
     VCT_CUDA(cudaMemcpyAsync(b->d_blob, h, b->blob_bytes, cudaMemcpyHostToDevice, st));
+    // A batched frame writes every level of the linear chain; the temporal
+    // filter reads last frame's level 0 from it.
+    for (vct_ctx* c : b->ctx) {
+        if (c->params.temporal_filter) {
+            vct_status s = sync_linear(c, st);
+            if (s != VCT_OK) return s;
+        }
+        c->linear_stale = 0;
+    }
     const ClearRange* d_clear = reinterpret_cast<const ClearRange*>(b->d_blob + b->off_clear);
     launch_clear_ranges(d_clear, tot.n_pre, tot.max_pre, st);
     VCT_CHECK_LAUNCH("batch: clear");

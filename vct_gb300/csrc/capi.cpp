@@ -486,11 +486,34 @@ vct_status ensure_texture(vct_ctx* ctx) {
     return VCT_OK;
 }
 
+// A fused frame whose sampler reads both the texture array and the bordered
+// chain writes the linear chain only from level `linear_stale` on: the levels
+// below are in the texture array, texel for texel the same binary16 values.
+// Entry points that read the linear chain copy them back first.
+vct_status sync_linear(vct_ctx* ctx, cudaStream_t s) {
+    if (ctx->linear_stale <= 0) return VCT_OK;
+    for (int l = 0; l < ctx->linear_stale; ++l) {
+        cudaArray_t arr;
+        VCT_CUDA(cudaGetMipmappedArrayLevel(&arr, ctx->tex_array, l));
+        int S = ctx->dim >> l;
+        cudaMemcpy3DParms p;
+        std::memset(&p, 0, sizeof p);
+        p.srcArray = arr;
+        p.dstPtr = make_cudaPitchedPtr(level_ptr(ctx->radiance, ctx, l), (size_t)S * 8, S, S);
+        p.extent = make_cudaExtent(S, S, S);
+        p.kind = cudaMemcpyDeviceToDevice;
+        VCT_CUDA(cudaMemcpy3DAsync(&p, s));
+    }
+    ctx->linear_stale = 0;
+    return VCT_OK;
+}
+
 // Copies the linear radiance chain into the mip-mapped array of the
 // texture-unit sampler.
 vct_status refresh_texture(vct_ctx* ctx, cudaStream_t s) {
     vct_status st = ensure_texture(ctx);
     if (st != VCT_OK) return st;
+    if ((st = sync_linear(ctx, s)) != VCT_OK) return st;
     for (int l = 0; l < ctx->levels; ++l) {
         cudaArray_t arr;
         VCT_CUDA(cudaGetMipmappedArrayLevel(&arr, ctx->tex_array, l));
@@ -550,6 +573,8 @@ vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], co
 
 vct_status ensure_padded_chain(vct_ctx* c, cudaStream_t st) {
     if (c->pad_ready) return VCT_OK;
+    vct_status s = sync_linear(c, st);
+    if (s != VCT_OK) return s;
     launch_pad_copy(c->radiance, c->pchain, c->dim, c->levels, st);
     VCT_CHECK_LAUNCH("bordered chain copy");
     c->pad_ready = true;
@@ -788,6 +813,17 @@ vct_status vct_volume_level(const vct_ctx* c, int32_t volume, int32_t level, con
         default: return fail(VCT_ERR_INVALID_ARGUMENT, "unknown volume");
     }
     if (level < 0 || level >= nl) return fail(VCT_ERR_INVALID_ARGUMENT, "level out of range for this volume");
+    if (volume == VCT_VOLUME_RADIANCE && level < c->linear_stale) {
+        // The level is in the texture array only (a fused frame's hybrid
+        // sampler): copied back once, after all work queued on the device.
+        vct_ctx* m = const_cast<vct_ctx*>(c);
+        DeviceScope ds(m->device);
+        VCT_CUDA(ds.err);
+        VCT_CUDA(cudaDeviceSynchronize());
+        vct_status s = sync_linear(m, nullptr);
+        if (s != VCT_OK) return s;
+        VCT_CUDA(cudaStreamSynchronize(nullptr));
+    }
     *data = reinterpret_cast<const uint16_t*>(base + c->level_off[level]);
     if (dim) *dim = c->dim >> level;
     return VCT_OK;
@@ -835,6 +871,8 @@ vct_status vct_normalize(vct_ctx* c, void* stream) {
     DeviceScope ds(c->device);
     VCT_CUDA(ds.err);
     cudaStream_t st = as_stream(stream);
+    vct_status s = sync_linear(c, st);  // the temporal filter reads last frame's level 0
+    if (s != VCT_OK) return s;
     if (c->stats_reset_pending) VCT_CUDA(cudaMemsetAsync(c->stats, 0, sizeof(StatsDev), st));
     NormalizeParams P;
     fill_norm(c, P);
@@ -880,6 +918,7 @@ vct_status vct_inject(vct_ctx* c, const vct_shadow_desc* shadow, const float eye
     InjectParams P;
     fill_inject(c, shadow, eye, P);
     cudaStream_t st = as_stream(stream);
+    if ((s = sync_linear(c, st)) != VCT_OK) return s;
     if (P.temporal && P.lighting && !P.dilate) {
         // the relit stores read the seeded radiance: one store per marked voxel
         VCT_CUDA(cudaMemsetAsync(c->lit, 0, (size_t)((c->nv + 31) / 32) * 4, st));
@@ -901,6 +940,8 @@ vct_status vct_build_mips(vct_ctx* c, int32_t volume, void* stream) {
     VCT_CUDA(ds.err);
     cudaStream_t st = as_stream(stream);
     if (volume == VCT_VOLUME_RADIANCE) {
+        vct_status s = sync_linear(c, st);
+        if (s != VCT_OK) return s;
         launch_mips(mip_levels(c, c->radiance, c->levels), 0, st);
         VCT_CHECK_LAUNCH("build mips");
         if (filter_uses_texture(c->params.trace_filter)) {
@@ -1012,6 +1053,8 @@ vct_status frame_volume(vct_ctx* c, const vct_triangles* tris, const vct_light* 
     const bool hw = filter_uses_texture(c->params.trace_filter);
     const bool pad = filter_uses_bordered(c->params.trace_filter);
     if (hw && (s = ensure_texture(c)) != VCT_OK) return s;
+    // The temporal filter reads last frame's level 0 from the linear chain.
+    if (c->params.temporal_filter && (s = sync_linear(c, st)) != VCT_OK) return s;
     ResolveParams R;
     std::memset(&R, 0, sizeof R);
     fill_norm(c, R.norm);
@@ -1027,8 +1070,14 @@ vct_status frame_volume(vct_ctx* c, const vct_triangles* tris, const vct_light* 
     R.mip_levels = std::min(4, c->levels - 1);
     // The sampler's own copy of the chain is written by the same kernels:
     // texture-unit surfaces, or the bordered chain of the software sampler.
+    // When the sampler reads both (hybrid) and no temporal filter reads last
+    // frame's radiance, the linear copy of the levels below the resolve's last
+    // one is not written: they are in the texture array, texel for texel, and
+    // sync_linear copies them back for the entry points that read them.  The
+    // last level stays, as the mip tail's source.
+    const int stale = (hw && pad && !c->params.temporal_filter) ? R.mip_levels : 0;
     for (int l = 0; l <= R.mip_levels; ++l) {
-        R.radiance_levels[l] = level_ptr(c->radiance, c, l);
+        R.radiance_levels[l] = l < stale ? nullptr : level_ptr(c->radiance, c, l);
         R.surf[l] = hw ? c->surf[l] : 0;
         R.pad_levels[l] = pad ? c->pchain + padded_level_offset(c->dim, l) : nullptr;
     }
@@ -1046,6 +1095,7 @@ vct_status frame_volume(vct_ctx* c, const vct_triangles* tris, const vct_light* 
     }
     c->tex_ready = hw;
     c->pad_ready = pad;
+    c->linear_stale = stale;
     c->stats_reset_pending = true;
     c->radiance_ready = true;
     c->mips_ready = true;
@@ -1227,6 +1277,8 @@ vct_status vct_decay_radiance(vct_ctx* c, void* stream) {
     if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
     DeviceScope ds(c->device);
     VCT_CUDA(ds.err);
+    vct_status s = sync_linear(c, as_stream(stream));
+    if (s != VCT_OK) return s;
     launch_decay(c->radiance, c->nv, c->params.temporal_decay, as_stream(stream));
     VCT_CHECK_LAUNCH("decay radiance");
     c->mips_ready = false;

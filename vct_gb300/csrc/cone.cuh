@@ -15,10 +15,12 @@ namespace cone {
 
 __device__ __forceinline__ f3 fnormalize(f3 v) { return mul(v, rsqrtf(dot(v, v))); }
 
-__device__ __forceinline__ float4 texel(const uint2* __restrict__ base, int S, int i, int j, int k) {
+// Texel (i, j, k) of level 0 from the bordered chain (0 outside the level).
+__device__ __forceinline__ float4 texel0(const float4* __restrict__ pchain, int S, int i, int j, int k) {
     if ((unsigned)i >= (unsigned)S || (unsigned)j >= (unsigned)S || (unsigned)k >= (unsigned)S)
         return make_float4(0.f, 0.f, 0.f, 0.f);
-    return unpack_h4(__ldg(base + ((k * S + j) * S + i)));
+    const int Pd = S + 2;
+    return __ldg(pchain + (((k + 1) * Pd + (j + 1)) * Pd + (i + 1)));
 }
 
 __device__ __forceinline__ float4 lerp4(float4 p, float4 q, float t) {
@@ -113,7 +115,7 @@ __device__ __forceinline__ float4 sample_lod(const TraceParams& P, const int* of
     }
     if (lambda <= 0.0f) {  // magnification: GL_NEAREST on level 0 (index S = border)
         const int S = P.dim;
-        return texel(P.chain, S, (int)floorf(p.x * S), (int)floorf(p.y * S), (int)floorf(p.z * S));
+        return texel0(P.pchain + off[0], S, (int)floorf(p.x * S), (int)floorf(p.y * S), (int)floorf(p.z * S));
     }
     const bool guard = warp_leaves_volume(P.warp.mode);
     if (lambda >= (float)q) return trilinear(P, off, q, p, guard);

@@ -40,6 +40,9 @@ struct vct_ctx {
     long long vox_scratch_bytes = 0;
     float4* pchain = nullptr;  // bordered fp32 radiance chain read by the software sampler
     bool pad_ready = false;   // pchain holds the current radiance chain
+    // Levels [0, linear_stale) of the linear radiance chain were left to the
+    // texture array by the last fused frame (sync_linear copies them back).
+    int linear_stale = 0;
     vct_tuning tuning;        // launch shapes (vct_set_tuning / vct_autotune)
     void* learned = nullptr;  // learned-trace scratch (quarter-res features, tile errors, fallback list)
     size_t learned_bytes = 0;
@@ -118,6 +121,9 @@ vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], co
                       TraceParams& P);
 // Makes the bordered fp32 chain of the software sampler current.
 vct_status ensure_padded_chain(vct_ctx* ctx, cudaStream_t s);
+// Makes every level of the linear radiance chain current (copies back the
+// levels a fused frame left in the texture array).
+vct_status sync_linear(vct_ctx* ctx, cudaStream_t s);
 
 }  // namespace host
 }  // namespace vct

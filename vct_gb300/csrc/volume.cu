@@ -128,7 +128,7 @@ __device__ __forceinline__ void reduce_level(const uint2* src, uint2* dst, int S
         }
         uint2 r = box8(c);
         dst[t] = r;
-        gdst[((long long)(gz0 + z) * gS + (gy0 + y)) * gS + (gx0 + x)] = r;
+        if (gdst) gdst[((long long)(gz0 + z) * gS + (gy0 + y)) * gS + (gx0 + x)] = r;
         if (surf) surf3Dwrite(r, surf, (gx0 + x) * (int)sizeof(uint2), gy0 + y, gz0 + z);
         if (pdst) pdst[pad_index(gx0 + x, gy0 + y, gz0 + z, gS)] = unpack_h4(r);
     }
@@ -270,7 +270,8 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
         }
         store4(P.color + v0, col);
         store4(P.normal + v0, nrm);
-        store4(P.radiance + v0, rad);
+        // the fused frame may leave the linear copy of level 0 to the texture array
+        if (!FUSED || R.radiance_levels[0]) store4((FUSED ? R.radiance_levels[0] : P.radiance) + v0, rad);
         if (FUSED) {
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
