@@ -380,25 +380,16 @@ def run_ours(args, rank, world):
     # uploads its triangles, shadow map and G-buffer from pinned host memory and reads its image
     # back, and those copies run on two copy streams beside the frames.  Step k+1's triangles and
     # shadow map go up once step k's volume pass has consumed them (during step k's trace), its
-    # G-buffer into the other of two device buffers, and step k's image comes back in two row
-    # halves while step k+1's volume pass runs.  The K steps are timed as one region; each step
-    # moves 138 MB in and 33 MB out and touches over 1 GB of HBM (more than L2), so no flush runs
-    # between them.
+    # G-buffer into the other of two device buffers, and step k's image comes back while step
+    # k+1's volume pass runs.  The K steps are timed as one region; each step moves 138 MB in and
+    # 33 MB out and touches over 1 GB of HBM (more than L2), so no flush runs between them.
     up = torch.cuda.Stream(device=dev)
     down = torch.cuda.Stream(device=dev)
     d_gb = [(d_gpos, d_gnrm, d_galb)] + [tuple(torch.empty_like(t) for t in (d_gpos, d_gnrm, d_galb))]
     d_col = [color, torch.empty_like(color)]
-    half = H // 2
-    rows = lambda t, r0, r1: t[r0 * W * 4:r1 * W * 4]  # noqa: E731
-    plans = []  # per buffer parity: the two halves' (gbuffer, trace_out, device rows, host rows)
-    for par in range(2):
-        gp, gn, ga = d_gb[par]
-        plans.append([(api.gbuffer(rows(gp, r0, r1), rows(gn, r0, r1), rows(ga, r0, r1), W, r1 - r0),
-                       api.trace_out(color=rows(d_col[par], r0, r1)), rows(d_col[par], r0, r1), rows(h_color, r0, r1))
-                      for r0, r1 in ((0, half), (half, H))])
+    plans = [(api.gbuffer(*d_gb[par], W, H), api.trace_out(color=d_col[par])) for par in range(2)]
     ev_tri, ev_vol = torch.cuda.Event(), torch.cuda.Event()
     ev_gb = [torch.cuda.Event(), torch.cuda.Event()]
-    ev_top = [torch.cuda.Event(), torch.cuda.Event()]
     ev_done = [torch.cuda.Event(), torch.cuda.Event()]
     ev_d2h = [torch.cuda.Event(), torch.cuda.Event()]
 
@@ -418,16 +409,12 @@ def run_ours(args, rank, world):
         ev_vol.record(stream)
         stream.wait_event(ev_gb[par])
         stream.wait_event(ev_d2h[par])  # the image of two steps ago has been read back
-        (g0, o0, c0, hc0), (g1, o1, c1, hc1) = plans[par]
-        ctx.trace(g0, sc.eye, o0, stream)
-        ev_top[par].record(stream)
-        ctx.trace(g1, sc.eye, o1, stream)
+        g, o = plans[par]
+        ctx.trace(g, sc.eye, o, stream)
         ev_done[par].record(stream)
-        down.wait_event(ev_top[par])
+        down.wait_event(ev_done[par])
         with torch.cuda.stream(down):
-            hc0.copy_(c0, non_blocking=True)
-            down.wait_event(ev_done[par])
-            hc1.copy_(c1, non_blocking=True)
+            h_color.copy_(d_col[par], non_blocking=True)
             ev_d2h[par].record(down)
 
     for k in range(max(3, args.warmup)):
@@ -533,9 +520,9 @@ def run_ours(args, rank, world):
         "samplers": samplers,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/frame", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
-                "path": "vct_frame_volume + two half-frame vct_trace calls per step, frames in flight: the next "
-                        "step's uploads run during this step's trace (G-buffer double-buffered), this step's image "
-                        "comes back during the next volume pass; K steps timed as one region",
+                "path": "vct_frame_volume + vct_trace per step, frames in flight: the next step's uploads run "
+                        "during this step's trace (G-buffer and image double-buffered), this step's image comes "
+                        "back during the next volume pass; K steps timed as one region",
                 "l2": "no flush: steps overlap, each moves 138 MB in and 33 MB out and touches over 1 GB of HBM"},
         "gpu_launches": int(launches),
         "roofline": roofline,
