@@ -542,7 +542,6 @@ vct_status fill_trace(vct_ctx* ctx, const vct_gbuffer* g, const float eye[3], co
     P.specular = reinterpret_cast<float4*>(out->specular_dev);
     P.color = reinterpret_cast<float4*>(out->color_dev);
     P.samples = out->sample_count_dev;
-    P.chain = ctx->radiance;
     P.pchain = ctx->pchain;
     P.dim = ctx->dim;
     P.levels = ctx->levels;

@@ -226,8 +226,7 @@ struct TraceParams {
     float4* specular;
     float4* color;
     unsigned long long* samples;
-    const uint2* chain;   // linear chain (nearest-level magnification)
-    const float4* pchain;  // bordered fp32 chain (software trilinear)
+    const float4* pchain;  // bordered fp32 chain (software trilinear, nearest-level magnification)
     int dim, levels;
     f3 vmin, vmax, vcenter, eye;
     vct_cone_settings diffuse, specular_cone;
