@@ -55,6 +55,14 @@ def warped(request):
     ctx2.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(irr2, spec2, col2, samples2))
     torch.cuda.synchronize()
     fused = dict(chain=read_chain(ctx2), irr=irr2.cpu().numpy(), stats=ctx2.stats())
+    # the fused frame with the hybrid sampler, on a third context
+    ctx3 = api.Context(api.config_for(sc))
+    ctx3.set_params(api.scene_params(sc, warp_mode=mode, trace_filter=L.VCT_FILTER_HYBRID))
+    irr3, spec3, col3, samples3 = g.new_outputs()
+    ctx3.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(irr3, spec3, col3, samples3))
+    torch.cuda.synchronize()
+    fused["hybrid_irr"] = irr3.cpu().numpy()
+    fused["hybrid_chain"] = read_chain(ctx3)
     return mode, sc, ref, ref64, stages, fused
 
 
@@ -133,6 +141,17 @@ def test_warped_trace_matches_oracles(warped):
     print(f"warp mode {mode}: irradiance rel L2 vs fp64 {e64:.2e}")
     assert e64 <= 1e-3
     assert np.array_equal(st["irr"].view(np.uint32), fused["irr"].view(np.uint32))
+
+
+def test_warped_hybrid_sampler_within_bar(warped):
+    """The hybrid sampler (the heavier-weighted level of each sample exact, the
+    other by the texture units) on the warped chain: held to the 1e-3 fp64 bar,
+    and its frame's chain equals the oracle's."""
+    mode, sc, ref, ref64, st, fused = warped
+    assert np.array_equal(fused["hybrid_chain"], ref["chain"])
+    e64 = rel_l2(rgb(fused["hybrid_irr"]), rgb(ref64[0]))
+    print(f"warp mode {mode}: hybrid irradiance rel L2 vs fp64 {e64:.2e}")
+    assert e64 <= 1e-3
 
 
 def test_batch_with_analytic_warp_equals_single_frames():
