@@ -1072,14 +1072,14 @@ def run_dynamic(args, rank, world):
 # stage, from one ncu capture of the large frame (`bench.py --profile-frames 3`, default
 # launch shapes): accumulate = setup + raster, resolve+mips = resolve + tail; only for the
 # default workload, and only while the frame kernels' sources hash to NCU_CAPTURE_DIGEST.
-NCU_CAPTURE_DIGEST = "3f49e0ad1e33aba5"
+NCU_CAPTURE_DIGEST = "5ead3d40972ea19f"
 NCU_CAPTURE_SAMPLER = "hybrid"
-NCU_TRAFFIC = {"accumulate": 18.890e6 + 317.639e6 + 180.502e6, "resolve+mips": 315.985e6 + 839.123e6 + 0.047e6,
-               "inject_mark": 18.286e6, "trace": 89.188e6 + 13.100e6}
+NCU_TRAFFIC = {"accumulate": 18.890e6 + 317.604e6 + 180.500e6, "resolve+mips": 308.164e6 + 837.048e6 + 0.047e6,
+               "inject_mark": 18.285e6, "trace": 89.186e6 + 12.669e6}
 # Issue-side figures of the cone tracer (hybrid sampler) from its full capture of the same
 # command: it is bound by issue and load latency at its occupancy, not HBM.
-NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.632, "fma_pipe_frac": 0.440, "l1_hit_rate": 0.971,
-                   "l1_lsu_data_pipe_frac": 0.661, "l1_tex_data_pipe_frac": 0.240}
+NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.636, "fma_pipe_frac": 0.438, "l1_hit_rate": 0.971,
+                   "l1_lsu_data_pipe_frac": 0.664, "l1_tex_data_pipe_frac": 0.241}
 
 
 def load_peaks() -> dict:
@@ -1220,7 +1220,7 @@ def irradiance_accuracy(gpu: np.ndarray, ref: np.ndarray, covered: np.ndarray, f
     return out
 
 
-KERNEL_SOURCES = ("cone.cuh", "vct_device.cuh", "warp.cuh", "voxelize.cu", "volume.cu", "trace.cu")
+KERNEL_SOURCES = ("cone.cuh", "vct_device.cuh", "vct_internal.h", "warp.cuh", "voxelize.cu", "volume.cu", "trace.cu")
 
 
 def kernel_sources_digest() -> str:

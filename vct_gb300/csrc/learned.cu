@@ -231,7 +231,7 @@ __device__ __forceinline__ void pixel_features(const LearnedParams& P, long long
     const f3 sp = mk(fmaf(N.x, step, vp.x), fmaf(N.y, step, vp.y), fmaf(N.z, step, vp.z));
     float4 near = make_float4(0.f, 0.f, 0.f, 0.f);
     if (sp.x >= 0.f && sp.y >= 0.f && sp.z >= 0.f && sp.x <= 1.f && sp.y <= 1.f && sp.z <= 1.f) {
-        const int off[2] = {0, (int)padded_level_offset(T.dim, 1)};
+        const int off[2] = {(int)padded_level_offset(T.dim, 0), (int)padded_level_offset(T.dim, 1)};
         near = cone::trilinear(T, off, 1, T.warp.mode ? apply_warp(T.warp, sp) : sp, warp_leaves_volume(T.warp.mode));
     }
     f[16] = bf16x2(N.x, N.y);

@@ -22,11 +22,19 @@ struct f3 {
 // which every level of side S is stored as (S+2)^3 voxels: the level plus a
 // one-voxel shell of zeros (the GL clamp-to-border colour), so that any
 // trilinear footprint of a position in [0,1]^3 lies inside the array.
-// Offset (in voxels) of padded level l:
-//   sum_{i<l} (S_i + 2)^3 = 8(N^3-S^3)/7 + 8(N^2-S^2) + 24(N-S) + 8l,  S = N >> l.
+// Each level starts at an odd texel offset: with rows of an even number of
+// 16-byte texels, the interior of every row then starts on a 32-byte sector,
+// and the resolve's rows of 16 texels fill whole sectors instead of sharing
+// one with the border or the neighbouring brick.  Offset (in texels) of
+// padded level l:
 VCT_HD inline long long padded_level_offset(int N, int l) {
-    const long long n = N, s = N >> l;
-    return (n * n * n - s * s * s) / 7 * 8 + 8 * (n * n - s * s) + 24 * (n - s) + 8LL * l;
+    long long off = 1;
+    for (int i = 0; i < l; ++i) {
+        const long long p = (N >> i) + 2;
+        off += p * p * p;
+        off += (off & 1) ? 0 : 1;
+    }
+    return off;
 }
 
 // Voxel warping (VCT_WARP_*): the texture mode's map is 32^3 RGBA16 unorm
