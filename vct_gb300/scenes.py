@@ -224,7 +224,9 @@ def _finish(name, tris, nrms, alb, lights, ls, dim, levels, vmax, shadow_size, e
         pv=colmajor(perspective(fovy, W / H, 1.0, 20.0) @ look_at(eye, target, (0, 1, 0))))
 
 
-BASELINE_CONES = dict(diffuse=(16, 60 * DEG, 1.0, 1.0, 0.5), specular=(32, 10 * DEG, 1.7, 0.5, 0.1))
+# The benchmark frames' cones (steps, aperture, bias, initial height, LOD offset): 6 diffuse
+# cones of 60 degrees and one specular cone of 10 degrees.
+FRAME_CONES = dict(diffuse=(16, 60 * DEG, 1.0, 1.0, 0.5), specular=(32, 10 * DEG, 1.7, 0.5, 0.1))
 
 
 def cornell(seed: int = 0, dim: int = 64, shadow: int = 512, gbuffer=(640, 360)) -> Scene:
@@ -252,7 +254,7 @@ def cornell(seed: int = 0, dim: int = 64, shadow: int = 512, gbuffer=(640, 360))
     levels = int(np.log2(dim)) + 1
     return _finish("cornell", np.concatenate(tris), np.concatenate(nrms), np.concatenate(alb), [light], ls, dim,
                    levels, 1.0, (shadow, shadow), np.array([0.0, 1.6, 2.6]), np.array([0.0, -0.4, 0.0]), 50 * DEG,
-                   tuple(gbuffer), BASELINE_CONES)
+                   tuple(gbuffer), FRAME_CONES)
 
 
 def large(seed: int = 0, dim: int = 256, shadow: int = 2048, gbuffer=(1920, 1080), n_boxes: int = 4096,
@@ -285,7 +287,7 @@ def large(seed: int = 0, dim: int = 256, shadow: int = 2048, gbuffer=(1920, 1080
     levels = int(np.log2(dim)) + 1
     return _finish("large", np.concatenate(tris), np.concatenate(nrms), np.concatenate(alb), lights, ls, dim, levels,
                    1.0, (shadow, shadow), np.array([0.0, 0.5, 2.8]), np.array([0.0, 0.0, 0.0]), 55 * DEG,
-                   tuple(gbuffer), BASELINE_CONES)
+                   tuple(gbuffer), FRAME_CONES)
 
 
 def tiny(seed: int = 0, dim: int = 16, shadow: int = 64, gbuffer=(48, 32), n_boxes: int = 6) -> Scene:
@@ -305,7 +307,7 @@ def tiny(seed: int = 0, dim: int = 16, shadow: int = 64, gbuffer=(48, 32), n_box
     levels = int(np.log2(dim)) + 1
     return _finish("tiny", np.concatenate(tris), np.concatenate(nrms), np.concatenate(alb), lights, ls, dim, levels,
                    1.0, (shadow, shadow), np.array([0.3, 0.9, 2.4]), np.array([0.0, 0.0, 0.0]), 50 * DEG,
-                   tuple(gbuffer), BASELINE_CONES)
+                   tuple(gbuffer), FRAME_CONES)
 
 
 def stacked_slivers(copies: int = 1600, seed: int = 0, dim: int = 64, shadow: int = 64,
@@ -325,7 +327,7 @@ def stacked_slivers(copies: int = 1600, seed: int = 0, dim: int = 64, shadow: in
     light, ls = _directional_light(rng, 1.0)
     levels = int(np.log2(dim)) + 1
     return _finish("slivers", tris, nrms, alb, [light], ls, dim, levels, 1.0, (shadow, shadow),
-                   np.array([0.0, 0.5, 2.5]), np.zeros(3), 50 * DEG, tuple(gbuffer), BASELINE_CONES)
+                   np.array([0.0, 0.5, 2.5]), np.zeros(3), 50 * DEG, tuple(gbuffer), FRAME_CONES)
 
 
 # Batched scene family: per scene a triangle count log-uniform in [1k, 200k]
@@ -361,7 +363,7 @@ def batch_scene(seed: int = 0, index: int = 0, shadow: int = 1024) -> Scene:
     eye = np.array([2.8 * np.sin(phi), rng.uniform(0.2, 1.0), 2.8 * np.cos(phi)])
     levels = int(np.log2(dim)) + 1
     return _finish(f"batch{index}", tris, nrms, alb, lights, ls, dim, levels, 1.0, (shadow, shadow), eye,
-                   np.zeros(3), 55 * DEG, gsize, BASELINE_CONES)
+                   np.zeros(3), 55 * DEG, gsize, FRAME_CONES)
 
 
 def _cylinders(radius, y0, y1, cx, cz, segments):
@@ -415,7 +417,7 @@ def large_family(seed: int = 0, dim: int = 256, shadow: int = 2048, gbuffer=(192
     levels = int(np.log2(dim)) + 1
     return _finish(f"family{seed}", np.concatenate([bt, ct]), np.concatenate([bn, cn]), np.concatenate([balb, calb]),
                    lights, ls, dim, levels, 1.0, (shadow, shadow), eye, np.zeros(3), 55 * DEG, tuple(gbuffer),
-                   BASELINE_CONES)
+                   FRAME_CONES)
 
 
 # Dynamic family: rigid actors (cylinders of 1k-4k segments, 2k-8k triangles)
@@ -479,7 +481,7 @@ def dynamic_scene(seed: int = 0, n_actors: int = 64, dim: int = 256, shadow: int
                     omega=rng.uniform(-2.0, 2.0, size=A))
     sc = _finish(f"dynamic{seed}", np.concatenate(tris).astype(np.float64), np.concatenate(nrms).astype(np.float64),
                  np.concatenate(albs), env.lights, np.eye(4), dim, env.levels, 1.0, env.shadow_size,
-                 np.array([0.0, 0.5, 2.8]), np.zeros(3), 55 * DEG, tuple(gbuffer), BASELINE_CONES)
+                 np.array([0.0, 0.5, 2.8]), np.zeros(3), 55 * DEG, tuple(gbuffer), FRAME_CONES)
     # keep the environment's light-space matrices
     sc.ls, sc.ls_inverse = env.ls, env.ls_inverse
     return sc, actors
@@ -577,7 +579,7 @@ def obj_scene(text: str, seed: int = 0, dim: int = 64, shadow: int = 512, gbuffe
     levels = int(np.log2(dim)) + 1
     return _finish("obj", np.concatenate(parts_t), np.concatenate(parts_n), np.concatenate(parts_a), [light], ls, dim,
                    levels, 1.0, (shadow, shadow), np.array([0.0, 1.6, 2.6]), np.array([0.0, -0.4, 0.0]), 50 * DEG,
-                   tuple(gbuffer), BASELINE_CONES)
+                   tuple(gbuffer), FRAME_CONES)
 
 
 def obj_text(tris: np.ndarray, normals: np.ndarray | None = None, quads: bool = False) -> str:
