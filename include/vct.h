@@ -489,6 +489,12 @@ vct_status vct_batch_autotune(vct_batch* batch, const vct_scene_desc* scenes, in
  * Synchronises `stream`; VCT_ERR_TIMEOUT if the MMA did not complete. */
 vct_status vct_tensor_core_check(const uint16_t* a_dev, const uint16_t* b_dev, int32_t k, int32_t n,
                                  int32_t variant, float* d_dev, void* stream);
+/* No counterpart in the reference.  Exercises the timeout path of the
+ * bounded device-side waits (the tensor-core kernels' mbarrier waits): one
+ * thread waits on an mbarrier that nothing arrives on, gives up after
+ * limit_ns (in [1e3, 1e9]) and records it.  Synchronises `stream` and
+ * returns VCT_ERR_TIMEOUT, the expected outcome; the device stays usable. */
+vct_status vct_timeout_probe(int64_t limit_ns, void* stream);
 
 /* The network: 42 inputs, three hidden layers of 64 with ReLU, 4 linear
  * outputs: irradiance RGB and the network's estimate of its own error there

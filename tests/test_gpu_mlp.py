@@ -40,6 +40,27 @@ def _gemm(k, n, variant, seed=0):
     return dd.cpu().numpy().reshape(128, n), ref
 
 
+def test_bounded_wait_times_out_and_device_stays_usable():
+    """The timeout path of the tensor-core kernels' bounded waits: a wait on an
+    mbarrier that nothing arrives on gives up after 2 ms and the call reports
+    VCT_ERR_TIMEOUT instead of hanging; the tensor-core path then still gives
+    the right product."""
+    import time
+
+    import torch
+
+    t0 = time.perf_counter()
+    with pytest.raises(L.VctError) as e:
+        L.call("vct_timeout_probe", 2_000_000, torch.cuda.current_stream().cuda_stream)
+    assert e.value.status == L.VCT_ERR_TIMEOUT
+    assert time.perf_counter() - t0 < 5.0
+    with pytest.raises(L.VctError) as e:
+        L.call("vct_timeout_probe", 10, None)
+    assert e.value.status == L.VCT_ERR_INVALID_ARGUMENT
+    d, ref = _gemm(64, 64, 0, seed=3)
+    assert np.abs(d - ref).max() / np.abs(ref).max() < 1e-5
+
+
 @pytest.mark.parametrize("k,n", [(16, 16), (48, 64), (64, 64), (64, 16), (32, 48)])
 def test_tensor_core_gemm(k, n):
     d, ref = _gemm(k, n, 0)

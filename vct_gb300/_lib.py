@@ -196,6 +196,7 @@ SIGNATURES = {
     "vct_batch_enable_timers": (st, [vp, C.c_int32]),
     "vct_batch_get_timers": (st, [vp, P(vct_timers)]),
     "vct_tensor_core_check": (st, [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, vp]),
+    "vct_timeout_probe": (st, [C.c_int64, vp]),
     "vct_mlp_create": (st, [C.c_int32, C.c_uint64, P(vp)]),
     "vct_mlp_destroy": (st, [vp]),
     "vct_mlp_set_params": (st, [vp, P(C.c_float), C.c_int64]),

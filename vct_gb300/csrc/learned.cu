@@ -947,6 +947,23 @@ __global__ void mlp_update_kernel(const MlpDev M, float lr, float beta1, float b
 
 }  // namespace
 
+// The timeout path of the bounded waits: one thread waits on an mbarrier that
+// nothing arrives on, gives up after `limit_ns` and records it in `status`,
+// exactly as the MLP kernels do when an MMA never completes.
+__global__ void wait_probe_kernel(uint32_t* status, unsigned long long limit_ns) {
+    __shared__ __align__(8) uint64_t mbar;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&mbar), 1);
+        fence_mbar_init();
+        if (!mbar_wait_for(smem_u32(&mbar), 0u, limit_ns)) atomicOr(status, 1u);
+    }
+}
+
+void launch_wait_probe(uint32_t* status, unsigned long long limit_ns, cudaStream_t s) {
+    wait_probe_kernel<<<1, 32, 0, s>>>(status, limit_ns);
+    note_launches(1);
+}
+
 void launch_umma_check(const uint16_t* A, const uint16_t* B, int K, int N, int swap, float* D, uint32_t* status,
                        cudaStream_t s) {
     cudaFuncSetAttribute(umma_check_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kCheckSmemA + kCheckSmemB);

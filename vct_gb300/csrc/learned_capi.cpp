@@ -183,6 +183,22 @@ vct_status vct_tensor_core_check(const uint16_t* a_dev, const uint16_t* b_dev, i
     return VCT_OK;
 }
 
+vct_status vct_timeout_probe(int64_t limit_ns, void* stream) {
+    if (limit_ns < 1000 || limit_ns > 1000000000) return fail(VCT_ERR_INVALID_ARGUMENT, "limit_ns must be in [1e3, 1e9]");
+    cudaStream_t st = as_stream(stream);
+    uint32_t* status = nullptr;
+    VCT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&status), sizeof(uint32_t), st));
+    VCT_CUDA(cudaMemsetAsync(status, 0, sizeof(uint32_t), st));
+    launch_wait_probe(status, (unsigned long long)limit_ns, st);
+    VCT_CHECK_LAUNCH("timeout probe");
+    uint32_t h = 0;
+    VCT_CUDA(cudaMemcpyAsync(&h, status, sizeof h, cudaMemcpyDeviceToHost, st));
+    VCT_CUDA(cudaFreeAsync(status, st));
+    VCT_CUDA(cudaStreamSynchronize(st));
+    if (h) return fail(VCT_ERR_TIMEOUT, "timeout probe: the bounded wait gave up, as designed");
+    return VCT_OK;
+}
+
 vct_status vct_mlp_create(int32_t device, uint64_t seed, vct_mlp** out) {
     if (!out) return fail(VCT_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;

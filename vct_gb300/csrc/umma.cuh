@@ -79,8 +79,8 @@ __device__ __forceinline__ uint64_t global_ns() {
 }
 
 // Waits for the completion of the mbarrier phase of parity `parity`, for at
-// most one second.  Returns false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+// most `limit_ns` nanoseconds.  Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait_for(uint32_t mbar, uint32_t parity, uint64_t limit_ns) {
     const uint64_t t0 = global_ns();
     while (true) {
         uint32_t done;
@@ -92,8 +92,13 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
             : "r"(mbar), "r"(parity)
             : "memory");
         if (done) return true;
-        if (global_ns() - t0 > 1000000000ull) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
+}
+
+// The kernels' waits: at most one second.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    return mbar_wait_for(mbar, parity, 1000000000ull);
 }
 
 // Generic-proxy shared-memory writes become visible to the tensor core's

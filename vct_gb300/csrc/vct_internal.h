@@ -458,6 +458,8 @@ void launch_shade(const ShadeParams& P, cudaStream_t s);
 void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, float4* mapf, cudaStream_t s);
 
 // Tensor-core GEMM check: D (128 x n, fp32) = A (128 x k) B^T (n x k), bf16.
+// One bounded mbarrier wait that nothing completes: sets status to 1 after limit_ns.
+void launch_wait_probe(uint32_t* status, unsigned long long limit_ns, cudaStream_t s);
 void launch_umma_check(const uint16_t* A, const uint16_t* B, int K, int N, int swap, float* D, uint32_t* status,
                        cudaStream_t s);
 // Copies every level of a linear chain into the interior of the bordered chain.
