@@ -433,7 +433,8 @@ typedef struct vct_scene_desc {
 vct_status vct_batch_create(const vct_config* configs, int32_t n_scenes, vct_batch** out);
 vct_status vct_batch_destroy(vct_batch* batch);
 /* Parameters of one scene (scene = -1: every scene); all scenes must use the
- * same trace_filter. */
+ * same trace_filter and voxeliser; warp modes may differ (scenes with
+ * VCT_WARP_TEXTURE build their maps inside the batched frame). */
 vct_status vct_batch_set_params(vct_batch* batch, int32_t scene, const vct_params* params);
 vct_status vct_batch_frame(vct_batch* batch, const vct_scene_desc* scenes, int32_t n_scenes, void* stream);
 /* Records vct_batch_frame for `scenes` into a CUDA graph owned by the batch

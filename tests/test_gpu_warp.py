@@ -154,7 +154,15 @@ def test_warped_hybrid_sampler_within_bar(warped):
     assert e64 <= 1e-3
 
 
-def test_batch_with_analytic_warp_equals_single_frames():
+_A, _T, _N = L.VCT_WARP_ANALYTIC, L.VCT_WARP_TEXTURE, L.VCT_WARP_NONE
+
+
+@pytest.mark.parametrize("modes", [(_A, _A, _A), (_T, _T, _T), (_T, _N, _A)], ids=["analytic", "texture", "mixed"])
+def test_batch_with_warps_equals_single_frames(modes):
+    """Batched frames with warped scenes: the analytic warp about each eye, the
+    texture warp (each scene's occupancy pass and map built inside the batched
+    frame), or a mix; chains, maps and irradiance equal single frames, bit for
+    bit."""
     import torch
 
     scs = [scenes.batch_scene(seed=5, index=i) for i in range(3)]
@@ -162,25 +170,24 @@ def test_batch_with_analytic_warp_equals_single_frames():
     for sc in scs:
         sc.eye = np.array([0.0, 0.0, 0.0], np.float32)  # warp about the centre
     ref = []
-    for sc, g in zip(scs, gs):
+    for sc, g, mode in zip(scs, gs, modes):
         ctx = api.Context(api.config_for(sc))
-        ctx.set_params(api.scene_params(sc, warp_mode=L.VCT_WARP_ANALYTIC))
+        ctx.set_params(api.scene_params(sc, warp_mode=mode))
         o = g.new_outputs()
         ctx.frame(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
         torch.cuda.synchronize()
-        ref.append((read_chain(ctx), o[0].cpu().numpy()))
+        wmap = ctx.read_warpmap().cpu().numpy() if mode == _T else None
+        ref.append((read_chain(ctx), o[0].cpu().numpy(), wmap))
     b = api.Batch([api.config_for(sc) for sc in scs])
-    for i, sc in enumerate(scs):
-        b.set_params(api.scene_params(sc, warp_mode=L.VCT_WARP_ANALYTIC), i)
+    for i, (sc, mode) in enumerate(zip(scs, modes)):
+        b.set_params(api.scene_params(sc, warp_mode=mode), i)
     outs = [g.new_outputs() for g in gs]
-    b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
-             for sc, g, o in zip(scs, gs, outs)])
-    torch.cuda.synchronize()
-    for i in range(len(scs)):
-        assert np.array_equal(read_chain(b.scenes[i]), ref[i][0])
-        assert np.array_equal(outs[i][0].cpu().numpy().view(np.uint32), ref[i][1].view(np.uint32))
-    # the texture warp is rejected by batches
-    b.set_params(api.scene_params(scs[0], warp_mode=L.VCT_WARP_TEXTURE), 0)
-    with pytest.raises(L.VctError):
+    for _ in range(2):  # the second frame checks that the occupancy masks were cleared
         b.frame([api.scene_desc(g.tris, g.lights, g.shadow, sc.eye, g.gb, api.trace_out(*o))
                  for sc, g, o in zip(scs, gs, outs)])
+    torch.cuda.synchronize()
+    for i, mode in enumerate(modes):
+        assert np.array_equal(read_chain(b.scenes[i]), ref[i][0])
+        assert np.array_equal(outs[i][0].cpu().numpy().view(np.uint32), ref[i][1].view(np.uint32))
+        if mode == _T:
+            assert np.array_equal(b.scenes[i].read_warpmap().cpu().numpy(), ref[i][2])

@@ -20,6 +20,7 @@ struct vct_batch {
     int n = 0, device = 0, num_sms = 0;
     std::vector<vct_ctx*> ctx;
     size_t off_accum = 0, off_inject = 0, off_resolve = 0, off_mips = 0, off_trace = 0, off_tables = 0, off_clear = 0;
+    size_t off_occ = 0, off_wmap = 0;  // warp maps: occupancy parameters and map arguments per scene
     size_t blob_bytes = 0;
     char* d_blob = nullptr;
     char* h_blob = nullptr;        // staging of vct_batch_frame
@@ -42,13 +43,14 @@ struct BatchTotals {
     long long tris = 0, texels = 0, bricks = 0, tiles = 0;
     // The frame's clears, zeroed by one launch each: before the voxeliser
     // (statistics, lit masks; carry tables and brick flags of the tessellation
-    // voxeliser) at [0, n_pre) of the blob's clear list, and after the resolve
+    // voxeliser; the occupancy masks of the warp maps) at [0, n_pre) of the blob's clear list, and after the resolve
     // (occupancy masks, for the next frame's accumulation) at [kClearPre n, +n).
     int n_pre = 0;
     long long max_pre = 0, max_post = 0;
+    bool any_map = false;  // some scene builds a warp map (VCT_WARP_TEXTURE)
 };
 
-constexpr int kClearPre = 4;  // clear-list entries per scene before the voxeliser (one more after the resolve)
+constexpr int kClearPre = 5;  // clear-list entries per scene before the voxeliser (one more after the resolve)
 
 // Validates the scene descriptors and fills the staging blob `h` (parameter
 // structs and prefix tables).  Allocates the voxeliser work arrays when the
@@ -75,8 +77,6 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         // the texture-unit surfaces, the bordered fp32 chain, or both (hybrid).
         const bool hw = filter_uses_texture(filter), pad = filter_uses_bordered(filter);
         if (hw && (s = ensure_texture(c)) != VCT_OK) return s;
-        if (c->params.warp_mode == VCT_WARP_TEXTURE)
-            return fail(VCT_ERR_UNSUPPORTED, "batches do not build warp maps: use another VCT_WARP_* mode");
         if (c->params.voxelize_tesselation != b->ctx[0]->params.voxelize_tesselation)
             return fail(VCT_ERR_INVALID_ARGUMENT, "all scenes of a batch must use the same voxeliser");
         if (c->params.voxelize_tesselation && d.triangles.count > (1LL << 24))
@@ -125,6 +125,24 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         std::memcpy(h + b->off_resolve + i * sizeof(ResolveParams), &R, sizeof R);
         std::memcpy(h + b->off_mips + i * sizeof(MipLevels), &M, sizeof M);
         std::memcpy(h + b->off_trace + i * sizeof(TraceParams), &T, sizeof T);
+        // VCT_WARP_TEXTURE: the 32^3 occupancy voxelisation (the rasteriser's rule at a
+        // 32^2 viewport, unwarped) and the map built from it, as build_warpmap does
+        AccumParams O = A;
+        WarpmapArgs WM;
+        std::memset(&WM, 0, sizeof WM);
+        O.occ = nullptr;
+        if (c->params.warp_mode == VCT_WARP_TEXTURE) {
+            O.dim = VCT_WARP_DIM;
+            O.occ = c->occ32;
+            O.acc = nullptr;
+            O.stats = nullptr;
+            O.warp.mode = VCT_WARP_NONE;
+            WM = WarpmapArgs{c->occ32, c->params.warp_high_resolution, c->params.warp_low_resolution, c->warpmap,
+                             c->warpmap_f};
+            tot.any_map = true;
+        }
+        std::memcpy(h + b->off_occ + i * sizeof(AccumParams), &O, sizeof O);
+        std::memcpy(h + b->off_wmap + i * sizeof(WarpmapArgs), &WM, sizeof WM);
         tri_off[i] = tot.tris;
         tex_off[i] = tot.texels;
         brick_off[i] = tot.bricks;
@@ -145,6 +163,7 @@ vct_status batch_stage(vct_batch* b, const vct_scene_desc* sc, int n, char* h, B
         const long long mask_words = (c->nv + 31) / 32;
         pre(c->stats, (long long)(sizeof(StatsDev) / 4));
         pre(c->lit, mask_words);
+        if (c->params.warp_mode == VCT_WARP_TEXTURE) pre(c->occ32, VCT_WARP_DIM * VCT_WARP_DIM * VCT_WARP_DIM / 32);
         if (c->params.voxelize_tesselation) {
             pre(c->carry, (long long)(kCarryBytes / 4));
             pre(c->brick_exact, c->nv / 4096 + 1);
@@ -196,6 +215,15 @@ vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cu
     const ClearRange* d_clear = reinterpret_cast<const ClearRange*>(b->d_blob + b->off_clear);
     launch_clear_ranges(d_clear, tot.n_pre, tot.max_pre, st);
     VCT_CHECK_LAUNCH("batch: clear");
+    if (tot.any_map) {
+        const long long* d_tri = reinterpret_cast<const long long*>(b->d_blob + b->off_tables);
+        launch_occupancy_batch(SceneBatch<AccumParams>{reinterpret_cast<const AccumParams*>(b->d_blob + b->off_occ),
+                                                       d_tri, n},
+                               tot.tris, st);
+        VCT_CHECK_LAUNCH("batch: warp occupancy");
+        launch_warpmap_batch(reinterpret_cast<const WarpmapArgs*>(b->d_blob + b->off_wmap), n, st);
+        VCT_CHECK_LAUNCH("batch: warp maps");
+    }
     const long long* d_tables = reinterpret_cast<const long long*>(b->d_blob + b->off_tables);
     AccumParams W0;
     W0.ntri = tot.tris;
@@ -287,6 +315,10 @@ vct_status vct_batch_create(const vct_config* configs, int32_t n, vct_batch** ou
     off = up256(off + sizeof(long long) * 4 * (n + 1));
     b->off_clear = off;
     off = up256(off + sizeof(ClearRange) * (kClearPre + 1) * n);
+    b->off_occ = off;
+    off = up256(off + sizeof(AccumParams) * n);
+    b->off_wmap = off;
+    off = up256(off + sizeof(WarpmapArgs) * n);
     b->blob_bytes = off;
     DeviceScope ds(b->device);
     cudaError_t e = cudaMalloc(&b->d_blob, off);

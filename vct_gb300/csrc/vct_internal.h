@@ -456,6 +456,19 @@ void launch_shade(const ShadeParams& P, cudaStream_t s);
 
 // Warp map of VCT_WARP_TEXTURE from a 32^3 occupancy bit mask.
 void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, float4* mapf, cudaStream_t s);
+// The warp map of one scene: its 32^3 occupancy mask, the high and low cell
+// widths, the RGBA16 unorm map and its bordered fp32 copy ((32+2)^3).
+struct WarpmapArgs {
+    const uint32_t* occ;
+    float high, low;
+    uint16_t* map;  // nullptr: the scene builds no map
+    float4* mapf;
+};
+// One map per scene of a batch (a device array of n arguments).
+void launch_warpmap_batch(const WarpmapArgs* args, int n, cudaStream_t s);
+// The 32^3 occupancy voxelisation of every scene of a batch whose occupancy
+// parameters name a mask (occ), over all the batch's triangles.
+void launch_occupancy_batch(const SceneBatch<AccumParams>& B, long long ntri, cudaStream_t s);
 
 // Tensor-core GEMM check: D (128 x n, fp32) = A (128 x k) B^T (n x k), bf16.
 // One bounded mbarrier wait that nothing completes: sets status to 1 after limit_ns.

@@ -499,14 +499,7 @@ __global__ void transform_actors_kernel(const ActorsDev A) {
 // empty ones, keeping each row's total of 32; stored as binary16 by the
 // weight textures), and per texel the warped coordinate of its cell centre,
 // stored RGBA16 unorm.
-struct WarpmapArgs {
-    const uint32_t* occ;  // 32^3 bit mask
-    float high, low;
-    uint16_t* map;
-    float4* mapf;  // bordered fp32 copy read by the lookups ((D+2)^3)
-};
-
-__global__ void __launch_bounds__(1024) warpmap_kernel(const WarpmapArgs A) {
+__device__ __forceinline__ void warpmap_block(const WarpmapArgs& A) {
     constexpr int D = kWarpDim;
     __shared__ uint8_t occ[D * D * D];
     __shared__ uint8_t part[3][D * D * D];  // inclusive prefix sums along x, y, z
@@ -581,10 +574,25 @@ __global__ void __launch_bounds__(1024) warpmap_kernel(const WarpmapArgs A) {
     }
 }
 
+__global__ void __launch_bounds__(1024) warpmap_kernel(const WarpmapArgs A) { warpmap_block(A); }
+
+// One CTA per scene of a batch; scenes without a texture warp have no map.
+__global__ void __launch_bounds__(1024) warpmap_batch_kernel(const WarpmapArgs* __restrict__ args) {
+    const WarpmapArgs A = args[blockIdx.x];
+    if (!A.map) return;
+    warpmap_block(A);
+}
+
 }  // namespace
 
 void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, float4* mapf, cudaStream_t s) {
     warpmap_kernel<<<1, 1024, 0, s>>>(WarpmapArgs{occ32, high, low, map, mapf});
+    note_launches(1);
+}
+
+void launch_warpmap_batch(const WarpmapArgs* args, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    warpmap_batch_kernel<<<n, 1024, 0, s>>>(args);
     note_launches(1);
 }
 

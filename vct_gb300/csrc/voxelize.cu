@@ -475,14 +475,21 @@ __device__ __forceinline__ void occupancy_fragment(const AccumParams& P, int axi
     atomicOr(P.occ + (v >> 5), 1u << (v & 31));
 }
 
-__global__ void __launch_bounds__(kOccThreads) occupancy_kernel(const AccumParams P) {
+template <class Scenes>
+__global__ void __launch_bounds__(kOccThreads) occupancy_kernel(const Scenes S, long long ntri) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const long long g = (long long)blockIdx.x * kOccThreads + threadIdx.x;
     RasterTri rt;
     float z[3] = {0.f, 0.f, 0.f};
-    int axis = 0;
-    const bool ok = g < P.ntri && project_triangle(P, g, rt, z, axis);
+    int axis = 0, scene = 0;
+    bool ok = false;
+    if (g < ntri) {
+        long long t;
+        scene = S.find(g, t);
+        const AccumParams& P = S.get(scene);
+        ok = P.occ != nullptr && project_triangle(P, t, rt, z, axis);  // scenes without a map: no occupancy
+    }
     int X[3] = {0, 0, 0}, Y[3] = {0, 0, 0}, dX[3], dY[3];
     int bias = 0, perm1 = 0, px0 = 0, py0 = 0, bw = 0, bh = 0;
     float inv = 0.f;
@@ -502,6 +509,7 @@ __global__ void __launch_bounds__(kOccThreads) occupancy_kernel(const AccumParam
     }
     const int npix = bw * bh;
     if (npix <= kOccLanePixels) {
+        const AccumParams& P = S.get(scene);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             dX[k] = X[(k + 2) % 3] - X[(k + 1) % 3];
@@ -533,15 +541,16 @@ __global__ void __launch_bounds__(kOccThreads) occupancy_kernel(const AccumParam
         }
         const int sbias = __shfl_sync(FULL, bias, src), sperm1 = __shfl_sync(FULL, perm1, src);
         const float sinv = __shfl_sync(FULL, inv, src);
-        const int saxis = __shfl_sync(FULL, axis, src);
+        const int saxis = __shfl_sync(FULL, axis, src), sscene = __shfl_sync(FULL, scene, src);
         const int spx0 = __shfl_sync(FULL, px0, src), spy0 = __shfl_sync(FULL, py0, src);
         const int sbw = __shfl_sync(FULL, bw, src), sn = __shfl_sync(FULL, npix, src);
+        const AccumParams& SP = S.get(sscene);
         for (int idx = lane; idx < sn; idx += 32) {
             const int row = idx / sbw;
             const int px = spx0 + (idx - row * sbw), py = spy0 + row;
             float l[3], zf;
             if (pixel_fragment(sX, sY, sdX, sdY, sbias, sperm1, sinv, sz, px, py, l, zf))
-                occupancy_fragment(P, saxis, px, py, zf);
+                occupancy_fragment(SP, saxis, px, py, zf);
         }
     }
 }
@@ -930,7 +939,15 @@ void accumulate_bind_scratch(AccumParams& P, void* scratch) {
 
 void launch_occupancy(const AccumParams& P, cudaStream_t s) {
     if (P.ntri <= 0) return;
-    occupancy_kernel<<<(unsigned)((P.ntri + kOccThreads - 1) / kOccThreads), kOccThreads, 0, s>>>(P);
+    occupancy_kernel<<<(unsigned)((P.ntri + kOccThreads - 1) / kOccThreads), kOccThreads, 0, s>>>(
+        OneScene<AccumParams>{P}, P.ntri);
+    note_launches(1);
+}
+
+void launch_occupancy_batch(const SceneBatch<AccumParams>& B, long long ntri, cudaStream_t s) {
+    if (ntri <= 0) return;
+    occupancy_kernel<<<(unsigned)((ntri + kOccThreads - 1) / kOccThreads), kOccThreads, 0, s>>>(
+        ManyScenes<AccumParams>{B}, ntri);
     note_launches(1);
 }
 
