@@ -1072,14 +1072,14 @@ def run_dynamic(args, rank, world):
 # stage, from one ncu capture of the large frame (`bench.py --profile-frames 3`, default
 # launch shapes): accumulate = setup + raster, resolve+mips = resolve + tail; only for the
 # default workload, and only while the frame kernels' sources hash to NCU_CAPTURE_DIGEST.
-NCU_CAPTURE_DIGEST = "5ead3d40972ea19f"
+NCU_CAPTURE_DIGEST = "4d89c42ecec6cbda"
 NCU_CAPTURE_SAMPLER = "hybrid"
-NCU_TRAFFIC = {"accumulate": 18.890e6 + 317.604e6 + 180.500e6, "resolve+mips": 308.164e6 + 837.048e6 + 0.047e6,
-               "inject_mark": 18.285e6, "trace": 89.186e6 + 12.669e6}
+NCU_TRAFFIC = {"accumulate": 18.890e6 + 317.623e6 + 180.766e6, "resolve+mips": 308.095e6 + 836.815e6 + 0.046e6,
+               "inject_mark": 18.285e6, "trace": 89.185e6 + 12.669e6}
 # Issue-side figures of the cone tracer (hybrid sampler) from its full capture of the same
 # command: it is bound by issue and load latency at its occupancy, not HBM.
-NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.636, "fma_pipe_frac": 0.438, "l1_hit_rate": 0.971,
-                   "l1_lsu_data_pipe_frac": 0.664, "l1_tex_data_pipe_frac": 0.241}
+NCU_TRACE_ISSUE = {"sm_throughput_frac": 0.633, "fma_pipe_frac": 0.437, "l1_hit_rate": 0.971,
+                   "l1_lsu_data_pipe_frac": 0.661, "l1_tex_data_pipe_frac": 0.240}
 
 
 def load_peaks() -> dict:
