@@ -298,8 +298,11 @@ vct_status vct_get_config(const vct_ctx* ctx, vct_config* out);
 vct_status vct_volume_level(const vct_ctx* ctx, int32_t volume, int32_t level,
                             const uint16_t** data_dev, int32_t* dim);
 /* Device pointers of the integer accumulators: one 8 x uint32 record per
- * voxel {count, r, g, b, nx, ny, nz, 0} (sums of round(x * 65535)), voxel v
- * at records_dev[8*v], and the occupancy bit mask (bit v%32 of word v/32).
+ * voxel {count, r, g, b, nx, ny, nz, 0} (sums of round(x * 65535)), and the
+ * occupancy bit mask (bit v%32 of word v/32 for voxel v = (z*dim + y)*dim + x).
+ * Voxel v's record is at records_dev[8*s], s being v with bit 1 (bit 1 of x)
+ * and bit log2(dim) (bit 0 of y) exchanged: each 128-byte line of records
+ * holds a 2 x 2 block of voxels in x and y.
  * Between vct_voxelize_accumulate and vct_normalize they hold the sums of
  * the frame; vct_normalize / vct_frame leave them zeroed. */
 vct_status vct_accumulators(const vct_ctx* ctx, const uint32_t** records_dev,

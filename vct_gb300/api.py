@@ -278,11 +278,16 @@ class Context:
         return device_view(ptr, (d * d * d * 4,), "<i2").clone()
 
     def read_accumulators(self):
-        """Copies of (records [dim^3, 8], occupancy mask) as int32 tensors
-        (uint32 bit patterns); record = {count, r, g, b, nx, ny, nz, 0}."""
+        """Copies of (records [dim^3, 8] in voxel order, occupancy mask) as
+        int32 tensors (uint32 bit patterns); record = {count, r, g, b, nx, ny,
+        nz, 0}."""
+        import torch
+
         rp, op = self.accumulator_ptrs()
         nv = self.dim ** 3
-        return (device_view(rp, (nv, 8), "<i4").clone(), device_view(op, ((nv + 31) // 32,), "<i4").clone())
+        rec = device_view(rp, (nv, 8), "<i4")
+        slots = torch.from_numpy(record_slots(self.dim)).to(rec.device)
+        return rec.index_select(0, slots), device_view(op, ((nv + 31) // 32,), "<i4").clone()
 
 
 def scene_desc(tris, lights, shadow, eye, gb, out) -> L.vct_scene_desc:
@@ -485,6 +490,15 @@ class _CudaArray:
     def __init__(self, ptr: int, shape: tuple, typestr: str):
         self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
                                          "version": 2, "strides": None}
+
+
+def record_slots(dim: int) -> np.ndarray:
+    """Slot of each voxel's record in vct_accumulators' buffer, in voxel
+    order (x fastest): bit 1 of x and bit 0 of y change places, so each
+    128-byte line holds a 2 x 2 block of records in x and y."""
+    v = np.arange(dim ** 3, dtype=np.int64)
+    d = ((v >> 1) ^ ((v & dim) != 0)) & 1
+    return v ^ (d * (dim + 2))
 
 
 def device_view(ptr: int, shape: tuple, typestr: str):

@@ -145,6 +145,18 @@ void accumulate_bind_scratch(AccumParams& P, void* scratch);
 // nz's exact 64-bit sum.
 constexpr int kAccWords = 8;
 
+// Record slot of voxel v = (z * N + y) * N + x (N = dim, a power of two of
+// at least 16): bit 1 of x and bit 0 of y change places, so the four 32-byte
+// records of each 128-byte line hold a 2 x 2 block in x and y instead of a
+// run of four along x.  DRAM moves whole lines around the records of the
+// occupied voxels, and a surface's occupied voxels fill more of each line in
+// 2 x 2 blocks: on the 262,144-triangle 256^3 frame, 5.18 M records touch
+// 1.99 M lines instead of 2.37 M.
+VCT_HD inline long long record_slot(long long v, int N) {
+    const long long d = ((v >> 1) ^ ((v & N) ? 1 : 0)) & 1;
+    return v ^ (d * (N + 2));
+}
+
 // Exact sums past VCT_MAX_EXACT_FRAGMENTS (the tessellation voxeliser, whose
 // slivers put up to ~10^5 points into one voxel): every 64-bit add returns
 // the word's old value, from which the adder sees whether its low field

@@ -199,14 +199,15 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
         uint32_t lb = 0;
         if (FUSED) lb = (__ldg(R.lit + (v0 >> 5)) >> (v0 & 31)) & 15u;
         uint4 rec[4][2];
-        uint4* recp = reinterpret_cast<uint4*>(P.acc + (long long)kAccWords * v0);
+        // x is a multiple of 4: voxel x + j's record is (j & 1) + (j >> 1) N slots on
+        uint4* recp = reinterpret_cast<uint4*>(P.acc + kAccWords * record_slot(v0, N));
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             if ((ob >> j) & 1u) {  // the whole 32-byte record in one streaming load
                 asm volatile("ld.global.cs.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
                              : "=r"(rec[j][0].x), "=r"(rec[j][0].y), "=r"(rec[j][0].z), "=r"(rec[j][0].w),
                                "=r"(rec[j][1].x), "=r"(rec[j][1].y), "=r"(rec[j][1].z), "=r"(rec[j][1].w)
-                             : "l"(recp + 2 * j));
+                             : "l"(recp + 2 * ((j & 1) + (j >> 1) * (long long)N)));
             } else {
                 rec[j][0] = rec[j][1] = make_uint4(0u, 0u, 0u, 0u);
             }
@@ -229,7 +230,8 @@ __global__ void __launch_bounds__(kThreads, 3) resolve_kernel(const Scenes S) {
             nrm[j] = make_uint2(0u, 0u);
             if ((ob >> j) & 1u) {
                 // zeroed for the next frame's accumulation, in one streaming store
-                asm volatile("st.global.cs.v8.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1};" ::"l"(recp + 2 * j), "r"(0u)
+                asm volatile("st.global.cs.v8.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1};"
+                             ::"l"(recp + 2 * ((j & 1) + (j >> 1) * (long long)N)), "r"(0u)
                              : "memory");
                 ++uniq;
                 mx = max(mx, c);

@@ -251,7 +251,7 @@ __device__ __forceinline__ void shade_fragment(const AccumParams& P, const FragQ
         color = mk(clampf(fin.x, 0.0f, 1.0f), clampf(fin.y, 0.0f, 1.0f), clampf(fin.z, 0.0f, 1.0f));
     }
     const f3 n01 = mk((Nf.x + 1.0f) * 0.5f, (Nf.y + 1.0f) * 0.5f, (Nf.z + 1.0f) * 0.5f);
-    unsigned long long* rec = reinterpret_cast<unsigned long long*>(P.acc + (long long)kAccWords * v);
+    unsigned long long* rec = reinterpret_cast<unsigned long long*>(P.acc + kAccWords * record_slot(v, P.dim));
     const unsigned long long qr = quant16(color.x), qg = quant16(color.y), qb = quant16(color.z);
     const unsigned long long qx = quant16(n01.x), qy = quant16(n01.y), qz = quant16(n01.z);
     // Fire-and-forget reductions: no result is waited for.  (Setting the
@@ -760,7 +760,7 @@ __device__ __forceinline__ void tess_store32(const Scenes& S, const TessQueue& q
         qy += py;
         qz += pz;
     }
-    unsigned long long* rec = reinterpret_cast<unsigned long long*>(P.acc + (long long)kAccWords * v);
+    unsigned long long* rec = reinterpret_cast<unsigned long long*>(P.acc + kAccWords * record_slot(v, P.dim));
     const unsigned long long a0 = cnt | ((unsigned long long)qr << 32);
     const unsigned long long a1 = (unsigned long long)qg | ((unsigned long long)qb << 32);
     const unsigned long long a2 = (unsigned long long)qx | ((unsigned long long)qy << 32);
@@ -801,7 +801,7 @@ __global__ void __launch_bounds__(256) carry_fixup_kernel(const Scenes S) {
     const uint32_t* e = P.carry + 8 * slot;
     if (e[0] == 0u) return;
     const long long v = (long long)e[0] - 1;
-    uint4* r = reinterpret_cast<uint4*>(P.acc + (long long)kAccWords * v);
+    uint4* r = reinterpret_cast<uint4*>(P.acc + kAccWords * record_slot(v, P.dim));
     const uint4 r0 = r[0], r1 = r[1];
     const unsigned long long t = 1ull << 32;
     // {count | r}, {g | b}, {nx | ny}, {nz | nz's carries}: a high field holds
