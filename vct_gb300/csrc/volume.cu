@@ -496,18 +496,20 @@ __global__ void transform_actors_kernel(const ActorsDev A) {
 
 // ------------------------------------------------------------- warp map
 // Application.cpp:300-371 + generateWarpmapWeights.frag + generateWarpmap.frag
-// for the 32^3 warp map, in one CTA: per-axis inclusive prefix sums of the
-// occupancy, the per-row resolution weights (high for occupied cells, low for
-// empty ones, keeping each row's total of 32; stored as binary16 by the
-// weight textures), and per texel the warped coordinate of its cell centre,
-// stored RGBA16 unorm.
-__device__ __forceinline__ void warpmap_block(const WarpmapArgs& A) {
+// for the 32^3 warp map: per-axis inclusive prefix counts of the occupancy,
+// the per-row resolution weights (high for occupied cells, low for empty
+// ones, keeping each row's total of 32; stored as binary16 by the weight
+// textures), and per texel the warped coordinate of its cell centre, stored
+// RGBA16 unorm.  One CTA per z slice, one thread per cell: a row of the
+// occupancy is one 32-bit word, so the x counts are population counts, and
+// the y and z counts walk the 4 KB mask, held in shared memory by every CTA.
+__device__ __forceinline__ void warpmap_slice(const WarpmapArgs& A, int z) {
     constexpr int D = kWarpDim;
-    __shared__ uint8_t occ[D * D * D];
-    __shared__ uint8_t part[3][D * D * D];  // inclusive prefix sums along x, y, z
-    __shared__ float wts[2][D + 1];          // binary16-rounded low / high weights per occupied count
+    static_assert(D == 32, "a warp-map row is one 32-bit occupancy word");
+    __shared__ uint32_t occ[D * D];   // word (z * D + y): row (y, z), bit x
+    __shared__ float wts[2][D + 1];  // binary16-rounded low / high weights per occupied count
     const int t = threadIdx.x;
-    for (int i = t; i < D * D * D; i += blockDim.x) occ[i] = (uint8_t)((A.occ[i >> 5] >> (i & 31)) & 1u);
+    occ[t] = A.occ[t];
     if (t <= D) {
         float l = 1.0f, h = 1.0f;
         if (t != 0 && t != D) {
@@ -523,78 +525,76 @@ __device__ __forceinline__ void warpmap_block(const WarpmapArgs& A) {
         wts[1][t] = __half2float(__float2half_rn(h));
     }
     __syncthreads();
-    {
-        const int a = t & (D - 1), b = t >> 5;
-        int sx = 0, sy = 0, sz = 0;
-        for (int k = 0; k < D; ++k) {
-            const int ix = (b * D + a) * D + k;  // x = k, y = a, z = b
-            const int iy = (b * D + k) * D + a;  // x = a, y = k, z = b
-            const int iz = (k * D + b) * D + a;  // x = a, y = b, z = k
-            sx += occ[ix];
-            part[0][ix] = (uint8_t)sx;
-            sy += occ[iy];
-            part[1][iy] = (uint8_t)sy;
-            sz += occ[iz];
-            part[2][iz] = (uint8_t)sz;
-        }
+    const int x = t & (D - 1), y = t >> 5;
+    const uint32_t row = occ[z * D + y];
+    const bool o = ((row >> x) & 1u) != 0u;
+    // inclusive prefix counts along x, y, z and each line's total
+    int ps[3], tot[3];
+    ps[0] = __popc(row & (0xffffffffu >> (31 - x)));
+    tot[0] = __popc(row);
+    int cy = 0, cz = 0;
+    ps[1] = ps[2] = 0;
+#pragma unroll 8
+    for (int k = 0; k < D; ++k) {
+        cy += (occ[z * D + k] >> x) & 1u;
+        cz += (occ[k * D + y] >> x) & 1u;
+        if (k == y) ps[1] = cy;
+        if (k == z) ps[2] = cz;
     }
-    __syncthreads();
-    for (int i = t; i < D * D * D; i += blockDim.x) {
-        const int x = i & (D - 1), y = (i >> 5) & (D - 1), z = i >> 10;
-        const bool o = occ[i] != 0;
-        const int idx[3] = {x, y, z};
-        const int tot[3] = {part[0][(z * D + y) * D + D - 1], part[1][(z * D + D - 1) * D + x],
-                            part[2][((D - 1) * D + y) * D + x]};
-        uint16_t out[4];
+    tot[1] = cy;
+    tot[2] = cz;
+    const int idx[3] = {x, y, z};
+    uint16_t out[4];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const float lo = wts[0][tot[k]], hi = wts[1][tot[k]];
-            const float res = o ? hi : lo;
-            const int ps = part[k][i];
-            const float prev = (float)(o ? ps - 1 : ps);
-            const float offset = lo * ((float)idx[k] - prev) + hi * prev;
-            const float inner = 0.5f * res;
-            const float w = (offset + inner) / (float)D;
-            out[k] = (uint16_t)__float2uint_rn(fminf(fmaxf(w, 0.0f), 1.0f) * 65535.0f);
-        }
-        // packCellInfo: totals (5 bits each) and the cell's occupancy
-        out[3] = (uint16_t)((tot[0] & 0x1F) | ((tot[1] & 0x1F) << 5) | ((tot[2] & 0x1F) << 10) | ((o ? 1 : 0) << 15));
-        reinterpret_cast<uint2*>(A.map)[i] =
-            make_uint2((uint32_t)out[0] | ((uint32_t)out[1] << 16), (uint32_t)out[2] | ((uint32_t)out[3] << 16));
-        const float4 f = make_float4(__fdiv_rn((float)out[0], 65535.0f), __fdiv_rn((float)out[1], 65535.0f),
-                                     __fdiv_rn((float)out[2], 65535.0f), __fdiv_rn((float)out[3], 65535.0f));
-        // the fp32 copy at (x+1, y+1, z+1), and on the border beside an edge
-        // texel (clamp-to-edge): up to 8 places for a corner texel
-        const int xs[2] = {x + 1, x == 0 ? 0 : x == D - 1 ? D + 1 : -1};
-        const int ys[2] = {y + 1, y == 0 ? 0 : y == D - 1 ? D + 1 : -1};
-        const int zs[2] = {z + 1, z == 0 ? 0 : z == D - 1 ? D + 1 : -1};
+    for (int k = 0; k < 3; ++k) {
+        const float lo = wts[0][tot[k]], hi = wts[1][tot[k]];
+        const float res = o ? hi : lo;
+        const float prev = (float)(o ? ps[k] - 1 : ps[k]);
+        const float offset = lo * ((float)idx[k] - prev) + hi * prev;
+        const float inner = 0.5f * res;
+        const float w = (offset + inner) / (float)D;
+        out[k] = (uint16_t)__float2uint_rn(fminf(fmaxf(w, 0.0f), 1.0f) * 65535.0f);
+    }
+    // packCellInfo: totals (5 bits each) and the cell's occupancy
+    out[3] = (uint16_t)((tot[0] & 0x1F) | ((tot[1] & 0x1F) << 5) | ((tot[2] & 0x1F) << 10) | ((o ? 1 : 0) << 15));
+    const int i = (z * D + y) * D + x;
+    reinterpret_cast<uint2*>(A.map)[i] =
+        make_uint2((uint32_t)out[0] | ((uint32_t)out[1] << 16), (uint32_t)out[2] | ((uint32_t)out[3] << 16));
+    const float4 f = make_float4(__fdiv_rn((float)out[0], 65535.0f), __fdiv_rn((float)out[1], 65535.0f),
+                                 __fdiv_rn((float)out[2], 65535.0f), __fdiv_rn((float)out[3], 65535.0f));
+    // the fp32 copy at (x+1, y+1, z+1), and on the border beside an edge
+    // texel (clamp-to-edge): up to 8 places for a corner texel
+    const int xs[2] = {x + 1, x == 0 ? 0 : x == D - 1 ? D + 1 : -1};
+    const int ys[2] = {y + 1, y == 0 ? 0 : y == D - 1 ? D + 1 : -1};
+    const int zs[2] = {z + 1, z == 0 ? 0 : z == D - 1 ? D + 1 : -1};
 #pragma unroll
-        for (int n = 0; n < 8; ++n) {
-            const int bx = xs[n & 1], by = ys[(n >> 1) & 1], bz = zs[n >> 2];
-            if (bx >= 0 && by >= 0 && bz >= 0) A.mapf[(bz * kWarpPad + by) * kWarpPad + bx] = f;
-        }
+    for (int n = 0; n < 8; ++n) {
+        const int bx = xs[n & 1], by = ys[(n >> 1) & 1], bz = zs[n >> 2];
+        if (bx >= 0 && by >= 0 && bz >= 0) A.mapf[(bz * kWarpPad + by) * kWarpPad + bx] = f;
     }
 }
 
-__global__ void __launch_bounds__(1024) warpmap_kernel(const WarpmapArgs A) { warpmap_block(A); }
+__global__ void __launch_bounds__(kWarpDim * kWarpDim) warpmap_kernel(const WarpmapArgs A) {
+    warpmap_slice(A, blockIdx.x);
+}
 
-// One CTA per scene of a batch; scenes without a texture warp have no map.
-__global__ void __launch_bounds__(1024) warpmap_batch_kernel(const WarpmapArgs* __restrict__ args) {
-    const WarpmapArgs A = args[blockIdx.x];
+// blockIdx.y: the scene of a batch; scenes without a texture warp have no map.
+__global__ void __launch_bounds__(kWarpDim * kWarpDim) warpmap_batch_kernel(const WarpmapArgs* __restrict__ args) {
+    const WarpmapArgs A = args[blockIdx.y];
     if (!A.map) return;
-    warpmap_block(A);
+    warpmap_slice(A, blockIdx.x);
 }
 
 }  // namespace
 
 void launch_warpmap(const uint32_t* occ32, float high, float low, uint16_t* map, float4* mapf, cudaStream_t s) {
-    warpmap_kernel<<<1, 1024, 0, s>>>(WarpmapArgs{occ32, high, low, map, mapf});
+    warpmap_kernel<<<kWarpDim, kWarpDim * kWarpDim, 0, s>>>(WarpmapArgs{occ32, high, low, map, mapf});
     note_launches(1);
 }
 
 void launch_warpmap_batch(const WarpmapArgs* args, int n, cudaStream_t s) {
     if (n <= 0) return;
-    warpmap_batch_kernel<<<n, 1024, 0, s>>>(args);
+    warpmap_batch_kernel<<<dim3(kWarpDim, n), kWarpDim * kWarpDim, 0, s>>>(args);
     note_launches(1);
 }
 
