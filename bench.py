@@ -1072,10 +1072,10 @@ def run_dynamic(args, rank, world):
 # stage, from one ncu capture of the large frame (`bench.py --profile-frames 3`, default
 # launch shapes): accumulate = setup + raster, resolve+mips = resolve + tail; only for the
 # default workload, and only while the frame kernels' sources hash to NCU_CAPTURE_DIGEST.
-NCU_CAPTURE_DIGEST = "57e5baa56c1e2b4f"
+NCU_CAPTURE_DIGEST = "4c6e578007e00823"
 NCU_CAPTURE_SAMPLER = "hybrid"
-NCU_TRAFFIC = {"accumulate": 18.890e6 + 263.292e6 + 163.454e6, "resolve+mips": 258.925e6 + 835.353e6 + 0.046e6,
-               "inject_mark": 18.258e6, "trace": 89.187e6 + 12.721e6}
+NCU_TRAFFIC = {"accumulate": 18.890e6 + 263.295e6 + 163.350e6, "resolve+mips": 259.105e6 + 835.401e6 + 0.055e6,
+               "inject_mark": 18.258e6 + 0.026e6, "trace": 89.187e6 + 12.733e6}
 # Issue-side figures of the cone tracer (hybrid sampler) from its full capture of the same
 # command: it is bound by issue and load latency at its occupancy, not HBM.  (Captured
 # before the accumulator records moved to 2 x 2 slots; the tracer reads no records and its
