@@ -400,39 +400,77 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
                 dX[k] = X[(k + 2) % 3] - X[(k + 1) % 3];
                 dY[k] = Y[(k + 2) % 3] - Y[(k + 1) % 3];
             }
-            const float rbw = 1.0f / (float)bw;  // row = idx / bw, corrected below
-            for (int c = p_begin; c < p_end; c += 32) {
-                const int idx = c + lane;
-                bool cov = false;
-                float l[3] = {0.f, 0.f, 0.f}, zf = 0.f;
-                int px = 0, py = 0;
-                if (idx < p_end) {
-                    int row = (int)((float)idx * rbw);
-                    if (row * bw > idx)
-                        --row;
-                    else if ((row + 1) * bw <= idx)
-                        ++row;
-                    py = py0 + row;
-                    px = px0 + (idx - row * bw);
-                    cov = pixel_fragment(X, Y, dX, dY, bias, perm1, inv, z, px, py, l, zf);
+            // The unit's pixels, row by row: each lane takes one of up to 32 rows
+            // and narrows it to the pixels between the triangle's crossings of
+            // the row's centre line (widened by one pixel each side, so that
+            // float rounding never drops a covered pixel); the warp then tests
+            // the rows' candidates 32 at a time.  A sliver fills a small part
+            // of its bounding box, over which the units are counted.
+            const int r_a = p_begin / bw, r_b = (p_end - 1) / bw;
+            float slope[3];  // x per unit y along edge k
+#pragma unroll
+            for (int k = 0; k < 3; ++k) slope[k] = dY[k] != 0 ? __fdividef((float)dX[k], (float)dY[k]) : 0.0f;
+            for (int rb = r_a; rb <= r_b; rb += 32) {
+                const int r = rb + lane;
+                int lo = 0, cnt = 0;
+                if (r <= r_b) {
+                    const int sy = (py0 + r) * (int)kSub + (int)kSub / 2;
+                    float xmin = 3.0e38f, xmax = -3.0e38f;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const int a = (k + 1) % 3, bb = (k + 2) % 3;
+                        if (min(Y[a], Y[bb]) <= sy && sy <= max(Y[a], Y[bb])) {
+                            const float x0 = dY[k] != 0 ? fmaf((float)(sy - Y[a]), slope[k], (float)X[a]) : (float)X[a];
+                            const float x1 = dY[k] != 0 ? x0 : (float)X[bb];
+                            xmin = fminf(xmin, fminf(x0, x1));
+                            xmax = fmaxf(xmax, fmaxf(x0, x1));
+                        }
+                    }
+                    if (xmin <= xmax) {
+                        const float rs = 1.0f / (float)kSub, hs = 0.5f * (float)kSub;
+                        const int s0 = (int)ceilf((xmin - hs) * rs) - 1 - px0;
+                        const int s1 = (int)floorf((xmax - hs) * rs) + 1 - px0;
+                        lo = max(max(p_begin - r * bw, 0), s0);
+                        cnt = max(min(min(p_end - r * bw, bw) - 1, s1) - lo + 1, 0);
+                    }
                 }
-                const unsigned m = __ballot_sync(FULL, cov);
-                if (cov) {
-                    const int slot = (head + qn + __popc(m & ((1u << lane) - 1u))) & (kQueue - 1);
-                    q.tri[slot] = (int)tl;
-                    q.pix[slot] = (uint32_t)px | ((uint32_t)py << 11) | ((uint32_t)axis << 22) |
-                                  ((uint32_t)scene << 24);
-                    q.l0[slot] = l[0];
-                    q.l1[slot] = l[1];
-                    q.l2[slot] = l[2];
-                    q.z[slot] = zf;
+                int excl = cnt;  // exclusive prefix of the rows' candidate counts
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(FULL, excl, o);
+                    if (lane >= o) excl += v;
                 }
-                qn += __popc(m);
-                pending += (unsigned)__popc(m);
-                if (qn >= 32) {
-                    shade32(32);
-                    head = (head + 32) & (kQueue - 1);
-                    qn -= 32;
+                const int ncand = __shfl_sync(FULL, excl, 31);
+                excl -= cnt;
+                for (int k0 = 0; k0 < ncand; k0 += 32) {
+                    const int kc = k0 + lane;
+                    int j = 0;  // the last row whose candidates start at or before kc
+#pragma unroll
+                    for (int st = 16; st > 0; st >>= 1)
+                        if (__shfl_sync(FULL, excl, j + st) <= kc) j += st;
+                    const int lo_j = __shfl_sync(FULL, lo, j), ex_j = __shfl_sync(FULL, excl, j);
+                    bool cov = false;
+                    float l[3] = {0.f, 0.f, 0.f}, zf = 0.f;
+                    const int py = py0 + rb + j, px = px0 + lo_j + (kc - ex_j);
+                    if (kc < ncand) cov = pixel_fragment(X, Y, dX, dY, bias, perm1, inv, z, px, py, l, zf);
+                    const unsigned m = __ballot_sync(FULL, cov);
+                    if (cov) {
+                        const int slot = (head + qn + __popc(m & ((1u << lane) - 1u))) & (kQueue - 1);
+                        q.tri[slot] = (int)tl;
+                        q.pix[slot] = (uint32_t)px | ((uint32_t)py << 11) | ((uint32_t)axis << 22) |
+                                      ((uint32_t)scene << 24);
+                        q.l0[slot] = l[0];
+                        q.l1[slot] = l[1];
+                        q.l2[slot] = l[2];
+                        q.z[slot] = zf;
+                    }
+                    qn += __popc(m);
+                    pending += (unsigned)__popc(m);
+                    if (qn >= 32) {
+                        shade32(32);
+                        head = (head + 32) & (kQueue - 1);
+                        qn -= 32;
+                    }
                 }
             }
         }
