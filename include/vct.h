@@ -457,7 +457,7 @@ vct_status vct_batch_get_timers(vct_batch* batch, vct_timers* out);
  * pipeline and the compute shaders' local sizes).  Every setting gives
  * bit-identical results; only speed differs. */
 typedef struct vct_tuning {
-    int32_t voxel_unit_pixels;   /* bounding-box pixels per voxeliser work unit: power of two in [32, 8192] (512) */
+    int32_t voxel_unit_pixels;   /* candidate pixels (rows' spans of the triangle) per voxeliser work unit, about: power of two in [32, 8192] (512) */
     int32_t voxel_blocks_per_sm; /* resident voxeliser raster CTAs per SM: 1..3 (3) */
     int32_t trace_tile_w;        /* pixel tile of one 256-thread trace CTA, tile_w * tile_h = 256: */
     int32_t trace_tile_h;        /*   tile_w a power of two in [4, 64] (16 x 16) */

@@ -89,7 +89,7 @@ struct AccumParams {
     uint32_t* brick_exact;  // with `carry`: per 16^3 brick, set by the carry pass for the bricks it rewrote
     StatsDev* stats;
     int num_sms;
-    int unit_log2;      // log2 of the bounding-box pixels per work unit
+    int unit_log2;      // log2 of the candidate pixels per work unit (whole rows of the bounding box)
     int blocks_per_sm;  // raster CTAs per SM (1..3)
     WarpDev warp;
     f3 vmin, vcenter, ext;  // voxelLinearPosition of the tessellation voxeliser

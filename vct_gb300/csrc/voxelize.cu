@@ -6,12 +6,13 @@
 //  1. voxelize_setup_kernel, one thread per triangle: the geometry-shader
 //     part (dominant axis from the summed vertex normals, per-axis ortho
 //     projection, snapping to the 1/256 sub-pixel grid, bounding box) into a
-//     48-byte record, and the triangle's share of work: its bounding box in
-//     units of 2^unit_log2 pixels (a tuning setting), with a block-local
-//     exclusive scan;
+//     48-byte record, and the triangle's share of work: its bounding box's
+//     rows in units of about 2^unit_log2 candidate pixels (a tuning
+//     setting), with a block-local exclusive scan;
 //  2. voxelize_scan_kernel, one CTA: exclusive scan of the per-block totals;
 //  3. voxelize_raster_kernel, persistent: warps take work units from a
-//     shared counter, test 32 pixel centres at a time for coverage, compact
+//     shared counter, narrow each row to the triangle's span, test 32 pixel
+//     centres at a time for coverage, compact
 //     covered fragments (clipped to the depth range) with a ballot into a
 //     per-warp ring queue in shared memory, and whenever 32 are queued each
 //     lane lights one fragment (all enabled lights, 5-tap PCF for shadow
@@ -124,11 +125,18 @@ __global__ void __launch_bounds__(kSetupThreads) voxelize_setup_kernel(const Sce
             uint4* rec = W.tri_rec + 3 * g;
             rec[0] = make_uint4((uint32_t)rt.X[0], (uint32_t)rt.Y[0], (uint32_t)rt.X[1], (uint32_t)rt.Y[1]);
             rec[1] = make_uint4((uint32_t)rt.X[2], (uint32_t)rt.Y[2], __float_as_uint(z[0]), __float_as_uint(z[1]));
+            // A work unit is R whole rows of the bounding box, R chosen so that
+            // the unit holds about 2^unit_log2 candidate pixels: a row's span
+            // of the triangle (the area over the rows, on average) and a
+            // pixel each side.  A sliver's rows are short, so its units take
+            // many rows.
+            const float row_px = (float)rt.area * (0.5f / (float)(kSub * kSub)) / (float)bh + 2.0f;
+            const uint32_t R = (uint32_t)fminf(fmaxf((float)(1u << W.unit_log2) / row_px, 1.0f), 1023.0f);
             rec[2] = make_uint4(__float_as_uint(z[2]), __float_as_uint(inv),
                                 (uint32_t)rt.px0 | ((uint32_t)rt.py0 << 11) | ((uint32_t)axis << 22) |
                                     ((uint32_t)rt.perm1 << 24) | (bias << 25),
-                                bw | (bh << 11));
-            units = (bw * bh + (1u << W.unit_log2) - 1) >> W.unit_log2;
+                                bw | (bh << 11) | (R << 22));
+            units = (bh + R - 1) / R;
         }
         W.tri_units[g] = units;
     }
@@ -391,22 +399,19 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
             const float inv = __uint_as_float(r2.y);
             const int px0 = (int)(r2.z & 0x7ffu), py0 = (int)((r2.z >> 11) & 0x7ffu);
             const int axis = (int)((r2.z >> 22) & 3u), perm1 = (int)((r2.z >> 24) & 1u), bias = (int)(r2.z >> 25);
-            const int bw = (int)(r2.w & 0x7ffu), bh = (int)(r2.w >> 11);
-            const int p_begin = (int)(u - start) << W.unit_log2;
-            const int p_end = min(p_begin + (1 << W.unit_log2), bw * bh);
+            const int bw = (int)(r2.w & 0x7ffu), bh = (int)((r2.w >> 11) & 0x7ffu), R = (int)(r2.w >> 22);
             int dX[3], dY[3];  // edge k: vertex k+2 minus vertex k+1
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 dX[k] = X[(k + 2) % 3] - X[(k + 1) % 3];
                 dY[k] = Y[(k + 2) % 3] - Y[(k + 1) % 3];
             }
-            // The unit's pixels, row by row: each lane takes one of up to 32 rows
-            // and narrows it to the pixels between the triangle's crossings of
-            // the row's centre line (widened by one pixel each side, so that
-            // float rounding never drops a covered pixel); the warp then tests
-            // the rows' candidates 32 at a time.  A sliver fills a small part
-            // of its bounding box, over which the units are counted.
-            const int r_a = p_begin / bw, r_b = (p_end - 1) / bw;
+            // The unit's rows of the bounding box, 32 at a time: each lane takes
+            // one row and narrows it to the pixels between the triangle's
+            // crossings of the row's centre line (widened by one pixel each
+            // side, so that float rounding never drops a covered pixel); the
+            // warp then tests the rows' candidates 32 at a time.
+            const int r_a = (int)(u - start) * R, r_b = min(r_a + R, bh) - 1;
             float slope[3];  // x per unit y along edge k
 #pragma unroll
             for (int k = 0; k < 3; ++k) slope[k] = dY[k] != 0 ? __fdividef((float)dX[k], (float)dY[k]) : 0.0f;
@@ -430,8 +435,8 @@ __global__ void __launch_bounds__(kWarps * 32, kRasterBlocksPerSM)
                         const float rs = 1.0f / (float)kSub, hs = 0.5f * (float)kSub;
                         const int s0 = (int)ceilf((xmin - hs) * rs) - 1 - px0;
                         const int s1 = (int)floorf((xmax - hs) * rs) + 1 - px0;
-                        lo = max(max(p_begin - r * bw, 0), s0);
-                        cnt = max(min(min(p_end - r * bw, bw) - 1, s1) - lo + 1, 0);
+                        lo = max(0, s0);
+                        cnt = max(min(bw - 1, s1) - lo + 1, 0);
                     }
                 }
                 int excl = cnt;  // exclusive prefix of the rows' candidate counts
