@@ -1072,10 +1072,10 @@ def run_dynamic(args, rank, world):
 # stage, from one ncu capture of the large frame (`bench.py --profile-frames 3`, default
 # launch shapes): accumulate = setup + raster, resolve+mips = resolve + tail; only for the
 # default workload, and only while the frame kernels' sources hash to NCU_CAPTURE_DIGEST.
-NCU_CAPTURE_DIGEST = "900eb37e94fa9559"
+NCU_CAPTURE_DIGEST = "438e8eac75de4cad"
 NCU_CAPTURE_SAMPLER = "hybrid"
-NCU_TRAFFIC = {"accumulate": 18.891e6 + 262.408e6 + 160.230e6, "resolve+mips": 258.924e6 + 835.374e6 + 0.047e6,
-               "inject_mark": 18.259e6 + 0.023e6, "trace": 89.196e6 + 13.108e6}
+NCU_TRAFFIC = {"accumulate": 18.891e6 + 262.704e6 + 161.262e6, "resolve+mips": 258.924e6 + 835.439e6 + 0.047e6,
+               "inject_mark": 18.258e6 + 0.023e6, "trace": 89.188e6 + 12.723e6}
 # Issue-side figures of the cone tracer (hybrid sampler) from its full capture of the same
 # command: it is bound by issue and load latency at its occupancy, not HBM.  (Captured
 # before the accumulator records moved to 2 x 2 slots; the tracer reads no records and its
