@@ -433,7 +433,7 @@ typedef struct vct_scene_desc {
     vct_trace_out out;
 } vct_scene_desc;
 
-vct_status vct_batch_create(const vct_config* configs, int32_t n_scenes, vct_batch** out);
+vct_status vct_batch_create(const vct_config* scene_cfg, int32_t n_scenes, vct_batch** out);
 vct_status vct_batch_destroy(vct_batch* batch);
 /* Parameters of one scene (scene = -1: every scene); all scenes must use the
  * same trace_filter and voxeliser; warp modes may differ (scenes with

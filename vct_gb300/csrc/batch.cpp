@@ -273,25 +273,25 @@ vct_status batch_enqueue(vct_batch* b, const char* h, const BatchTotals& tot, cu
 
 extern "C" {
 
-vct_status vct_batch_create(const vct_config* configs, int32_t n, vct_batch** out) {
+vct_status vct_batch_create(const vct_config* scene_cfg, int32_t n, vct_batch** out) {
     if (!out) return fail(VCT_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
-    if (!configs || n < 1 || n > accumulate_batch_max_scenes())
+    if (!scene_cfg || n < 1 || n > accumulate_batch_max_scenes())
         return fail(VCT_ERR_INVALID_ARGUMENT, "a batch holds 1..256 scenes");
     for (int i = 0; i < n; ++i) {
-        vct_status s = validate_config(&configs[i]);
+        vct_status s = validate_config(&scene_cfg[i]);
         if (s != VCT_OK) return s;
-        if (configs[i].voxel_dim > 256) return fail(VCT_ERR_UNSUPPORTED, "batched scenes are limited to 256^3 grids");
-        if (configs[i].device != configs[0].device) return fail(VCT_ERR_INVALID_ARGUMENT, "a batch lives on one device");
+        if (scene_cfg[i].voxel_dim > 256) return fail(VCT_ERR_UNSUPPORTED, "batched scenes are limited to 256^3 grids");
+        if (scene_cfg[i].device != scene_cfg[0].device) return fail(VCT_ERR_INVALID_ARGUMENT, "a batch lives on one device");
     }
     vct_batch* b = new (std::nothrow) vct_batch;
     if (!b) return fail(VCT_ERR_OUT_OF_MEMORY, "host allocation failed");
     b->n = n;
-    b->device = configs[0].device;
+    b->device = scene_cfg[0].device;
     default_tuning(b->tuning);
     for (int i = 0; i < n; ++i) {
         vct_ctx* c = nullptr;
-        vct_status s = vct_create(&configs[i], &c);
+        vct_status s = vct_create(&scene_cfg[i], &c);
         if (s != VCT_OK) {
             std::string msg = g_err;
             vct_batch_destroy(b);
