@@ -307,6 +307,8 @@ vct_status vct_volume_level(const vct_ctx* ctx, int32_t volume, int32_t level,
  * the frame; vct_normalize / vct_frame leave them zeroed. */
 vct_status vct_accumulators(const vct_ctx* ctx, const uint32_t** records_dev,
                             const uint32_t** occupancy_dev);
+/* The slot s of voxel v's record (records_dev[8*s]) in a dim^3 grid. */
+int64_t vct_record_slot(int64_t v, int32_t dim);
 
 /* ---- stages ----------------------------------------------------------- */
 /* voxelize.geom/.frag: rasterise every triangle along its dominant axis and

@@ -63,6 +63,14 @@ int main(void) {
     CHECK(vct_voxelize_static(&cfg, &p, &tris, NULL, 0, NULL, NULL, NULL, NULL, NULL, NULL) ==
           VCT_ERR_INVALID_ARGUMENT);
 
+    /* accumulator record slots: bit 1 of x and bit 0 of y exchanged */
+    CHECK(vct_record_slot(0, 16) == 0);
+    CHECK(vct_record_slot(2, 16) == 16);  /* x = 2, y = 0 */
+    CHECK(vct_record_slot(16, 16) == 2);  /* x = 0, y = 1 */
+    CHECK(vct_record_slot(3, 16) == 17);  /* x = 3, y = 0 */
+    CHECK(vct_record_slot(18, 16) == 18); /* x = 2, y = 1 */
+    CHECK(vct_record_slot(4096 + 17, 16) == 4096 + 3);
+
     if (failures == 0) printf("abi_check ok\n");
     return failures == 0 ? 0 : 1;
 }

@@ -39,8 +39,9 @@ def _cuda_include() -> str | None:
 @pytest.mark.skipif(shutil.which("g++") is None or _cuda_include() is None, reason="no C++ compiler or CUDA headers")
 def test_record_slots_match_the_kernels_layout(tmp_path):
     """The accumulator-record slot that the kernels use (record_slot) equals
-    api.record_slots, which read_accumulators inverts; the map is a
-    permutation whose 128-byte lines (4 records) are 2 x 2 blocks in x, y."""
+    the exported vct_record_slot and api.record_slots, which
+    read_accumulators inverts; the map is a permutation whose 128-byte lines
+    (4 records) are 2 x 2 blocks in x, y."""
     import numpy as np
 
     from vct_gb300.api import record_slots
@@ -49,11 +50,17 @@ def test_record_slots_match_the_kernels_layout(tmp_path):
     src.write_text('#include "vct_internal.h"\n#include <cstdio>\n#include <cstdlib>\n'
                    "int main(int argc, char** argv) {\n"
                    "    const int n = atoi(argv[1]);\n"
-                   "    for (long long v = 0; v < (long long)n * n * n; ++v) printf(\"%lld\\n\", vct::record_slot(v, n));\n"
+                   "    for (long long v = 0; v < (long long)n * n * n; ++v) {\n"
+                   "        if (vct::record_slot(v, n) != vct_record_slot(v, n)) return 1;\n"
+                   "        printf(\"%lld\\n\", vct::record_slot(v, n));\n"
+                   "    }\n"
                    "}\n")
     exe = str(tmp_path / "slots")
+    lib = os.path.join(LIBDIR, "libvct.so")
+    if not os.path.exists(lib):
+        pytest.skip("libvct.so not built")
     cmd = ["g++", "-std=c++17", "-I", os.path.join(ROOT, "vct_gb300", "csrc"), "-I", _cuda_include(), str(src),
-           "-o", exe]
+           "-L", LIBDIR, "-lvct", "-Wl,-rpath," + LIBDIR, "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     for n in (16, 32):

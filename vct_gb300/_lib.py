@@ -159,6 +159,7 @@ SIGNATURES = {
     "vct_get_config": (st, [vp, P(vct_config)]),
     "vct_volume_level": (st, [vp, C.c_int32, C.c_int32, P(vp), P(C.c_int32)]),
     "vct_accumulators": (st, [vp, P(vp), P(vp)]),
+    "vct_record_slot": (C.c_int64, [C.c_int64, C.c_int32]),
     "vct_voxelize_accumulate": (st, [vp, P(vct_triangles), P(vct_light), C.c_int32, P(vct_shadow_desc),
                                      P(C.c_float), vp]),
     "vct_normalize": (st, [vp, vp]),

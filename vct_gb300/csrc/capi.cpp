@@ -828,6 +828,8 @@ vct_status vct_volume_level(const vct_ctx* c, int32_t volume, int32_t level, con
     return VCT_OK;
 }
 
+int64_t vct_record_slot(int64_t v, int32_t dim) { return record_slot(v, dim); }
+
 vct_status vct_accumulators(const vct_ctx* c, const uint32_t** records, const uint32_t** occupancy) {
     if (!c) return fail(VCT_ERR_INVALID_ARGUMENT, "ctx is NULL");
     if (records) *records = c->acc;
